@@ -1,0 +1,86 @@
+"""Loading of the golden vectors (tests/golden/*.npz) and rebuilding the
+cases they were made from.  The goldens were produced by the reference's own
+parser and kernels executed on the CPU (tests/golden/make_golden.py)."""
+from __future__ import annotations
+
+import hashlib
+import json
+import os
+import tempfile
+
+import numpy as np
+
+import oracle
+from md_gpu_gb300 import synth
+
+GOLDEN_DIR = os.path.join(os.path.dirname(os.path.abspath(__file__)), "golden")
+REF_ROOT = "/root/reference"
+
+
+def names():
+    with open(os.path.join(GOLDEN_DIR, "index.json")) as fh:
+        return list(json.load(fh).keys())
+
+
+def load_golden(name):
+    z = np.load(os.path.join(GOLDEN_DIR, name + ".npz"))
+    g = {k: z[k] for k in z.files}
+    g["hashes"] = json.loads(str(g["hashes"]))
+    g["meta"] = json.loads(str(g["meta"]))
+    return g
+
+
+def sha(a) -> str:
+    return hashlib.sha256(np.ascontiguousarray(a).tobytes()).hexdigest()
+
+
+def write_synth(spec, directory):
+    spec = dict(spec)
+    fn = getattr(synth, spec.pop("fn"))
+    return synth.write_case(fn(**spec), directory, "case")
+
+
+def case_from_golden(g) -> oracle.Case:
+    """An oracle.Case for a golden: synthetic cases are regenerated and parsed
+    by the oracle; example cases are rebuilt from their stored parsed arrays."""
+    meta = g["meta"]
+    if meta["kind"] == "synth":
+        with tempfile.TemporaryDirectory() as td:
+            return oracle.load(write_synth(meta["spec"], td))
+    pv = g["params"]
+    p = oracle.Params()
+    p.rcutsq, p.reacf, p.alfa, p.skin = (float(x) for x in pv[:4])
+    p.nmaxlist, p.dt, p.temper_0 = int(pv[4]), float(pv[5]), float(pv[6])
+    p.lkspace, p.enstype, p.timrun, p.rdel = int(pv[7]), int(pv[8]), int(pv[9]), float(pv[10])
+    p.tau_t = 100.0
+    f = oracle.FField()
+    cnt = g["fld_counts"]
+    f.ntype, f.tbonds, f.tangle = int(cnt[0]), int(cnt[1]), int(cnt[2])
+    for k in range(f.ntype):
+        f.mass[k] = float(g["mass"][k])
+    for k in range(64):
+        f.lj1[k] = float(g["lj1"][k]); f.lj2[k] = float(g["lj2"][k])
+    for k in range(8):
+        f.bnd1[k] = float(g["bnd1"][k]); f.bnd2[k] = float(g["bnd2"][k])
+        f.ang1[k] = float(g["ang1"][k]); f.ang2[k] = float(g["ang2"][k])
+    n = int(g["itype"].shape[0])
+    pos_in = g["pos_in"].reshape(n, 4)
+    vel_in = g["vel_in"].reshape(n, 4)
+    box = g["box"][:3].astype(np.float32)
+    return oracle.Case(params=p, fld=f, natom=n, box=box, boxi=g["box"][3:].astype(np.float32),
+                       itype=g["itype"].astype(np.int32), q=pos_in[:, 3].copy(),
+                       pos=np.ascontiguousarray(pos_in[:, :3]), vel=np.ascontiguousarray(vel_in[:, :3]),
+                       mass=vel_in[:, 3].copy(),
+                       bonds=g["bonds"].reshape(-1, 3).astype(np.int32),
+                       angles=g["angles"].reshape(-1, 4).astype(np.int32))
+
+
+def rows_canonical(nn, nm, n, width):
+    """Row-major (N, width) neighbour table with 0xffffffff fill, as the golden stores it."""
+    pt = nm.shape[0]
+    out = np.full((n, width), 0xFFFFFFFF, np.uint32)
+    cols = nn.reshape(-1, pt)
+    for k in range(width):
+        m = nm[:n] > k
+        out[m, k] = cols[k, :n][m]
+    return out
