@@ -1,0 +1,282 @@
+#!/usr/bin/env python
+"""Benchmark: MD steps of 64000-ion molten NaCl (LJ + Wolf Coulomb, alpha 0.2/A,
+rc 12 A, skin 1 A, Berendsen leapfrog NVT at 1200 K, dt 2 fs) on one GB300.
+
+One bench "step" is one segment of --md-steps MD steps (list check and
+rebuilds at their natural rate, forces, integration) run through md_step as
+captured CUDA graphs.  L2 is flushed (512 MB write) before every timed segment;
+inside a segment the ~80 MB working set stays resident, as in any MD run.
+
+    python bench.py [--gpus N] [--steps K] [--warmup W] [--impl ours|reference]
+
+--impl reference times the reference's algorithm on the host cores: the
+oracle's FP32 restatement of md_gpu's step loop (O(N^2) list rebuilt on the
+skin/2 criterion, full-list pair forces, leapfrog Berendsen), OpenMP over all
+host threads (the reference itself has no CPU implementation).
+With N > 1 (torchrun) every rank runs an independent replica of the system
+(different seed): no data exchange, weak scaling.
+"""
+from __future__ import annotations
+
+import argparse
+import json
+import os
+import statistics
+import subprocess
+import sys
+import tempfile
+import time
+
+import numpy as np
+
+ROOT = os.path.dirname(os.path.abspath(__file__))
+sys.path.insert(0, ROOT)
+
+METRIC = "atom-steps/s at 1 GB300 vs plain FP64 at ≤1e-5 force err; adjoint param-grads/s"
+UNIT = "atom-steps/s"
+WORKLOAD = ("nacl64k: 64000-ion molten NaCl, rocksalt 20^3x8 at 1.5 g/cm^3, LJ (Lorentz-Berthelot) + "
+            "Wolf Coulomb alpha 0.2/A rc 12 A skin 1 A, Berendsen leapfrog NVT 1200 K tau 100 fs, dt 2 fs")
+DT_FS = 2.0
+FLOPS_PER_PAIR = 60.0     # LJ + Wolf per unique pair inside rc (algorithmic count)
+# ncu dram__bytes_read.sum + dram__bytes_write.sum of one pair-kernel launch on
+# this workload (profiles/pair_wolf_nacl64k.md); None until captured.
+PAIR_TRAFFIC_BYTES = None
+
+
+def rank_info():
+    return (int(os.environ.get("RANK", 0)), int(os.environ.get("WORLD_SIZE", 1)),
+            int(os.environ.get("LOCAL_RANK", 0)))
+
+
+class Clocks:
+    """nvidia-smi sampled every 200 ms while the timed region runs."""
+
+    def __init__(self, index):
+        self.index = index
+        self.proc = None
+        self.path = None
+
+    def __enter__(self):
+        fd, self.path = tempfile.mkstemp(suffix=".csv")
+        os.close(fd)
+        q = ("index,clocks.sm,clocks.max.sm,power.draw,clocks_event_reasons.active,"
+             "clocks_event_reasons.hw_slowdown,clocks_event_reasons.hw_thermal_slowdown,"
+             "clocks_event_reasons.sw_thermal_slowdown,clocks_event_reasons.sw_power_cap")
+        try:
+            self.fh = open(self.path, "w")
+            self.proc = subprocess.Popen(["nvidia-smi", f"--id={self.index}", f"--query-gpu={q}",
+                                          "--format=csv,noheader,nounits", "-lms", "200"],
+                                         stdout=self.fh, stderr=subprocess.DEVNULL)
+        except OSError:
+            self.proc = None
+        return self
+
+    def __exit__(self, *a):
+        if self.proc:
+            self.proc.terminate()
+            try:
+                self.proc.wait(5)
+            except subprocess.TimeoutExpired:
+                self.proc.kill()
+            self.fh.close()
+
+    def summary(self):
+        if not self.proc or not self.path:
+            return None
+        rows = []
+        with open(self.path) as fh:
+            for line in fh:
+                f = [x.strip() for x in line.split(",")]
+                if len(f) >= 9:
+                    rows.append(f)
+        os.unlink(self.path)
+        if not rows:
+            return None
+        sm = [float(r[1]) for r in rows if r[1].replace(".", "").isdigit()]
+        mx = [float(r[2]) for r in rows if r[2].replace(".", "").isdigit()]
+        names = ["hw_slowdown", "hw_thermal_slowdown", "sw_thermal_slowdown", "sw_power_cap"]
+        reasons = sorted({n for r in rows for n, v in zip(names, r[5:9]) if v.lower() == "active"})
+        return {"sm_mhz": statistics.median(sm) if sm else None,
+                "sm_max_mhz": max(mx) if mx else None, "reasons": reasons, "samples": len(rows)}
+
+
+def make_case(seed, ncell, tmp):
+    from md_gpu_gb300 import synth
+    return synth.write_case(synth.nacl_rocksalt(ncell=ncell, seed=seed), tmp, "nacl")
+
+
+def cpu_reference_sample(base, samples, warmup, md_steps):
+    """Time the oracle's restatement of the reference loop on the host cores."""
+    import oracle
+    case = oracle.load(base)
+    pos4, vel4 = case.pos4(), case.vel4()
+    temper = None
+    for _ in range(warmup):
+        _, _, _, temper = oracle.md_ref_run(case, pos4, vel4, md_steps, temper=temper)
+    t0 = time.perf_counter()
+    for _ in range(samples):
+        _, _, _, temper = oracle.md_ref_run(case, pos4, vel4, md_steps, temper=temper)
+    dt = time.perf_counter() - t0
+    return case.natom * md_steps * samples / dt, dt, oracle.lib().orc_num_threads()
+
+
+def run_reference(args):
+    rank, world, _ = rank_info()
+    if rank != 0:
+        return
+    with tempfile.TemporaryDirectory() as tmp:
+        base = make_case(1, args.ncell, tmp)
+        n = 8 * args.ncell ** 3
+        ms = args.ref_md_steps
+        value, dt, cores = cpu_reference_sample(base, args.steps, args.warmup, ms)
+    sample = (f"{args.steps} samples of {ms} MD steps each (each sample starts with an O(N^2) list build, "
+              f"then rebuilds on the skin/2 criterion), N={n}")
+    line = {"impl": "reference", "metric": METRIC, "value": value, "unit": UNIT, "n_gpus": world,
+            "steps": args.steps, "warmup": args.warmup, "ms_per_step": 1e3 * dt / args.steps,
+            "higher_is_better": True, "scaling": "weak", "vs_baseline": None, "dtype": "f32",
+            "data": "synthetic", "config": {"workload": WORKLOAD, "natom": n, "md_steps_per_step": ms,
+                                            "parallelism": "host threads (OpenMP)"},
+            "cpu_baseline": {"value": value, "unit": UNIT, "cores": cores, "kind": "port",
+                             "sample": sample},
+            "e2e": {"value": value, "unit": UNIT, "h2d_bytes_per_step": 0, "d2h_bytes_per_step": 0}}
+    print(json.dumps(line), flush=True)
+
+
+def run_ours(args):
+    import torch
+    rank, world, local = rank_info()
+    torch.cuda.set_device(local)
+    if world > 1:
+        import torch.distributed as dist
+        dist.init_process_group("nccl")
+
+    def barrier():
+        if world > 1:
+            torch.distributed.barrier()
+        torch.cuda.synchronize()
+
+    from md_gpu_gb300 import build as mdbuild
+    mdbuild.build()
+    import md_gpu_gb300 as md
+
+    tmp = tempfile.mkdtemp(prefix="mdbench_")
+    base = make_case(1 + rank, args.ncell, tmp)
+    sim = md.MDSystem.from_files(base)
+    n = sim.natom
+    flush = torch.empty(512 * 1024 * 1024, dtype=torch.uint8, device="cuda")
+
+    for _ in range(args.warmup):
+        sim.step(args.md_steps)
+    builds0 = sim.info()["builds"]
+
+    seg_ms = []
+    barrier()
+    with Clocks(local) as clk:
+        for _ in range(args.steps):
+            flush.zero_()
+            torch.cuda.synchronize()
+            sim.step(args.md_steps)
+            seg_ms.append(sim.last_step_ms())
+        barrier()
+    clocks = clk.summary()
+    total_ms = float(sum(seg_ms))
+    info = sim.info()
+    builds = info["builds"] - builds0
+    if world > 1:
+        t = torch.tensor([total_ms], device="cuda")
+        torch.distributed.all_reduce(t, op=torch.distributed.ReduceOp.MAX)
+        total_ms = float(t.item())
+    atom_steps = n * args.md_steps * args.steps * world
+    value = atom_steps / (total_ms * 1e-3)
+    md_steps_per_s = args.md_steps * args.steps / (total_ms * 1e-3)
+
+    extra = {}
+    if rank == 0:
+        import oracle
+        # roofline of the dominant kernel (pair forces), timed alone on the same state
+        pair_ms = sim.time_pair(50)
+        pos = sim.positions().astype(np.float32)
+        case = oracle.load(base)
+        pos4 = np.ascontiguousarray(np.concatenate([pos, np.zeros((n, 1), np.float32)], 1))
+        p = case.params
+        pc = oracle.count_pairs(pos4, case.box, p.rcutsq)
+        achieved = FLOPS_PER_PAIR * pc / (pair_ms * 1e-3) / 1e12
+        peak = md.fp32_peak_tflops()
+        roof = {"bound": "fp32", "achieved": achieved, "peak": peak, "unit": "TFLOP/s",
+                "frac": achieved / peak, "traffic": PAIR_TRAFFIC_BYTES,
+                "kernel": "k_pair<Wolf> (LJ + Wolf, full list, 4 lanes per atom)",
+                "pair_ms": pair_ms, "pairs_inside_rc": int(pc), "flops_per_pair": FLOPS_PER_PAIR,
+                "peak_source": "measured FP32 FMA probe (md_probe_fp32_peak); no FP32 entry in "
+                               "MEASURED_PEAKS.json"}
+        # accuracy of the first frame against the FP64 plain form
+        case = oracle.load(base)
+        with md.MDSystem.from_files(base) as fresh:
+            fresh.compute_forces(md.TERM_PAIR)
+            F = fresh.forces()
+            fpos4 = case.pos4()
+            excl = oracle.exclusions(n, case.bonds)
+            nn, nm, _ = oracle.nlist(fpos4, case.box, case.boxi, oracle.rskinsq(p.skin, p.rcutsq), excl, 512)
+            f64, _ = oracle.pair_f64(1, fpos4, case.itype, case.q, case.box, nn, nm, case.fld.ntype,
+                                     case.lj1, case.lj2, p.rcutsq, 0.0, p.alfa)
+            err = float(np.sqrt(((F[:, :3] - f64[:, :3]) ** 2).sum() / (f64[:, :3] ** 2).sum()))
+        # end to end through the C ABI from pinned host buffers
+        hp = torch.empty((n, 3), dtype=torch.float64, pin_memory=True).numpy()
+        hv = torch.empty((n, 3), dtype=torch.float64, pin_memory=True).numpy()
+        hp[:] = sim.positions()
+        hv[:] = sim.velocities()
+        e2e_reps = max(1, min(args.steps, 5))
+        t0 = time.perf_counter()
+        for _ in range(e2e_reps):
+            hp2, hv2, _ = sim.run_host(hp, hv, args.md_steps)
+            hp[:], hv[:] = hp2, hv2
+        e2e_dt = (time.perf_counter() - t0) / e2e_reps
+        e2e = {"value": n * args.md_steps / e2e_dt, "unit": UNIT,
+               "h2d_bytes_per_step": 2 * 3 * n * 8,
+               "d2h_bytes_per_step": 2 * 3 * n * 8 + args.md_steps * 72,
+               "call": "md_run_host (upload pos/vel, list build, md_steps steps, download records + pos/vel)"}
+        cpu_v, cpu_dt, cores = cpu_reference_sample(base, 1, 0, args.ref_md_steps)
+        extra = {"roofline": roof, "e2e": e2e, "force_rms_rel_err_vs_fp64": err,
+                 "cpu_baseline": {"value": cpu_v, "unit": UNIT, "cores": cores, "kind": "port",
+                                  "sample": f"{args.ref_md_steps} MD steps of the same system (one O(N^2) "
+                                            "list build, then rebuilds on the skin/2 criterion), oracle "
+                                            "FP32 restatement, OpenMP"}}
+    line = {"metric": METRIC, "value": value, "unit": UNIT, "n_gpus": world, "steps": args.steps,
+            "warmup": args.warmup, "ms_per_step": total_ms / args.steps, "higher_is_better": True,
+            "scaling": "weak", "vs_baseline": None, "dtype": "f32",
+            "data": "synthetic (seeded rocksalt lattice with 0.25 A jitter, Maxwell-Boltzmann velocities)",
+            "config": {"workload": WORKLOAD, "natom": n, "md_steps_per_step": args.md_steps,
+                       "l2": "flushed (512 MB write) before every timed segment",
+                       "parallelism": "replicas" if world > 1 else "single system",
+                       "ns_per_day": md_steps_per_s * DT_FS * 0.0864,
+                       "list_builds_in_timed_region": builds,
+                       "pair_threads_per_atom": info["pair_tpa"]},
+            "gpu_launches": info["kernels_per_step"] * args.md_steps * args.steps,
+            "clocks": clocks}
+    line.update(extra)
+    if rank == 0:
+        print(json.dumps(line), flush=True)
+    sim.close()
+    if world > 1:
+        torch.distributed.destroy_process_group()
+
+
+def main():
+    ap = argparse.ArgumentParser()
+    ap.add_argument("--gpus", type=int, default=1)
+    ap.add_argument("--steps", type=int, default=20)
+    ap.add_argument("--warmup", type=int, default=3)
+    ap.add_argument("--impl", choices=["ours", "reference"], default="ours")
+    ap.add_argument("--md-steps", type=int, default=100)
+    ap.add_argument("--ref-md-steps", type=int, default=10)
+    ap.add_argument("--ncell", type=int, default=20)
+    args = ap.parse_args()
+    if args.warmup < 3 and args.impl == "ours":
+        args.warmup = 3
+    if args.impl == "reference":
+        run_reference(args)
+    else:
+        run_ours(args)
+
+
+if __name__ == "__main__":
+    main()

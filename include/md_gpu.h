@@ -1,0 +1,182 @@
+/*
+ * md_gpu.h -- C ABI of libmdgpu_gb300: md_gpu's per-step force-and-integrate
+ * path (neighbour list, LJ + Wolf / reaction-field pair forces, harmonic
+ * bonds and angles, leapfrog / Berendsen / velocity-Verlet / Nose-Hoover
+ * integrators) as hand-written sm_103a kernels.
+ *
+ * Plain C types only.  Every call returns an md_status (the reference exits
+ * the process on any CUDA error, gpu_properties.cu:75-81).  One md_ctx per
+ * system; distinct contexts may be used from distinct host threads.  Unless
+ * stated otherwise host arrays are in the original atom order of the input.
+ *
+ * Units as in the reference: A, fs, g/mol, kJ/mol, e.  Masses in the
+ * descriptor are g/mol * 1e4, the reference's stored unit (simulation.cu:177).
+ */
+#ifndef MD_GPU_H
+#define MD_GPU_H
+
+#ifdef __cplusplus
+extern "C" {
+#endif
+
+typedef struct md_ctx md_ctx;
+
+typedef enum {
+    MD_OK = 0,
+    MD_ERR_ARG = 1,            /* invalid argument */
+    MD_ERR_IO = 2,             /* file cannot be opened */
+    MD_ERR_PARSE = 3,          /* input file does not follow the grammar */
+    MD_ERR_CUDA = 4,           /* CUDA runtime error (see md_last_error) */
+    MD_ERR_LIST_OVERFLOW = 5,  /* an atom has more neighbours than the list holds */
+    MD_ERR_BONDED = 6,         /* more than four bonds / angles on one atom */
+    MD_ERR_UNSUPPORTED = 7,    /* option not implemented (e.g. NPT) */
+    MD_ERR_BOX = 8             /* cutoff + skin larger than half the box */
+} md_status;
+
+/* Integrators.  LEAPFROG follows nve_leapfrog.cu / nvt_leapfrog_ber.cu (the
+ * reference's active path, runGPU.cu:71); VV is velocity Verlet NVE with the
+ * half kick counted once (nve_vverlet.cu:49 adds it twice); NH is velocity
+ * Verlet with one Nose-Hoover thermostat (nvt_vverlet_nh.cu has no such
+ * implementation: it is a copy of the Berendsen file). */
+typedef enum { MD_LEAPFROG = 0, MD_VV = 1, MD_NH = 2 } md_integrator;
+
+/* Force terms for md_compute_forces (bit mask). */
+enum { MD_TERM_PAIR = 1, MD_TERM_BOND = 2, MD_TERM_ANGLE = 4, MD_TERM_ALL = 7 };
+
+/* A system as the reference holds it after SimulationInit (simulation.h:51-122). */
+typedef struct {
+    int natom;
+    int ntype;                  /* <= 8 (forces.cu:48-49) */
+    float box[3];               /* box edge, A; coordinates centred in [-L/2, L/2] */
+    const int *itype;           /* natom, 0-based */
+    const float *charge;        /* natom, e */
+    const float *pos;           /* 3*natom */
+    const float *vel;           /* 3*natom, A/fs (may be NULL: zero) */
+    const float *type_mass;     /* ntype, g/mol * 1e4 */
+    const float *lj1;           /* ntype*ntype (row stride ntype): 48 eps sig^12 or 12 A */
+    const float *lj2;           /* ntype*ntype: 24 eps sig^6 or 6 B */
+    int nbonds;
+    const int *bonds;           /* 3*nbonds: type, i, j (0-based) */
+    const float *bnd1, *bnd2;   /* per bond type: 2k, r0 */
+    int nangle;
+    const int *angles;          /* 4*nangle: type, i, j (centre), k (0-based) */
+    const float *ang1, *ang2;   /* per angle type: 2k, theta0 (rad) */
+    /* run parameters (params / integr, simulation.h:88-122) */
+    int lkspace;                /* 0 reaction field, 1 Wolf, 2 Ewald real space (alpha only) */
+    float rcutsq;               /* squared cutoff, A^2 */
+    float reacf;                /* 2(eps-1)/(2eps+1)/rc^3 (lkspace 0) */
+    float alfa;                 /* damping alpha, 1/A (lkspace 1, 2) */
+    float skin;                 /* list skin, A */
+    int nmaxlist;               /* list capacity per atom (minimum) */
+    int enstype;                /* 0 NVE, 1 NVT */
+    float temper_0;             /* K */
+    float dt;                   /* fs */
+    float tau_t;                /* thermostat time constant, fs (Berendsen and NH) */
+    int integrator;             /* md_integrator */
+} md_system_desc;
+
+/* Thermodynamic record of one step (FP64 reductions on the device). */
+typedef struct {
+    long long step;
+    double ke;           /* kJ/mol */
+    double temper;       /* K, 2 KE / ((3N-3) R) */
+    double pe;           /* kJ/mol, consistent potential (when computed, else 0) */
+    double virial;       /* sum over pairs of F.r / ... : sum ff r^2 / 6 (when computed) */
+    double conserved;    /* KE + PE (+ NH terms) (when PE computed) */
+    double xi;           /* NH thermostat variable, 1/fs */
+    double lambda;       /* Berendsen scale of the step */
+    int builds;          /* neighbour-list builds so far */
+    int flags;           /* bit 0: energies computed this step */
+} md_thermo;
+
+const char *md_status_string(md_status s);
+/* Copies the last error message of ctx (may be NULL for global errors). */
+md_status md_last_error(const md_ctx *ctx, char *buf, int len);
+
+/* SimulationInit + config_init + forces_init + neighborlist_init +
+ * integrate_init (simulation.cu:40, runGPU.cu:53-60): reads <base>.inp,
+ * <base>.fld and <base>.cfg in the reference grammar, uploads the system
+ * and builds the first neighbour list.  stream: cudaStream_t or NULL. */
+md_status md_create_from_files(const char *base, void *stream, md_ctx **out);
+/* The same from arrays (no files). */
+md_status md_create(const md_system_desc *desc, void *stream, md_ctx **out);
+/* forces_finish + config_finish + integrate_finish + neighborlist_finish
+ * (runGPU.cu:107-113). */
+md_status md_destroy(md_ctx *ctx);
+
+/* config_HostToDevice / config_DeviceToHost (config.cu:56-77), original order. */
+md_status md_set_positions(md_ctx *ctx, const double *pos3);
+md_status md_set_velocities(md_ctx *ctx, const double *vel3);
+md_status md_get_positions(md_ctx *ctx, double *pos3);
+md_status md_get_velocities(md_ctx *ctx, double *vel3);
+/* Forces of the last force evaluation: fx, fy, fz, sum ff r^2 per atom
+ * (the reference's float4 force record, pair_forces.cu:117-120). */
+md_status md_get_forces(md_ctx *ctx, double *force4);
+/* Per-atom potential energy of the last energy evaluation (half of each pair). */
+md_status md_get_energies(md_ctx *ctx, double *epot);
+
+/* neighborlist() (neighborlist.cu:109-146) without the host round trip:
+ * force = 1 rebuilds unconditionally, 0 only if an atom moved >= skin/2. */
+md_status md_update_neighbors(md_ctx *ctx, int force);
+/* The current list in the reference's layout (neighborlist.cu:284):
+ * nnlist[i + pitch*k] = j (original indices, ascending), nnlist_max[i].
+ * nnlist holds pitch*nmax entries; returns MD_ERR_LIST_OVERFLOW if any
+ * atom has more than nmax neighbours. */
+md_status md_get_neighbor_list(md_ctx *ctx, unsigned *nnlist, unsigned *nnlist_max, int pitch,
+                               int nmax);
+
+/* forces() + energy() (forces.cu:189-231): pair, bond and angle terms
+ * selected by `terms`; energy != 0 also computes per-atom potential energy
+ * and the virial (FP64 totals, see md_get_thermo). */
+md_status md_compute_forces(md_ctx *ctx, int terms, int energy);
+
+/* nsteps iterations of the reference's loop body (runGPU.cu:69-104):
+ * list check and rebuild, forces, integrate.  energy_every > 0 computes
+ * energies on steps that are multiples of it (the reference's timprn).
+ * Steps run as a captured CUDA graph; no host synchronisation inside. */
+md_status md_step(md_ctx *ctx, int nsteps, int energy_every);
+/* Record of the most recent step (synchronises the stream). */
+md_status md_get_thermo(md_ctx *ctx, md_thermo *out);
+/* The last min(n, nsteps run) records, oldest first; returns the count in *got. */
+md_status md_get_thermo_history(md_ctx *ctx, md_thermo *out, int n, int *got);
+
+/* One call end to end from host buffers: uploads pos/vel (3N doubles),
+ * runs nsteps, downloads pos/vel and the per-step records (nsteps). */
+md_status md_run_host(md_ctx *ctx, double *pos3, double *vel3, int nsteps, int energy_every,
+                      md_thermo *records);
+
+/* Current configuration in the reference's .cfg grammar (simulation.cu:331-339),
+ * with full float precision. */
+md_status md_write_cfg(md_ctx *ctx, const char *path);
+
+/* Introspection for tests and tools. */
+typedef struct {
+    int natom, pitch, capacity, ncell[3], stencil[3];
+    float binlen[3];
+    int pair_threads_per_atom, list_threads_per_atom;
+    int builds;
+    int max_neighbors;
+    int kernels_per_step;   /* kernel launches of one md_step step */
+} md_info;
+md_status md_get_info(md_ctx *ctx, md_info *out);
+/* Sorted -> original index map of the current atom order. */
+md_status md_get_order(md_ctx *ctx, int *perm);
+/* Hilbert rank of every cell (linear index x + nx*(y + ny*z)). */
+md_status md_get_cell_ranks(md_ctx *ctx, int *rank);
+/* Tuning knobs (threads per atom of the pair kernel and of the list build);
+ * values must be 1, 2, 4, 8, 16 or 32. */
+md_status md_set_tuning(md_ctx *ctx, int pair_tpa, int list_tpa);
+/* Milliseconds of device time of the last md_step call (CUDA events). */
+md_status md_last_step_ms(md_ctx *ctx, float *ms);
+/* The pair-force kernel alone, nrep launches on the context's stream between
+ * CUDA events: average milliseconds per launch (the force arrays are
+ * recomputed afterwards, so the state is unchanged). */
+md_status md_time_pair(md_ctx *ctx, int nrep, float *ms_per_launch);
+/* FP32 FMA throughput of the current device (TFLOP/s, best of 5): the
+ * measured FP32-pipe peak the pair kernel is compared against. */
+md_status md_probe_fp32_peak(double *tflops);
+
+#ifdef __cplusplus
+}
+#endif
+#endif

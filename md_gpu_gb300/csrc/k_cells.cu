@@ -1,0 +1,320 @@
+/*
+ * k_cells.cu -- neighbour-list maintenance: displacement check, cell binning,
+ * Hilbert-order atom sort and the list build.
+ *
+ * Semantics follow neighborlist.cu: the list of atom i holds every j != i,
+ * not excluded, with FP32 min-image r^2 < rskinsq evaluated exactly as the
+ * reference writes it (neighborlist.cu:268-283; each operation rounded on its
+ * own, so the set is bit-identical to the O(N^2) kernel's); it is rebuilt when
+ * any atom moved >= skin/2 since the last build (neighborlist.cu:157-176).
+ * Unlike the reference the candidates come from the 27..125 cells around i
+ * (cells of side >= rl/2), the atoms are re-sorted along a Hilbert curve of
+ * cells at every build, and the rebuild decision never leaves the device.
+ */
+#include "md_internal.h"
+
+namespace {
+
+/* (x + L/2) / bin truncated and clamped: the binning rule of the reference's
+ * sketch (neighborlist_kernel_o.cu:20-25) with IEEE add and divide. */
+__device__ __forceinline__ int cell_of(float x, float box, float binlen, int nc)
+{
+    float s = __fdiv_rn(__fadd_rn(x, box / 2.0f), binlen);
+    int c = (s <= 0.0f) ? 0 : (int)s;
+    return c >= nc ? nc - 1 : c;
+}
+
+/* min-image r^2 with every operation rounded separately (no contraction). */
+__device__ __forceinline__ float rsq_exact(float4 a, float4 b, const md_kparams &kp)
+{
+    float dx = __fsub_rn(a.x, b.x);
+    float dy = __fsub_rn(a.y, b.y);
+    float dz = __fsub_rn(a.z, b.z);
+    dx = __fsub_rn(dx, __fmul_rn(kp.box[0], rintf(__fmul_rn(dx, kp.boxi[0]))));
+    dy = __fsub_rn(dy, __fmul_rn(kp.box[1], rintf(__fmul_rn(dy, kp.boxi[1]))));
+    dz = __fsub_rn(dz, __fmul_rn(kp.box[2], rintf(__fmul_rn(dz, kp.boxi[2]))));
+    return __fadd_rn(__fadd_rn(__fmul_rn(dx, dx), __fmul_rn(dy, dy)), __fmul_rn(dz, dz));
+}
+
+__global__ void k_check(md_kparams kp, const float4 *__restrict__ pos4,
+                        const float4 *__restrict__ pos_old, md_devstate *st)
+{
+    int i = blockIdx.x * blockDim.x + threadIdx.x;
+    if (i >= kp.n) return;
+    if (rsq_exact(pos4[i], pos_old[i], kp) >= kp.rmaxdif) st->update = 1;
+}
+
+/* Cell rank (Hilbert order) of every atom and the per-cell counts. */
+__global__ void k_cell_key(md_kparams kp, const md_devstate *st, int always,
+                           const float4 *__restrict__ pos4, const int *__restrict__ cell_rank,
+                           int *key, int *cell_count)
+{
+    if (!always && !st->update) return;
+    int i = blockIdx.x * blockDim.x + threadIdx.x;
+    if (i >= kp.n) return;
+    float4 p = pos4[i];
+    int cx = cell_of(p.x, kp.box[0], kp.binlen[0], kp.ncell[0]);
+    int cy = cell_of(p.y, kp.box[1], kp.binlen[1], kp.ncell[1]);
+    int cz = cell_of(p.z, kp.box[2], kp.binlen[2], kp.ncell[2]);
+    int r = cell_rank[cx + kp.ncell[0] * (cy + kp.ncell[1] * cz)];
+    key[i] = r;
+    atomicAdd(&cell_count[r], 1);
+}
+
+/* Exclusive scan of the cell counts (one block), then zero the counters for
+ * the next build.  cell_start has ncells + 1 entries. */
+__global__ void k_cell_scan(md_kparams kp, md_devstate *st, int always, int ncells,
+                            int *cell_count, int *cell_start, int *cell_fill)
+{
+    if (!always && !st->update) return;
+    __shared__ int part[1024];
+    int t = threadIdx.x, nt = blockDim.x;
+    int chunk = (ncells + nt - 1) / nt;
+    int b = t * chunk, e = min(ncells, b + chunk);
+    int s = 0;
+    for (int c = b; c < e; c++) s += cell_count[c];
+    part[t] = s;
+    __syncthreads();
+    for (int off = 1; off < nt; off <<= 1) {
+        int v = t >= off ? part[t - off] : 0;
+        __syncthreads();
+        part[t] += v;
+        __syncthreads();
+    }
+    int run = part[t] - s;
+    for (int c = b; c < e; c++) {
+        cell_start[c] = run;
+        run += cell_count[c];
+        cell_count[c] = 0;
+        cell_fill[c] = 0;
+    }
+    if (t == nt - 1) cell_start[ncells] = part[t];
+    if (t == 0) st->builds += 1;
+}
+
+__global__ void k_cell_scatter(md_kparams kp, const md_devstate *st, int always,
+                               const int *__restrict__ key, const int *__restrict__ cell_start,
+                               int *cell_fill, int *src)
+{
+    if (!always && !st->update) return;
+    int i = blockIdx.x * blockDim.x + threadIdx.x;
+    if (i >= kp.n) return;
+    int r = key[i];
+    src[cell_start[r] + atomicAdd(&cell_fill[r], 1)] = i;
+}
+
+/* Within each cell, order atoms by original index: the sorted order is then a
+ * function of the positions alone. */
+__global__ void k_cell_order(md_kparams kp, const md_devstate *st, int always, int ncells,
+                             const int *__restrict__ cell_start, const int *__restrict__ perm,
+                             int *src)
+{
+    if (!always && !st->update) return;
+    int c = blockIdx.x * blockDim.x + threadIdx.x;
+    if (c >= ncells) return;
+    int b = cell_start[c], e = cell_start[c + 1];
+    for (int k = b + 1; k < e; k++) {
+        int a = src[k], ka = perm[a];
+        int m = k - 1;
+        while (m >= b && perm[src[m]] > ka) {
+            src[m + 1] = src[m];
+            m--;
+        }
+        src[m + 1] = a;
+    }
+}
+
+__global__ void k_permute(md_kparams kp, const md_devstate *st, int always,
+                          const int *__restrict__ src, const double *__restrict__ x,
+                          const double *__restrict__ v, const double *__restrict__ mass,
+                          const float4 *__restrict__ pos4, const int *__restrict__ perm,
+                          const int *__restrict__ type, double *tmp_d, float4 *tmp4, int *tmp_i)
+{
+    if (!always && !st->update) return;
+    int s = blockIdx.x * blockDim.x + threadIdx.x;
+    if (s >= kp.n) return;
+    int o = src[s], P = kp.pitch;
+    for (int d = 0; d < 3; d++) {
+        tmp_d[d * P + s] = x[d * P + o];
+        tmp_d[(3 + d) * P + s] = v[d * P + o];
+    }
+    tmp_d[6 * P + s] = mass[o];
+    tmp4[s] = pos4[o];
+    tmp_i[s] = perm[o];
+    tmp_i[P + s] = type[o];
+}
+
+__global__ void k_copyback(md_kparams kp, const md_devstate *st, int always,
+                           const double *__restrict__ tmp_d, const float4 *__restrict__ tmp4,
+                           const int *__restrict__ tmp_i, double *x, double *v, double *mass,
+                           float4 *pos4, int *perm, int *iperm, int *type)
+{
+    if (!always && !st->update) return;
+    int s = blockIdx.x * blockDim.x + threadIdx.x;
+    if (s >= kp.n) return;
+    int P = kp.pitch;
+    for (int d = 0; d < 3; d++) {
+        x[d * P + s] = tmp_d[d * P + s];
+        v[d * P + s] = tmp_d[(3 + d) * P + s];
+    }
+    mass[s] = tmp_d[6 * P + s];
+    pos4[s] = tmp4[s];
+    int o = tmp_i[s];
+    perm[s] = o;
+    iperm[o] = s;
+    type[s] = tmp_i[P + s];
+}
+
+/* Exclusions and bonded lists re-expressed in the new sorted indices. */
+__global__ void k_remap(md_kparams kp, const md_devstate *st, int always,
+                        const int *__restrict__ perm, const int *__restrict__ iperm,
+                        const uint4 *__restrict__ excl_orig, uint4 *excl_s,
+                        const int2 *__restrict__ bl_o, const int *__restrict__ bl_on, int2 *bl_s,
+                        int *bl_sn, const int4 *__restrict__ al_o, const int *__restrict__ al_on,
+                        int4 *al_s, int *al_sn, int has_bonds, int has_angles)
+{
+    if (!always && !st->update) return;
+    int s = blockIdx.x * blockDim.x + threadIdx.x;
+    if (s >= kp.n) return;
+    int o = perm[s], P = kp.pitch;
+    uint4 e = excl_orig[o];
+    uint4 m;
+    m.x = e.x == MD_EXCL_NONE ? MD_EXCL_NONE : (unsigned)iperm[e.x];
+    m.y = e.y == MD_EXCL_NONE ? MD_EXCL_NONE : (unsigned)iperm[e.y];
+    m.z = e.z == MD_EXCL_NONE ? MD_EXCL_NONE : (unsigned)iperm[e.z];
+    m.w = e.w == MD_EXCL_NONE ? MD_EXCL_NONE : (unsigned)iperm[e.w];
+    excl_s[s] = m;
+    if (has_bonds) {
+        int nb = bl_on[o];
+        for (int k = 0; k < nb; k++) {
+            int2 b = bl_o[4 * o + k];
+            bl_s[k * P + s] = make_int2(iperm[b.x], b.y);
+        }
+        bl_sn[s] = nb;
+    }
+    if (has_angles) {
+        int na = al_on[o];
+        for (int k = 0; k < na; k++) {
+            int4 a = al_o[4 * o + k];
+            al_s[k * P + s] = make_int4(a.x, iperm[a.y], iperm[a.z], a.w);
+        }
+        al_sn[s] = na;
+    }
+}
+
+/* List build: TPA lanes per atom scan the stencil cells; lane l tests the
+ * candidates l, l+TPA, ... of each cell and the lanes append their hits in
+ * candidate order with a ballot, so the list order is fixed by the cell
+ * traversal order alone. */
+template <int TPA>
+__global__ void __launch_bounds__(256) k_build_list(
+    md_kparams kp, md_devstate *st, int always, const float4 *__restrict__ pos4,
+    const int *__restrict__ type, const uint4 *__restrict__ excl_s,
+    const int *__restrict__ cell_rank, const int *__restrict__ cell_start,
+    const unsigned *__restrict__ type_mask, unsigned *nl, int *nl_n, float4 *pos_old)
+{
+    if (!always && !st->update) return;
+    int gt = blockIdx.x * blockDim.x + threadIdx.x;
+    int i = gt / TPA, lane = gt % TPA;
+    int lane_w = threadIdx.x & 31;
+    unsigned gmask = (TPA == 32) ? 0xffffffffu : (((1u << TPA) - 1u) << (lane_w & ~(TPA - 1)));
+    bool active = i < kp.n;
+    int ii = active ? i : 0;
+    float4 p = pos4[ii];
+    int ti = type[ii];
+    uint4 ex = excl_s[ii];
+    unsigned tmask = type_mask[ti];
+    int c3[3];
+    c3[0] = cell_of(p.x, kp.box[0], kp.binlen[0], kp.ncell[0]);
+    c3[1] = cell_of(p.y, kp.box[1], kp.binlen[1], kp.ncell[1]);
+    c3[2] = cell_of(p.z, kp.box[2], kp.binlen[2], kp.ncell[2]);
+    int lo[3], hi[3];
+    for (int d = 0; d < 3; d++) {
+        if (kp.stencil[d] < 0) { lo[d] = 0; hi[d] = kp.ncell[d] - 1; }
+        else { lo[d] = c3[d] - kp.stencil[d]; hi[d] = c3[d] + kp.stencil[d]; }
+    }
+    int cnt = 0;
+    const int P = kp.pitch;
+    for (int zz = lo[2]; zz <= hi[2]; zz++) {
+        int cz = zz < 0 ? zz + kp.ncell[2] : (zz >= kp.ncell[2] ? zz - kp.ncell[2] : zz);
+        for (int yy = lo[1]; yy <= hi[1]; yy++) {
+            int cy = yy < 0 ? yy + kp.ncell[1] : (yy >= kp.ncell[1] ? yy - kp.ncell[1] : yy);
+            for (int xx = lo[0]; xx <= hi[0]; xx++) {
+                int cx = xx < 0 ? xx + kp.ncell[0] : (xx >= kp.ncell[0] ? xx - kp.ncell[0] : xx);
+                int r = cell_rank[cx + kp.ncell[0] * (cy + kp.ncell[1] * cz)];
+                int b = cell_start[r], e = cell_start[r + 1];
+                for (int j0 = b; j0 < e; j0 += TPA) {
+                    int j = j0 + lane;
+                    bool ok = false;
+                    unsigned entry = 0;
+                    if (active && j < e) {
+                        float4 q = pos4[j];
+                        unsigned uj = (unsigned)j;
+                        int tj = type[j];
+                        ok = rsq_exact(p, q, kp) < kp.rskinsq && j != i && uj != ex.x &&
+                             uj != ex.y && uj != ex.z && uj != ex.w && !((tmask >> tj) & 1u);
+                        entry = uj | ((unsigned)tj << MD_TYPE_SHIFT);
+                    }
+                    unsigned bal = __ballot_sync(gmask, ok);
+                    if (ok) {
+                        int slot = cnt + __popc(bal & ((1u << lane_w) - 1u));
+                        if (slot < kp.cap) nl[(size_t)slot * P + i] = entry;
+                    }
+                    cnt += __popc(bal);
+                }
+            }
+        }
+    }
+    if (active && lane == 0) {
+        nl_n[i] = cnt < kp.cap ? cnt : kp.cap;
+        pos_old[i] = p;
+        if (cnt > kp.cap) atomicMax(&st->list_overflow, cnt);
+    }
+}
+
+}  // namespace
+
+void launch_check(md_ctx *c, const md_kparams &kp)
+{
+    int nb = (kp.n + 255) / 256;
+    k_check<<<nb, 256, 0, c->stream>>>(kp, c->pos4, c->pos_old, c->st);
+}
+
+void launch_rebuild(md_ctx *c, const md_kparams &kp, bool unconditional)
+{
+    int always = unconditional ? 1 : 0;
+    int nb = (kp.n + 255) / 256;
+    cudaStream_t s = c->stream;
+    k_cell_key<<<nb, 256, 0, s>>>(kp, c->st, always, c->pos4, c->cell_rank, c->key, c->cell_count);
+    k_cell_scan<<<1, 1024, 0, s>>>(kp, c->st, always, c->ncells, c->cell_count, c->cell_start,
+                                   c->cell_fill);
+    k_cell_scatter<<<nb, 256, 0, s>>>(kp, c->st, always, c->key, c->cell_start, c->cell_fill, c->src);
+    k_cell_order<<<(c->ncells + 255) / 256, 256, 0, s>>>(kp, c->st, always, c->ncells,
+                                                          c->cell_start, c->perm, c->src);
+    k_permute<<<nb, 256, 0, s>>>(kp, c->st, always, c->src, c->x, c->v, c->mass, c->pos4, c->perm,
+                                 c->type, c->tmp_d, c->tmp4, c->tmp_i);
+    k_copyback<<<nb, 256, 0, s>>>(kp, c->st, always, c->tmp_d, c->tmp4, c->tmp_i, c->x, c->v,
+                                  c->mass, c->pos4, c->perm, c->iperm, c->type);
+    k_remap<<<nb, 256, 0, s>>>(kp, c->st, always, c->perm, c->iperm, c->excl_orig, c->excl_s,
+                               c->bl_o, c->bl_on, c->bl_s, c->bl_sn, c->al_o, c->al_on, c->al_s,
+                               c->al_sn, c->has_bonds, c->has_angles);
+    long long threads = (long long)kp.n * c->list_tpa;
+    int lb = (int)((threads + 255) / 256);
+    switch (c->list_tpa) {
+#define MD_LIST_CASE(T)                                                                            \
+    case T:                                                                                        \
+        k_build_list<T><<<lb, 256, 0, s>>>(kp, c->st, always, c->pos4, c->type, c->excl_s,         \
+                                           c->cell_rank, c->cell_start, c->type_mask_dev, c->nl,   \
+                                           c->nl_n, c->pos_old);                                   \
+        break;
+        MD_LIST_CASE(1)
+        MD_LIST_CASE(2)
+        MD_LIST_CASE(4)
+        MD_LIST_CASE(8)
+        MD_LIST_CASE(16)
+        MD_LIST_CASE(32)
+#undef MD_LIST_CASE
+    default:
+        break;
+    }
+}

@@ -1,0 +1,1007 @@
+/*
+ * md_api.cu -- host side of libmdgpu_gb300: input parsing, context set-up,
+ * the CUDA-graph step driver and the C ABI declared in include/md_gpu.h.
+ *
+ * Reference counterparts: SimulationInit / FFieldInput / ConfigInput
+ * (simulation.cu:40-316), config_init (config.cu:22-40), forces_init
+ * (forces.cu:75-186), neighborlist_init (neighborlist.cu:30-107),
+ * integrate_init (integrator.cu:47-97) and the step loop of
+ * SimulationRun_CUDA (runGPU.cu:69-104).
+ */
+#include <math.h>
+#include <stdio.h>
+#include <stdlib.h>
+#include <string.h>
+
+#include <algorithm>
+#include <new>
+#include <string>
+#include <vector>
+
+#include "md_internal.h"
+
+namespace {
+
+std::string g_last_error;
+
+/* ---------------- input files (own restatement of simulation.cu) ---------------- */
+
+struct parsed_run {
+    md_system_desc d;
+    std::vector<int> itype, bonds, angles;
+    std::vector<float> charge, pos, vel, mass, lj1, lj2, bnd1, bnd2, ang1, ang2;
+    int timprn = 1;
+    float rdel = 0.02f;
+};
+
+/* .inp (simulation.cu:58-105): label tokens skipped; reacf and alfa derived
+ * with the reference's float/double mix; extension lines after rdel. */
+md_status parse_inp(const char *path, parsed_run &r)
+{
+    FILE *fin = fopen(path, "r");
+    if (!fin) return MD_ERR_IO;
+    char lab[256], ens[64];
+    md_system_desc &d = r.d;
+    int timeq, timrun;
+    float rc;
+    md_status st = MD_ERR_PARSE;
+    d.tau_t = 100.0f;
+    d.integrator = MD_LEAPFROG;
+    if (fscanf(fin, "%255s %63s", lab, ens) != 2) goto out;
+    d.enstype = 0;
+    if (!strcmp(ens, "nvt")) {
+        d.enstype = 1;
+        if (fscanf(fin, "%255s %f", lab, &d.temper_0) != 2) goto out;
+    } else if (!strcmp(ens, "npt")) {
+        st = MD_ERR_UNSUPPORTED;
+        goto out;
+    }
+    if (fscanf(fin, "%255s %d %d %d %f", lab, &timeq, &timrun, &r.timprn, &d.dt) != 5) goto out;
+    if (fscanf(fin, "%255s %f %d", lab, &rc, &d.lkspace) != 3) goto out;
+    if (d.lkspace == 0) {
+        float eps;
+        if (fscanf(fin, "%255s %f", lab, &eps) != 2) goto out;
+        float num = 2.0f * (eps - 1.0f) / (2.0f * eps + 1.0f);
+        d.reacf = (float)((double)num / pow((double)rc, 3.0));
+    } else if (d.lkspace == 1) {
+        if (fscanf(fin, "%255s %f", lab, &d.alfa) != 2) goto out;
+    } else {
+        int kmax;
+        if (fscanf(fin, "%255s %d", lab, &kmax) != 2) goto out;
+        d.alfa = (float)(3.09 / (double)rc);
+    }
+    d.rcutsq = rc * rc;
+    if (fscanf(fin, "%255s %f %d", lab, &d.skin, &d.nmaxlist) != 3) goto out;
+    if (fscanf(fin, "%255s %f", lab, &r.rdel) != 2) goto out;
+    {
+        char val[64];
+        while (fscanf(fin, "%255s %63s", lab, val) == 2) {
+            if (!strcmp(lab, "tau_t:")) d.tau_t = strtof(val, nullptr);
+            else if (!strcmp(lab, "integrator:"))
+                d.integrator = !strcmp(val, "vv") ? MD_VV : (!strcmp(val, "nh") ? MD_NH : MD_LEAPFROG);
+        }
+    }
+    st = MD_OK;
+out:
+    fclose(fin);
+    return st;
+}
+
+/* .fld (simulation.cu:144-264). */
+md_status parse_fld(const char *path, parsed_run &r)
+{
+    FILE *fin = fopen(path, "r");
+    if (!fin) return MD_ERR_IO;
+    char lab[256], name[64], form[64];
+    int ntype, iaux, cnt, nvdw, i, j;
+    float a, b;
+    md_status st = MD_ERR_PARSE;
+    if (fscanf(fin, "%255s %d", lab, &ntype) != 2 || ntype < 1 || ntype > MD_MAXTYPE) goto out;
+    r.mass.assign(ntype, 0.0f);
+    r.lj1.assign(ntype * ntype, 0.0f);
+    r.lj2.assign(ntype * ntype, 0.0f);
+    for (int t = 0; t < ntype; t++) {
+        float m, q;
+        if (fscanf(fin, "%d %d", &iaux, &cnt) != 2) goto out;
+        if (fscanf(fin, "%63s %f %f", name, &m, &q) != 3) goto out;
+        r.mass[t] = (float)((double)m * 10000.0);
+    }
+    if (fscanf(fin, "%255s %d", lab, &nvdw) != 2) goto out;
+    for (int t = 0; t < nvdw; t++) {
+        if (fscanf(fin, "%d %d %63s %f %f", &i, &j, form, &a, &b) != 5) goto out;
+        i--; j--;
+        if (i < 0 || j < 0 || i >= ntype || j >= ntype) goto out;
+        float l1, l2;
+        if (!strcmp(form, "LJ")) {
+            l1 = (float)((double)(12.0f * 4.0f * b) * pow((double)a, 12.0));
+            l2 = (float)((double)(6.0f * 4.0f * b) * pow((double)a, 6.0));
+        } else if (!strcmp(form, "12-6")) {
+            l1 = 12.0f * a;
+            l2 = 6.0f * b;
+        } else {
+            continue;
+        }
+        r.lj1[i * ntype + j] = r.lj1[j * ntype + i] = l1;
+        r.lj2[i * ntype + j] = r.lj2[j * ntype + i] = l2;
+    }
+    int tb, ta, nb, na;
+    if (fscanf(fin, "%255s %d", lab, &tb) != 2 || tb < 0 || tb > MD_MAXTYPE) goto out;
+    r.bnd1.assign(MD_MAXTYPE, 0.0f);
+    r.bnd2.assign(MD_MAXTYPE, 0.0f);
+    for (int t = 0; t < tb; t++) {
+        if (fscanf(fin, "%d %f %f", &iaux, &r.bnd1[t], &r.bnd2[t]) != 3) goto out;
+        r.bnd1[t] *= 2.0f;
+    }
+    if (fscanf(fin, "%255s %d", lab, &ta) != 2 || ta < 0 || ta > MD_MAXTYPE) goto out;
+    r.ang1.assign(MD_MAXTYPE, 0.0f);
+    r.ang2.assign(MD_MAXTYPE, 0.0f);
+    for (int t = 0; t < ta; t++) {
+        if (fscanf(fin, "%d %f %f", &iaux, &r.ang1[t], &r.ang2[t]) != 3) goto out;
+        r.ang1[t] *= 2.0f;
+        r.ang2[t] *= 3.1415927f / 180.0f;
+    }
+    if (fscanf(fin, "%255s %d", lab, &nb) != 2 || nb < 0) goto out;
+    r.bonds.resize(3 * (size_t)nb);
+    for (int t = 0; t < nb; t++) {
+        int ty, bi, bj;
+        if (fscanf(fin, "%d %d %d %d", &iaux, &ty, &bi, &bj) != 4) goto out;
+        r.bonds[3 * t] = ty - 1; r.bonds[3 * t + 1] = bi - 1; r.bonds[3 * t + 2] = bj - 1;
+    }
+    if (fscanf(fin, "%255s %d", lab, &na) != 2 || na < 0) goto out;
+    r.angles.resize(4 * (size_t)na);
+    for (int t = 0; t < na; t++) {
+        int ty, ai, aj, ak;
+        if (fscanf(fin, "%d %d %d %d %d", &iaux, &ty, &ai, &aj, &ak) != 5) goto out;
+        r.angles[4 * t] = ty - 1; r.angles[4 * t + 1] = ai - 1;
+        r.angles[4 * t + 2] = aj - 1; r.angles[4 * t + 3] = ak - 1;
+    }
+    r.d.ntype = ntype;
+    r.d.nbonds = nb;
+    r.d.nangle = na;
+    st = MD_OK;
+out:
+    fclose(fin);
+    return st;
+}
+
+/* .cfg (simulation.cu:278-316). */
+md_status parse_cfg(const char *path, parsed_run &r)
+{
+    FILE *fin = fopen(path, "r");
+    if (!fin) return MD_ERR_IO;
+    int n, cftyp, iaux;
+    md_status st = MD_ERR_PARSE;
+    if (fscanf(fin, "%d %d", &n, &cftyp) != 2 || n <= 0) goto out;
+    if (fscanf(fin, "%f %f %f", &r.d.box[0], &r.d.box[1], &r.d.box[2]) != 3) goto out;
+    r.itype.resize(n);
+    r.charge.resize(n);
+    r.pos.assign(3 * (size_t)n, 0.0f);
+    r.vel.assign(3 * (size_t)n, 0.0f);
+    for (int i = 0; i < n; i++) {
+        if (fscanf(fin, "%d %d %f", &iaux, &r.itype[i], &r.charge[i]) != 3) goto out;
+        r.itype[i] -= 1;
+        if (fscanf(fin, "%f %f %f", &r.pos[3 * i], &r.pos[3 * i + 1], &r.pos[3 * i + 2]) != 3) goto out;
+        if (cftyp > 0)
+            if (fscanf(fin, "%f %f %f", &r.vel[3 * i], &r.vel[3 * i + 1], &r.vel[3 * i + 2]) != 3) goto out;
+    }
+    r.d.natom = n;
+    st = MD_OK;
+out:
+    fclose(fin);
+    return st;
+}
+
+/* ---------------- derived constants ---------------- */
+
+/* forces.cu:97-110 (C++: sqrt of a float is the float overload). */
+void wolf_consts(float alfa, float rcutsq, float out[4])
+{
+    const float P = 0.3275911f, A1 = 0.254829592f, A2 = -0.284496736f, A3 = 1.421413741f,
+                A4 = -1.453152027f, A5 = 1.061405429f;
+    float palfa = alfa * P;
+    float spiialfa = 2.0f / sqrtf(3.1415927f) * alfa;
+    float alfasq = -alfa * alfa / logf(2.0f);
+    float ff = 1.0f / (1.0f + palfa * sqrtf(rcutsq));
+    float wolf = spiialfa * sqrtf(rcutsq) + ((((A5 * ff + A4) * ff + A3) * ff + A2) * ff + A1) * ff;
+    wolf *= exp2f(alfasq * rcutsq) / sqrtf(rcutsq);
+    out[0] = palfa; out[1] = spiialfa; out[2] = alfasq; out[3] = wolf;
+}
+
+/* 3-D Hilbert index (Skilling, AIP Conf. Proc. 707 (2004) 381). */
+unsigned long long hilbert3(unsigned x, unsigned y, unsigned z, int bits)
+{
+    unsigned X[3] = {x, y, z};
+    unsigned M = 1u << (bits - 1), P, Q, t;
+    for (Q = M; Q > 1; Q >>= 1) {
+        P = Q - 1;
+        for (int i = 0; i < 3; i++) {
+            if (X[i] & Q) X[0] ^= P;
+            else { t = (X[0] ^ X[i]) & P; X[0] ^= t; X[i] ^= t; }
+        }
+    }
+    for (int i = 1; i < 3; i++) X[i] ^= X[i - 1];
+    t = 0;
+    for (Q = M; Q > 1; Q >>= 1)
+        if (X[2] & Q) t ^= Q - 1;
+    for (int i = 0; i < 3; i++) X[i] ^= t;
+    unsigned long long h = 0;
+    for (int b = bits - 1; b >= 0; b--)
+        for (int i = 0; i < 3; i++) h = (h << 1) | ((X[i] >> b) & 1u);
+    return h;
+}
+
+template <class T>
+cudaError_t dalloc(T **p, size_t count)
+{
+    return cudaMalloc((void **)p, sizeof(T) * (count > 0 ? count : 1));
+}
+
+md_status fail(md_ctx *c, md_status s, const std::string &msg)
+{
+    if (c) c->last_error = msg;
+    g_last_error = msg;
+    return s;
+}
+
+void free_device(md_ctx *c)
+{
+    void *ptrs[] = {c->x, c->v, c->mass, c->pos4, c->pos_old, c->type, c->perm, c->iperm, c->f,
+                    c->vir, c->epot, c->nl, c->nl_n, c->excl_orig, c->excl_s, c->cell_rank,
+                    c->cell_count, c->cell_start, c->cell_fill, c->key, c->src, c->tmp_d, c->tmp4,
+                    c->tmp_i, c->bl_o, c->bl_on, c->al_o, c->al_on, c->bl_s, c->bl_sn, c->al_s,
+                    c->al_sn, c->partials, c->st, c->rec, c->lj_dev, c->bonded_par,
+                    c->type_mask_dev, c->io_dev};
+    for (void *p : ptrs)
+        if (p) cudaFree(p);
+}
+
+md_status check_overflow_and_sync(md_ctx *c)
+{
+    MD_CUDA_TRY(c, cudaStreamSynchronize(c->stream));
+    md_devstate h;
+    MD_CUDA_TRY(c, cudaMemcpy(&h, c->st, sizeof(h), cudaMemcpyDeviceToHost));
+    if (h.list_overflow > 0)
+        return fail(c, MD_ERR_LIST_OVERFLOW,
+                    "neighbour list overflow: " + std::to_string(h.list_overflow) + " > capacity " +
+                        std::to_string(c->cap));
+    return MD_OK;
+}
+
+md_status alloc_list(md_ctx *c, int cap)
+{
+    if (c->nl) cudaFree(c->nl);
+    c->nl = nullptr;
+    c->cap = cap;
+    MD_CUDA_TRY(c, dalloc(&c->nl, (size_t)cap * c->pitch));
+    return MD_OK;
+}
+
+/* Record (or launch eagerly) the kernels of `nsteps` steps. */
+void enqueue_steps(md_ctx *c, int nsteps, int energy_first)
+{
+    md_kparams kp = md_make_kparams(c);
+    for (int k = 0; k < nsteps; k++) {
+        int energy = (energy_first && k == 0) ? 1 : 0;
+        if (c->integrator == MD_LEAPFROG) {
+            cudaMemsetAsync(&c->st->update, 0, sizeof(int), c->stream);
+            launch_check(c, kp);
+            launch_rebuild(c, kp, false);
+            launch_forces(c, kp, energy != 0, MD_TERM_ALL);
+            launch_leapfrog(c, kp, energy);
+        } else {
+            launch_vv_first(c, kp);
+            cudaMemsetAsync(&c->st->update, 0, sizeof(int), c->stream);
+            launch_check(c, kp);
+            launch_rebuild(c, kp, false);
+            launch_forces(c, kp, energy != 0, MD_TERM_ALL);
+            launch_vv_second(c, kp, energy);
+        }
+    }
+}
+
+md_status capture_graph(md_ctx *c, int nsteps, int energy_first)
+{
+    if (c->gexec) {
+        cudaGraphExecDestroy(c->gexec);
+        c->gexec = nullptr;
+    }
+    cudaGraph_t g = nullptr;
+    MD_CUDA_TRY(c, cudaStreamBeginCapture(c->stream, cudaStreamCaptureModeThreadLocal));
+    enqueue_steps(c, nsteps, energy_first);
+    cudaError_t e = cudaStreamEndCapture(c->stream, &g);
+    if (e != cudaSuccess) return fail(c, MD_ERR_CUDA, std::string("graph capture: ") + cudaGetErrorString(e));
+    e = cudaGraphInstantiate(&c->gexec, g, 0);
+    cudaGraphDestroy(g);
+    if (e != cudaSuccess) return fail(c, MD_ERR_CUDA, std::string("graph instantiate: ") + cudaGetErrorString(e));
+    c->gsteps = nsteps;
+    c->genergy = energy_first;
+    return MD_OK;
+}
+
+md_status initial_build(md_ctx *c)
+{
+    md_kparams kp = md_make_kparams(c);
+    launch_rebuild(c, kp, true);
+    md_status s = check_overflow_and_sync(c);
+    if (s == MD_ERR_LIST_OVERFLOW) {
+        md_devstate h;
+        MD_CUDA_TRY(c, cudaMemcpy(&h, c->st, sizeof(h), cudaMemcpyDeviceToHost));
+        int cap = ((h.list_overflow * 5 / 4 + 16) + 31) / 32 * 32;
+        md_status a = alloc_list(c, cap);
+        if (a != MD_OK) return a;
+        int zero = 0;
+        MD_CUDA_TRY(c, cudaMemcpy(&c->st->list_overflow, &zero, sizeof(int), cudaMemcpyHostToDevice));
+        kp = md_make_kparams(c);
+        launch_rebuild(c, kp, true);
+        s = check_overflow_and_sync(c);
+    }
+    return s;
+}
+
+/* Forces (and KE/T) of the current state, so VV can start and records exist. */
+md_status refresh_state(md_ctx *c)
+{
+    md_kparams kp = md_make_kparams(c);
+    launch_forces(c, kp, true, MD_TERM_ALL);
+    launch_thermo_from_state(c, kp, 1);
+    return check_overflow_and_sync(c);
+}
+
+}  // namespace
+
+md_kparams md_make_kparams(const md_ctx *c)
+{
+    md_kparams kp;
+    memset(&kp, 0, sizeof(kp));
+    kp.n = c->n;
+    kp.pitch = c->pitch;
+    kp.cap = c->cap;
+    kp.ntype = c->ntype;
+    for (int d = 0; d < 3; d++) {
+        kp.box[d] = c->box[d];
+        kp.boxi[d] = c->boxi[d];
+        kp.boxd[d] = (double)c->box[d];
+        kp.ncell[d] = c->ncell[d];
+        kp.binlen[d] = c->binlen[d];
+        kp.stencil[d] = c->stencil[d];
+    }
+    kp.rcutsq = c->rcutsq;
+    kp.reacf = c->reacf;
+    kp.rskinsq = c->rskinsq;
+    kp.rmaxdif = c->rmaxdif;
+    kp.palfa = c->wc[0];
+    kp.spiialfa = c->wc[1];
+    kp.alfasq = c->wc[2];
+    kp.wolf = c->wc[3];
+    kp.lkspace = c->lkspace;
+    kp.dt = c->dt;
+    return kp;
+}
+
+extern "C" {
+
+const char *md_status_string(md_status s)
+{
+    switch (s) {
+    case MD_OK: return "ok";
+    case MD_ERR_ARG: return "invalid argument";
+    case MD_ERR_IO: return "cannot open file";
+    case MD_ERR_PARSE: return "input does not follow the .inp/.fld/.cfg grammar";
+    case MD_ERR_CUDA: return "CUDA error";
+    case MD_ERR_LIST_OVERFLOW: return "neighbour list overflow";
+    case MD_ERR_BONDED: return "more than four bonds or angles on an atom";
+    case MD_ERR_UNSUPPORTED: return "unsupported option";
+    case MD_ERR_BOX: return "cutoff plus skin exceeds half the box";
+    }
+    return "unknown status";
+}
+
+md_status md_last_error(const md_ctx *ctx, char *buf, int len)
+{
+    if (!buf || len <= 0) return MD_ERR_ARG;
+    const std::string &m = ctx ? ctx->last_error : g_last_error;
+    snprintf(buf, (size_t)len, "%s", m.c_str());
+    return MD_OK;
+}
+
+md_status md_create(const md_system_desc *d, void *stream, md_ctx **out)
+{
+    if (!d || !out || d->natom <= 0 || d->ntype < 1 || d->ntype > MD_MAXTYPE || !d->itype ||
+        !d->charge || !d->pos || !d->type_mass || !d->lj1 || !d->lj2)
+        return fail(nullptr, MD_ERR_ARG, "md_create: missing or invalid descriptor fields");
+    if (d->nbonds > 0 && (!d->bonds || !d->bnd1 || !d->bnd2))
+        return fail(nullptr, MD_ERR_ARG, "md_create: bonds without tables");
+    if (d->nangle > 0 && (!d->angles || !d->ang1 || !d->ang2))
+        return fail(nullptr, MD_ERR_ARG, "md_create: angles without tables");
+    if (d->lkspace < 0 || d->lkspace > 2 || d->rcutsq <= 0 || d->skin < 0 || d->dt <= 0 ||
+        d->integrator < 0 || d->integrator > 2 || d->enstype < 0 || d->enstype > 1)
+        return fail(nullptr, MD_ERR_ARG, "md_create: invalid run parameters");
+    md_ctx *c = new (std::nothrow) md_ctx();
+    if (!c) return fail(nullptr, MD_ERR_ARG, "out of host memory");
+    const int n = d->natom;
+    c->n = n;
+    c->ntype = d->ntype;
+    c->pitch = ((n + 255) / 256) * 256;
+    for (int k = 0; k < 3; k++) {
+        c->box[k] = d->box[k];
+        c->boxi[k] = (float)(1.0 / (double)d->box[k]);   /* simulation.cu:290-292 */
+    }
+    c->lkspace = d->lkspace;
+    c->rcutsq = d->rcutsq;
+    c->reacf = d->lkspace == 0 ? d->reacf : 0.0f;
+    c->alfa = d->alfa;
+    c->skin = d->skin;
+    c->nmaxlist = d->nmaxlist > 0 ? d->nmaxlist : 64;
+    c->enstype = d->enstype;
+    c->temper_0 = d->temper_0;
+    c->dt = d->dt;
+    c->tau_t = d->tau_t > 0 ? d->tau_t : 100.0f;
+    c->integrator = d->integrator;
+    if (c->lkspace > 0) wolf_consts(c->alfa, c->rcutsq, c->wc);
+    if (c->lkspace != 1) c->wc[3] = 0.0f;
+    c->rskinsq = (float)pow((double)(c->skin + sqrtf(c->rcutsq)), 2.0);   /* neighborlist.cu:35 */
+    c->rmaxdif = c->skin * c->skin / 4.0f;                                /* neighborlist.cu:36 */
+    float rl = sqrtf(c->rcutsq) + c->skin;
+    for (int k = 0; k < 3; k++)
+        if (2.0f * rl > c->box[k]) {
+            md_status s = fail(c, MD_ERR_BOX, "cutoff + skin exceeds half the box");
+            delete c;
+            return s;
+        }
+    memset(c->lj1, 0, sizeof(c->lj1));
+    memset(c->lj2, 0, sizeof(c->lj2));
+    for (int k = 0; k < d->ntype * d->ntype; k++) {
+        c->lj1[k] = d->lj1[k];
+        c->lj2[k] = d->lj2[k];
+    }
+    for (int k = 0; k < MD_MAXTYPE; k++) {
+        c->bnd1[k] = d->bnd1 && d->nbonds > 0 ? d->bnd1[k] : 0.0f;
+        c->bnd2[k] = d->bnd2 && d->nbonds > 0 ? d->bnd2[k] : 0.0f;
+        c->ang1[k] = d->ang1 && d->nangle > 0 ? d->ang1[k] : 0.0f;
+        c->ang2[k] = d->ang2 && d->nangle > 0 ? d->ang2[k] : 0.0f;
+        c->type_mass[k] = k < d->ntype ? d->type_mass[k] : 0.0f;
+    }
+    c->itype.assign(d->itype, d->itype + n);
+    c->charge.assign(d->charge, d->charge + n);
+    for (int i = 0; i < n; i++)
+        if (c->itype[i] < 0 || c->itype[i] >= d->ntype) {
+            md_status s = fail(c, MD_ERR_ARG, "atom type out of range");
+            delete c;
+            return s;
+        }
+    if (d->nbonds > 0) c->bonds.assign(d->bonds, d->bonds + 3 * (size_t)d->nbonds);
+    if (d->nangle > 0) c->angles.assign(d->angles, d->angles + 4 * (size_t)d->nangle);
+
+    /* exclusions with the reference's slot rule (neighborlist.cu:64-97) */
+    c->excl_host.assign(4 * (size_t)n, MD_EXCL_NONE);
+    for (size_t b = 0; b < c->bonds.size() / 3; b++) {
+        unsigned i = (unsigned)c->bonds[3 * b + 1], j = (unsigned)c->bonds[3 * b + 2];
+        if (i >= (unsigned)n || j >= (unsigned)n) {
+            md_status s = fail(c, MD_ERR_ARG, "bond atom out of range");
+            delete c;
+            return s;
+        }
+        unsigned *ei = &c->excl_host[4 * i], *ej = &c->excl_host[4 * j];
+        auto empty = [](unsigned v) { return v == MD_EXCL_NONE; };
+        if (empty(ei[0])) ei[0] = j;
+        else if (empty(ei[1])) ei[1] = j;
+        else if (empty(ei[2])) ei[2] = j;
+        else if (empty(ei[3])) ei[3] = j;
+        if (empty(ej[0])) ej[0] = i;
+        else if (empty(ei[1])) ej[1] = i;
+        else if (empty(ei[2])) ej[2] = i;
+        else if (empty(ei[3])) ej[3] = i;
+    }
+    /* original-space bonded lists (forces.cu:118-173), at most four per atom */
+    std::vector<int2> blo(4 * (size_t)n);
+    std::vector<int> blon(n, 0);
+    std::vector<int4> alo(4 * (size_t)n);
+    std::vector<int> alon(n, 0);
+    for (size_t b = 0; b < c->bonds.size() / 3; b++) {
+        int t = c->bonds[3 * b], i = c->bonds[3 * b + 1], j = c->bonds[3 * b + 2];
+        if (blon[i] >= 4 || blon[j] >= 4) {
+            md_status s = fail(c, MD_ERR_BONDED, "more than four bonds on an atom");
+            delete c;
+            return s;
+        }
+        blo[4 * i + blon[i]++] = make_int2(j, t);
+        blo[4 * j + blon[j]++] = make_int2(i, t);
+    }
+    for (size_t a = 0; a < c->angles.size() / 4; a++) {
+        int t = c->angles[4 * a], i = c->angles[4 * a + 1], j = c->angles[4 * a + 2],
+            k = c->angles[4 * a + 3];
+        if (i < 0 || j < 0 || k < 0 || i >= n || j >= n || k >= n || alon[i] >= 4 || alon[j] >= 4 ||
+            alon[k] >= 4) {
+            md_status s = fail(c, MD_ERR_BONDED, "more than four angles on an atom (or bad index)");
+            delete c;
+            return s;
+        }
+        alo[4 * i + alon[i]++] = make_int4(0, j, k, t);
+        alo[4 * j + alon[j]++] = make_int4(1, i, k, t);
+        alo[4 * k + alon[k]++] = make_int4(0, j, i, t);
+    }
+    c->has_bonds = c->bonds.empty() ? 0 : 1;
+    c->has_angles = c->angles.empty() ? 0 : 1;
+
+    /* cells of side >= rl/2 and their Hilbert ranks */
+    int bits = 1;
+    for (int k = 0; k < 3; k++) {
+        int nc = (int)floorf(c->box[k] / (0.5f * rl * 1.0001f));
+        nc = std::max(1, std::min(nc, 1024));
+        c->ncell[k] = nc;
+        c->binlen[k] = c->box[k] / (float)nc;
+        int sten = (int)ceilf(rl / c->binlen[k]);
+        c->stencil[k] = (2 * sten + 1 >= nc) ? -1 : sten;
+        while ((1 << bits) < nc) bits++;
+    }
+    c->ncells = c->ncell[0] * c->ncell[1] * c->ncell[2];
+    std::vector<std::pair<unsigned long long, int>> hk(c->ncells);
+    for (int z = 0; z < c->ncell[2]; z++)
+        for (int y = 0; y < c->ncell[1]; y++)
+            for (int x = 0; x < c->ncell[0]; x++) {
+                int lin = x + c->ncell[0] * (y + c->ncell[1] * z);
+                hk[lin] = std::make_pair(hilbert3(x, y, z, bits), lin);
+            }
+    std::sort(hk.begin(), hk.end());
+    std::vector<int> rank(c->ncells);
+    for (int r = 0; r < c->ncells; r++) rank[hk[r].second] = r;
+
+    /* device memory */
+    if (stream) {
+        c->stream = (cudaStream_t)stream;
+    } else {
+        if (cudaStreamCreateWithFlags(&c->stream, cudaStreamNonBlocking) != cudaSuccess) {
+            md_status s = fail(c, MD_ERR_CUDA, "stream creation failed");
+            delete c;
+            return s;
+        }
+        c->own_stream = true;
+    }
+    cudaGetDevice(&c->device);
+    const size_t P = c->pitch;
+    cudaError_t e = cudaSuccess;
+#define MD_ALLOC(ptr, cnt) if (e == cudaSuccess) e = dalloc(&(ptr), (cnt))
+    MD_ALLOC(c->x, 3 * P); MD_ALLOC(c->v, 3 * P); MD_ALLOC(c->mass, P);
+    MD_ALLOC(c->pos4, P); MD_ALLOC(c->pos_old, P);
+    MD_ALLOC(c->type, P); MD_ALLOC(c->perm, P); MD_ALLOC(c->iperm, P);
+    MD_ALLOC(c->f, 3 * P); MD_ALLOC(c->vir, P); MD_ALLOC(c->epot, P);
+    MD_ALLOC(c->nl_n, P);
+    MD_ALLOC(c->excl_orig, P); MD_ALLOC(c->excl_s, P);
+    MD_ALLOC(c->cell_rank, c->ncells); MD_ALLOC(c->cell_count, c->ncells);
+    MD_ALLOC(c->cell_start, c->ncells + 1); MD_ALLOC(c->cell_fill, c->ncells);
+    MD_ALLOC(c->key, P); MD_ALLOC(c->src, P);
+    MD_ALLOC(c->tmp_d, 7 * P); MD_ALLOC(c->tmp4, P); MD_ALLOC(c->tmp_i, 3 * P);
+    MD_ALLOC(c->bl_o, 4 * P); MD_ALLOC(c->bl_on, P); MD_ALLOC(c->al_o, 4 * P); MD_ALLOC(c->al_on, P);
+    MD_ALLOC(c->bl_s, 4 * P); MD_ALLOC(c->bl_sn, P); MD_ALLOC(c->al_s, 4 * P); MD_ALLOC(c->al_sn, P);
+    c->npart = (int)(P / 256);
+    MD_ALLOC(c->partials, 3 * (size_t)c->npart + 8);
+    MD_ALLOC(c->st, 1);
+    c->rec_cap = 4096;
+    MD_ALLOC(c->rec, c->rec_cap);
+    MD_ALLOC(c->lj_dev, 2 * MD_MAXTYPE * MD_MAXTYPE);
+    MD_ALLOC(c->bonded_par, 4 * MD_MAXTYPE);
+    MD_ALLOC(c->type_mask_dev, MD_MAXTYPE);
+    MD_ALLOC(c->io_dev, 4 * P);
+#undef MD_ALLOC
+    if (e != cudaSuccess) {
+        md_status s = fail(c, MD_ERR_CUDA, std::string("device allocation: ") + cudaGetErrorString(e));
+        free_device(c);
+        if (c->own_stream) cudaStreamDestroy(c->stream);
+        delete c;
+        return s;
+    }
+    cudaEventCreate(&c->ev0);
+    cudaEventCreate(&c->ev1);
+    /* host staging in sorted order = original order before the first build */
+    std::vector<double> hx(3 * P, 0.0), hv(3 * P, 0.0), hm(P, 1.0);
+    std::vector<float4> hp(P, make_float4(0, 0, 0, 0));
+    std::vector<int> ht(P, 0), hperm(P), hiperm(P);
+    std::vector<uint4> hex(P, make_uint4(MD_EXCL_NONE, MD_EXCL_NONE, MD_EXCL_NONE, MD_EXCL_NONE));
+    for (int i = 0; i < n; i++) {
+        for (int k = 0; k < 3; k++) {
+            hx[k * P + i] = d->pos[3 * i + k];
+            hv[k * P + i] = d->vel ? d->vel[3 * i + k] : 0.0;
+        }
+        hm[i] = c->type_mass[c->itype[i]];
+        hp[i] = make_float4(d->pos[3 * i], d->pos[3 * i + 1], d->pos[3 * i + 2], c->charge[i]);
+        ht[i] = c->itype[i];
+        hex[i] = make_uint4(c->excl_host[4 * i], c->excl_host[4 * i + 1], c->excl_host[4 * i + 2],
+                            c->excl_host[4 * i + 3]);
+    }
+    for (size_t i = 0; i < P; i++) { hperm[i] = (int)i; hiperm[i] = (int)i; }
+    std::vector<float> ljh(2 * MD_MAXTYPE * MD_MAXTYPE, 0.0f);
+    for (int a = 0; a < c->ntype; a++)
+        for (int b = 0; b < c->ntype; b++) {
+            ljh[2 * (a * MD_MAXTYPE + b)] = c->lj1[a * c->ntype + b];
+            ljh[2 * (a * MD_MAXTYPE + b) + 1] = c->lj2[a * c->ntype + b];
+        }
+    std::vector<float> bp(4 * MD_MAXTYPE);
+    for (int k = 0; k < MD_MAXTYPE; k++) {
+        bp[k] = c->bnd1[k]; bp[MD_MAXTYPE + k] = c->bnd2[k];
+        bp[2 * MD_MAXTYPE + k] = c->ang1[k]; bp[3 * MD_MAXTYPE + k] = c->ang2[k];
+    }
+    md_devstate hs;
+    memset(&hs, 0, sizeof(hs));
+    hs.temper = c->temper_0;   /* integrator.cu:77 */
+    hs.vscale = 1.0;
+    hs.lambda = 1.0;
+    std::vector<int> zeros(c->ncells, 0);
+    auto up = [&](void *dst, const void *srcp, size_t bytes) {
+        if (e == cudaSuccess) e = cudaMemcpy(dst, srcp, bytes, cudaMemcpyHostToDevice);
+    };
+    up(c->x, hx.data(), sizeof(double) * 3 * P);
+    up(c->v, hv.data(), sizeof(double) * 3 * P);
+    up(c->mass, hm.data(), sizeof(double) * P);
+    up(c->pos4, hp.data(), sizeof(float4) * P);
+    up(c->type, ht.data(), sizeof(int) * P);
+    up(c->perm, hperm.data(), sizeof(int) * P);
+    up(c->iperm, hiperm.data(), sizeof(int) * P);
+    up(c->excl_orig, hex.data(), sizeof(uint4) * P);
+    up(c->cell_rank, rank.data(), sizeof(int) * c->ncells);
+    up(c->cell_count, zeros.data(), sizeof(int) * c->ncells);
+    up(c->cell_fill, zeros.data(), sizeof(int) * c->ncells);
+    up(c->bl_o, blo.data(), sizeof(int2) * 4 * n);
+    up(c->bl_on, blon.data(), sizeof(int) * n);
+    up(c->al_o, alo.data(), sizeof(int4) * 4 * n);
+    up(c->al_on, alon.data(), sizeof(int) * n);
+    up(c->lj_dev, ljh.data(), sizeof(float) * ljh.size());
+    up(c->bonded_par, bp.data(), sizeof(float) * bp.size());
+    up(c->type_mask_dev, c->type_excl_mask, sizeof(unsigned) * MD_MAXTYPE);
+    up(c->st, &hs, sizeof(hs));
+    if (e == cudaSuccess) e = cudaMemset(c->f, 0, sizeof(long long) * 3 * P);
+    if (e == cudaSuccess) e = cudaMemset(c->vir, 0, sizeof(float) * P);
+    if (e == cudaSuccess) e = cudaMemset(c->epot, 0, sizeof(float) * P);
+    if (e == cudaSuccess) e = cudaMemset(c->bl_sn, 0, sizeof(int) * P);
+    if (e == cudaSuccess) e = cudaMemset(c->al_sn, 0, sizeof(int) * P);
+    if (e == cudaSuccess) e = cudaMemset(c->nl_n, 0, sizeof(int) * P);
+    if (e != cudaSuccess) {
+        md_status s = fail(c, MD_ERR_CUDA, std::string("upload: ") + cudaGetErrorString(e));
+        md_destroy(c);
+        return s;
+    }
+    md_status s = alloc_list(c, (c->nmaxlist + 31) / 32 * 32);
+    if (s == MD_OK) s = initial_build(c);
+    if (s == MD_OK) s = refresh_state(c);
+    if (s != MD_OK) {
+        g_last_error = c->last_error;
+        md_destroy(c);
+        return s;
+    }
+    *out = c;
+    return MD_OK;
+}
+
+md_status md_create_from_files(const char *base, void *stream, md_ctx **out)
+{
+    if (!base || !out) return fail(nullptr, MD_ERR_ARG, "md_create_from_files: null argument");
+    parsed_run r;
+    memset(&r.d, 0, sizeof(r.d));
+    std::string b(base);
+    md_status s = parse_inp((b + ".inp").c_str(), r);
+    if (s != MD_OK) return fail(nullptr, s, "reading " + b + ".inp: " + md_status_string(s));
+    s = parse_fld((b + ".fld").c_str(), r);
+    if (s != MD_OK) return fail(nullptr, s, "reading " + b + ".fld: " + md_status_string(s));
+    s = parse_cfg((b + ".cfg").c_str(), r);
+    if (s != MD_OK) return fail(nullptr, s, "reading " + b + ".cfg: " + md_status_string(s));
+    for (int t : r.itype)
+        if (t < 0 || t >= r.d.ntype) return fail(nullptr, MD_ERR_PARSE, "atom type out of range in .cfg");
+    md_system_desc &d = r.d;
+    d.itype = r.itype.data();
+    d.charge = r.charge.data();
+    d.pos = r.pos.data();
+    d.vel = r.vel.data();
+    d.type_mass = r.mass.data();
+    d.lj1 = r.lj1.data();
+    d.lj2 = r.lj2.data();
+    d.bonds = r.bonds.data();
+    d.angles = r.angles.data();
+    d.bnd1 = r.bnd1.data();
+    d.bnd2 = r.bnd2.data();
+    d.ang1 = r.ang1.data();
+    d.ang2 = r.ang2.data();
+    s = md_create(&d, stream, out);
+    if (s == MD_OK) (*out)->timprn = r.timprn;
+    return s;
+}
+
+md_status md_destroy(md_ctx *c)
+{
+    if (!c) return MD_ERR_ARG;
+    if (c->stream) cudaStreamSynchronize(c->stream);
+    if (c->gexec) cudaGraphExecDestroy(c->gexec);
+    free_device(c);
+    if (c->ev0) cudaEventDestroy(c->ev0);
+    if (c->ev1) cudaEventDestroy(c->ev1);
+    if (c->own_stream && c->stream) cudaStreamDestroy(c->stream);
+    delete c;
+    return MD_OK;
+}
+
+static md_status gather_to_host(md_ctx *c, int what, double *dst, size_t count)
+{
+    md_kparams kp = md_make_kparams(c);
+    launch_gather_out(c, kp, what, c->io_dev);
+    MD_CUDA_TRY(c, cudaMemcpyAsync(dst, c->io_dev, sizeof(double) * count, cudaMemcpyDeviceToHost,
+                                   c->stream));
+    MD_CUDA_TRY(c, cudaStreamSynchronize(c->stream));
+    return MD_OK;
+}
+
+md_status md_get_positions(md_ctx *c, double *pos3)
+{
+    if (!c || !pos3) return MD_ERR_ARG;
+    return gather_to_host(c, 0, pos3, 3 * (size_t)c->n);
+}
+
+md_status md_get_velocities(md_ctx *c, double *vel3)
+{
+    if (!c || !vel3) return MD_ERR_ARG;
+    return gather_to_host(c, 1, vel3, 3 * (size_t)c->n);
+}
+
+md_status md_get_forces(md_ctx *c, double *force4)
+{
+    if (!c || !force4) return MD_ERR_ARG;
+    return gather_to_host(c, 2, force4, 4 * (size_t)c->n);
+}
+
+md_status md_get_energies(md_ctx *c, double *epot)
+{
+    if (!c || !epot) return MD_ERR_ARG;
+    return gather_to_host(c, 3, epot, (size_t)c->n);
+}
+
+static md_status scatter_from_host(md_ctx *c, int what, const double *src)
+{
+    md_kparams kp = md_make_kparams(c);
+    MD_CUDA_TRY(c, cudaMemcpyAsync(c->io_dev, src, sizeof(double) * 3 * (size_t)c->n,
+                                   cudaMemcpyHostToDevice, c->stream));
+    launch_scatter_in(c, kp, what, c->io_dev);
+    return MD_OK;
+}
+
+md_status md_set_positions(md_ctx *c, const double *pos3)
+{
+    if (!c || !pos3) return MD_ERR_ARG;
+    md_status s = scatter_from_host(c, 0, pos3);
+    if (s != MD_OK) return s;
+    s = initial_build(c);
+    if (s != MD_OK) return s;
+    return refresh_state(c);
+}
+
+md_status md_set_velocities(md_ctx *c, const double *vel3)
+{
+    if (!c || !vel3) return MD_ERR_ARG;
+    md_status s = scatter_from_host(c, 1, vel3);
+    if (s != MD_OK) return s;
+    md_kparams kp = md_make_kparams(c);
+    launch_thermo_from_state(c, kp, 0);
+    return check_overflow_and_sync(c);
+}
+
+md_status md_update_neighbors(md_ctx *c, int force)
+{
+    if (!c) return MD_ERR_ARG;
+    md_kparams kp = md_make_kparams(c);
+    if (force) return initial_build(c);
+    MD_CUDA_TRY(c, cudaMemsetAsync(&c->st->update, 0, sizeof(int), c->stream));
+    launch_check(c, kp);
+    launch_rebuild(c, kp, false);
+    return check_overflow_and_sync(c);
+}
+
+md_status md_get_neighbor_list(md_ctx *c, unsigned *nnlist, unsigned *nnlist_max, int pitch, int nmax)
+{
+    if (!c || !nnlist || !nnlist_max || pitch < c->n || nmax <= 0) return MD_ERR_ARG;
+    MD_CUDA_TRY(c, cudaStreamSynchronize(c->stream));
+    const size_t P = c->pitch;
+    std::vector<unsigned> nl((size_t)c->cap * P);
+    std::vector<int> cnt(P), perm(P);
+    MD_CUDA_TRY(c, cudaMemcpy(nl.data(), c->nl, sizeof(unsigned) * nl.size(), cudaMemcpyDeviceToHost));
+    MD_CUDA_TRY(c, cudaMemcpy(cnt.data(), c->nl_n, sizeof(int) * P, cudaMemcpyDeviceToHost));
+    MD_CUDA_TRY(c, cudaMemcpy(perm.data(), c->perm, sizeof(int) * P, cudaMemcpyDeviceToHost));
+    md_status s = MD_OK;
+    std::vector<unsigned> row;
+    for (int i = 0; i < pitch; i++) nnlist_max[i] = 0;
+    for (int si = 0; si < c->n; si++) {
+        row.clear();
+        for (int k = 0; k < cnt[si]; k++) row.push_back((unsigned)perm[nl[(size_t)k * P + si] & MD_INDEX_MASK]);
+        std::sort(row.begin(), row.end());
+        int o = perm[si];
+        nnlist_max[o] = (unsigned)row.size();
+        if ((int)row.size() > nmax) s = MD_ERR_LIST_OVERFLOW;
+        for (size_t k = 0; k < row.size() && (int)k < nmax; k++) nnlist[o + (size_t)pitch * k] = row[k];
+    }
+    return s;
+}
+
+md_status md_compute_forces(md_ctx *c, int terms, int energy)
+{
+    if (!c || (terms & ~MD_TERM_ALL)) return MD_ERR_ARG;
+    md_kparams kp = md_make_kparams(c);
+    launch_forces(c, kp, energy != 0, terms);
+    if (energy) launch_thermo_from_state(c, kp, 1);
+    return check_overflow_and_sync(c);
+}
+
+md_status md_step(md_ctx *c, int nsteps, int energy_every)
+{
+    if (!c || nsteps < 0 || energy_every < 0) return MD_ERR_ARG;
+    MD_CUDA_TRY(c, cudaEventRecord(c->ev0, c->stream));
+    int left = nsteps;
+    while (left > 0) {
+        int aligned = energy_every > 0 ? (int)(c->host_step % energy_every == 0) : 1;
+        int g = energy_every > 0 ? energy_every : std::min(nsteps, 32);
+        if (!aligned || left < g) {
+            /* eager steps up to the next aligned step / the remainder */
+            int k = left;
+            if (energy_every > 0 && !aligned) {
+                long long next = (c->host_step / energy_every + 1) * energy_every;
+                k = (int)std::min<long long>(left, next - c->host_step);
+            }
+            for (int t = 0; t < k; t++) {
+                int en = energy_every > 0 && (c->host_step % energy_every == 0);
+                enqueue_steps(c, 1, en);
+                c->host_step++;
+            }
+            left -= k;
+            continue;
+        }
+        int en = energy_every > 0 ? 1 : 0;
+        if (!c->gexec || c->gsteps != g || c->genergy != en) {
+            md_status s = capture_graph(c, g, en);
+            if (s != MD_OK) return s;
+        }
+        while (left >= g && (energy_every == 0 || c->host_step % energy_every == 0)) {
+            MD_CUDA_TRY(c, cudaGraphLaunch(c->gexec, c->stream));
+            c->host_step += g;
+            left -= g;
+        }
+    }
+    MD_CUDA_TRY(c, cudaEventRecord(c->ev1, c->stream));
+    MD_CUDA_TRY(c, cudaGetLastError());
+    return check_overflow_and_sync(c);
+}
+
+md_status md_last_step_ms(md_ctx *c, float *ms)
+{
+    if (!c || !ms) return MD_ERR_ARG;
+    MD_CUDA_TRY(c, cudaEventSynchronize(c->ev1));
+    MD_CUDA_TRY(c, cudaEventElapsedTime(ms, c->ev0, c->ev1));
+    return MD_OK;
+}
+
+md_status md_get_thermo(md_ctx *c, md_thermo *out)
+{
+    if (!c || !out) return MD_ERR_ARG;
+    MD_CUDA_TRY(c, cudaStreamSynchronize(c->stream));
+    md_devstate h;
+    MD_CUDA_TRY(c, cudaMemcpy(&h, c->st, sizeof(h), cudaMemcpyDeviceToHost));
+    if (h.step == 0) {
+        memset(out, 0, sizeof(*out));
+        out->ke = h.ke;
+        out->temper = 2.0 * h.ke / (std::max(1, 3 * c->n - 3) * 8.314e-3);
+        out->pe = h.pe;
+        out->virial = h.virial;
+        out->conserved = h.ke + h.pe;
+        out->builds = h.builds;
+        out->lambda = 1.0;
+        return MD_OK;
+    }
+    MD_CUDA_TRY(c, cudaMemcpy(out, c->rec + (h.step - 1) % c->rec_cap, sizeof(md_thermo),
+                              cudaMemcpyDeviceToHost));
+    return MD_OK;
+}
+
+md_status md_get_thermo_history(md_ctx *c, md_thermo *out, int n, int *got)
+{
+    if (!c || !out || n < 0 || !got) return MD_ERR_ARG;
+    MD_CUDA_TRY(c, cudaStreamSynchronize(c->stream));
+    md_devstate h;
+    MD_CUDA_TRY(c, cudaMemcpy(&h, c->st, sizeof(h), cudaMemcpyDeviceToHost));
+    long long avail = std::min<long long>(h.step, c->rec_cap);
+    int k = (int)std::min<long long>(avail, n);
+    for (int t = 0; t < k; t++) {
+        long long s = h.step - k + t;
+        MD_CUDA_TRY(c, cudaMemcpy(out + t, c->rec + s % c->rec_cap, sizeof(md_thermo),
+                                  cudaMemcpyDeviceToHost));
+    }
+    *got = k;
+    return MD_OK;
+}
+
+md_status md_run_host(md_ctx *c, double *pos3, double *vel3, int nsteps, int energy_every,
+                      md_thermo *records)
+{
+    if (!c || !pos3 || !vel3 || nsteps < 0) return MD_ERR_ARG;
+    if (nsteps > c->rec_cap && records) return MD_ERR_ARG;
+    md_status s = md_set_positions(c, pos3);
+    if (s == MD_OK) s = md_set_velocities(c, vel3);
+    if (s == MD_OK) s = md_step(c, nsteps, energy_every);
+    if (s == MD_OK && records) {
+        int got = 0;
+        s = md_get_thermo_history(c, records, nsteps, &got);
+    }
+    if (s == MD_OK) s = md_get_positions(c, pos3);
+    if (s == MD_OK) s = md_get_velocities(c, vel3);
+    return s;
+}
+
+md_status md_write_cfg(md_ctx *c, const char *path)
+{
+    if (!c || !path) return MD_ERR_ARG;
+    std::vector<double> p(3 * (size_t)c->n), v(3 * (size_t)c->n);
+    md_status s = md_get_positions(c, p.data());
+    if (s == MD_OK) s = md_get_velocities(c, v.data());
+    if (s != MD_OK) return s;
+    FILE *fo = fopen(path, "w");
+    if (!fo) return fail(c, MD_ERR_IO, std::string("cannot write ") + path);
+    fprintf(fo, "%d %d\n", c->n, 1);
+    fprintf(fo, "%.9g %.9g %.9g\n", c->box[0], c->box[1], c->box[2]);
+    for (int i = 0; i < c->n; i++) {
+        fprintf(fo, "%d %d %.9g\n", i + 1, c->itype[i] + 1, c->charge[i]);
+        fprintf(fo, "%.17g %.17g %.17g\n", p[3 * i], p[3 * i + 1], p[3 * i + 2]);
+        fprintf(fo, "%.17g %.17g %.17g\n", v[3 * i], v[3 * i + 1], v[3 * i + 2]);
+    }
+    fclose(fo);
+    return MD_OK;
+}
+
+md_status md_get_info(md_ctx *c, md_info *out)
+{
+    if (!c || !out) return MD_ERR_ARG;
+    MD_CUDA_TRY(c, cudaStreamSynchronize(c->stream));
+    md_devstate h;
+    MD_CUDA_TRY(c, cudaMemcpy(&h, c->st, sizeof(h), cudaMemcpyDeviceToHost));
+    std::vector<int> cnt(c->pitch);
+    MD_CUDA_TRY(c, cudaMemcpy(cnt.data(), c->nl_n, sizeof(int) * c->pitch, cudaMemcpyDeviceToHost));
+    out->natom = c->n;
+    out->pitch = c->pitch;
+    out->capacity = c->cap;
+    for (int k = 0; k < 3; k++) {
+        out->ncell[k] = c->ncell[k];
+        out->stencil[k] = c->stencil[k];
+        out->binlen[k] = c->binlen[k];
+    }
+    out->pair_threads_per_atom = c->pair_tpa;
+    out->list_threads_per_atom = c->list_tpa;
+    out->builds = h.builds;
+    out->max_neighbors = *std::max_element(cnt.begin(), cnt.begin() + c->n);
+    /* check, 8 list-maintenance kernels (they return at once unless a rebuild
+     * is due), pair, bonded (if any), integrator (+ its reduction) */
+    out->kernels_per_step = 1 + 8 + 1 + ((c->has_bonds || c->has_angles) ? 1 : 0) +
+                            (c->integrator == MD_LEAPFROG ? 2 : 3);
+    return MD_OK;
+}
+
+md_status md_get_order(md_ctx *c, int *perm)
+{
+    if (!c || !perm) return MD_ERR_ARG;
+    MD_CUDA_TRY(c, cudaStreamSynchronize(c->stream));
+    MD_CUDA_TRY(c, cudaMemcpy(perm, c->perm, sizeof(int) * c->n, cudaMemcpyDeviceToHost));
+    return MD_OK;
+}
+
+md_status md_get_cell_ranks(md_ctx *c, int *rank)
+{
+    if (!c || !rank) return MD_ERR_ARG;
+    MD_CUDA_TRY(c, cudaMemcpy(rank, c->cell_rank, sizeof(int) * c->ncells, cudaMemcpyDeviceToHost));
+    return MD_OK;
+}
+
+md_status md_set_tuning(md_ctx *c, int pair_tpa, int list_tpa)
+{
+    if (!c) return MD_ERR_ARG;
+    auto ok = [](int t) { return t == 1 || t == 2 || t == 4 || t == 8 || t == 16 || t == 32; };
+    if (!ok(pair_tpa) || !ok(list_tpa)) return MD_ERR_ARG;
+    c->pair_tpa = pair_tpa;
+    c->list_tpa = list_tpa;
+    if (c->gexec) {
+        cudaGraphExecDestroy(c->gexec);
+        c->gexec = nullptr;
+    }
+    return MD_OK;
+}
+
+}  /* extern "C" */

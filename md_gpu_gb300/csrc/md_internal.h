@@ -1,0 +1,161 @@
+/*
+ * md_internal.h -- device data layout and kernel launchers of libmdgpu_gb300.
+ *
+ * One md_ctx holds one system resident in HBM.  Atoms live in cell order:
+ * every neighbour-list build bins the atoms into cells of side >= rl/2,
+ * orders the cells along a 3-D Hilbert curve and permutes every per-atom
+ * array into that order (ties inside a cell broken by original index, so the
+ * order is deterministic).  perm[] maps sorted -> original index, iperm[] the
+ * reverse; everything the caller sees is in original order.
+ *
+ * Per sorted atom s:
+ *   x,v      FP64 SoA (x[0..N) y[N..2N) z[2N..3N)), the integrated state
+ *   pos4     float4 (x, y, z, q): FP32 copy the force kernels read
+ *   fx,fy,fz int64 fixed point (FX_SCALE units of kJ/mol/A): every force
+ *            term adds into these, so the sum is order independent
+ *   vir      float, sum of ff r^2 (the reference's force.w, 6 x virial)
+ *   nl       neighbour list, column-major nl[k*pitch + s], entry =
+ *            j | (type_j << 29)
+ */
+#ifndef MD_INTERNAL_H
+#define MD_INTERNAL_H
+
+#include <cuda_runtime.h>
+#include <stdint.h>
+
+#include <string>
+#include <vector>
+
+#include "../../include/md_gpu.h"
+
+#define MD_MAXTYPE 8
+#define MD_TYPE_SHIFT 29
+#define MD_INDEX_MASK 0x1FFFFFFFu
+#define MD_EXCL_NONE 0xFFFFFFFFu
+#define FX_SCALE 4294967296.0      /* 2^32 */
+#define FX_INV (1.0 / 4294967296.0)
+
+/* Step control and thermodynamic state kept on the device (no host syncs
+ * inside a step). */
+struct md_devstate {
+    int update;          /* neighbour-list rebuild requested this step */
+    int list_overflow;   /* largest list length seen beyond capacity, or 0 */
+    int status;          /* sticky device-side error code */
+    int builds;          /* neighbour-list builds so far */
+    long long step;
+    double temper;       /* temperature after the last step, K */
+    double ke;           /* kinetic energy, kJ/mol */
+    double pe;           /* potential energy (when computed), kJ/mol */
+    double virial;       /* sum ff r^2 / 6 (when computed) */
+    double xi, eta;      /* Nose-Hoover thermostat variable and its integral */
+    double xi_a, eta_a;  /* the same after the first thermostat half step of a step */
+    double vscale;       /* velocity scale pending from the last thermostat half step */
+    double lambda;       /* last Berendsen scale */
+};
+
+/* Everything a kernel needs about the system, passed by value. */
+struct md_kparams {
+    int n, pitch, cap, ntype;
+    float box[3], boxi[3];
+    double boxd[3];
+    float rcutsq, reacf, rskinsq, rmaxdif;
+    float palfa, spiialfa, alfasq, wolf;
+    int lkspace;
+    int ncell[3];
+    float binlen[3];
+    int stencil[3];   /* cell range per axis: +-stencil, or -1 = all cells */
+    double dt;
+};
+
+struct md_ctx {
+    /* ---- host copy of the run ---- */
+    int n = 0, ntype = 0, pitch = 0, cap = 0;
+    float box[3] = {0, 0, 0}, boxi[3] = {0, 0, 0};
+    int lkspace = 1, enstype = 0, integrator = 0, nmaxlist = 0, timprn = 1;
+    float rcutsq = 0, reacf = 0, alfa = 0, skin = 0, temper_0 = 0, dt = 1, tau_t = 100, rdel = 0.02f;
+    float wc[4] = {0, 0, 0, 0};
+    float rskinsq = 0, rmaxdif = 0;
+    float lj1[64], lj2[64];
+    float bnd1[MD_MAXTYPE], bnd2[MD_MAXTYPE], ang1[MD_MAXTYPE], ang2[MD_MAXTYPE];
+    float type_mass[MD_MAXTYPE];
+    std::vector<int> itype;          /* original order, 0-based */
+    std::vector<float> charge;
+    std::vector<int> bonds;          /* type, i, j (0-based) */
+    std::vector<int> angles;         /* type, i, j(centre), k (0-based) */
+    std::vector<unsigned> excl_host; /* 4 per atom, the reference's slot rule */
+    unsigned type_excl_mask[MD_MAXTYPE] = {0};
+    int ncell[3] = {1, 1, 1}, ncells = 1;
+    float binlen[3] = {0, 0, 0};
+    int stencil[3] = {0, 0, 0};
+    std::string last_error;
+
+    /* ---- device ---- */
+    cudaStream_t stream = nullptr;
+    bool own_stream = false;
+    int device = 0;
+    double *x = nullptr, *v = nullptr, *mass = nullptr;   /* sorted order */
+    float4 *pos4 = nullptr, *pos_old = nullptr;
+    int *type = nullptr, *perm = nullptr, *iperm = nullptr;
+    long long *f = nullptr;                               /* 3*pitch, SoA */
+    float *vir = nullptr, *epot = nullptr;
+    unsigned *nl = nullptr;
+    int *nl_n = nullptr;
+    uint4 *excl_orig = nullptr, *excl_s = nullptr;
+    int *cell_rank = nullptr, *cell_count = nullptr, *cell_start = nullptr, *cell_fill = nullptr;
+    int *key = nullptr, *src = nullptr;
+    double *tmp_d = nullptr;                              /* 7*pitch scratch for permutation */
+    float4 *tmp4 = nullptr;
+    int *tmp_i = nullptr;                                 /* 3*pitch */
+    /* bonded lists: original-space CSR (fixed) and sorted-space per-atom slots */
+    int2 *bl_o = nullptr; int *bl_on = nullptr;           /* 4 per original atom */
+    int4 *al_o = nullptr; int *al_on = nullptr;
+    int2 *bl_s = nullptr; int *bl_sn = nullptr;           /* column-major, 4*pitch */
+    int4 *al_s = nullptr; int *al_sn = nullptr;
+    int has_bonds = 0, has_angles = 0;
+    double *partials = nullptr;                           /* per-block reductions */
+    int npart = 0;
+    md_devstate *st = nullptr;
+    md_thermo *rec = nullptr;                             /* device ring of records */
+    int rec_cap = 0;
+    float *lj_dev = nullptr;                              /* lj1,lj2 interleaved (64 float2) */
+    float *bonded_par = nullptr;                          /* bnd1,bnd2,ang1,ang2 (4x8) */
+    unsigned *type_mask_dev = nullptr;
+
+    /* graph of gsteps steps (energy on its first step when genergy) */
+    cudaGraphExec_t gexec = nullptr;
+    int gsteps = 0;
+    int genergy = 0;
+    long long host_step = 0;       /* steps run so far (mirrors st->step) */
+    double *io_dev = nullptr;      /* 4*pitch doubles for host transfers */
+    int pair_tpa = 4;    /* threads per atom in the pair kernel */
+    int list_tpa = 8;    /* threads per atom in the list build */
+
+    /* timing of the last md_step call (CUDA events on the stream) */
+    cudaEvent_t ev0 = nullptr, ev1 = nullptr;
+};
+
+md_kparams md_make_kparams(const md_ctx *c);
+
+/* ---- launchers (k_cells.cu) ---- */
+void launch_check(md_ctx *c, const md_kparams &kp);
+void launch_rebuild(md_ctx *c, const md_kparams &kp, bool unconditional);
+/* ---- launchers (k_forces.cu) ---- */
+void launch_forces(md_ctx *c, const md_kparams &kp, bool energy, int terms);
+/* ---- launchers (k_integrate.cu) ---- */
+void launch_leapfrog(md_ctx *c, const md_kparams &kp, int energy);
+void launch_vv_first(md_ctx *c, const md_kparams &kp);
+void launch_vv_second(md_ctx *c, const md_kparams &kp, int energy);
+void launch_thermo_from_state(md_ctx *c, const md_kparams &kp, int energy);
+void launch_gather_out(md_ctx *c, const md_kparams &kp, int what, void *dst);
+void launch_scatter_in(md_ctx *c, const md_kparams &kp, int what, const void *src);
+
+#define MD_CUDA_TRY(c, expr)                                                   \
+    do {                                                                       \
+        cudaError_t e_ = (expr);                                               \
+        if (e_ != cudaSuccess) {                                               \
+            (c)->last_error = std::string(#expr) + ": " + cudaGetErrorString(e_); \
+            return MD_ERR_CUDA;                                                \
+        }                                                                      \
+    } while (0)
+
+#endif

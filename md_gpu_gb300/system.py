@@ -1,0 +1,311 @@
+"""Python mirror of the C ABI (include/md_gpu.h) over ctypes.
+
+This is the host-side interface a user of md_gpu's step loop calls: create a
+system from the reference's .inp/.fld/.cfg files or from arrays, step it,
+read positions, velocities, forces, energies, neighbour lists and the per
+step thermodynamic records.  All compute happens in libmdgpu_gb300.so; there
+is no CPU path, and loading fails loudly when the library is missing.
+"""
+from __future__ import annotations
+
+import ctypes as C
+import os
+from typing import Optional
+
+import numpy as np
+
+HERE = os.path.dirname(os.path.abspath(__file__))
+LIB_PATH = os.path.join(HERE, "_build", "libmdgpu_gb300.so")
+
+MD_LEAPFROG, MD_VV, MD_NH = 0, 1, 2
+TERM_PAIR, TERM_BOND, TERM_ANGLE, TERM_ALL = 1, 2, 4, 7
+STATUS = {0: "ok", 1: "invalid argument", 2: "cannot open file", 3: "parse error", 4: "CUDA error",
+          5: "neighbour list overflow", 6: "more than four bonds/angles on an atom",
+          7: "unsupported option", 8: "cutoff + skin exceeds half the box"}
+
+
+class MDError(RuntimeError):
+    def __init__(self, status, msg=""):
+        super().__init__(f"{STATUS.get(status, status)}: {msg}")
+        self.status = status
+
+
+class SystemDesc(C.Structure):
+    _fields_ = [("natom", C.c_int), ("ntype", C.c_int), ("box", C.c_float * 3),
+                ("itype", C.POINTER(C.c_int)), ("charge", C.POINTER(C.c_float)),
+                ("pos", C.POINTER(C.c_float)), ("vel", C.POINTER(C.c_float)),
+                ("type_mass", C.POINTER(C.c_float)), ("lj1", C.POINTER(C.c_float)),
+                ("lj2", C.POINTER(C.c_float)), ("nbonds", C.c_int), ("bonds", C.POINTER(C.c_int)),
+                ("bnd1", C.POINTER(C.c_float)), ("bnd2", C.POINTER(C.c_float)),
+                ("nangle", C.c_int), ("angles", C.POINTER(C.c_int)),
+                ("ang1", C.POINTER(C.c_float)), ("ang2", C.POINTER(C.c_float)),
+                ("lkspace", C.c_int), ("rcutsq", C.c_float), ("reacf", C.c_float),
+                ("alfa", C.c_float), ("skin", C.c_float), ("nmaxlist", C.c_int),
+                ("enstype", C.c_int), ("temper_0", C.c_float), ("dt", C.c_float),
+                ("tau_t", C.c_float), ("integrator", C.c_int)]
+
+
+class Thermo(C.Structure):
+    _fields_ = [("step", C.c_longlong), ("ke", C.c_double), ("temper", C.c_double),
+                ("pe", C.c_double), ("virial", C.c_double), ("conserved", C.c_double),
+                ("xi", C.c_double), ("lambda_", C.c_double), ("builds", C.c_int),
+                ("flags", C.c_int)]
+
+    def as_dict(self):
+        return {k: getattr(self, k) for k, _ in self._fields_}
+
+
+class Info(C.Structure):
+    _fields_ = [("natom", C.c_int), ("pitch", C.c_int), ("capacity", C.c_int),
+                ("ncell", C.c_int * 3), ("stencil", C.c_int * 3), ("binlen", C.c_float * 3),
+                ("pair_threads_per_atom", C.c_int), ("list_threads_per_atom", C.c_int),
+                ("builds", C.c_int), ("max_neighbors", C.c_int), ("kernels_per_step", C.c_int)]
+
+
+_lib = None
+
+
+def library(path: Optional[str] = None):
+    """Load libmdgpu_gb300.so (build it with md_gpu_gb300.build.build())."""
+    global _lib
+    if _lib is not None:
+        return _lib
+    p = path or LIB_PATH
+    if not os.path.exists(p):
+        raise RuntimeError(f"libmdgpu_gb300.so not built ({p}); run md_gpu_gb300.build.build()")
+    L = C.CDLL(p)
+    vp = C.c_void_p
+    L.md_status_string.restype = C.c_char_p
+    L.md_create.argtypes = [C.POINTER(SystemDesc), vp, C.POINTER(vp)]
+    L.md_create_from_files.argtypes = [C.c_char_p, vp, C.POINTER(vp)]
+    L.md_destroy.argtypes = [vp]
+    for fn in ("md_set_positions", "md_set_velocities", "md_get_positions", "md_get_velocities",
+               "md_get_forces", "md_get_energies"):
+        getattr(L, fn).argtypes = [vp, vp]
+    L.md_update_neighbors.argtypes = [vp, C.c_int]
+    L.md_get_neighbor_list.argtypes = [vp, vp, vp, C.c_int, C.c_int]
+    L.md_compute_forces.argtypes = [vp, C.c_int, C.c_int]
+    L.md_step.argtypes = [vp, C.c_int, C.c_int]
+    L.md_get_thermo.argtypes = [vp, C.POINTER(Thermo)]
+    L.md_get_thermo_history.argtypes = [vp, C.POINTER(Thermo), C.c_int, C.POINTER(C.c_int)]
+    L.md_run_host.argtypes = [vp, vp, vp, C.c_int, C.c_int, C.POINTER(Thermo)]
+    L.md_write_cfg.argtypes = [vp, C.c_char_p]
+    L.md_get_info.argtypes = [vp, C.POINTER(Info)]
+    L.md_get_order.argtypes = [vp, vp]
+    L.md_get_cell_ranks.argtypes = [vp, vp]
+    L.md_set_tuning.argtypes = [vp, C.c_int, C.c_int]
+    L.md_last_step_ms.argtypes = [vp, C.POINTER(C.c_float)]
+    L.md_last_error.argtypes = [vp, C.c_char_p, C.c_int]
+    L.md_time_pair.argtypes = [vp, C.c_int, C.POINTER(C.c_float)]
+    L.md_probe_fp32_peak.argtypes = [C.POINTER(C.c_double)]
+    _lib = L
+    return L
+
+
+def fp32_peak_tflops():
+    """Measured FP32 FMA throughput of the current GPU, TFLOP/s."""
+    t = C.c_double()
+    _check(library().md_probe_fp32_peak(C.byref(t)))
+    return t.value
+
+
+def _err(ctx=None):
+    buf = C.create_string_buffer(1024)
+    library().md_last_error(ctx, buf, 1024)
+    return buf.value.decode(errors="replace")
+
+
+def _check(status, ctx=None):
+    if status != 0:
+        raise MDError(status, _err(ctx))
+
+
+def _ptr(a, ct):
+    return a.ctypes.data_as(C.POINTER(ct))
+
+
+class MDSystem:
+    """One system resident on the GPU (an md_ctx)."""
+
+    def __init__(self, ctx, natom):
+        self._ctx = ctx
+        self.natom = natom
+
+    # ---- construction ----
+    @classmethod
+    def from_files(cls, base: str, stream=None) -> "MDSystem":
+        L = library()
+        ctx = C.c_void_p()
+        _check(L.md_create_from_files(base.encode(), stream, C.byref(ctx)))
+        n = Info()
+        _check(L.md_get_info(ctx, C.byref(n)), ctx)
+        return cls(ctx, n.natom)
+
+    @classmethod
+    def from_arrays(cls, *, box, itype, charge, pos, vel, type_mass, lj1, lj2, lkspace, rcutsq,
+                    skin, nmaxlist, dt, reacf=0.0, alfa=0.0, enstype=0, temper_0=0.0, tau_t=100.0,
+                    integrator=MD_LEAPFROG, bonds=None, bnd1=None, bnd2=None, angles=None,
+                    ang1=None, ang2=None, stream=None) -> "MDSystem":
+        """Arrays in the reference's in-memory conventions: itype 0-based,
+        masses g/mol*1e4 per type, lj tables ntype x ntype, bonds (type,i,j)
+        and angles (type,i,j,k) 0-based, bnd1/ang1 = 2k, ang2 in rad."""
+        L = library()
+        keep = []
+
+        def f32(a):
+            a = np.ascontiguousarray(a, np.float32)
+            keep.append(a)
+            return _ptr(a, C.c_float)
+
+        def i32(a):
+            a = np.ascontiguousarray(a, np.int32)
+            keep.append(a)
+            return _ptr(a, C.c_int)
+
+        n = int(np.asarray(itype).shape[0])
+        ntype = int(np.asarray(type_mass).shape[0])
+        d = SystemDesc()
+        d.natom, d.ntype = n, ntype
+        for k in range(3):
+            d.box[k] = float(box[k])
+        d.itype, d.charge = i32(itype), f32(charge)
+        d.pos = f32(np.asarray(pos).reshape(-1))
+        d.vel = f32(np.asarray(vel).reshape(-1)) if vel is not None else None
+        d.type_mass = f32(type_mass)
+        d.lj1, d.lj2 = f32(np.asarray(lj1).reshape(-1)), f32(np.asarray(lj2).reshape(-1))
+        pad8 = lambda a: np.pad(np.asarray(a, np.float32), (0, 8 - len(a)))
+        if bonds is not None and len(bonds):
+            d.nbonds = len(bonds)
+            d.bonds = i32(np.asarray(bonds).reshape(-1))
+            d.bnd1, d.bnd2 = f32(pad8(bnd1)), f32(pad8(bnd2))
+        if angles is not None and len(angles):
+            d.nangle = len(angles)
+            d.angles = i32(np.asarray(angles).reshape(-1))
+            d.ang1, d.ang2 = f32(pad8(ang1)), f32(pad8(ang2))
+        d.lkspace, d.rcutsq, d.reacf, d.alfa = lkspace, rcutsq, reacf, alfa
+        d.skin, d.nmaxlist, d.enstype, d.temper_0 = skin, nmaxlist, enstype, temper_0
+        d.dt, d.tau_t, d.integrator = dt, tau_t, integrator
+        ctx = C.c_void_p()
+        _check(L.md_create(C.byref(d), stream, C.byref(ctx)))
+        return cls(ctx, n)
+
+    def close(self):
+        if self._ctx:
+            library().md_destroy(self._ctx)
+            self._ctx = None
+
+    def __del__(self):
+        try:
+            self.close()
+        except Exception:
+            pass
+
+    def __enter__(self):
+        return self
+
+    def __exit__(self, *a):
+        self.close()
+
+    # ---- state ----
+    def _get(self, fn, cols):
+        out = np.zeros((self.natom, cols), np.float64) if cols > 1 else np.zeros(self.natom)
+        _check(getattr(library(), fn)(self._ctx, out.ctypes.data), self._ctx)
+        return out
+
+    def positions(self):
+        return self._get("md_get_positions", 3)
+
+    def velocities(self):
+        return self._get("md_get_velocities", 3)
+
+    def forces(self):
+        """(N, 4): fx, fy, fz, sum ff r^2 (kJ/mol/A; kJ/mol)."""
+        return self._get("md_get_forces", 4)
+
+    def energies(self):
+        return self._get("md_get_energies", 1)
+
+    def set_positions(self, pos):
+        a = np.ascontiguousarray(pos, np.float64)
+        _check(library().md_set_positions(self._ctx, a.ctypes.data), self._ctx)
+
+    def set_velocities(self, vel):
+        a = np.ascontiguousarray(vel, np.float64)
+        _check(library().md_set_velocities(self._ctx, a.ctypes.data), self._ctx)
+
+    # ---- work ----
+    def update_neighbors(self, force=True):
+        _check(library().md_update_neighbors(self._ctx, 1 if force else 0), self._ctx)
+
+    def compute_forces(self, terms=TERM_ALL, energy=False):
+        _check(library().md_compute_forces(self._ctx, terms, 1 if energy else 0), self._ctx)
+
+    def step(self, nsteps, energy_every=0):
+        _check(library().md_step(self._ctx, int(nsteps), int(energy_every)), self._ctx)
+
+    def last_step_ms(self):
+        ms = C.c_float()
+        _check(library().md_last_step_ms(self._ctx, C.byref(ms)), self._ctx)
+        return ms.value
+
+    def run_host(self, pos, vel, nsteps, energy_every=0):
+        """End to end from host buffers; returns (pos, vel, records)."""
+        p = np.ascontiguousarray(pos, np.float64).copy()
+        v = np.ascontiguousarray(vel, np.float64).copy()
+        rec = (Thermo * max(nsteps, 1))()
+        _check(library().md_run_host(self._ctx, p.ctypes.data, v.ctypes.data, nsteps, energy_every,
+                                     rec), self._ctx)
+        return p, v, [rec[i].as_dict() for i in range(nsteps)]
+
+    # ---- observation ----
+    def thermo(self):
+        t = Thermo()
+        _check(library().md_get_thermo(self._ctx, C.byref(t)), self._ctx)
+        return t.as_dict()
+
+    def history(self, n):
+        buf = (Thermo * max(n, 1))()
+        got = C.c_int()
+        _check(library().md_get_thermo_history(self._ctx, buf, n, C.byref(got)), self._ctx)
+        return [buf[i].as_dict() for i in range(got.value)]
+
+    def info(self):
+        i = Info()
+        _check(library().md_get_info(self._ctx, C.byref(i)), self._ctx)
+        return {"natom": i.natom, "pitch": i.pitch, "capacity": i.capacity,
+                "ncell": list(i.ncell), "stencil": list(i.stencil), "binlen": list(i.binlen),
+                "pair_tpa": i.pair_threads_per_atom, "list_tpa": i.list_threads_per_atom,
+                "builds": i.builds, "max_neighbors": i.max_neighbors,
+                "kernels_per_step": i.kernels_per_step}
+
+    def neighbor_list(self, nmax):
+        """Reference layout (neighborlist.cu:284): (nnlist[pitch*nmax], nnlist_max[pitch])."""
+        pitch = ((self.natom + 255) // 256) * 256
+        nn = np.zeros(pitch * nmax, np.uint32)
+        nm = np.zeros(pitch, np.uint32)
+        _check(library().md_get_neighbor_list(self._ctx, nn.ctypes.data, nm.ctypes.data, pitch, nmax),
+               self._ctx)
+        return nn, nm
+
+    def order(self):
+        p = np.zeros(self.natom, np.int32)
+        _check(library().md_get_order(self._ctx, p.ctypes.data), self._ctx)
+        return p
+
+    def cell_ranks(self):
+        info = self.info()
+        r = np.zeros(int(np.prod(info["ncell"])), np.int32)
+        _check(library().md_get_cell_ranks(self._ctx, r.ctypes.data), self._ctx)
+        return r
+
+    def time_pair(self, nrep=20):
+        """Average ms per launch of the pair kernel (CUDA events, own stream)."""
+        ms = C.c_float()
+        _check(library().md_time_pair(self._ctx, nrep, C.byref(ms)), self._ctx)
+        return ms.value
+
+    def set_tuning(self, pair_tpa, list_tpa):
+        _check(library().md_set_tuning(self._ctx, pair_tpa, list_tpa), self._ctx)
+
+    def write_cfg(self, path):
+        _check(library().md_write_cfg(self._ctx, path.encode()), self._ctx)

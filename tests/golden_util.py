@@ -84,3 +84,48 @@ def rows_canonical(nn, nm, n, width):
         m = nm[:n] > k
         out[m, k] = cols[k, :n][m]
     return out
+
+
+def system_from_case(case, integrator=None, nmaxlist=None, tau_t=100.0, stream=None):
+    """The same inputs the oracle sees, uploaded through the C ABI."""
+    from md_gpu_gb300 import MDSystem
+    p = case.params
+    nt = case.fld.ntype
+    bonds = case.bonds.copy()
+    angles = case.angles.copy()
+    if len(bonds):
+        bonds -= 1          # file convention (1-based) -> 0-based
+    if len(angles):
+        angles -= 1
+    tm = np.ctypeslib.as_array(case.fld.mass)[:nt].astype(np.float32)
+    lj1 = np.ctypeslib.as_array(case.fld.lj1)[:nt * nt].astype(np.float32)
+    lj2 = np.ctypeslib.as_array(case.fld.lj2)[:nt * nt].astype(np.float32)
+    arr = lambda k: np.ctypeslib.as_array(getattr(case.fld, k)).astype(np.float32)
+    return MDSystem.from_arrays(
+        box=case.box, itype=case.itype, charge=case.q, pos=case.pos, vel=case.vel, type_mass=tm,
+        lj1=lj1, lj2=lj2, lkspace=p.lkspace, rcutsq=p.rcutsq, reacf=p.reacf, alfa=p.alfa,
+        skin=p.skin, nmaxlist=nmaxlist or p.nmaxlist, dt=p.dt, enstype=p.enstype,
+        temper_0=p.temper_0, tau_t=tau_t,
+        integrator=p.integrator if integrator is None else integrator,
+        bonds=bonds if len(bonds) else None, bnd1=arr("bnd1"), bnd2=arr("bnd2"),
+        angles=angles if len(angles) else None, ang1=arr("ang1"), ang2=arr("ang2"),
+        stream=stream)
+
+
+def oracle_state(case):
+    """Oracle list (reference layout) and FP64 plain-form forces/energies."""
+    p = case.params
+    pos4 = case.pos4()
+    excl = oracle.exclusions(case.natom, case.bonds)
+    nn, nm, mx = oracle.nlist(pos4, case.box, case.boxi, oracle.rskinsq(p.skin, p.rcutsq), excl,
+                              max(p.nmaxlist, 1024))
+    kind = 0 if p.lkspace == 0 else 1
+    f64, ep = oracle.pair_f64(kind, pos4, case.itype, case.q, case.box, nn, nm, case.fld.ntype,
+                              case.lj1, case.lj2, p.rcutsq, p.reacf if kind == 0 else 0.0, p.alfa)
+    return dict(pos4=pos4, excl=excl, nn=nn, nm=nm, mx=mx, kind=kind, f64=f64, ep64=ep)
+
+
+def rms_rel(a, b):
+    a = np.asarray(a, np.float64)
+    b = np.asarray(b, np.float64)
+    return float(np.sqrt(((a - b) ** 2).sum() / (b ** 2).sum()))

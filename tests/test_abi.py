@@ -1,0 +1,89 @@
+"""The C ABI without a GPU: the library loads, exports every entry point the
+header declares, and rejects bad input on the host before any device work."""
+import ctypes as C
+import os
+import re
+import tempfile
+
+import pytest
+
+from md_gpu_gb300 import build as mdbuild
+from md_gpu_gb300 import synth
+from md_gpu_gb300.system import MDError, MDSystem, library
+
+ROOT = os.path.dirname(os.path.dirname(os.path.abspath(__file__)))
+
+
+@pytest.fixture(scope="module")
+def lib():
+    mdbuild.build()
+    return library()
+
+
+def declared_functions():
+    names = []
+    for h in sorted(os.listdir(os.path.join(ROOT, "include"))):
+        if h.endswith(".h"):
+            text = open(os.path.join(ROOT, "include", h)).read()
+            names += re.findall(r"^\s*(?:md_status|const char \*)\s*(md_\w+)\s*\(", text, re.M)
+    return sorted(set(names))
+
+
+def test_exports_every_declared_symbol(lib):
+    names = declared_functions()
+    assert len(names) >= 20
+    for n in names:
+        assert hasattr(lib, n), n
+
+
+def test_status_strings(lib):
+    lib.md_status_string.restype = C.c_char_p
+    assert lib.md_status_string(0) == b"ok"
+    assert b"overflow" in lib.md_status_string(5)
+
+
+def _case(tmp, **kw):
+    return synth.write_case(synth.nacl_rocksalt(ncell=5, seed=1, **kw), tmp, "c")
+
+
+def test_missing_files(lib):
+    with pytest.raises(MDError) as e:
+        MDSystem.from_files("/nonexistent/run")
+    assert e.value.status == 2
+
+
+def test_malformed_inputs(lib):
+    with tempfile.TemporaryDirectory() as tmp:
+        base = _case(tmp)
+        with open(base + ".cfg", "w") as fh:
+            fh.write("12 1\n10.0 10.0\n")
+        with pytest.raises(MDError) as e:
+            MDSystem.from_files(base)
+        assert e.value.status == 3
+    with tempfile.TemporaryDirectory() as tmp:
+        base = _case(tmp)
+        with open(base + ".inp", "w") as fh:
+            fh.write("ensemble: npt\ntemper: 300 1\n")
+        with pytest.raises(MDError) as e:
+            MDSystem.from_files(base)
+        assert e.value.status == 7
+
+
+def test_box_too_small_for_cutoff(lib):
+    with tempfile.TemporaryDirectory() as tmp:
+        base = synth.write_case(synth.nacl_rocksalt(ncell=4, seed=1), tmp, "c")   # L = 25.5 < 2 (rc + skin)
+        with pytest.raises(MDError) as e:
+            MDSystem.from_files(base)
+        assert e.value.status == 8
+
+
+def test_too_many_bonds(lib):
+    with tempfile.TemporaryDirectory() as tmp:
+        s = synth.water_grid(nside=8, seed=1)
+        import numpy as np
+        extra = np.array([[1, 1, 4], [1, 1, 5], [1, 1, 6]])   # atom 1 gets five bonds
+        s.bonds = np.concatenate([s.bonds, extra])
+        base = synth.write_case(s, tmp, "w")
+        with pytest.raises(MDError) as e:
+            MDSystem.from_files(base)
+        assert e.value.status == 6

@@ -1,0 +1,319 @@
+"""CUDA path vs the oracle, through the C ABI (libmdgpu_gb300.so).
+
+Tolerances (stated, per the path's precision contract):
+* neighbour lists: bit-exact as sets and as sorted rows (integer work);
+* forces: RMS relative error <= 1e-5 against the FP64 plain form
+  (sqrt(sum |F - F64|^2 / sum |F64|^2)), same Coulomb model (A&S 7.1.26);
+* energies: RMS relative <= 2e-5 per atom, 1e-6 on totals;
+* one integrator step: velocity increments RMS relative <= 2e-5, positions
+  to 1e-6 A.
+"""
+import os
+import tempfile
+
+import numpy as np
+import pytest
+
+import oracle
+import golden_util as gu
+from md_gpu_gb300 import MD_LEAPFROG, MD_NH, MD_VV, TERM_ALL, TERM_ANGLE, TERM_BOND, TERM_PAIR
+from md_gpu_gb300 import build as mdbuild
+from md_gpu_gb300 import synth
+
+pytestmark = pytest.mark.gpu
+
+FORCE_TOL = 1e-5
+
+
+@pytest.fixture(scope="module", autouse=True)
+def _lib():
+    mdbuild.build()
+
+
+@pytest.fixture(scope="module", params=gu.names())
+def gcase(request):
+    g = gu.load_golden(request.param)
+    case = gu.case_from_golden(g)
+    return request.param, g, case
+
+
+def test_neighbour_list_bit_exact(gcase):
+    name, g, case = gcase
+    orc = gu.oracle_state(case)
+    with gu.system_from_case(case) as sim:
+        width = g["meta"]["list_width"]
+        nn, nm = sim.neighbor_list(width)
+        n = case.natom
+        assert np.array_equal(nm[:n], orc["nm"][:n])
+        rows = gu.rows_canonical(nn, nm, n, width)
+        assert np.array_equal(rows, gu.rows_canonical(orc["nn"], orc["nm"], n, width))
+        assert gu.sha(rows) == g["hashes"]["nnlist_rows"]
+
+
+def test_pair_forces_vs_fp64(gcase):
+    name, g, case = gcase
+    orc = gu.oracle_state(case)
+    with gu.system_from_case(case) as sim:
+        sim.compute_forces(TERM_PAIR)
+        F = sim.forces()
+    err = gu.rms_rel(F[:, :3], orc["f64"][:, :3])
+    assert err <= FORCE_TOL, err
+    assert gu.rms_rel(F[:, 3], orc["f64"][:, 3]) <= FORCE_TOL
+
+
+def test_pair_forces_vs_reference_kernel(gcase):
+    """Against the reference kernel's own FP32 result (golden samples)."""
+    name, g, case = gcase
+    with gu.system_from_case(case) as sim:
+        sim.compute_forces(TERM_PAIR)
+        F = sim.forces()
+    idx = g["sample_idx"]
+    ref = g["sample__force_pair"].astype(np.float64)
+    assert gu.rms_rel(F[idx, :3], ref[:, :3]) <= 2 * FORCE_TOL
+
+
+def test_energies_vs_fp64(gcase):
+    name, g, case = gcase
+    orc = gu.oracle_state(case)
+    with gu.system_from_case(case) as sim:
+        sim.compute_forces(TERM_PAIR, energy=True)
+        ep = sim.energies()
+        th = sim.thermo()
+    assert gu.rms_rel(ep, orc["ep64"]) <= 2e-5
+    assert abs(th["pe"] - orc["ep64"].sum()) <= 1e-6 * np.abs(orc["ep64"]).sum()
+
+
+def test_bonded_forces_vs_fp64(gcase):
+    name, g, case = gcase
+    if not len(case.bonds) and not len(case.angles):
+        pytest.skip("no bonded terms")
+    pos4 = case.pos4()
+    f = np.zeros((case.natom, 4))
+    ep = np.zeros(case.natom)
+    arr = lambda k: np.ctypeslib.as_array(getattr(case.fld, k)).astype(np.float32)
+    if len(case.bonds):
+        oracle.bonds_f64(pos4, case.box, case.bonds, arr("bnd1"), arr("bnd2"), f, ep)
+    if len(case.angles):
+        oracle.angles_f64(pos4, case.box, case.angles, arr("ang1"), arr("ang2"), f, ep)
+    with gu.system_from_case(case) as sim:
+        sim.compute_forces(TERM_BOND | TERM_ANGLE, energy=True)
+        F = sim.forces()
+        E = sim.energies()
+    assert gu.rms_rel(F[:, :3], f[:, :3]) <= FORCE_TOL
+    assert gu.rms_rel(E, ep) <= 2e-5
+
+
+def test_total_forces(gcase):
+    name, g, case = gcase
+    orc = gu.oracle_state(case)
+    f = orc["f64"].copy()
+    ep = np.zeros(case.natom)
+    arr = lambda k: np.ctypeslib.as_array(getattr(case.fld, k)).astype(np.float32)
+    pos4 = orc["pos4"]
+    if len(case.bonds):
+        oracle.bonds_f64(pos4, case.box, case.bonds, arr("bnd1"), arr("bnd2"), f, ep)
+    if len(case.angles):
+        oracle.angles_f64(pos4, case.box, case.angles, arr("ang1"), arr("ang2"), f, ep)
+    with gu.system_from_case(case) as sim:
+        sim.compute_forces(TERM_ALL)
+        F = sim.forces()
+    assert gu.rms_rel(F[:, :3], f[:, :3]) <= FORCE_TOL
+
+
+def test_leapfrog_one_step(gcase):
+    name, g, case = gcase
+    orc = gu.oracle_state(case)
+    f = orc["f64"][:, :3].copy()
+    arr = lambda k: np.ctypeslib.as_array(getattr(case.fld, k)).astype(np.float32)
+    f4 = np.zeros((case.natom, 4))
+    ep = np.zeros(case.natom)
+    if len(case.bonds):
+        oracle.bonds_f64(orc["pos4"], case.box, case.bonds, arr("bnd1"), arr("bnd2"), f4, ep)
+    if len(case.angles):
+        oracle.angles_f64(orc["pos4"], case.box, case.angles, arr("ang1"), arr("ang2"), f4, ep)
+    f += f4[:, :3]
+    p = case.params
+    m = case.mass.astype(np.float64)
+    x0 = case.pos.astype(np.float64)
+    v0 = case.vel.astype(np.float64)
+    v1 = v0 + f * p.dt / m[:, None]          # first Berendsen step has lambda = 1
+    x1 = x0 + v1 * p.dt
+    L = case.box.astype(np.float64)
+    x1 -= L * np.trunc(x1 * 2.0 / L)
+    with gu.system_from_case(case, integrator=MD_LEAPFROG) as sim:
+        sim.step(1)
+        X, V = sim.positions(), sim.velocities()
+    assert gu.rms_rel(V - v0, v1 - v0) <= 2e-5
+    assert np.abs(X - x1).max() <= 1e-6 * max(1.0, float(L.max()))
+
+
+def test_determinism():
+    case = oracle.load(_write(synth.nacl_rocksalt(ncell=6, seed=5)))
+    outs = []
+    for _ in range(2):
+        with gu.system_from_case(case) as sim:
+            sim.step(40)
+            outs.append((sim.positions(), sim.velocities(), sim.forces(), sim.thermo()["temper"]))
+    for a, b in zip(outs[0], outs[1]):
+        assert np.array_equal(np.asarray(a), np.asarray(b))
+
+
+_TMP = tempfile.mkdtemp(prefix="mdgpu_")
+
+
+def _write(system, name="case"):
+    d = tempfile.mkdtemp(dir=_TMP)
+    return synth.write_case(system, d, name)
+
+
+def test_files_and_arrays_agree():
+    base = _write(synth.water_grid(nside=8, seed=2))
+    case = oracle.load(base)
+    from md_gpu_gb300 import MDSystem
+    with MDSystem.from_files(base) as a, gu.system_from_case(case) as b:
+        a.compute_forces()
+        b.compute_forces()
+        assert np.array_equal(a.forces(), b.forces())
+        assert np.array_equal(a.positions(), b.positions())
+
+
+def test_cell_order_is_hilbert_sorted():
+    case = oracle.load(_write(synth.nacl_rocksalt(ncell=6, seed=9)))
+    p = case.params
+    rl = np.float32(np.sqrt(np.float32(p.rcutsq))) + np.float32(p.skin)
+    nc, bl = oracle.cell_dims(case.box, rl)
+    with gu.system_from_case(case) as sim:
+        info = sim.info()
+        assert list(nc) == info["ncell"]
+        assert np.array_equal(bl, np.array(info["binlen"], np.float32))
+        ranks = sim.cell_ranks()
+        bits = max(1, int(np.ceil(np.log2(max(nc)))))
+        keys = []
+        for z in range(nc[2]):
+            for y in range(nc[1]):
+                for x in range(nc[0]):
+                    keys.append((oracle.hilbert3(x, y, z, bits), x + nc[0] * (y + nc[1] * z)))
+        expect = np.zeros(len(keys), np.int32)
+        for r, (_, lin) in enumerate(sorted(keys)):
+            expect[lin] = r
+        assert np.array_equal(ranks, expect)
+        cell = oracle.cell_index(case.pos4(), case.box, nc, bl)
+        lin = cell[:, 0] + nc[0] * (cell[:, 1] + nc[1] * cell[:, 2])
+        expect_order = np.lexsort((np.arange(case.natom), expect[lin]))
+        assert np.array_equal(sim.order(), expect_order)
+
+
+def test_berendsen_temperatures_vs_plain():
+    case = oracle.load(_write(synth.nacl_rocksalt(ncell=5, seed=3, nmaxlist=512)))
+    x = case.pos.astype(np.float64).copy()
+    v = case.vel.astype(np.float64).copy()
+    st, rec = oracle.md_plain_run(case, x, v, 5, 0)
+    with gu.system_from_case(case, integrator=MD_LEAPFROG) as sim:
+        sim.step(5)
+        hist = sim.history(5)
+        X = sim.positions()
+    t_gpu = np.array([h["temper"] for h in hist])
+    t_orc = 2.0 * rec[:, 0] / ((3 * case.natom - 3) * 8.314e-3)
+    assert np.abs(t_gpu / t_orc - 1).max() <= 1e-5
+    d = X - x
+    L = case.box.astype(np.float64)
+    d -= L * np.rint(d / L)
+    assert np.abs(d).max() <= 1e-4
+
+
+def test_velocity_verlet_energy_and_plain_form():
+    case = oracle.load(_write(synth.argon_fcc(ncell=5, seed=4, integrator="vv")))
+    x = case.pos.astype(np.float64).copy()
+    v = case.vel.astype(np.float64).copy()
+    st, rec = oracle.md_plain_run(case, x, v, 50, 1)
+    with gu.system_from_case(case, integrator=MD_VV) as sim:
+        sim.step(50, energy_every=1)
+        hist = sim.history(50)
+    ke = np.array([h["ke"] for h in hist])
+    pe = np.array([h["pe"] for h in hist])
+    assert np.abs(ke - rec[:, 0]).max() <= 1e-4 * np.abs(rec[:, 0]).max()
+    assert np.abs(pe - rec[:, 1]).max() <= 1e-4 * np.abs(rec[:, 1]).max()
+    e = ke + pe
+    assert np.ptp(e) <= 5e-3 * np.abs(pe).mean()
+
+
+def test_nose_hoover_conserved():
+    case = oracle.load(_write(synth.water_grid(nside=8, seed=8, integrator="nh", dt=0.5)))
+    x = case.pos.astype(np.float64).copy()
+    v = case.vel.astype(np.float64).copy()
+    st, rec = oracle.md_plain_run(case, x, v, 20, 2)
+    with gu.system_from_case(case, integrator=MD_NH) as sim:
+        sim.step(20, energy_every=1)
+        hist = sim.history(20)
+    cons = np.array([h["conserved"] for h in hist])
+    ke = np.array([h["ke"] for h in hist])
+    assert np.abs(ke - rec[:, 0]).max() <= 1e-4 * np.abs(rec[:, 0]).max()
+    assert np.abs(cons - rec[:, 2]).max() <= 1e-4 * np.abs(rec[:, 2]).max()
+    assert np.abs(np.array([h["xi"] for h in hist])).max() > 0
+
+
+def test_run_host_matches_step():
+    case = oracle.load(_write(synth.nacl_rocksalt(ncell=5, seed=12, nmaxlist=512)))
+    with gu.system_from_case(case) as a, gu.system_from_case(case) as b:
+        p0, v0 = a.positions(), a.velocities()
+        p, v, recs = a.run_host(p0, v0, 12)
+        b.step(12)
+        assert np.array_equal(p, b.positions())
+        assert np.array_equal(v, b.velocities())
+        assert [r["temper"] for r in recs] == [h["temper"] for h in b.history(12)]
+
+
+def test_list_rebuilds_keep_parity():
+    """After many steps (several rebuilds and re-sorts) the list is still the
+    O(N^2) reference list of the current positions."""
+    case = oracle.load(_write(synth.nacl_rocksalt(ncell=5, seed=21, nmaxlist=512)))
+    with gu.system_from_case(case) as sim:
+        sim.step(60)
+        info = sim.info()
+        assert info["builds"] >= 2
+        pos = sim.positions().astype(np.float32)
+        # the list was built at the last rebuild; rebuild now at the current positions
+        sim.update_neighbors(force=True)
+        nn, nm = sim.neighbor_list(512)
+    q = case.q
+    pos4 = np.concatenate([pos, (case.itype.astype(np.float32) + np.float32(0.1) * (q + np.float32(5.0)))[:, None]], 1)
+    pos4 = np.ascontiguousarray(pos4, np.float32)
+    p = case.params
+    onn, onm, _ = oracle.nlist(pos4, case.box, case.boxi, oracle.rskinsq(p.skin, p.rcutsq),
+                               oracle.exclusions(case.natom, case.bonds), 512)
+    n = case.natom
+    assert np.array_equal(nm[:n], onm[:n])
+    assert np.array_equal(gu.rows_canonical(nn, nm, n, 512), gu.rows_canonical(onn, onm, n, 512))
+
+
+@pytest.mark.parametrize("tpa", [1, 2, 8, 16])
+def test_thread_split_variants(tpa):
+    case = oracle.load(_write(synth.nacl_rocksalt(ncell=5, seed=30, nmaxlist=512)))
+    orc = gu.oracle_state(case)
+    with gu.system_from_case(case) as sim:
+        sim.set_tuning(tpa, tpa)
+        sim.update_neighbors(force=True)
+        sim.compute_forces(TERM_PAIR)
+        F = sim.forces()
+        nn, nm = sim.neighbor_list(512)
+    assert gu.rms_rel(F[:, :3], orc["f64"][:, :3]) <= FORCE_TOL
+    n = case.natom
+    assert np.array_equal(gu.rows_canonical(nn, nm, n, 512), gu.rows_canonical(orc["nn"], orc["nm"], n, 512))
+
+
+def test_full_size_nacl_64k():
+    """The 64000-ion system: bit-exact list, forces within tolerance, and
+    size-independent properties (momentum, Newton's third law in sum)."""
+    base = _write(synth.nacl_rocksalt(ncell=20, seed=1), "nacl64k")
+    case = oracle.load(base)
+    orc = gu.oracle_state(case)
+    from md_gpu_gb300 import MDSystem
+    with MDSystem.from_files(base) as sim:
+        nn, nm = sim.neighbor_list(512)
+        sim.compute_forces(TERM_PAIR)
+        F = sim.forces()
+    n = case.natom
+    assert np.array_equal(nm[:n], orc["nm"][:n])
+    assert np.array_equal(gu.rows_canonical(nn, nm, n, 512), gu.rows_canonical(orc["nn"], orc["nm"], n, 512))
+    assert gu.rms_rel(F[:, :3], orc["f64"][:, :3]) <= FORCE_TOL
+    assert np.abs(F[:, :3].sum(0)).max() <= 1e-3 * np.sqrt((F[:, :3] ** 2).sum(1)).mean() * np.sqrt(n)
