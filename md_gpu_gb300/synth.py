@@ -157,8 +157,10 @@ def nacl_rocksalt(ncell: int = 20, seed: int = 1, temp: float = 1200.0, density:
 
 def water_grid(nside: int = 32, seed: int = 1, temp: float = 300.0, rc: float = 10.0,
                skin: float = 1.0, alpha: float = 0.2, dt: float = 0.5, nsteps: int = 20000,
-               nmaxlist: int = 768, integrator: str = "nh") -> System:
-    """Flexible 3-site water, nside^3 molecules at 0.997 g/cm^3."""
+               nmaxlist: int = 768, integrator: str = "nh", h_jitter: float = 0.02) -> System:
+    """Flexible 3-site water, nside^3 molecules at 0.997 g/cm^3.  Hydrogens
+    are displaced uniformly by up to +-h_jitter A from the equilibrium
+    geometry (thermal bond stretches are ~0.02 A at 300 K)."""
     mO, mH = 15.9994, 1.008
     nmol = nside ** 3
     rho_mol = 0.997 / (mO + 2 * mH) * AVOGADRO * 1e-24
@@ -175,6 +177,8 @@ def water_grid(nside: int = 32, seed: int = 1, temp: float = 300.0, rc: float = 
     w /= np.linalg.norm(w, axis=1, keepdims=True)
     h1 = o + r0 * (np.cos(th0 / 2) * u + np.sin(th0 / 2) * w)
     h2 = o + r0 * (np.cos(th0 / 2) * u - np.sin(th0 / 2) * w)
+    h1 = h1 + rng.uniform(-h_jitter, h_jitter, h1.shape)
+    h2 = h2 + rng.uniform(-h_jitter, h_jitter, h2.shape)
     pos = np.empty((3 * nmol, 3))
     pos[0::3], pos[1::3], pos[2::3] = o, h1, h2
     itype = np.tile(np.array([1, 2, 2]), nmol)
