@@ -176,6 +176,20 @@ md_status md_time_pair(md_ctx *ctx, int nrep, float *ms_per_launch);
  * measured FP32-pipe peak the pair kernel is compared against. */
 md_status md_probe_fp32_peak(double *tflops);
 
+/* Kinetic energy and temperature of a velocity array in the reference's
+ * float4 layout (vx, vy, vz, m*1e4; the gpu_config vel buffer, config.h:114),
+ * without allocating any device memory.  No counterpart in the reference: it
+ * serves callers that cannot let a library call cudaMalloc, such as hosts that
+ * manage all device memory through their own allocator and budget, or step
+ * loops that must not risk the device synchronisation cudaMalloc/cudaFree can
+ * cause.  vel4 and out are device pointers supplied by the caller; out[0] =
+ * KE (kJ/mol, FP64 fixed-order sum), out[1] = T = 2 KE / ((3N-3) R).  Scratch
+ * is a fixed 32 KB __device__ array shared by all calls: at most 1,048,576
+ * atoms (larger calls return MD_ERR_ARG), and calls that overlap on the GPU
+ * race.  The first call on a device resolves the array's address; make it
+ * before any stream capture.  stream: cudaStream_t or NULL. */
+md_status md_ref_kinetic_energy_noalloc(const void *vel4, int natom, double *out, void *stream);
+
 #ifdef __cplusplus
 }
 #endif

@@ -349,6 +349,8 @@ md_status refresh_state(md_ctx *c)
 
 }  // namespace
 
+void md_set_global_error(const std::string &msg) { g_last_error = msg; }
+
 md_kparams md_make_kparams(const md_ctx *c)
 {
     md_kparams kp;

@@ -135,6 +135,8 @@ struct md_ctx {
 };
 
 md_kparams md_make_kparams(const md_ctx *c);
+/* Message returned by md_last_error(NULL, ...). */
+void md_set_global_error(const std::string &msg);
 
 /* ---- launchers (k_cells.cu) ---- */
 void launch_check(md_ctx *c, const md_kparams &kp);

@@ -98,6 +98,7 @@ def library(path: Optional[str] = None):
     L.md_last_error.argtypes = [vp, C.c_char_p, C.c_int]
     L.md_time_pair.argtypes = [vp, C.c_int, C.POINTER(C.c_float)]
     L.md_probe_fp32_peak.argtypes = [C.POINTER(C.c_double)]
+    L.md_ref_kinetic_energy_noalloc.argtypes = [vp, C.c_int, vp, vp]
     _lib = L
     return L
 
