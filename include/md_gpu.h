@@ -163,8 +163,9 @@ md_status md_get_info(md_ctx *ctx, md_info *out);
 md_status md_get_order(md_ctx *ctx, int *perm);
 /* Hilbert rank of every cell (linear index x + nx*(y + ny*z)). */
 md_status md_get_cell_ranks(md_ctx *ctx, int *rank);
-/* Tuning knobs (threads per atom of the pair kernel and of the list build);
- * values must be 1, 2, 4, 8, 16 or 32. */
+/* Tuning knobs: threads per atom of the pair kernel (1, 2, 4, 8, 16, 32) and
+ * the list builder (0 = one warp per cell, the default; or 1..32 threads per
+ * atom).  Every setting builds the identical list. */
 md_status md_set_tuning(md_ctx *ctx, int pair_tpa, int list_tpa);
 /* Milliseconds of device time of the last md_step call (CUDA events). */
 md_status md_last_step_ms(md_ctx *ctx, float *ms);

@@ -11,7 +11,7 @@
  * (cells of side >= rl/2), the atoms are re-sorted along a Hilbert curve of
  * cells at every build, and the rebuild decision never leaves the device.
  */
-#include "md_internal.h"
+#include "md_device.cuh"
 
 namespace {
 
@@ -24,24 +24,12 @@ __device__ __forceinline__ int cell_of(float x, float box, float binlen, int nc)
     return c >= nc ? nc - 1 : c;
 }
 
-/* min-image r^2 with every operation rounded separately (no contraction). */
-__device__ __forceinline__ float rsq_exact(float4 a, float4 b, const md_kparams &kp)
-{
-    float dx = __fsub_rn(a.x, b.x);
-    float dy = __fsub_rn(a.y, b.y);
-    float dz = __fsub_rn(a.z, b.z);
-    dx = __fsub_rn(dx, __fmul_rn(kp.box[0], rintf(__fmul_rn(dx, kp.boxi[0]))));
-    dy = __fsub_rn(dy, __fmul_rn(kp.box[1], rintf(__fmul_rn(dy, kp.boxi[1]))));
-    dz = __fsub_rn(dz, __fmul_rn(kp.box[2], rintf(__fmul_rn(dz, kp.boxi[2]))));
-    return __fadd_rn(__fadd_rn(__fmul_rn(dx, dx), __fmul_rn(dy, dy)), __fmul_rn(dz, dz));
-}
-
 __global__ void k_check(md_kparams kp, const float4 *__restrict__ pos4,
                         const float4 *__restrict__ pos_old, md_devstate *st)
 {
     int i = blockIdx.x * blockDim.x + threadIdx.x;
     if (i >= kp.n) return;
-    if (rsq_exact(pos4[i], pos_old[i], kp) >= kp.rmaxdif) st->update = 1;
+    if (md_rsq_exact(pos4[i], pos_old[i], kp) >= kp.rmaxdif) st->update = 1;
 }
 
 /* Cell rank (Hilbert order) of every atom and the per-cell counts. */
@@ -202,6 +190,17 @@ __global__ void k_remap(md_kparams kp, const md_devstate *st, int always,
     }
 }
 
+/* Ends a rebuild (or a step without one): the next step's check sets the
+ * request again. */
+__global__ void k_clear_update(md_devstate *st) { st->update = 0; }
+
+/* First node of a captured step graph: the rebuild condition of its first
+ * step comes from the check done by the step before the graph. */
+__global__ void k_set_condition(cudaGraphConditionalHandle h, const md_devstate *st)
+{
+    cudaGraphSetConditional(h, st->update ? 1u : 0u);
+}
+
 /* List build: TPA lanes per atom scan the stencil cells; lane l tests the
  * candidates l, l+TPA, ... of each cell and the lanes append their hits in
  * candidate order with a ballot, so the list order is fixed by the cell
@@ -251,7 +250,7 @@ __global__ void __launch_bounds__(256) k_build_list(
                         float4 q = pos4[j];
                         unsigned uj = (unsigned)j;
                         int tj = type[j];
-                        ok = rsq_exact(p, q, kp) < kp.rskinsq && j != i && uj != ex.x &&
+                        ok = md_rsq_exact(p, q, kp) < kp.rskinsq && j != i && uj != ex.x &&
                              uj != ex.y && uj != ex.z && uj != ex.w && !((tmask >> tj) & 1u);
                         entry = uj | ((unsigned)tj << MD_TYPE_SHIFT);
                     }
@@ -269,6 +268,94 @@ __global__ void __launch_bounds__(256) k_build_list(
         nl_n[i] = cnt < kp.cap ? cnt : kp.cap;
         pos_old[i] = p;
         if (cnt > kp.cap) atomicMax(&st->list_overflow, cnt);
+    }
+}
+
+/* List build, one warp per cell: every atom of a cell shares the cell's
+ * stencil, so the warp streams each stencil cell's atoms once (lane = j) and
+ * tests them against the cell's atoms (held in shared memory) one i at a
+ * time; a ballot appends the hits to i's list.  Entries land in the same
+ * order as in k_build_list (stencil cells in traversal order, ascending j),
+ * so both builders produce identical lists. */
+constexpr int CW_WARPS = 4;
+constexpr int CW_MAXI = 32;
+
+__global__ void __launch_bounds__(CW_WARPS * 32) k_build_cells(
+    md_kparams kp, md_devstate *st, int always, int ncells, const float4 *__restrict__ pos4,
+    const int *__restrict__ type, const uint4 *__restrict__ excl_s,
+    const int *__restrict__ cell_rank, const int *__restrict__ cell_lin,
+    const int *__restrict__ cell_start, const unsigned *__restrict__ type_mask, unsigned *nl,
+    int *nl_n, float4 *pos_old)
+{
+    if (!always && !st->update) return;
+    __shared__ float4 s_p[CW_WARPS][CW_MAXI];
+    __shared__ uint4 s_ex[CW_WARPS][CW_MAXI];
+    __shared__ unsigned s_tm[CW_WARPS][CW_MAXI];
+    const int w = threadIdx.x >> 5, lane = threadIdx.x & 31;
+    const int r = blockIdx.x * CW_WARPS + w;
+    if (r >= ncells) return;
+    const int ib = cell_start[r], ie = cell_start[r + 1];
+    if (ib == ie) return;
+    const int lin = cell_lin[r];
+    const int nx = kp.ncell[0], ny = kp.ncell[1], nz = kp.ncell[2];
+    const int c3[3] = {lin % nx, (lin / nx) % ny, lin / (nx * ny)};
+    int lo[3], hi[3];
+    for (int d = 0; d < 3; d++) {
+        if (kp.stencil[d] < 0) { lo[d] = 0; hi[d] = kp.ncell[d] - 1; }
+        else { lo[d] = c3[d] - kp.stencil[d]; hi[d] = c3[d] + kp.stencil[d]; }
+    }
+    const unsigned lt = (1u << lane) - 1u;
+    const size_t P = (size_t)kp.pitch;
+    for (int i0 = ib; i0 < ie; i0 += CW_MAXI) {
+        const int ni = min(CW_MAXI, ie - i0);
+        if (lane < ni) {
+            int i = i0 + lane;
+            s_p[w][lane] = pos4[i];
+            s_ex[w][lane] = excl_s[i];
+            s_tm[w][lane] = type_mask[type[i]];
+        }
+        __syncwarp();
+        int mycnt = 0;   /* list length of atom i0 + lane */
+        for (int zz = lo[2]; zz <= hi[2]; zz++) {
+            int cz = zz < 0 ? zz + nz : (zz >= nz ? zz - nz : zz);
+            for (int yy = lo[1]; yy <= hi[1]; yy++) {
+                int cy = yy < 0 ? yy + ny : (yy >= ny ? yy - ny : yy);
+                for (int xx = lo[0]; xx <= hi[0]; xx++) {
+                    int cx = xx < 0 ? xx + nx : (xx >= nx ? xx - nx : xx);
+                    int r2 = cell_rank[cx + nx * (cy + ny * cz)];
+                    int jb = cell_start[r2], je = cell_start[r2 + 1];
+                    for (int j0 = jb; j0 < je; j0 += 32) {
+                        int j = j0 + lane;
+                        bool vj = j < je;
+                        float4 q = vj ? pos4[j] : make_float4(0.f, 0.f, 0.f, 0.f);
+                        int tj = vj ? type[j] : 0;
+                        unsigned entry = (unsigned)j | ((unsigned)tj << MD_TYPE_SHIFT);
+                        for (int a = 0; a < ni; a++) {
+                            float4 p = s_p[w][a];
+                            uint4 ex = s_ex[w][a];
+                            unsigned uj = (unsigned)j;
+                            bool ok = vj && md_rsq_exact(p, q, kp) < kp.rskinsq && j != i0 + a &&
+                                      uj != ex.x && uj != ex.y && uj != ex.z && uj != ex.w &&
+                                      !((s_tm[w][a] >> tj) & 1u);
+                            unsigned bal = __ballot_sync(0xffffffffu, ok);
+                            int base = __shfl_sync(0xffffffffu, mycnt, a);
+                            if (ok) {
+                                int slot = base + __popc(bal & lt);
+                                if (slot < kp.cap) nl[(size_t)slot * P + i0 + a] = entry;
+                            }
+                            if (lane == a) mycnt += __popc(bal);
+                        }
+                    }
+                }
+            }
+        }
+        if (lane < ni) {
+            int i = i0 + lane;
+            nl_n[i] = mycnt < kp.cap ? mycnt : kp.cap;
+            pos_old[i] = s_p[w][lane];
+            if (mycnt > kp.cap) atomicMax(&st->list_overflow, mycnt);
+        }
+        __syncwarp();
     }
 }
 
@@ -301,6 +388,11 @@ void launch_rebuild(md_ctx *c, const md_kparams &kp, bool unconditional)
     long long threads = (long long)kp.n * c->list_tpa;
     int lb = (int)((threads + 255) / 256);
     switch (c->list_tpa) {
+    case 0:
+        k_build_cells<<<(c->ncells + CW_WARPS - 1) / CW_WARPS, CW_WARPS * 32, 0, s>>>(
+            kp, c->st, always, c->ncells, c->pos4, c->type, c->excl_s, c->cell_rank, c->cell_lin,
+            c->cell_start, c->type_mask_dev, c->nl, c->nl_n, c->pos_old);
+        break;
 #define MD_LIST_CASE(T)                                                                            \
     case T:                                                                                        \
         k_build_list<T><<<lb, 256, 0, s>>>(kp, c->st, always, c->pos4, c->type, c->excl_s,         \
@@ -317,4 +409,10 @@ void launch_rebuild(md_ctx *c, const md_kparams &kp, bool unconditional)
     default:
         break;
     }
+    k_clear_update<<<1, 1, 0, s>>>(c->st);
+}
+
+void launch_set_condition(md_ctx *c, unsigned long long handle)
+{
+    k_set_condition<<<1, 1, 0, c->stream>>>((cudaGraphConditionalHandle)handle, c->st);
 }

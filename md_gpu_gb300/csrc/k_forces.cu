@@ -33,7 +33,20 @@ struct pair_consts {
     float rcinv;   /* 1/rc */
 };
 
-template <int KIND, int TPA, bool ENERGY>
+/* Round to nearest even for |t| < 2^22 with two FP32 adds (no conversion
+ * instruction): the minimum-image shift rint(d / L). */
+__device__ __forceinline__ float rint_small(float t)
+{
+    const float M = 12582912.0f;   /* 1.5 * 2^23 */
+    return __fsub_rn(__fadd_rn(t, M), M);
+}
+
+/* Pair forces of atom i from its list: TPA lanes per atom, lane l takes the
+ * entries l, l+TPA, ...  Each lane loads B list entries and then B
+ * positions before computing, so B independent loads are in flight; it sums
+ * in FP32 and converts its sum to int64 once.  Lane sums are combined with
+ * integer shuffles (exact), so the result depends only on TPA. */
+template <int KIND, int TPA, int B, bool ENERGY>
 __global__ void __launch_bounds__(128) k_pair(md_kparams kp, pair_consts pc,
                                               const float4 *__restrict__ pos4,
                                               const int *__restrict__ type,
@@ -45,37 +58,43 @@ __global__ void __launch_bounds__(128) k_pair(md_kparams kp, pair_consts pc,
     __shared__ float2 lj[MD_MAXTYPE * MD_MAXTYPE];
     if (threadIdx.x < MD_MAXTYPE * MD_MAXTYPE) lj[threadIdx.x] = ljtab[threadIdx.x];
     __syncthreads();
-    constexpr int CH = 8;
     int gt = blockIdx.x * blockDim.x + threadIdx.x;
     int i = gt / TPA, lane = gt % TPA;
     bool active = i < kp.n;
     int ii = active ? i : 0;
-    float4 pi = pos4[ii];
-    int cnt = active ? nl_n[ii] : 0;
+    const float4 pi = pos4[ii];
+    const int cnt = active ? nl_n[ii] : 0;
     const float2 *ljrow = lj + type[ii] * MD_MAXTYPE;
     const float qi = QFAC * pi.w;
     const float L0 = kp.box[0], L1 = kp.box[1], L2 = kp.box[2];
     const float I0 = kp.boxi[0], I1 = kp.boxi[1], I2 = kp.boxi[2];
-    long long ax = 0, ay = 0, az = 0;
-    float aw = 0.0f, ae = 0.0f;
+    const float rcsq = kp.rcutsq;
+    float fx = 0.0f, fy = 0.0f, fz = 0.0f, fw = 0.0f, fe = 0.0f;
     const size_t P = (size_t)kp.pitch;
-    for (int k0 = lane; k0 < cnt; k0 += TPA * CH) {
-        float fx = 0.0f, fy = 0.0f, fz = 0.0f;
+    const unsigned *lp = nl + (size_t)lane * P + ii;
+    for (int k0 = lane; k0 < cnt; k0 += TPA * B) {
+        unsigned e[B];
 #pragma unroll
-        for (int c = 0; c < CH; c++) {
-            int k = k0 + c * TPA;
-            if (k >= cnt) break;
-            unsigned e = nl[(size_t)k * P + i];
-            float4 pj = pos4[e & MD_INDEX_MASK];
-            float2 l = ljrow[e >> MD_TYPE_SHIFT];
-            float dx = pi.x - pj.x, dy = pi.y - pj.y, dz = pi.z - pj.z;
-            dx -= L0 * rintf(dx * I0);
-            dy -= L1 * rintf(dy * I1);
-            dz -= L2 * rintf(dz * I2);
+        for (int b = 0; b < B; b++) {
+            int k = k0 + b * TPA;
+            e[b] = (k < cnt) ? __ldg(lp + (size_t)b * TPA * P) : (unsigned)ii;
+        }
+        lp += (size_t)TPA * B * P;
+        float4 pj[B];
+#pragma unroll
+        for (int b = 0; b < B; b++) pj[b] = __ldg(pos4 + (e[b] & MD_INDEX_MASK));
+#pragma unroll
+        for (int b = 0; b < B; b++) {
+            bool valid = k0 + b * TPA < cnt;
+            float2 l = ljrow[e[b] >> MD_TYPE_SHIFT];
+            float dx = pi.x - pj[b].x, dy = pi.y - pj[b].y, dz = pi.z - pj[b].z;
+            dx -= L0 * rint_small(dx * I0);
+            dy -= L1 * rint_small(dy * I1);
+            dz -= L2 * rint_small(dz * I2);
             float rsq = dx * dx + dy * dy + dz * dz;
             float ri = rsqrtf(rsq);
             float ri2 = ri * ri;
-            float qq = qi * pj.w;
+            float qq = qi * pj[b].w;
             float ff, uc = 0.0f;
             if (KIND == 1) {
                 float r = rsq * ri;
@@ -90,39 +109,39 @@ __global__ void __launch_bounds__(128) k_pair(md_kparams kp, pair_consts pc,
             }
             float ri6 = ri2 * ri2 * ri2;
             ff = ff * ri2 + (l.x * ri6 - l.y) * ri6 * ri2;
-            bool in = rsq <= kp.rcutsq;
+            bool in = valid && rsq <= rcsq;
             ff = in ? ff : 0.0f;
             fx += ff * dx;
             fy += ff * dy;
             fz += ff * dz;
-            aw += ff * rsq;
+            fw += ff * rsq;
             if (ENERGY) {
                 float ulj = l.x * (1.0f / 12.0f) * (ri6 * ri6 - pc.rc6i * pc.rc6i) -
                             l.y * (1.0f / 6.0f) * (ri6 - pc.rc6i);
-                ae += in ? 0.5f * (uc + ulj) : 0.0f;
+                fe += in ? 0.5f * (uc + ulj) : 0.0f;
             }
         }
-        ax += __float2ll_rn(fx * 4294967296.0f);
-        ay += __float2ll_rn(fy * 4294967296.0f);
-        az += __float2ll_rn(fz * 4294967296.0f);
     }
+    long long ax = __float2ll_rn(fx * 4294967296.0f);
+    long long ay = __float2ll_rn(fy * 4294967296.0f);
+    long long az = __float2ll_rn(fz * 4294967296.0f);
     if (TPA > 1) {
-        unsigned mask = 0xffffffffu;
+        const unsigned mask = 0xffffffffu;
 #pragma unroll
         for (int off = TPA / 2; off > 0; off >>= 1) {
             ax += __shfl_down_sync(mask, ax, off, TPA);
             ay += __shfl_down_sync(mask, ay, off, TPA);
             az += __shfl_down_sync(mask, az, off, TPA);
-            aw += __shfl_down_sync(mask, aw, off, TPA);
-            if (ENERGY) ae += __shfl_down_sync(mask, ae, off, TPA);
+            fw += __shfl_down_sync(mask, fw, off, TPA);
+            if (ENERGY) fe += __shfl_down_sync(mask, fe, off, TPA);
         }
     }
     if (active && lane == 0) {
         f[i] = ax;
         f[P + i] = ay;
         f[2 * P + i] = az;
-        vir[i] = aw;
-        if (ENERGY) epot[i] = ae;
+        vir[i] = fw;
+        if (ENERGY) epot[i] = fe;
     }
 }
 
@@ -209,8 +228,8 @@ void pair_dispatch(md_ctx *c, const md_kparams &kp, const pair_consts &pc)
     switch (c->pair_tpa) {
 #define MD_PAIR_CASE(T)                                                                          \
     case T:                                                                                      \
-        k_pair<KIND, T, ENERGY><<<nb, 128, 0, c->stream>>>(kp, pc, c->pos4, c->type, c->nl,      \
-                                                           c->nl_n, lj, c->f, c->vir, c->epot);  \
+        k_pair<KIND, T, (T >= 8 ? 4 : 8), ENERGY><<<nb, 128, 0, c->stream>>>(                      \
+            kp, pc, c->pos4, c->type, c->nl, c->nl_n, lj, c->f, c->vir, c->epot);                \
         break;
         MD_PAIR_CASE(1)
         MD_PAIR_CASE(2)

@@ -6,17 +6,22 @@
  * with lambda = sqrt(1 + dt/tau (T0/T_prev - 1)) for Berendsen NVT
  * (integrator.cu:146-147, tau = 100 fs there) and 1 for NVE.  Positions and
  * velocities are FP64 here; the FP32 copy pos4 is refreshed in the same pass.
- * The kinetic energy is reduced in FP64, per block then in one block in a
- * fixed order (replacing the reference's single-block FP32 tree,
+ * The kinetic energy is reduced in FP64, per block then by the last block to
+ * finish in a fixed order (replacing the reference's single-block FP32 tree,
  * nvt_leapfrog_ber.cu:83-110, whose width is the block count).
  *
- * Velocity Verlet: half kick + drift, forces, half kick.  Nose-Hoover adds a
- * thermostat half step on each side (single thermostat, Trotter splitting):
+ * The same pass performs the next step's neighbour-list check (any atom moved
+ * >= skin/2 since the last build, neighborlist.cu:157-176) and, inside a
+ * captured step graph, sets the condition of the rebuild node that follows.
+ *
+ * Velocity Verlet: half kick + drift (+ list check), forces, half kick.
+ * Nose-Hoover adds a thermostat half step on each side (one thermostat,
+ * Trotter splitting):
  *   xi += G dt/4;  v *= exp(-xi dt/2);  eta += xi dt/2;  xi += G dt/4,
  *   G = (2 KE - ndf k T0) / Q,  Q = ndf k T0 tau^2,
  * with the conserved quantity KE + PE + Q xi^2/2 + ndf k T0 eta.
  */
-#include "md_internal.h"
+#include "md_device.cuh"
 
 namespace {
 
@@ -25,6 +30,18 @@ constexpr double RGAS = 8.314e-3;   /* kJ/mol/K, as integrator.cu:155 (1000/8.31
 struct thermo_par {
     double t0, tau, q_nh;
     int ndf, berendsen, nh, energy;
+};
+
+/* Per-step bookkeeping buffers and the graph condition to set. */
+struct step_io {
+    md_devstate *st;
+    double *partials;
+    md_thermo *rec;
+    int rec_cap;
+    unsigned *counter;
+    const float4 *pos_old;
+    cudaGraphConditionalHandle cond;
+    int has_cond;
 };
 
 /* Sum of a double over the block; result valid in thread 0. */
@@ -46,39 +63,12 @@ __device__ __forceinline__ double wrap(double x, double L)
     return x - L * trunc(x * 2.0 / L);
 }
 
-__global__ void __launch_bounds__(256) k_leapfrog(md_kparams kp, thermo_par tp,
-                                                  const md_devstate *st, double *x, double *v,
-                                                  const double *__restrict__ mass, float4 *pos4,
-                                                  const long long *__restrict__ f,
-                                                  const float *__restrict__ epot,
-                                                  const float *__restrict__ vir, double *partials)
+__device__ __forceinline__ void write_partials(double ke, double pe, double w, int energy,
+                                               double *partials, double *sh)
 {
-    __shared__ double sh[8];
-    int s = blockIdx.x * blockDim.x + threadIdx.x;
-    const int P = kp.pitch;
-    double lam = 1.0;
-    if (tp.berendsen) lam = sqrt(1.0 + kp.dt / tp.tau * (tp.t0 / st->temper - 1.0));
-    double ke = 0.0, pe = 0.0, w = 0.0;
-    if (s < kp.n) {
-        double m = mass[s], dtm = kp.dt / m;
-        double xn[3];
-        for (int d = 0; d < 3; d++) {
-            double F = (double)f[d * P + s] * FX_INV;
-            double vv = (v[d * P + s] + F * dtm) * lam;
-            v[d * P + s] = vv;
-            double xx = wrap(x[d * P + s] + vv * kp.dt, kp.boxd[d]);
-            x[d * P + s] = xx;
-            xn[d] = xx;
-            ke += vv * vv;
-        }
-        ke *= 0.5 * m;
-        float4 p = pos4[s];
-        pos4[s] = make_float4((float)xn[0], (float)xn[1], (float)xn[2], p.w);
-        if (tp.energy) { pe = epot[s]; w = vir[s]; }
-    }
     double a = block_sum(ke, sh);
     if (threadIdx.x == 0) partials[blockIdx.x] = a;
-    if (tp.energy) {
+    if (energy) {
         double b = block_sum(pe, sh);
         double c = block_sum(w, sh);
         if (threadIdx.x == 0) {
@@ -88,109 +78,32 @@ __global__ void __launch_bounds__(256) k_leapfrog(md_kparams kp, thermo_par tp,
     }
 }
 
-/* Velocity Verlet first half: thermostat half step (NH), half kick, drift. */
-__global__ void __launch_bounds__(256) k_vv_first(md_kparams kp, thermo_par tp, md_devstate *st,
-                                                  double *x, double *v,
-                                                  const double *__restrict__ mass, float4 *pos4,
-                                                  const long long *__restrict__ f)
+/* Fixed-order totals of the block partials, then (thread 0) temperature,
+ * thermostat bookkeeping and the step record.  mode 0 leapfrog, 1 VV / NH,
+ * 2 observe only (no step, the Berendsen reference temperature kept). */
+__device__ void finalize(const md_kparams &kp, const thermo_par &tp, int mode, int npart,
+                         const double *partials, md_devstate *st, md_thermo *rec, int rec_cap,
+                         double *sh)
 {
-    int s = blockIdx.x * blockDim.x + threadIdx.x;
-    const int P = kp.pitch;
-    double scale = st->vscale;
-    if (tp.nh) {
-        /* every thread evaluates the same scalar update; one thread stores it */
-        double kt = RGAS * tp.t0, ke = st->ke, xi = st->xi, eta = st->eta;
-        xi += 0.25 * kp.dt * (2.0 * ke - tp.ndf * kt) / tp.q_nh;
-        double s1 = exp(-0.5 * kp.dt * xi);
-        ke *= s1 * s1;
-        eta += 0.5 * kp.dt * xi;
-        xi += 0.25 * kp.dt * (2.0 * ke - tp.ndf * kt) / tp.q_nh;
-        scale *= s1;
-        if (s == 0) { st->xi_a = xi; st->eta_a = eta; }
-    }
-    if (s >= kp.n) return;
-    double m = mass[s], hdtm = 0.5 * kp.dt / m;
-    double xn[3];
-    for (int d = 0; d < 3; d++) {
-        double F = (double)f[d * P + s] * FX_INV;
-        double vv = v[d * P + s] * scale + F * hdtm;
-        v[d * P + s] = vv;
-        double xx = wrap(x[d * P + s] + vv * kp.dt, kp.boxd[d]);
-        x[d * P + s] = xx;
-        xn[d] = xx;
-    }
-    float4 p = pos4[s];
-    pos4[s] = make_float4((float)xn[0], (float)xn[1], (float)xn[2], p.w);
-}
-
-/* Velocity Verlet second half kick and the block partials of KE (and PE,
- * virial); scale != 1 only for the state read-out kernel below. */
-__global__ void __launch_bounds__(256) k_vv_second(md_kparams kp, thermo_par tp, int kick,
-                                                   const md_devstate *st, double *v,
-                                                   const double *__restrict__ mass,
-                                                   const long long *__restrict__ f,
-                                                   const float *__restrict__ epot,
-                                                   const float *__restrict__ vir,
-                                                   double *partials)
-{
-    __shared__ double sh[8];
-    int s = blockIdx.x * blockDim.x + threadIdx.x;
-    const int P = kp.pitch;
-    double ke = 0.0, pe = 0.0, w = 0.0;
-    double scale = kick ? 1.0 : st->vscale;
-    if (s < kp.n) {
-        double m = mass[s], hdtm = 0.5 * kp.dt / m;
-        for (int d = 0; d < 3; d++) {
-            double vv = v[d * P + s];
-            if (kick) {
-                vv += (double)f[d * P + s] * FX_INV * hdtm;
-                v[d * P + s] = vv;
-            } else {
-                vv *= scale;
-            }
-            ke += vv * vv;
-        }
-        ke *= 0.5 * m;
-        if (tp.energy) { pe = epot[s]; w = vir[s]; }
-    }
-    double a = block_sum(ke, sh);
-    if (threadIdx.x == 0) partials[blockIdx.x] = a;
-    if (tp.energy) {
-        double b = block_sum(pe, sh);
-        double c = block_sum(w, sh);
-        if (threadIdx.x == 0) {
-            partials[gridDim.x + blockIdx.x] = b;
-            partials[2 * gridDim.x + blockIdx.x] = c;
-        }
-    }
-}
-
-/* One block: fixed-order sums of the partials, temperature, thermostat
- * bookkeeping and the step record.  mode 0 leapfrog, 1 VV / NH, 2 observe
- * only (no step). */
-__global__ void __launch_bounds__(256) k_finalize(md_kparams kp, thermo_par tp, int mode,
-                                                  int npart, const double *__restrict__ partials,
-                                                  md_devstate *st, md_thermo *rec, int rec_cap)
-{
-    __shared__ double sh[8];
     double a = 0.0, b = 0.0, c = 0.0;
     for (int k = threadIdx.x; k < npart; k += blockDim.x) {
-        a += partials[k];
-        if (tp.energy) { b += partials[npart + k]; c += partials[2 * npart + k]; }
+        a += __ldcg(partials + k);
+        if (tp.energy) { b += __ldcg(partials + npart + k); c += __ldcg(partials + 2 * npart + k); }
     }
     double ke = block_sum(a, sh);
     double pe = tp.energy ? block_sum(b, sh) : 0.0;
     double w = tp.energy ? block_sum(c, sh) : 0.0;
     if (threadIdx.x != 0) return;
+    volatile md_devstate *vs = st;
     double kt = RGAS * tp.t0;
     double lam = 1.0;
-    if (mode == 0 && tp.berendsen) lam = sqrt(1.0 + kp.dt / tp.tau * (tp.t0 / st->temper - 1.0));
-    double xi = st->xi, eta = st->eta;
+    if (mode == 0 && tp.berendsen) lam = sqrt(1.0 + kp.dt / tp.tau * (tp.t0 / vs->temper - 1.0));
+    double xi = vs->xi, eta = vs->eta;
     if (mode == 1) {
         st->vscale = 1.0;
         if (tp.nh) {
-            xi = st->xi_a;
-            eta = st->eta_a;
+            xi = vs->xi_a;
+            eta = vs->eta_a;
             xi += 0.25 * kp.dt * (2.0 * ke - tp.ndf * kt) / tp.q_nh;
             double s2 = exp(-0.5 * kp.dt * xi);
             ke *= s2 * s2;
@@ -209,7 +122,7 @@ __global__ void __launch_bounds__(256) k_finalize(md_kparams kp, thermo_par tp, 
     if (mode == 2) return;
     st->temper = temper;
     st->lambda = lam;
-    long long step = st->step;
+    long long step = vs->step;
     md_thermo r;
     r.step = step;
     r.ke = ke;
@@ -219,10 +132,150 @@ __global__ void __launch_bounds__(256) k_finalize(md_kparams kp, thermo_par tp, 
     r.conserved = tp.energy ? ke + pe + (tp.nh ? 0.5 * tp.q_nh * xi * xi + tp.ndf * kt * eta : 0.0) : 0.0;
     r.xi = xi;
     r.lambda = lam;
-    r.builds = st->builds;
+    r.builds = vs->builds;
     r.flags = tp.energy ? 1 : 0;
     rec[step % rec_cap] = r;
     st->step = step + 1;
+}
+
+__device__ __forceinline__ void check_moved(float4 p, float4 old, const md_kparams &kp,
+                                            md_devstate *st)
+{
+    if (md_rsq_exact(p, old, kp) >= kp.rmaxdif) st->update = 1;
+}
+
+__device__ __forceinline__ void set_condition(const step_io &io)
+{
+    if (io.has_cond) {
+        volatile md_devstate *vs = io.st;
+        cudaGraphSetConditional(io.cond, vs->update ? 1u : 0u);
+    }
+}
+
+/* Leapfrog update + list check + KE partials; the last block finalises. */
+__global__ void __launch_bounds__(256) k_leapfrog(md_kparams kp, thermo_par tp, step_io io,
+                                                  double *x, double *v,
+                                                  const double *__restrict__ mass, float4 *pos4,
+                                                  const long long *__restrict__ f,
+                                                  const float *__restrict__ epot,
+                                                  const float *__restrict__ vir)
+{
+    __shared__ double sh[8];
+    int s = blockIdx.x * blockDim.x + threadIdx.x;
+    const int P = kp.pitch;
+    double lam = 1.0;
+    if (tp.berendsen) lam = sqrt(1.0 + kp.dt / tp.tau * (tp.t0 / io.st->temper - 1.0));
+    double ke = 0.0, pe = 0.0, w = 0.0;
+    if (s < kp.n) {
+        double m = mass[s], dtm = kp.dt / m;
+        double xn[3];
+        for (int d = 0; d < 3; d++) {
+            double F = (double)f[d * P + s] * FX_INV;
+            double vv = (v[d * P + s] + F * dtm) * lam;
+            v[d * P + s] = vv;
+            double xx = wrap(x[d * P + s] + vv * kp.dt, kp.boxd[d]);
+            x[d * P + s] = xx;
+            xn[d] = xx;
+            ke += vv * vv;
+        }
+        ke *= 0.5 * m;
+        float4 p = pos4[s];
+        p = make_float4((float)xn[0], (float)xn[1], (float)xn[2], p.w);
+        pos4[s] = p;
+        check_moved(p, io.pos_old[s], kp, io.st);
+        if (tp.energy) { pe = epot[s]; w = vir[s]; }
+    }
+    write_partials(ke, pe, w, tp.energy, io.partials, sh);
+    if (md_last_block(io.counter)) {
+        finalize(kp, tp, 0, gridDim.x, io.partials, io.st, io.rec, io.rec_cap, sh);
+        if (threadIdx.x == 0) {
+            set_condition(io);
+            *io.counter = 0;
+        }
+    }
+}
+
+/* Velocity Verlet first half: thermostat half step (NH), half kick, drift,
+ * list check; the last block sets the rebuild condition. */
+__global__ void __launch_bounds__(256) k_vv_first(md_kparams kp, thermo_par tp, step_io io,
+                                                  double *x, double *v,
+                                                  const double *__restrict__ mass, float4 *pos4,
+                                                  const long long *__restrict__ f)
+{
+    int s = blockIdx.x * blockDim.x + threadIdx.x;
+    const int P = kp.pitch;
+    md_devstate *st = io.st;
+    double scale = st->vscale;
+    if (tp.nh) {
+        /* every thread evaluates the same scalar update; one thread stores it */
+        double kt = RGAS * tp.t0, ke = st->ke, xi = st->xi, eta = st->eta;
+        xi += 0.25 * kp.dt * (2.0 * ke - tp.ndf * kt) / tp.q_nh;
+        double s1 = exp(-0.5 * kp.dt * xi);
+        ke *= s1 * s1;
+        eta += 0.5 * kp.dt * xi;
+        xi += 0.25 * kp.dt * (2.0 * ke - tp.ndf * kt) / tp.q_nh;
+        scale *= s1;
+        if (s == 0) { st->xi_a = xi; st->eta_a = eta; }
+    }
+    if (s < kp.n) {
+        double m = mass[s], hdtm = 0.5 * kp.dt / m;
+        double xn[3];
+        for (int d = 0; d < 3; d++) {
+            double F = (double)f[d * P + s] * FX_INV;
+            double vv = v[d * P + s] * scale + F * hdtm;
+            v[d * P + s] = vv;
+            double xx = wrap(x[d * P + s] + vv * kp.dt, kp.boxd[d]);
+            x[d * P + s] = xx;
+            xn[d] = xx;
+        }
+        float4 p = pos4[s];
+        p = make_float4((float)xn[0], (float)xn[1], (float)xn[2], p.w);
+        pos4[s] = p;
+        check_moved(p, io.pos_old[s], kp, st);
+    }
+    if (md_last_block(io.counter)) {
+        if (threadIdx.x == 0) {
+            set_condition(io);
+            *io.counter = 0;
+        }
+    }
+}
+
+/* Velocity Verlet second half kick and KE (PE, virial) partials; the last
+ * block finalises.  kick = 0: observe the state only (pending NH scale
+ * applied), mode 2. */
+__global__ void __launch_bounds__(256) k_vv_second(md_kparams kp, thermo_par tp, int kick,
+                                                   step_io io, double *v,
+                                                   const double *__restrict__ mass,
+                                                   const long long *__restrict__ f,
+                                                   const float *__restrict__ epot,
+                                                   const float *__restrict__ vir)
+{
+    __shared__ double sh[8];
+    int s = blockIdx.x * blockDim.x + threadIdx.x;
+    const int P = kp.pitch;
+    double ke = 0.0, pe = 0.0, w = 0.0;
+    double scale = kick ? 1.0 : io.st->vscale;
+    if (s < kp.n) {
+        double m = mass[s], hdtm = 0.5 * kp.dt / m;
+        for (int d = 0; d < 3; d++) {
+            double vv = v[d * P + s];
+            if (kick) {
+                vv += (double)f[d * P + s] * FX_INV * hdtm;
+                v[d * P + s] = vv;
+            } else {
+                vv *= scale;
+            }
+            ke += vv * vv;
+        }
+        ke *= 0.5 * m;
+        if (tp.energy) { pe = epot[s]; w = vir[s]; }
+    }
+    write_partials(ke, pe, w, tp.energy, io.partials, sh);
+    if (md_last_block(io.counter)) {
+        finalize(kp, tp, kick ? 1 : 2, gridDim.x, io.partials, io.st, io.rec, io.rec_cap, sh);
+        if (threadIdx.x == 0) *io.counter = 0;
+    }
 }
 
 /* Original-order output: what 0 positions (3), 1 velocities (3, pending NH
@@ -288,40 +341,48 @@ thermo_par make_tp(const md_ctx *c, int energy)
     return tp;
 }
 
-}  // namespace
-
-void launch_leapfrog(md_ctx *c, const md_kparams &kp, int energy)
+step_io make_io(md_ctx *c, unsigned long long cond, int has_cond)
 {
-    thermo_par tp = make_tp(c, energy);
-    int nb = (kp.n + 255) / 256;
-    k_leapfrog<<<nb, 256, 0, c->stream>>>(kp, tp, c->st, c->x, c->v, c->mass, c->pos4, c->f,
-                                          c->epot, c->vir, c->partials);
-    k_finalize<<<1, 256, 0, c->stream>>>(kp, tp, 0, nb, c->partials, c->st, c->rec, c->rec_cap);
+    step_io io;
+    io.st = c->st;
+    io.partials = c->partials;
+    io.rec = c->rec;
+    io.rec_cap = c->rec_cap;
+    io.counter = &c->st->blocks_done;
+    io.pos_old = c->pos_old;
+    io.cond = (cudaGraphConditionalHandle)cond;
+    io.has_cond = has_cond;
+    return io;
 }
 
-void launch_vv_first(md_ctx *c, const md_kparams &kp)
+}  // namespace
+
+void launch_leapfrog(md_ctx *c, const md_kparams &kp, int energy, unsigned long long cond, int has_cond)
 {
-    thermo_par tp = make_tp(c, 0);
     int nb = (kp.n + 255) / 256;
-    k_vv_first<<<nb, 256, 0, c->stream>>>(kp, tp, c->st, c->x, c->v, c->mass, c->pos4, c->f);
+    k_leapfrog<<<nb, 256, 0, c->stream>>>(kp, make_tp(c, energy), make_io(c, cond, has_cond), c->x,
+                                          c->v, c->mass, c->pos4, c->f, c->epot, c->vir);
+}
+
+void launch_vv_first(md_ctx *c, const md_kparams &kp, unsigned long long cond, int has_cond)
+{
+    int nb = (kp.n + 255) / 256;
+    k_vv_first<<<nb, 256, 0, c->stream>>>(kp, make_tp(c, 0), make_io(c, cond, has_cond), c->x,
+                                          c->v, c->mass, c->pos4, c->f);
 }
 
 void launch_vv_second(md_ctx *c, const md_kparams &kp, int energy)
 {
-    thermo_par tp = make_tp(c, energy);
     int nb = (kp.n + 255) / 256;
-    k_vv_second<<<nb, 256, 0, c->stream>>>(kp, tp, 1, c->st, c->v, c->mass, c->f, c->epot,
-                                           c->vir, c->partials);
-    k_finalize<<<1, 256, 0, c->stream>>>(kp, tp, 1, nb, c->partials, c->st, c->rec, c->rec_cap);
+    k_vv_second<<<nb, 256, 0, c->stream>>>(kp, make_tp(c, energy), 1, make_io(c, 0, 0), c->v,
+                                           c->mass, c->f, c->epot, c->vir);
 }
 
 void launch_thermo_from_state(md_ctx *c, const md_kparams &kp, int energy)
 {
-    thermo_par tp = make_tp(c, energy);
     int nb = (kp.n + 255) / 256;
-    k_vv_second<<<nb, 256, 0, c->stream>>>(kp, tp, 0, c->st, c->v, c->mass, c->f, c->epot,
-                                           c->vir, c->partials);
-    k_finalize<<<1, 256, 0, c->stream>>>(kp, tp, 2, nb, c->partials, c->st, c->rec, c->rec_cap);
+    k_vv_second<<<nb, 256, 0, c->stream>>>(kp, make_tp(c, energy), 0, make_io(c, 0, 0), c->v,
+                                           c->mass, c->f, c->epot, c->vir);
 }
 
 void launch_gather_out(md_ctx *c, const md_kparams &kp, int what, void *dst)

@@ -246,7 +246,7 @@ md_status fail(md_ctx *c, md_status s, const std::string &msg)
 void free_device(md_ctx *c)
 {
     void *ptrs[] = {c->x, c->v, c->mass, c->pos4, c->pos_old, c->type, c->perm, c->iperm, c->f,
-                    c->vir, c->epot, c->nl, c->nl_n, c->excl_orig, c->excl_s, c->cell_rank,
+                    c->vir, c->epot, c->nl, c->nl_n, c->excl_orig, c->excl_s, c->cell_rank, c->cell_lin,
                     c->cell_count, c->cell_start, c->cell_fill, c->key, c->src, c->tmp_d, c->tmp4,
                     c->tmp_i, c->bl_o, c->bl_on, c->al_o, c->al_on, c->bl_s, c->bl_sn, c->al_s,
                     c->al_sn, c->partials, c->st, c->rec, c->lj_dev, c->bonded_par,
@@ -276,22 +276,19 @@ md_status alloc_list(md_ctx *c, int cap)
     return MD_OK;
 }
 
-/* Record (or launch eagerly) the kernels of `nsteps` steps. */
+/* Launch the kernels of `nsteps` steps eagerly (outside a graph): the list
+ * kernels return at once unless the previous step's check asked for a build. */
 void enqueue_steps(md_ctx *c, int nsteps, int energy_first)
 {
     md_kparams kp = md_make_kparams(c);
     for (int k = 0; k < nsteps; k++) {
         int energy = (energy_first && k == 0) ? 1 : 0;
         if (c->integrator == MD_LEAPFROG) {
-            cudaMemsetAsync(&c->st->update, 0, sizeof(int), c->stream);
-            launch_check(c, kp);
             launch_rebuild(c, kp, false);
             launch_forces(c, kp, energy != 0, MD_TERM_ALL);
-            launch_leapfrog(c, kp, energy);
+            launch_leapfrog(c, kp, energy, 0, 0);
         } else {
-            launch_vv_first(c, kp);
-            cudaMemsetAsync(&c->st->update, 0, sizeof(int), c->stream);
-            launch_check(c, kp);
+            launch_vv_first(c, kp, 0, 0);
             launch_rebuild(c, kp, false);
             launch_forces(c, kp, energy != 0, MD_TERM_ALL);
             launch_vv_second(c, kp, energy);
@@ -299,17 +296,89 @@ void enqueue_steps(md_ctx *c, int nsteps, int energy_first)
     }
 }
 
+/* Inside a capture on c->stream: a conditional (if) node whose body is the
+ * list rebuild, captured through c->stream2. */
+md_status capture_rebuild_node(md_ctx *c, const md_kparams &kp, cudaGraphConditionalHandle h)
+{
+    cudaStreamCaptureStatus cs;
+    cudaGraph_t g = nullptr;
+    const cudaGraphNode_t *deps = nullptr;
+    size_t nd = 0;
+    MD_CUDA_TRY(c, cudaStreamGetCaptureInfo(c->stream, &cs, nullptr, &g, &deps, nullptr, &nd));
+    cudaGraphNodeParams p = {cudaGraphNodeTypeConditional};
+    p.conditional.handle = h;
+    p.conditional.type = cudaGraphCondTypeIf;
+    p.conditional.size = 1;
+    cudaGraphNode_t node;
+    MD_CUDA_TRY(c, cudaGraphAddNode(&node, g, deps, nullptr, nd, &p));
+    MD_CUDA_TRY(c, cudaStreamUpdateCaptureDependencies(c->stream, &node, nullptr, 1,
+                                                       cudaStreamSetCaptureDependencies));
+    cudaGraph_t body = p.conditional.phGraph_out[0];
+    MD_CUDA_TRY(c, cudaStreamBeginCaptureToGraph(c->stream2, body, nullptr, nullptr, 0,
+                                                 cudaStreamCaptureModeThreadLocal));
+    cudaStream_t keep = c->stream;
+    c->stream = c->stream2;
+    launch_rebuild(c, kp, true);
+    c->stream = keep;
+    cudaGraph_t out = nullptr;
+    MD_CUDA_TRY(c, cudaStreamEndCapture(c->stream2, &out));
+    return MD_OK;
+}
+
+/* A graph of `nsteps` steps.  Each step's rebuild is a conditional node set
+ * by the kernel that performed the displacement check, so a step without a
+ * rebuild costs only its force and integration kernels. */
 md_status capture_graph(md_ctx *c, int nsteps, int energy_first)
 {
     if (c->gexec) {
         cudaGraphExecDestroy(c->gexec);
         c->gexec = nullptr;
     }
+    md_kparams kp = md_make_kparams(c);
     cudaGraph_t g = nullptr;
-    MD_CUDA_TRY(c, cudaStreamBeginCapture(c->stream, cudaStreamCaptureModeThreadLocal));
-    enqueue_steps(c, nsteps, energy_first);
-    cudaError_t e = cudaStreamEndCapture(c->stream, &g);
-    if (e != cudaSuccess) return fail(c, MD_ERR_CUDA, std::string("graph capture: ") + cudaGetErrorString(e));
+    MD_CUDA_TRY(c, cudaGraphCreate(&g, 0));
+    std::vector<cudaGraphConditionalHandle> h(nsteps);
+    for (int k = 0; k < nsteps; k++) {
+        cudaError_t e = cudaGraphConditionalHandleCreate(&h[k], g, 0, cudaGraphCondAssignDefault);
+        if (e != cudaSuccess) {
+            cudaGraphDestroy(g);
+            return fail(c, MD_ERR_CUDA, std::string("conditional handle: ") + cudaGetErrorString(e));
+        }
+    }
+    cudaError_t e = cudaStreamBeginCaptureToGraph(c->stream, g, nullptr, nullptr, 0,
+                                                  cudaStreamCaptureModeThreadLocal);
+    if (e != cudaSuccess) {
+        cudaGraphDestroy(g);
+        return fail(c, MD_ERR_CUDA, std::string("graph capture: ") + cudaGetErrorString(e));
+    }
+    md_status s = MD_OK;
+    if (c->integrator == MD_LEAPFROG) launch_set_condition(c, (unsigned long long)h[0]);
+    for (int k = 0; k < nsteps && s == MD_OK; k++) {
+        int energy = (energy_first && k == 0) ? 1 : 0;
+        if (c->integrator == MD_LEAPFROG) {
+            s = capture_rebuild_node(c, kp, h[k]);
+            if (s != MD_OK) break;
+            launch_forces(c, kp, energy != 0, MD_TERM_ALL);
+            int next = k + 1 < nsteps;
+            launch_leapfrog(c, kp, energy, next ? (unsigned long long)h[k + 1] : 0ull, next);
+        } else {
+            launch_vv_first(c, kp, (unsigned long long)h[k], 1);
+            s = capture_rebuild_node(c, kp, h[k]);
+            if (s != MD_OK) break;
+            launch_forces(c, kp, energy != 0, MD_TERM_ALL);
+            launch_vv_second(c, kp, energy);
+        }
+    }
+    cudaGraph_t out = nullptr;
+    e = cudaStreamEndCapture(c->stream, &out);
+    if (s != MD_OK) {
+        cudaGraphDestroy(g);
+        return s;
+    }
+    if (e != cudaSuccess) {
+        cudaGraphDestroy(g);
+        return fail(c, MD_ERR_CUDA, std::string("graph capture: ") + cudaGetErrorString(e));
+    }
     e = cudaGraphInstantiate(&c->gexec, g, 0);
     cudaGraphDestroy(g);
     if (e != cudaSuccess) return fail(c, MD_ERR_CUDA, std::string("graph instantiate: ") + cudaGetErrorString(e));
@@ -559,6 +628,12 @@ md_status md_create(const md_system_desc *d, void *stream, md_ctx **out)
         }
         c->own_stream = true;
     }
+    if (cudaStreamCreateWithFlags(&c->stream2, cudaStreamNonBlocking) != cudaSuccess) {
+        md_status s = fail(c, MD_ERR_CUDA, "stream creation failed");
+        if (c->own_stream) cudaStreamDestroy(c->stream);
+        delete c;
+        return s;
+    }
     cudaGetDevice(&c->device);
     const size_t P = c->pitch;
     cudaError_t e = cudaSuccess;
@@ -569,7 +644,7 @@ md_status md_create(const md_system_desc *d, void *stream, md_ctx **out)
     MD_ALLOC(c->f, 3 * P); MD_ALLOC(c->vir, P); MD_ALLOC(c->epot, P);
     MD_ALLOC(c->nl_n, P);
     MD_ALLOC(c->excl_orig, P); MD_ALLOC(c->excl_s, P);
-    MD_ALLOC(c->cell_rank, c->ncells); MD_ALLOC(c->cell_count, c->ncells);
+    MD_ALLOC(c->cell_rank, c->ncells); MD_ALLOC(c->cell_lin, c->ncells); MD_ALLOC(c->cell_count, c->ncells);
     MD_ALLOC(c->cell_start, c->ncells + 1); MD_ALLOC(c->cell_fill, c->ncells);
     MD_ALLOC(c->key, P); MD_ALLOC(c->src, P);
     MD_ALLOC(c->tmp_d, 7 * P); MD_ALLOC(c->tmp4, P); MD_ALLOC(c->tmp_i, 3 * P);
@@ -589,6 +664,7 @@ md_status md_create(const md_system_desc *d, void *stream, md_ctx **out)
         md_status s = fail(c, MD_ERR_CUDA, std::string("device allocation: ") + cudaGetErrorString(e));
         free_device(c);
         if (c->own_stream) cudaStreamDestroy(c->stream);
+        cudaStreamDestroy(c->stream2);
         delete c;
         return s;
     }
@@ -640,6 +716,11 @@ md_status md_create(const md_system_desc *d, void *stream, md_ctx **out)
     up(c->iperm, hiperm.data(), sizeof(int) * P);
     up(c->excl_orig, hex.data(), sizeof(uint4) * P);
     up(c->cell_rank, rank.data(), sizeof(int) * c->ncells);
+    {
+        std::vector<int> lin(c->ncells);
+        for (int r = 0; r < c->ncells; r++) lin[r] = hk[r].second;
+        up(c->cell_lin, lin.data(), sizeof(int) * c->ncells);
+    }
     up(c->cell_count, zeros.data(), sizeof(int) * c->ncells);
     up(c->cell_fill, zeros.data(), sizeof(int) * c->ncells);
     up(c->bl_o, blo.data(), sizeof(int2) * 4 * n);
@@ -715,6 +796,7 @@ md_status md_destroy(md_ctx *c)
     if (c->ev0) cudaEventDestroy(c->ev0);
     if (c->ev1) cudaEventDestroy(c->ev1);
     if (c->own_stream && c->stream) cudaStreamDestroy(c->stream);
+    if (c->stream2) cudaStreamDestroy(c->stream2);
     delete c;
     return MD_OK;
 }
@@ -970,10 +1052,10 @@ md_status md_get_info(md_ctx *c, md_info *out)
     out->list_threads_per_atom = c->list_tpa;
     out->builds = h.builds;
     out->max_neighbors = *std::max_element(cnt.begin(), cnt.begin() + c->n);
-    /* check, 8 list-maintenance kernels (they return at once unless a rebuild
-     * is due), pair, bonded (if any), integrator (+ its reduction) */
-    out->kernels_per_step = 1 + 8 + 1 + ((c->has_bonds || c->has_angles) ? 1 : 0) +
-                            (c->integrator == MD_LEAPFROG ? 2 : 3);
+    /* in a step graph without a rebuild: pair, bonded (if any), integrator
+     * (leapfrog: one kernel; VV: two); a rebuild adds 9 kernels */
+    out->kernels_per_step = 1 + ((c->has_bonds || c->has_angles) ? 1 : 0) +
+                            (c->integrator == MD_LEAPFROG ? 1 : 2);
     return MD_OK;
 }
 
@@ -996,7 +1078,7 @@ md_status md_set_tuning(md_ctx *c, int pair_tpa, int list_tpa)
 {
     if (!c) return MD_ERR_ARG;
     auto ok = [](int t) { return t == 1 || t == 2 || t == 4 || t == 8 || t == 16 || t == 32; };
-    if (!ok(pair_tpa) || !ok(list_tpa)) return MD_ERR_ARG;
+    if (!ok(pair_tpa) || !(list_tpa == 0 || ok(list_tpa))) return MD_ERR_ARG;
     c->pair_tpa = pair_tpa;
     c->list_tpa = list_tpa;
     if (c->gexec) {

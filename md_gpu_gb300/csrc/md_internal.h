@@ -51,6 +51,7 @@ struct md_devstate {
     double xi_a, eta_a;  /* the same after the first thermostat half step of a step */
     double vscale;       /* velocity scale pending from the last thermostat half step */
     double lambda;       /* last Berendsen scale */
+    unsigned blocks_done; /* blocks finished in the current reduction kernel */
 };
 
 /* Everything a kernel needs about the system, passed by value. */
@@ -91,6 +92,7 @@ struct md_ctx {
 
     /* ---- device ---- */
     cudaStream_t stream = nullptr;
+    cudaStream_t stream2 = nullptr;  /* captures the bodies of conditional graph nodes */
     bool own_stream = false;
     int device = 0;
     double *x = nullptr, *v = nullptr, *mass = nullptr;   /* sorted order */
@@ -102,6 +104,7 @@ struct md_ctx {
     int *nl_n = nullptr;
     uint4 *excl_orig = nullptr, *excl_s = nullptr;
     int *cell_rank = nullptr, *cell_count = nullptr, *cell_start = nullptr, *cell_fill = nullptr;
+    int *cell_lin = nullptr;                              /* rank -> linear cell index */
     int *key = nullptr, *src = nullptr;
     double *tmp_d = nullptr;                              /* 7*pitch scratch for permutation */
     float4 *tmp4 = nullptr;
@@ -128,7 +131,7 @@ struct md_ctx {
     long long host_step = 0;       /* steps run so far (mirrors st->step) */
     double *io_dev = nullptr;      /* 4*pitch doubles for host transfers */
     int pair_tpa = 4;    /* threads per atom in the pair kernel */
-    int list_tpa = 8;    /* threads per atom in the list build */
+    int list_tpa = 0;    /* list build: 0 = one warp per cell, else threads per atom */
 
     /* timing of the last md_step call (CUDA events on the stream) */
     cudaEvent_t ev0 = nullptr, ev1 = nullptr;
@@ -141,11 +144,15 @@ void md_set_global_error(const std::string &msg);
 /* ---- launchers (k_cells.cu) ---- */
 void launch_check(md_ctx *c, const md_kparams &kp);
 void launch_rebuild(md_ctx *c, const md_kparams &kp, bool unconditional);
+void launch_set_condition(md_ctx *c, unsigned long long handle);
 /* ---- launchers (k_forces.cu) ---- */
 void launch_forces(md_ctx *c, const md_kparams &kp, bool energy, int terms);
 /* ---- launchers (k_integrate.cu) ---- */
-void launch_leapfrog(md_ctx *c, const md_kparams &kp, int energy);
-void launch_vv_first(md_ctx *c, const md_kparams &kp);
+/* cond / has_cond: graph condition (cudaGraphConditionalHandle) the kernel's
+ * last block sets to "rebuild the list before the next force evaluation". */
+void launch_leapfrog(md_ctx *c, const md_kparams &kp, int energy, unsigned long long cond,
+                     int has_cond);
+void launch_vv_first(md_ctx *c, const md_kparams &kp, unsigned long long cond, int has_cond);
 void launch_vv_second(md_ctx *c, const md_kparams &kp, int energy);
 void launch_thermo_from_state(md_ctx *c, const md_kparams &kp, int energy);
 void launch_gather_out(md_ctx *c, const md_kparams &kp, int what, void *dst);

@@ -286,12 +286,12 @@ def test_list_rebuilds_keep_parity():
     assert np.array_equal(gu.rows_canonical(nn, nm, n, 512), gu.rows_canonical(onn, onm, n, 512))
 
 
-@pytest.mark.parametrize("tpa", [1, 2, 8, 16])
-def test_thread_split_variants(tpa):
+@pytest.mark.parametrize("pair_tpa,list_tpa", [(1, 1), (2, 0), (8, 8), (16, 0), (32, 32)])
+def test_thread_split_variants(pair_tpa, list_tpa):
     case = oracle.load(_write(synth.nacl_rocksalt(ncell=5, seed=30, nmaxlist=512)))
     orc = gu.oracle_state(case)
     with gu.system_from_case(case) as sim:
-        sim.set_tuning(tpa, tpa)
+        sim.set_tuning(pair_tpa, list_tpa)
         sim.update_neighbors(force=True)
         sim.compute_forces(TERM_PAIR)
         F = sim.forces()
