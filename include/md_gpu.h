@@ -173,6 +173,9 @@ md_status md_last_step_ms(md_ctx *ctx, float *ms);
  * CUDA events: average milliseconds per launch (the force arrays are
  * recomputed afterwards, so the state is unchanged). */
 md_status md_time_pair(md_ctx *ctx, int nrep, float *ms_per_launch);
+/* A full list build (binning, Hilbert sort, permutation, list), nrep times
+ * between CUDA events on the context's stream: average milliseconds. */
+md_status md_time_rebuild(md_ctx *ctx, int nrep, float *ms_per_build);
 /* FP32 FMA throughput of the current device (TFLOP/s, best of 5): the
  * measured FP32-pipe peak the pair kernel is compared against. */
 md_status md_probe_fp32_peak(double *tflops);

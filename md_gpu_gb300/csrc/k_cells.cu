@@ -272,13 +272,16 @@ __global__ void __launch_bounds__(256) k_build_list(
 }
 
 /* List build, one warp per cell: every atom of a cell shares the cell's
- * stencil, so the warp streams each stencil cell's atoms once (lane = j) and
- * tests them against the cell's atoms (held in shared memory) one i at a
- * time; a ballot appends the hits to i's list.  Entries land in the same
- * order as in k_build_list (stencil cells in traversal order, ascending j),
- * so both builders produce identical lists. */
+ * stencil.  The warp first gathers the stencil cells' atom ranges into
+ * shared memory (in traversal order) with their prefix sums, then streams the
+ * concatenated candidates 32 at a time (lane = candidate, located by binary
+ * search over the prefix sums) and tests them against the cell's atoms one i
+ * at a time; a ballot appends the hits to i's list.  Entries land in the
+ * same order as in k_build_list (stencil cells in traversal order, ascending
+ * j), so both builders produce identical lists. */
 constexpr int CW_WARPS = 4;
 constexpr int CW_MAXI = 32;
+constexpr int CW_MAXST = 128;
 
 __global__ void __launch_bounds__(CW_WARPS * 32) k_build_cells(
     md_kparams kp, md_devstate *st, int always, int ncells, const float4 *__restrict__ pos4,
@@ -291,6 +294,8 @@ __global__ void __launch_bounds__(CW_WARPS * 32) k_build_cells(
     __shared__ float4 s_p[CW_WARPS][CW_MAXI];
     __shared__ uint4 s_ex[CW_WARPS][CW_MAXI];
     __shared__ unsigned s_tm[CW_WARPS][CW_MAXI];
+    __shared__ int s_jb[CW_WARPS][CW_MAXST];
+    __shared__ int s_pre[CW_WARPS][CW_MAXST + 1];
     const int w = threadIdx.x >> 5, lane = threadIdx.x & 31;
     const int r = blockIdx.x * CW_WARPS + w;
     if (r >= ncells) return;
@@ -299,13 +304,43 @@ __global__ void __launch_bounds__(CW_WARPS * 32) k_build_cells(
     const int lin = cell_lin[r];
     const int nx = kp.ncell[0], ny = kp.ncell[1], nz = kp.ncell[2];
     const int c3[3] = {lin % nx, (lin / nx) % ny, lin / (nx * ny)};
-    int lo[3], hi[3];
+    int lo[3], len[3];
     for (int d = 0; d < 3; d++) {
-        if (kp.stencil[d] < 0) { lo[d] = 0; hi[d] = kp.ncell[d] - 1; }
-        else { lo[d] = c3[d] - kp.stencil[d]; hi[d] = c3[d] + kp.stencil[d]; }
+        if (kp.stencil[d] < 0) { lo[d] = 0; len[d] = kp.ncell[d]; }
+        else { lo[d] = c3[d] - kp.stencil[d]; len[d] = 2 * kp.stencil[d] + 1; }
     }
+    const int nst = len[0] * len[1] * len[2];   /* <= 125 with cells of side >= rl/2 */
+    /* stencil ranges in traversal order (z outer, x inner); lane k takes k, k+32, ... */
+    int run = 0;
+    for (int k0 = 0; k0 < nst; k0 += 32) {
+        int k = k0 + lane;
+        int cnt = 0, jb = 0;
+        if (k < nst) {
+            int dx = k % len[0], dy = (k / len[0]) % len[1], dz = k / (len[0] * len[1]);
+            int xx = lo[0] + dx, yy = lo[1] + dy, zz = lo[2] + dz;
+            int cx = xx < 0 ? xx + nx : (xx >= nx ? xx - nx : xx);
+            int cy = yy < 0 ? yy + ny : (yy >= ny ? yy - ny : yy);
+            int cz = zz < 0 ? zz + nz : (zz >= nz ? zz - nz : zz);
+            int r2 = cell_rank[cx + nx * (cy + ny * cz)];
+            jb = cell_start[r2];
+            cnt = cell_start[r2 + 1] - jb;
+        }
+        int incl = cnt;
+        for (int o = 1; o < 32; o <<= 1) {
+            int v = __shfl_up_sync(0xffffffffu, incl, o);
+            if (lane >= o) incl += v;
+        }
+        if (k < nst) {
+            s_jb[w][k] = jb;
+            s_pre[w][k] = run + incl - cnt;
+        }
+        run += __shfl_sync(0xffffffffu, incl, 31);
+    }
+    if (lane == 0) s_pre[w][nst] = run;
+    const int total = run;
     const unsigned lt = (1u << lane) - 1u;
     const size_t P = (size_t)kp.pitch;
+    __syncwarp();
     for (int i0 = ib; i0 < ie; i0 += CW_MAXI) {
         const int ni = min(CW_MAXI, ie - i0);
         if (lane < ni) {
@@ -316,37 +351,35 @@ __global__ void __launch_bounds__(CW_WARPS * 32) k_build_cells(
         }
         __syncwarp();
         int mycnt = 0;   /* list length of atom i0 + lane */
-        for (int zz = lo[2]; zz <= hi[2]; zz++) {
-            int cz = zz < 0 ? zz + nz : (zz >= nz ? zz - nz : zz);
-            for (int yy = lo[1]; yy <= hi[1]; yy++) {
-                int cy = yy < 0 ? yy + ny : (yy >= ny ? yy - ny : yy);
-                for (int xx = lo[0]; xx <= hi[0]; xx++) {
-                    int cx = xx < 0 ? xx + nx : (xx >= nx ? xx - nx : xx);
-                    int r2 = cell_rank[cx + nx * (cy + ny * cz)];
-                    int jb = cell_start[r2], je = cell_start[r2 + 1];
-                    for (int j0 = jb; j0 < je; j0 += 32) {
-                        int j = j0 + lane;
-                        bool vj = j < je;
-                        float4 q = vj ? pos4[j] : make_float4(0.f, 0.f, 0.f, 0.f);
-                        int tj = vj ? type[j] : 0;
-                        unsigned entry = (unsigned)j | ((unsigned)tj << MD_TYPE_SHIFT);
-                        for (int a = 0; a < ni; a++) {
-                            float4 p = s_p[w][a];
-                            uint4 ex = s_ex[w][a];
-                            unsigned uj = (unsigned)j;
-                            bool ok = vj && md_rsq_exact(p, q, kp) < kp.rskinsq && j != i0 + a &&
-                                      uj != ex.x && uj != ex.y && uj != ex.z && uj != ex.w &&
-                                      !((s_tm[w][a] >> tj) & 1u);
-                            unsigned bal = __ballot_sync(0xffffffffu, ok);
-                            int base = __shfl_sync(0xffffffffu, mycnt, a);
-                            if (ok) {
-                                int slot = base + __popc(bal & lt);
-                                if (slot < kp.cap) nl[(size_t)slot * P + i0 + a] = entry;
-                            }
-                            if (lane == a) mycnt += __popc(bal);
-                        }
-                    }
+        for (int g0 = 0; g0 < total; g0 += 32) {
+            int g = g0 + lane;
+            bool vj = g < total;
+            int j = 0;
+            if (vj) {
+                int a = 0, b = nst;   /* largest k with s_pre[k] <= g */
+                while (b - a > 1) {
+                    int m = (a + b) >> 1;
+                    if (s_pre[w][m] <= g) a = m; else b = m;
                 }
+                j = s_jb[w][a] + (g - s_pre[w][a]);
+            }
+            float4 q = vj ? pos4[j] : make_float4(0.f, 0.f, 0.f, 0.f);
+            int tj = vj ? type[j] : 0;
+            unsigned entry = (unsigned)j | ((unsigned)tj << MD_TYPE_SHIFT);
+            unsigned uj = (unsigned)j;
+            for (int a = 0; a < ni; a++) {
+                float4 p = s_p[w][a];
+                uint4 ex = s_ex[w][a];
+                bool ok = vj && md_rsq_exact(p, q, kp) < kp.rskinsq && j != i0 + a &&
+                          uj != ex.x && uj != ex.y && uj != ex.z && uj != ex.w &&
+                          !((s_tm[w][a] >> tj) & 1u);
+                unsigned bal = __ballot_sync(0xffffffffu, ok);
+                int base = __shfl_sync(0xffffffffu, mycnt, a);
+                if (ok) {
+                    int slot = base + __popc(bal & lt);
+                    if (slot < kp.cap) nl[(size_t)slot * P + i0 + a] = entry;
+                }
+                if (lane == a) mycnt += __popc(bal);
             }
         }
         if (lane < ni) {
@@ -385,9 +418,15 @@ void launch_rebuild(md_ctx *c, const md_kparams &kp, bool unconditional)
     k_remap<<<nb, 256, 0, s>>>(kp, c->st, always, c->perm, c->iperm, c->excl_orig, c->excl_s,
                                c->bl_o, c->bl_on, c->bl_s, c->bl_sn, c->al_o, c->al_on, c->al_s,
                                c->al_sn, c->has_bonds, c->has_angles);
-    long long threads = (long long)kp.n * c->list_tpa;
+    int ltpa = c->list_tpa;
+    if (ltpa == 0) {   /* the warp-per-cell builder keeps up to 128 stencil cells in shared memory */
+        int nst = 1;
+        for (int d = 0; d < 3; d++) nst *= c->stencil[d] < 0 ? c->ncell[d] : 2 * c->stencil[d] + 1;
+        if (nst > CW_MAXST) ltpa = 8;
+    }
+    long long threads = (long long)kp.n * (ltpa > 0 ? ltpa : 1);
     int lb = (int)((threads + 255) / 256);
-    switch (c->list_tpa) {
+    switch (ltpa) {
     case 0:
         k_build_cells<<<(c->ncells + CW_WARPS - 1) / CW_WARPS, CW_WARPS * 32, 0, s>>>(
             kp, c->st, always, c->ncells, c->pos4, c->type, c->excl_s, c->cell_rank, c->cell_lin,

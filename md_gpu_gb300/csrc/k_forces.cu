@@ -228,7 +228,7 @@ void pair_dispatch(md_ctx *c, const md_kparams &kp, const pair_consts &pc)
     switch (c->pair_tpa) {
 #define MD_PAIR_CASE(T)                                                                          \
     case T:                                                                                      \
-        k_pair<KIND, T, (T >= 8 ? 4 : 8), ENERGY><<<nb, 128, 0, c->stream>>>(                      \
+        k_pair<KIND, T, (T >= 16 ? 4 : 8), ENERGY><<<nb, 128, 0, c->stream>>>(                     \
             kp, pc, c->pos4, c->type, c->nl, c->nl_n, lj, c->f, c->vir, c->epot);                \
         break;
         MD_PAIR_CASE(1)

@@ -44,6 +44,24 @@ extern "C" md_status md_time_pair(md_ctx *c, int nrep, float *ms_per_launch)
     return MD_OK;
 }
 
+extern "C" md_status md_time_rebuild(md_ctx *c, int nrep, float *ms_per_build)
+{
+    if (!c || nrep <= 0 || !ms_per_build) return MD_ERR_ARG;
+    md_kparams kp = md_make_kparams(c);
+    launch_rebuild(c, kp, true);   /* warm */
+    MD_CUDA_TRY(c, cudaEventRecord(c->ev0, c->stream));
+    for (int r = 0; r < nrep; r++) launch_rebuild(c, kp, true);
+    MD_CUDA_TRY(c, cudaEventRecord(c->ev1, c->stream));
+    MD_CUDA_TRY(c, cudaEventSynchronize(c->ev1));
+    float ms = 0.0f;
+    MD_CUDA_TRY(c, cudaEventElapsedTime(&ms, c->ev0, c->ev1));
+    *ms_per_build = ms / nrep;
+    /* positions did not change: forces of the re-sorted state are recomputed */
+    launch_forces(c, kp, false, MD_TERM_ALL);
+    MD_CUDA_TRY(c, cudaStreamSynchronize(c->stream));
+    return MD_OK;
+}
+
 extern "C" md_status md_probe_fp32_peak(double *tflops)
 {
     if (!tflops) return MD_ERR_ARG;

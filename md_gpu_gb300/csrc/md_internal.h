@@ -130,7 +130,7 @@ struct md_ctx {
     int genergy = 0;
     long long host_step = 0;       /* steps run so far (mirrors st->step) */
     double *io_dev = nullptr;      /* 4*pitch doubles for host transfers */
-    int pair_tpa = 4;    /* threads per atom in the pair kernel */
+    int pair_tpa = 8;    /* threads per atom in the pair kernel */
     int list_tpa = 0;    /* list build: 0 = one warp per cell, else threads per atom */
 
     /* timing of the last md_step call (CUDA events on the stream) */

@@ -98,6 +98,7 @@ def library(path: Optional[str] = None):
     L.md_last_error.argtypes = [vp, C.c_char_p, C.c_int]
     L.md_time_pair.argtypes = [vp, C.c_int, C.POINTER(C.c_float)]
     L.md_probe_fp32_peak.argtypes = [C.POINTER(C.c_double)]
+    L.md_time_rebuild.argtypes = [vp, C.c_int, C.POINTER(C.c_float)]
     L.md_ref_kinetic_energy_noalloc.argtypes = [vp, C.c_int, vp, vp]
     _lib = L
     return L
@@ -303,6 +304,12 @@ class MDSystem:
         """Average ms per launch of the pair kernel (CUDA events, own stream)."""
         ms = C.c_float()
         _check(library().md_time_pair(self._ctx, nrep, C.byref(ms)), self._ctx)
+        return ms.value
+
+    def time_rebuild(self, nrep=10):
+        """Average ms of a full list build (CUDA events, own stream)."""
+        ms = C.c_float()
+        _check(library().md_time_rebuild(self._ctx, nrep, C.byref(ms)), self._ctx)
         return ms.value
 
     def set_tuning(self, pair_tpa, list_tpa):
