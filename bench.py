@@ -159,11 +159,13 @@ def run_ours(args):
     mdbuild.build()
     import md_gpu_gb300 as md
 
+    from md_gpu_gb300.replicas import aggregate_rate, replica_seed
     tmp = tempfile.mkdtemp(prefix="mdbench_")
-    base = make_case(1 + rank, args.ncell, tmp)
+    base = make_case(replica_seed(1, rank), args.ncell, tmp)
     sim = md.MDSystem.from_files(base)
     n = sim.natom
     flush = torch.empty(512 * 1024 * 1024, dtype=torch.uint8, device="cuda")
+    tuned = sim.autotune() if not args.no_autotune else None
 
     for _ in range(args.warmup):
         sim.step(args.md_steps)
@@ -179,15 +181,10 @@ def run_ours(args):
             seg_ms.append(sim.last_step_ms())
         barrier()
     clocks = clk.summary()
-    total_ms = float(sum(seg_ms))
     info = sim.info()
     builds = info["builds"] - builds0
-    if world > 1:
-        t = torch.tensor([total_ms], device="cuda")
-        torch.distributed.all_reduce(t, op=torch.distributed.ReduceOp.MAX)
-        total_ms = float(t.item())
-    atom_steps = n * args.md_steps * args.steps * world
-    value = atom_steps / (total_ms * 1e-3)
+    value, total_ms = aggregate_rate(n * args.md_steps * args.steps, float(sum(seg_ms)), world,
+                                     device="cuda")
     md_steps_per_s = args.md_steps * args.steps / (total_ms * 1e-3)
 
     extra = {}
@@ -204,7 +201,7 @@ def run_ours(args):
         peak = md.fp32_peak_tflops()
         roof = {"bound": "fp32", "achieved": achieved, "peak": peak, "unit": "TFLOP/s",
                 "frac": achieved / peak, "traffic": PAIR_TRAFFIC_BYTES,
-                "kernel": "k_pair<Wolf> (LJ + Wolf, full list, 4 lanes per atom)",
+                "kernel": f"k_pair<Wolf> (LJ + Wolf, full list, {info['pair_tpa']} lanes per atom)",
                 "pair_ms": pair_ms, "pairs_inside_rc": int(pc), "flops_per_pair": FLOPS_PER_PAIR,
                 "peak_source": "measured FP32 FMA probe (md_probe_fp32_peak); no FP32 entry in "
                                "MEASURED_PEAKS.json"}
@@ -249,7 +246,10 @@ def run_ours(args):
                        "parallelism": "replicas" if world > 1 else "single system",
                        "ns_per_day": md_steps_per_s * DT_FS * 0.0864,
                        "list_builds_in_timed_region": builds,
-                       "pair_threads_per_atom": info["pair_tpa"]},
+                       "pair_threads_per_atom": info["pair_tpa"],
+                       "list_builder": "warp per cell" if info["list_tpa"] == 0
+                       else f"{info['list_tpa']} threads per atom",
+                       "autotuned": tuned is not None},
             "gpu_launches": info["kernels_per_step"] * args.md_steps * args.steps,
             "clocks": clocks}
     line.update(extra)
@@ -269,6 +269,7 @@ def main():
     ap.add_argument("--md-steps", type=int, default=100)
     ap.add_argument("--ref-md-steps", type=int, default=10)
     ap.add_argument("--ncell", type=int, default=20)
+    ap.add_argument("--no-autotune", action="store_true")
     args = ap.parse_args()
     if args.warmup < 3 and args.impl == "ours":
         args.warmup = 3

@@ -167,6 +167,14 @@ md_status md_get_cell_ranks(md_ctx *ctx, int *rank);
  * the list builder (0 = one warp per cell, the default; or 1..32 threads per
  * atom).  Every setting builds the identical list. */
 md_status md_set_tuning(md_ctx *ctx, int pair_tpa, int list_tpa);
+/* Autotuner: times the pair kernel for 2/4/8/16 threads per atom and the list
+ * builders (warp per cell, 4/8/16 threads per atom) on the current state and
+ * keeps the fastest of each; returns the choice. */
+md_status md_autotune(md_ctx *ctx, int *pair_tpa, int *list_tpa);
+/* Per-type exclusions (no counterpart in the reference, which excludes only
+ * 1-2 bonded pairs): bit b of mask[a] excludes every pair of types a and b
+ * from the neighbour list (made symmetric); ntype entries.  Rebuilds the list. */
+md_status md_set_type_exclusions(md_ctx *ctx, const unsigned *mask);
 /* Milliseconds of device time of the last md_step call (CUDA events). */
 md_status md_last_step_ms(md_ctx *ctx, float *ms);
 /* The pair-force kernel alone, nrep launches on the context's stream between

@@ -41,11 +41,78 @@ __device__ __forceinline__ float rint_small(float t)
     return __fsub_rn(__fadd_rn(t, M), M);
 }
 
+/* The hardware approximations (PTX ISA ex2/rsqrt/rcp .approx.ftz): relative
+ * errors ~2^-22, well inside the 1e-5 force tolerance; arguments here are
+ * never denormal. */
+__device__ __forceinline__ float ex2_approx(float x)
+{
+    float y;
+    asm("ex2.approx.ftz.f32 %0, %1;" : "=f"(y) : "f"(x));
+    return y;
+}
+__device__ __forceinline__ float rsqrt_approx(float x)
+{
+    float y;
+    asm("rsqrt.approx.ftz.f32 %0, %1;" : "=f"(y) : "f"(x));
+    return y;
+}
+__device__ __forceinline__ float rcp_approx(float x)
+{
+    float y;
+    asm("rcp.approx.ftz.f32 %0, %1;" : "=f"(y) : "f"(x));
+    return y;
+}
+
+struct pair_acc {
+    float fx, fy, fz, fw, fe;
+};
+
+/* One pair: F_i += ff d, w_i += ff r^2 (pair_forces.cu:165-200 / :74-120). */
+template <int KIND, bool ENERGY>
+__device__ __forceinline__ void pair_term(const md_kparams &kp, const pair_consts &pc, float4 pi,
+                                          float qi, float4 pj, float2 l, bool valid, pair_acc &a)
+{
+    float dx = pi.x - pj.x, dy = pi.y - pj.y, dz = pi.z - pj.z;
+    dx -= kp.box[0] * rint_small(dx * kp.boxi[0]);
+    dy -= kp.box[1] * rint_small(dy * kp.boxi[1]);
+    dz -= kp.box[2] * rint_small(dz * kp.boxi[2]);
+    float rsq = dx * dx + dy * dy + dz * dz;
+    float ri = rsqrt_approx(rsq);
+    float ri2 = ri * ri;
+    float qq = qi * pj.w;
+    float ff, uc = 0.0f;
+    if (KIND == 1) {
+        float r = rsq * ri;
+        float t = rcp_approx(1.0f + kp.palfa * r);
+        float poly = ((((A5 * t + A4) * t + A3) * t + A2) * t + A1) * t;
+        float ex = ex2_approx(kp.alfasq * rsq);
+        ff = ((kp.spiialfa * r + poly) * ex * ri - kp.wolf) * qq;
+        if (ENERGY) uc = qq * (poly * ex * ri - pc.ucc + kp.wolf * __logf(r * pc.rcinv));
+    } else {
+        ff = qq * (ri - kp.reacf * rsq);
+        if (ENERGY) uc = qq * (ri + 0.5f * kp.reacf * rsq - pc.ucc);
+    }
+    float ri6 = ri2 * ri2 * ri2;
+    ff = ff * ri2 + (l.x * ri6 - l.y) * ri6 * ri2;
+    bool in = valid && rsq <= kp.rcutsq;
+    ff = in ? ff : 0.0f;
+    a.fx += ff * dx;
+    a.fy += ff * dy;
+    a.fz += ff * dz;
+    a.fw += ff * rsq;
+    if (ENERGY) {
+        float ulj = l.x * (1.0f / 12.0f) * (ri6 * ri6 - pc.rc6i * pc.rc6i) -
+                    l.y * (1.0f / 6.0f) * (ri6 - pc.rc6i);
+        a.fe += in ? 0.5f * (uc + ulj) : 0.0f;
+    }
+}
+
 /* Pair forces of atom i from its list: TPA lanes per atom, lane l takes the
- * entries l, l+TPA, ...  Each lane loads B list entries and then B
- * positions before computing, so B independent loads are in flight; it sums
- * in FP32 and converts its sum to int64 once.  Lane sums are combined with
- * integer shuffles (exact), so the result depends only on TPA. */
+ * entries l, l+TPA, ... in batches of B.  The loads are software pipelined:
+ * while batch t is computed, the positions of batch t+1 and the list entries
+ * of batch t+2 are already in flight.  Each lane sums in FP32 and converts
+ * its sum to int64 once; lane sums are combined with integer shuffles
+ * (exact), so the result depends only on TPA. */
 template <int KIND, int TPA, int B, bool ENERGY>
 __global__ void __launch_bounds__(128) k_pair(md_kparams kp, pair_consts pc,
                                               const float4 *__restrict__ pos4,
@@ -66,65 +133,49 @@ __global__ void __launch_bounds__(128) k_pair(md_kparams kp, pair_consts pc,
     const int cnt = active ? nl_n[ii] : 0;
     const float2 *ljrow = lj + type[ii] * MD_MAXTYPE;
     const float qi = QFAC * pi.w;
-    const float L0 = kp.box[0], L1 = kp.box[1], L2 = kp.box[2];
-    const float I0 = kp.boxi[0], I1 = kp.boxi[1], I2 = kp.boxi[2];
-    const float rcsq = kp.rcutsq;
-    float fx = 0.0f, fy = 0.0f, fz = 0.0f, fw = 0.0f, fe = 0.0f;
+    pair_acc acc = {0.0f, 0.0f, 0.0f, 0.0f, 0.0f};
     const size_t P = (size_t)kp.pitch;
     const unsigned *lp = nl + (size_t)lane * P + ii;
-    for (int k0 = lane; k0 < cnt; k0 += TPA * B) {
-        unsigned e[B];
+    const size_t step = (size_t)TPA * P;
+    const int nb = (cnt - lane + TPA * B - 1) / (TPA * B);   /* batches of this lane */
+    unsigned e0[B], e1[B];
+    float4 p0[B];
 #pragma unroll
-        for (int b = 0; b < B; b++) {
-            int k = k0 + b * TPA;
-            e[b] = (k < cnt) ? __ldg(lp + (size_t)b * TPA * P) : (unsigned)ii;
-        }
-        lp += (size_t)TPA * B * P;
-        float4 pj[B];
-#pragma unroll
-        for (int b = 0; b < B; b++) pj[b] = __ldg(pos4 + (e[b] & MD_INDEX_MASK));
-#pragma unroll
-        for (int b = 0; b < B; b++) {
-            bool valid = k0 + b * TPA < cnt;
-            float2 l = ljrow[e[b] >> MD_TYPE_SHIFT];
-            float dx = pi.x - pj[b].x, dy = pi.y - pj[b].y, dz = pi.z - pj[b].z;
-            dx -= L0 * rint_small(dx * I0);
-            dy -= L1 * rint_small(dy * I1);
-            dz -= L2 * rint_small(dz * I2);
-            float rsq = dx * dx + dy * dy + dz * dz;
-            float ri = rsqrtf(rsq);
-            float ri2 = ri * ri;
-            float qq = qi * pj[b].w;
-            float ff, uc = 0.0f;
-            if (KIND == 1) {
-                float r = rsq * ri;
-                float t = __fdividef(1.0f, 1.0f + kp.palfa * r);
-                float poly = ((((A5 * t + A4) * t + A3) * t + A2) * t + A1) * t;
-                float ex = exp2f(kp.alfasq * rsq);
-                ff = ((kp.spiialfa * r + poly) * ex * ri - kp.wolf) * qq;
-                if (ENERGY) uc = qq * (poly * ex * ri - pc.ucc + kp.wolf * __logf(r * pc.rcinv));
-            } else {
-                ff = qq * (ri - kp.reacf * rsq);
-                if (ENERGY) uc = qq * (ri + 0.5f * kp.reacf * rsq - pc.ucc);
-            }
-            float ri6 = ri2 * ri2 * ri2;
-            ff = ff * ri2 + (l.x * ri6 - l.y) * ri6 * ri2;
-            bool in = valid && rsq <= rcsq;
-            ff = in ? ff : 0.0f;
-            fx += ff * dx;
-            fy += ff * dy;
-            fz += ff * dz;
-            fw += ff * rsq;
-            if (ENERGY) {
-                float ulj = l.x * (1.0f / 12.0f) * (ri6 * ri6 - pc.rc6i * pc.rc6i) -
-                            l.y * (1.0f / 6.0f) * (ri6 - pc.rc6i);
-                fe += in ? 0.5f * (uc + ulj) : 0.0f;
-            }
-        }
+    for (int b = 0; b < B; b++) {
+        int k = lane + b * TPA;
+        e0[b] = k < cnt ? __ldg(lp + b * step) : (unsigned)ii;
+        int k1 = k + TPA * B;
+        e1[b] = k1 < cnt ? __ldg(lp + (b + B) * step) : (unsigned)ii;
     }
-    long long ax = __float2ll_rn(fx * 4294967296.0f);
-    long long ay = __float2ll_rn(fy * 4294967296.0f);
-    long long az = __float2ll_rn(fz * 4294967296.0f);
+#pragma unroll
+    for (int b = 0; b < B; b++) p0[b] = __ldg(pos4 + (e0[b] & MD_INDEX_MASK));
+    for (int t = 0; t < nb; t++) {
+        const int kb = lane + t * TPA * B;
+        float4 p1[B];
+        unsigned e2[B];
+#pragma unroll
+        for (int b = 0; b < B; b++) p1[b] = __ldg(pos4 + (e1[b] & MD_INDEX_MASK));
+#pragma unroll
+        for (int b = 0; b < B; b++) {
+            int k2 = kb + (2 * B + b) * TPA;
+            e2[b] = k2 < cnt ? __ldg(lp + (2 * B + b) * step) : (unsigned)ii;
+        }
+#pragma unroll
+        for (int b = 0; b < B; b++)
+            pair_term<KIND, ENERGY>(kp, pc, pi, qi, p0[b], ljrow[e0[b] >> MD_TYPE_SHIFT],
+                                    kb + b * TPA < cnt, acc);
+#pragma unroll
+        for (int b = 0; b < B; b++) {
+            e0[b] = e1[b];
+            p0[b] = p1[b];
+            e1[b] = e2[b];
+        }
+        lp += B * step;
+    }
+    long long ax = __float2ll_rn(acc.fx * 4294967296.0f);
+    long long ay = __float2ll_rn(acc.fy * 4294967296.0f);
+    long long az = __float2ll_rn(acc.fz * 4294967296.0f);
+    float fw = acc.fw, fe = acc.fe;
     if (TPA > 1) {
         const unsigned mask = 0xffffffffu;
 #pragma unroll
@@ -228,7 +279,7 @@ void pair_dispatch(md_ctx *c, const md_kparams &kp, const pair_consts &pc)
     switch (c->pair_tpa) {
 #define MD_PAIR_CASE(T)                                                                          \
     case T:                                                                                      \
-        k_pair<KIND, T, (T >= 16 ? 4 : 8), ENERGY><<<nb, 128, 0, c->stream>>>(                     \
+        k_pair<KIND, T, (T >= 8 ? 4 : 8), ENERGY><<<nb, 128, 0, c->stream>>>(                      \
             kp, pc, c->pos4, c->type, c->nl, c->nl_n, lj, c->f, c->vir, c->epot);                \
         break;
         MD_PAIR_CASE(1)

@@ -1074,6 +1074,55 @@ md_status md_get_cell_ranks(md_ctx *c, int *rank)
     return MD_OK;
 }
 
+md_status md_set_type_exclusions(md_ctx *c, const unsigned *mask)
+{
+    if (!c || !mask) return MD_ERR_ARG;
+    unsigned m[MD_MAXTYPE] = {0};
+    for (int a = 0; a < c->ntype; a++)
+        for (int b = 0; b < c->ntype; b++)
+            if (((mask[a] >> b) & 1u) || ((mask[b] >> a) & 1u)) m[a] |= 1u << b;
+    memcpy(c->type_excl_mask, m, sizeof(m));
+    MD_CUDA_TRY(c, cudaMemcpyAsync(c->type_mask_dev, m, sizeof(m), cudaMemcpyHostToDevice, c->stream));
+    md_status s = initial_build(c);
+    if (s != MD_OK) return s;
+    return refresh_state(c);
+}
+
+md_status md_autotune(md_ctx *c, int *pair_tpa, int *list_tpa)
+{
+    if (!c) return MD_ERR_ARG;
+    const int pt[] = {2, 4, 8, 16};
+    const int lt[] = {0, 4, 8, 16};
+    float best = 1e30f;
+    int bp = c->pair_tpa, bl = c->list_tpa;
+    for (int t : pt) {
+        c->pair_tpa = t;
+        float ms = 0.0f, m2 = 0.0f;
+        md_status s = md_time_pair(c, 5, &ms);
+        if (s == MD_OK) s = md_time_pair(c, 10, &m2);
+        if (s != MD_OK) return s;
+        if (m2 < best) { best = m2; bp = t; }
+    }
+    c->pair_tpa = bp;
+    best = 1e30f;
+    for (int t : lt) {
+        c->list_tpa = t;
+        float ms = 0.0f, m2 = 0.0f;
+        md_status s = md_time_rebuild(c, 2, &ms);
+        if (s == MD_OK) s = md_time_rebuild(c, 5, &m2);
+        if (s != MD_OK) return s;
+        if (m2 < best) { best = m2; bl = t; }
+    }
+    c->list_tpa = bl;
+    if (c->gexec) {
+        cudaGraphExecDestroy(c->gexec);
+        c->gexec = nullptr;
+    }
+    if (pair_tpa) *pair_tpa = bp;
+    if (list_tpa) *list_tpa = bl;
+    return MD_OK;
+}
+
 md_status md_set_tuning(md_ctx *c, int pair_tpa, int list_tpa)
 {
     if (!c) return MD_ERR_ARG;

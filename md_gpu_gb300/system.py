@@ -99,6 +99,8 @@ def library(path: Optional[str] = None):
     L.md_time_pair.argtypes = [vp, C.c_int, C.POINTER(C.c_float)]
     L.md_probe_fp32_peak.argtypes = [C.POINTER(C.c_double)]
     L.md_time_rebuild.argtypes = [vp, C.c_int, C.POINTER(C.c_float)]
+    L.md_autotune.argtypes = [vp, C.POINTER(C.c_int), C.POINTER(C.c_int)]
+    L.md_set_type_exclusions.argtypes = [vp, vp]
     L.md_ref_kinetic_energy_noalloc.argtypes = [vp, C.c_int, vp, vp]
     _lib = L
     return L
@@ -311,6 +313,17 @@ class MDSystem:
         ms = C.c_float()
         _check(library().md_time_rebuild(self._ctx, nrep, C.byref(ms)), self._ctx)
         return ms.value
+
+    def autotune(self):
+        """Pick the fastest pair / list-build variants; returns (pair_tpa, list_tpa)."""
+        a, b = C.c_int(), C.c_int()
+        _check(library().md_autotune(self._ctx, C.byref(a), C.byref(b)), self._ctx)
+        return a.value, b.value
+
+    def set_type_exclusions(self, mask):
+        """mask[a] bit b: exclude all pairs of types a and b (0-based)."""
+        m = np.ascontiguousarray(mask, np.uint32)
+        _check(library().md_set_type_exclusions(self._ctx, m.ctypes.data), self._ctx)
 
     def set_tuning(self, pair_tpa, list_tpa):
         _check(library().md_set_tuning(self._ctx, pair_tpa, list_tpa), self._ctx)

@@ -317,3 +317,61 @@ def test_full_size_nacl_64k():
     assert np.array_equal(gu.rows_canonical(nn, nm, n, 512), gu.rows_canonical(orc["nn"], orc["nm"], n, 512))
     assert gu.rms_rel(F[:, :3], orc["f64"][:, :3]) <= FORCE_TOL
     assert np.abs(F[:, :3].sum(0)).max() <= 1e-3 * np.sqrt((F[:, :3] ** 2).sum(1)).mean() * np.sqrt(n)
+
+
+def test_type_exclusions():
+    """Excluding every O-H pair by type removes exactly those pairs from the
+    reference list."""
+    case = oracle.load(_write(synth.water_grid(nside=8, seed=4)))
+    orc = gu.oracle_state(case)
+    n = case.natom
+    with gu.system_from_case(case) as sim:
+        sim.set_type_exclusions(np.array([1 << 1, 0], np.uint32))
+        nn, nm = sim.neighbor_list(768)
+    rows = oracle.nlist_rows(orc["nn"], orc["nm"], n)
+    t = case.itype
+    for i in range(n):
+        keep = rows[i][t[rows[i]] == t[i]]
+        got = nn.reshape(-1, nm.shape[0])[:nm[i], i]
+        assert np.array_equal(got, keep), i
+
+
+def test_autotune_keeps_results():
+    case = oracle.load(_write(synth.nacl_rocksalt(ncell=5, seed=40, nmaxlist=512)))
+    orc = gu.oracle_state(case)
+    with gu.system_from_case(case) as sim:
+        pt, lt = sim.autotune()
+        assert pt in (2, 4, 8, 16) and lt in (0, 4, 8, 16)
+        sim.compute_forces(TERM_PAIR)
+        F = sim.forces()
+        nn, nm = sim.neighbor_list(512)
+    n = case.natom
+    assert gu.rms_rel(F[:, :3], orc["f64"][:, :3]) <= FORCE_TOL
+    assert np.array_equal(gu.rows_canonical(nn, nm, n, 512), gu.rows_canonical(orc["nn"], orc["nm"], n, 512))
+
+
+def _drift_kt_per_atom_ns(e, n, dt_fs, t0):
+    """Linear-fit slope of the total energy, per atom, in kT per ns."""
+    t_ns = np.arange(len(e)) * dt_fs * 1e-6
+    slope = np.polyfit(t_ns, e, 1)[0]
+    return slope / n / (8.314e-3 * t0)
+
+
+def test_nve_drift_argon():
+    """Velocity-Verlet NVE drift of LJ argon (reduced units mapped to A, fs)
+    against the FP64 plain form of the same run; gate 1e-4 kT/atom/ns on the
+    difference."""
+    case = oracle.load(_write(synth.argon_fcc(ncell=5, seed=6, integrator="vv")))
+    nsteps = 2000
+    x = case.pos.astype(np.float64).copy()
+    v = case.vel.astype(np.float64).copy()
+    st, rec = oracle.md_plain_run(case, x, v, nsteps, 1)
+    with gu.system_from_case(case, integrator=MD_VV) as sim:
+        sim.step(nsteps, energy_every=1)
+        hist = sim.history(nsteps)
+    e_gpu = np.array([h["ke"] + h["pe"] for h in hist])
+    t0 = 0.72 / 8.314e-3
+    d_gpu = _drift_kt_per_atom_ns(e_gpu, case.natom, 0.5, t0)
+    d_ref = _drift_kt_per_atom_ns(rec[:, 0] + rec[:, 1], case.natom, 0.5, t0)
+    print(f"NVE drift: GPU {d_gpu:.3e}, FP64 plain {d_ref:.3e} kT/atom/ns")
+    assert abs(d_gpu - d_ref) <= 1e-4 + 0.1 * abs(d_ref)
