@@ -233,7 +233,6 @@ __global__ void __launch_bounds__(256) k_build_list(
         else { lo[d] = c3[d] - kp.stencil[d]; hi[d] = c3[d] + kp.stencil[d]; }
     }
     int cnt = 0;
-    const int P = kp.pitch;
     for (int zz = lo[2]; zz <= hi[2]; zz++) {
         int cz = zz < 0 ? zz + kp.ncell[2] : (zz >= kp.ncell[2] ? zz - kp.ncell[2] : zz);
         for (int yy = lo[1]; yy <= hi[1]; yy++) {
@@ -257,12 +256,18 @@ __global__ void __launch_bounds__(256) k_build_list(
                     unsigned bal = __ballot_sync(gmask, ok);
                     if (ok) {
                         int slot = cnt + __popc(bal & ((1u << lane_w) - 1u));
-                        if (slot < kp.cap) nl[(size_t)slot * P + i] = entry;
+                        if (slot < kp.cap) nl[(size_t)i * kp.cap + slot] = entry;
                     }
                     cnt += __popc(bal);
                 }
             }
         }
+    }
+    if (active) {
+        /* pad the row to the next multiple of 32 with the atom itself */
+        int lim = min(kp.cap, (cnt + MD_LIST_QUANTUM - 1) / MD_LIST_QUANTUM * MD_LIST_QUANTUM);
+        unsigned self = (unsigned)i | ((unsigned)ti << MD_TYPE_SHIFT);
+        for (int k = cnt + lane; k < lim; k += TPA) nl[(size_t)i * kp.cap + k] = self;
     }
     if (active && lane == 0) {
         nl_n[i] = cnt < kp.cap ? cnt : kp.cap;
@@ -296,6 +301,7 @@ __global__ void __launch_bounds__(CW_WARPS * 32) k_build_cells(
     __shared__ unsigned s_tm[CW_WARPS][CW_MAXI];
     __shared__ int s_jb[CW_WARPS][CW_MAXST];
     __shared__ int s_pre[CW_WARPS][CW_MAXST + 1];
+    __shared__ unsigned char s_sh[CW_WARPS][CW_MAXST];   /* image code per stencil cell */
     const int w = threadIdx.x >> 5, lane = threadIdx.x & 31;
     const int r = blockIdx.x * CW_WARPS + w;
     if (r >= ncells) return;
@@ -314,10 +320,14 @@ __global__ void __launch_bounds__(CW_WARPS * 32) k_build_cells(
     int run = 0;
     for (int k0 = 0; k0 < nst; k0 += 32) {
         int k = k0 + lane;
-        int cnt = 0, jb = 0;
+        int cnt = 0, jb = 0, code = 0;
         if (k < nst) {
             int dx = k % len[0], dy = (k / len[0]) % len[1], dz = k / (len[0] * len[1]);
             int xx = lo[0] + dx, yy = lo[1] + dy, zz = lo[2] + dz;
+            /* code per axis: 0 no image, 1 the cell wrapped from below (the
+             * reference's rint(d/L) = -1), 2 from above (+1) */
+            code = (xx < 0 ? 1 : (xx >= nx ? 2 : 0)) | ((yy < 0 ? 1 : (yy >= ny ? 2 : 0)) << 2) |
+                   ((zz < 0 ? 1 : (zz >= nz ? 2 : 0)) << 4);
             int cx = xx < 0 ? xx + nx : (xx >= nx ? xx - nx : xx);
             int cy = yy < 0 ? yy + ny : (yy >= ny ? yy - ny : yy);
             int cz = zz < 0 ? zz + nz : (zz >= nz ? zz - nz : zz);
@@ -333,28 +343,35 @@ __global__ void __launch_bounds__(CW_WARPS * 32) k_build_cells(
         if (k < nst) {
             s_jb[w][k] = jb;
             s_pre[w][k] = run + incl - cnt;
+            s_sh[w][k] = (unsigned char)code;
         }
         run += __shfl_sync(0xffffffffu, incl, 31);
     }
     if (lane == 0) s_pre[w][nst] = run;
     const int total = run;
     const unsigned lt = (1u << lane) - 1u;
-    const size_t P = (size_t)kp.pitch;
+    const float L0 = kp.box[0], L1 = kp.box[1], L2 = kp.box[2];
     __syncwarp();
     for (int i0 = ib; i0 < ie; i0 += CW_MAXI) {
         const int ni = min(CW_MAXI, ie - i0);
+        bool any_excl = false;
         if (lane < ni) {
             int i = i0 + lane;
             s_p[w][lane] = pos4[i];
-            s_ex[w][lane] = excl_s[i];
-            s_tm[w][lane] = type_mask[type[i]];
+            uint4 ex = excl_s[i];
+            s_ex[w][lane] = ex;
+            unsigned tm = type_mask[type[i]];
+            s_tm[w][lane] = tm;
+            any_excl = ex.x != MD_EXCL_NONE || ex.y != MD_EXCL_NONE || ex.z != MD_EXCL_NONE ||
+                       ex.w != MD_EXCL_NONE || tm != 0u;
         }
+        const unsigned excl_bits = __ballot_sync(0xffffffffu, any_excl);
         __syncwarp();
         int mycnt = 0;   /* list length of atom i0 + lane */
         for (int g0 = 0; g0 < total; g0 += 32) {
             int g = g0 + lane;
             bool vj = g < total;
-            int j = 0;
+            int j = 0, code = 0;
             if (vj) {
                 int a = 0, b = nst;   /* largest k with s_pre[k] <= g */
                 while (b - a > 1) {
@@ -362,24 +379,51 @@ __global__ void __launch_bounds__(CW_WARPS * 32) k_build_cells(
                     if (s_pre[w][m] <= g) a = m; else b = m;
                 }
                 j = s_jb[w][a] + (g - s_pre[w][a]);
+                code = s_sh[w][a];
             }
             float4 q = vj ? pos4[j] : make_float4(0.f, 0.f, 0.f, 0.f);
             int tj = vj ? type[j] : 0;
+            /* exact images: u = L * rint(d / L) is -L, 0 or +L by stencil cell */
+            const float ux = (code & 3) == 1 ? -L0 : ((code & 3) == 2 ? L0 : 0.0f);
+            const float uy = ((code >> 2) & 3) == 1 ? -L1 : (((code >> 2) & 3) == 2 ? L1 : 0.0f);
+            const float uz = ((code >> 4) & 3) == 1 ? -L2 : (((code >> 4) & 3) == 2 ? L2 : 0.0f);
             unsigned entry = (unsigned)j | ((unsigned)tj << MD_TYPE_SHIFT);
             unsigned uj = (unsigned)j;
             for (int a = 0; a < ni; a++) {
                 float4 p = s_p[w][a];
-                uint4 ex = s_ex[w][a];
-                bool ok = vj && md_rsq_exact(p, q, kp) < kp.rskinsq && j != i0 + a &&
-                          uj != ex.x && uj != ex.y && uj != ex.z && uj != ex.w &&
-                          !((s_tm[w][a] >> tj) & 1u);
+                float rsq;
+                if (kp.cell_shift) {
+                    /* fl(fl(px - qx) - u) is the reference's fl(d - fl(L rint(d/L))) */
+                    float dx = __fsub_rn(__fsub_rn(p.x, q.x), ux);
+                    float dy = __fsub_rn(__fsub_rn(p.y, q.y), uy);
+                    float dz = __fsub_rn(__fsub_rn(p.z, q.z), uz);
+                    rsq = __fadd_rn(__fadd_rn(__fmul_rn(dx, dx), __fmul_rn(dy, dy)), __fmul_rn(dz, dz));
+                } else {
+                    rsq = md_rsq_exact(p, q, kp);
+                }
+                bool ok = vj && rsq < kp.rskinsq && j != i0 + a;
+                if ((excl_bits >> a) & 1u) {
+                    uint4 ex = s_ex[w][a];
+                    ok = ok && uj != ex.x && uj != ex.y && uj != ex.z && uj != ex.w &&
+                         !((s_tm[w][a] >> tj) & 1u);
+                }
                 unsigned bal = __ballot_sync(0xffffffffu, ok);
                 int base = __shfl_sync(0xffffffffu, mycnt, a);
                 if (ok) {
                     int slot = base + __popc(bal & lt);
-                    if (slot < kp.cap) nl[(size_t)slot * P + i0 + a] = entry;
+                    if (slot < kp.cap) nl[(size_t)(i0 + a) * kp.cap + slot] = entry;
                 }
                 if (lane == a) mycnt += __popc(bal);
+            }
+        }
+        /* pad every row to a multiple of 32 with the atom itself */
+        for (int a = 0; a < ni; a++) {
+            int c = __shfl_sync(0xffffffffu, mycnt, a);
+            int lim = min(kp.cap, (c + MD_LIST_QUANTUM - 1) / MD_LIST_QUANTUM * MD_LIST_QUANTUM);
+            int k = c + lane;
+            if (k < lim) {
+                int ta = type[i0 + a];
+                nl[(size_t)(i0 + a) * kp.cap + k] = (unsigned)(i0 + a) | ((unsigned)ta << MD_TYPE_SHIFT);
             }
         }
         if (lane < ni) {

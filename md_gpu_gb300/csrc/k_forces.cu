@@ -94,7 +94,8 @@ __device__ __forceinline__ void pair_term(const md_kparams &kp, const pair_const
     }
     float ri6 = ri2 * ri2 * ri2;
     ff = ff * ri2 + (l.x * ri6 - l.y) * ri6 * ri2;
-    bool in = valid && rsq <= kp.rcutsq;
+    /* list padding entries point at the atom itself: r = 0 is skipped */
+    bool in = valid && rsq <= kp.rcutsq && rsq > 0.0f;
     ff = in ? ff : 0.0f;
     a.fx += ff * dx;
     a.fy += ff * dy;
@@ -108,11 +109,12 @@ __device__ __forceinline__ void pair_term(const md_kparams &kp, const pair_const
 }
 
 /* Pair forces of atom i from its list: TPA lanes per atom, lane l takes the
- * entries l, l+TPA, ... in batches of B.  The loads are software pipelined:
- * while batch t is computed, the positions of batch t+1 and the list entries
- * of batch t+2 are already in flight.  Each lane sums in FP32 and converts
- * its sum to int64 once; lane sums are combined with integer shuffles
- * (exact), so the result depends only on TPA. */
+ * entries l, l+TPA, ... in batches of B (TPA*B divides 32, the padding
+ * quantum of the list rows, so no entry needs a bounds test).  The loads are
+ * software pipelined: while batch t is computed, the positions of batch t+1
+ * and the list entries of batch t+2 are in flight.  Each lane sums in FP32
+ * and converts its sum to int64 once; lane sums are combined with integer
+ * shuffles (exact), so the result depends only on TPA. */
 template <int KIND, int TPA, int B, bool ENERGY>
 __global__ void __launch_bounds__(128) k_pair(md_kparams kp, pair_consts pc,
                                               const float4 *__restrict__ pos4,
@@ -122,6 +124,7 @@ __global__ void __launch_bounds__(128) k_pair(md_kparams kp, pair_consts pc,
                                               const float2 *__restrict__ ljtab, long long *f,
                                               float *vir, float *epot)
 {
+    static_assert(MD_LIST_QUANTUM % (TPA * B) == 0, "batch must divide the list padding");
     __shared__ float2 lj[MD_MAXTYPE * MD_MAXTYPE];
     if (threadIdx.x < MD_MAXTYPE * MD_MAXTYPE) lj[threadIdx.x] = ljtab[threadIdx.x];
     __syncthreads();
@@ -131,46 +134,44 @@ __global__ void __launch_bounds__(128) k_pair(md_kparams kp, pair_consts pc,
     int ii = active ? i : 0;
     const float4 pi = pos4[ii];
     const int cnt = active ? nl_n[ii] : 0;
+    const int nb = ((cnt + MD_LIST_QUANTUM - 1) / MD_LIST_QUANTUM) * (MD_LIST_QUANTUM / (TPA * B));
     const float2 *ljrow = lj + type[ii] * MD_MAXTYPE;
     const float qi = QFAC * pi.w;
     pair_acc acc = {0.0f, 0.0f, 0.0f, 0.0f, 0.0f};
-    const size_t P = (size_t)kp.pitch;
-    const unsigned *lp = nl + (size_t)lane * P + ii;
-    const size_t step = (size_t)TPA * P;
-    const int nb = (cnt - lane + TPA * B - 1) / (TPA * B);   /* batches of this lane */
+    const unsigned *lp = nl + (size_t)ii * kp.cap + lane;
     unsigned e0[B], e1[B];
     float4 p0[B];
+    if (nb > 0) {
 #pragma unroll
-    for (int b = 0; b < B; b++) {
-        int k = lane + b * TPA;
-        e0[b] = k < cnt ? __ldg(lp + b * step) : (unsigned)ii;
-        int k1 = k + TPA * B;
-        e1[b] = k1 < cnt ? __ldg(lp + (b + B) * step) : (unsigned)ii;
+        for (int b = 0; b < B; b++) e0[b] = __ldg(lp + b * TPA);
+#pragma unroll
+        for (int b = 0; b < B; b++) p0[b] = __ldg(pos4 + (e0[b] & MD_INDEX_MASK));
     }
+    if (nb > 1) {
 #pragma unroll
-    for (int b = 0; b < B; b++) p0[b] = __ldg(pos4 + (e0[b] & MD_INDEX_MASK));
+        for (int b = 0; b < B; b++) e1[b] = __ldg(lp + (B + b) * TPA);
+    }
+#pragma unroll 2
     for (int t = 0; t < nb; t++) {
-        const int kb = lane + t * TPA * B;
         float4 p1[B];
         unsigned e2[B];
+        if (t + 1 < nb) {
 #pragma unroll
-        for (int b = 0; b < B; b++) p1[b] = __ldg(pos4 + (e1[b] & MD_INDEX_MASK));
+            for (int b = 0; b < B; b++) p1[b] = __ldg(pos4 + (e1[b] & MD_INDEX_MASK));
+        }
+        if (t + 2 < nb) {
 #pragma unroll
-        for (int b = 0; b < B; b++) {
-            int k2 = kb + (2 * B + b) * TPA;
-            e2[b] = k2 < cnt ? __ldg(lp + (2 * B + b) * step) : (unsigned)ii;
+            for (int b = 0; b < B; b++) e2[b] = __ldg(lp + ((t + 2) * B + b) * TPA);
         }
 #pragma unroll
         for (int b = 0; b < B; b++)
-            pair_term<KIND, ENERGY>(kp, pc, pi, qi, p0[b], ljrow[e0[b] >> MD_TYPE_SHIFT],
-                                    kb + b * TPA < cnt, acc);
+            pair_term<KIND, ENERGY>(kp, pc, pi, qi, p0[b], ljrow[e0[b] >> MD_TYPE_SHIFT], true, acc);
 #pragma unroll
         for (int b = 0; b < B; b++) {
             e0[b] = e1[b];
             p0[b] = p1[b];
             e1[b] = e2[b];
         }
-        lp += B * step;
     }
     long long ax = __float2ll_rn(acc.fx * 4294967296.0f);
     long long ay = __float2ll_rn(acc.fy * 4294967296.0f);
@@ -187,6 +188,7 @@ __global__ void __launch_bounds__(128) k_pair(md_kparams kp, pair_consts pc,
             if (ENERGY) fe += __shfl_down_sync(mask, fe, off, TPA);
         }
     }
+    const size_t P = (size_t)kp.pitch;
     if (active && lane == 0) {
         f[i] = ax;
         f[P + i] = ay;
@@ -279,7 +281,8 @@ void pair_dispatch(md_ctx *c, const md_kparams &kp, const pair_consts &pc)
     switch (c->pair_tpa) {
 #define MD_PAIR_CASE(T)                                                                          \
     case T:                                                                                      \
-        k_pair<KIND, T, (T >= 8 ? 4 : 8), ENERGY><<<nb, 128, 0, c->stream>>>(                      \
+        k_pair<KIND, T, (T >= 32 ? 1 : (T >= 16 ? 2 : (T >= 8 ? 4 : 8))), ENERGY>               \
+            <<<nb, 128, 0, c->stream>>>(                                                         \
             kp, pc, c->pos4, c->type, c->nl, c->nl_n, lj, c->f, c->vir, c->epot);                \
         break;
         MD_PAIR_CASE(1)

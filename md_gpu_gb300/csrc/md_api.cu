@@ -436,6 +436,12 @@ md_kparams md_make_kparams(const md_ctx *c)
         kp.binlen[d] = c->binlen[d];
         kp.stencil[d] = c->stencil[d];
     }
+    /* The image of a stencil cell gives the reference's rint(d/L) exactly when
+     * every candidate pair is well inside half a box: |d| <= (S+1) bin < 0.49 L. */
+    kp.cell_shift = 1;
+    for (int d = 0; d < 3; d++)
+        if (c->stencil[d] < 0 || (c->stencil[d] + 1) * (double)c->binlen[d] >= 0.49 * (double)c->box[d])
+            kp.cell_shift = 0;
     kp.rcutsq = c->rcutsq;
     kp.reacf = c->reacf;
     kp.rskinsq = c->rskinsq;
@@ -890,7 +896,8 @@ md_status md_get_neighbor_list(md_ctx *c, unsigned *nnlist, unsigned *nnlist_max
     for (int i = 0; i < pitch; i++) nnlist_max[i] = 0;
     for (int si = 0; si < c->n; si++) {
         row.clear();
-        for (int k = 0; k < cnt[si]; k++) row.push_back((unsigned)perm[nl[(size_t)k * P + si] & MD_INDEX_MASK]);
+        for (int k = 0; k < cnt[si]; k++)
+            row.push_back((unsigned)perm[nl[(size_t)si * c->cap + k] & MD_INDEX_MASK]);
         std::sort(row.begin(), row.end());
         int o = perm[si];
         nnlist_max[o] = (unsigned)row.size();

@@ -14,8 +14,10 @@
  *   fx,fy,fz int64 fixed point (FX_SCALE units of kJ/mol/A): every force
  *            term adds into these, so the sum is order independent
  *   vir      float, sum of ff r^2 (the reference's force.w, 6 x virial)
- *   nl       neighbour list, column-major nl[k*pitch + s], entry =
- *            j | (type_j << 29)
+ *   nl       neighbour list, one row of `cap` entries per atom
+ *            (nl[s*cap + k]), entry = j | (type_j << 29); each row is padded
+ *            to a multiple of 32 entries with the atom itself (r = 0, which
+ *            the force kernel skips), so readers need no bounds predicate
  */
 #ifndef MD_INTERNAL_H
 #define MD_INTERNAL_H
@@ -32,6 +34,7 @@
 #define MD_TYPE_SHIFT 29
 #define MD_INDEX_MASK 0x1FFFFFFFu
 #define MD_EXCL_NONE 0xFFFFFFFFu
+#define MD_LIST_QUANTUM 32   /* list rows are padded to multiples of this */
 #define FX_SCALE 4294967296.0      /* 2^32 */
 #define FX_INV (1.0 / 4294967296.0)
 
@@ -65,6 +68,7 @@ struct md_kparams {
     int ncell[3];
     float binlen[3];
     int stencil[3];   /* cell range per axis: +-stencil, or -1 = all cells */
+    int cell_shift;   /* 1: a stencil cell's periodic image fixes the min-image shift */
     double dt;
 };
 
