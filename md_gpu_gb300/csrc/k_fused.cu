@@ -1,0 +1,115 @@
+/*
+ * k_fused.cu -- one kernel per leapfrog step for systems without bonded
+ * terms: pair forces (pair_forces.cu:133-205 / :34-131), then in the same
+ * thread the leapfrog update of that atom (nve_leapfrog.cu:31-60,
+ * nvt_leapfrog_ber.cu:29-80), the next step's list check
+ * (neighborlist.cu:157-176) and the FP64 kinetic-energy partial; the last
+ * block to finish reduces the partials and sets the rebuild condition.
+ *
+ * Positions are double buffered: the step reads pos4 and writes the updated
+ * copy to pos4_next, so no thread sees a neighbour that has already moved.
+ * The forces never leave the registers except for the copy kept for
+ * read-out.
+ */
+#include "md_pair.cuh"
+#include "md_thermo.cuh"
+
+namespace {
+
+template <int KIND, int TPA, int B>
+__global__ void __launch_bounds__(128) k_pair_leapfrog(
+    md_kparams kp, pair_consts pc, thermo_par tp, step_io io, const float4 *__restrict__ pos4,
+    float4 *__restrict__ pos4_next, const int *__restrict__ type, const unsigned *__restrict__ nl,
+    const int *__restrict__ nl_n, const float2 *__restrict__ ljtab, long long *f, float *vir,
+    double *x, double *v, const double *__restrict__ mass)
+{
+    __shared__ float2 lj[MD_MAXTYPE * MD_MAXTYPE];
+    __shared__ double sh[8];
+    if (threadIdx.x < MD_MAXTYPE * MD_MAXTYPE) lj[threadIdx.x] = ljtab[threadIdx.x];
+    __syncthreads();
+    int gt = blockIdx.x * blockDim.x + threadIdx.x;
+    int i = gt / TPA, lane = gt % TPA;
+    bool active = i < kp.n;
+    pair_total t = pair_sum<KIND, TPA, B, false>(kp, pc, active ? i : 0, active, lane, pos4, type,
+                                                 nl, nl_n, lj);
+    double ke = 0.0;
+    if (active && lane == 0) {
+        const size_t P = (size_t)kp.pitch;
+        f[i] = t.fx;
+        f[P + i] = t.fy;
+        f[2 * P + i] = t.fz;
+        vir[i] = t.fw;
+        double lam = 1.0;
+        if (tp.berendsen) lam = sqrt(1.0 + kp.dt / tp.tau * (tp.t0 / io.st->temper - 1.0));
+        const long long fi[3] = {t.fx, t.fy, t.fz};
+        double m = mass[i], dtm = kp.dt / m;
+        double xn[3];
+        for (int d = 0; d < 3; d++) {
+            double F = (double)fi[d] * FX_INV;
+            double vv = (v[d * P + i] + F * dtm) * lam;
+            v[d * P + i] = vv;
+            double xx = wrap(x[d * P + i] + vv * kp.dt, kp.boxd[d]);
+            x[d * P + i] = xx;
+            xn[d] = xx;
+            ke += vv * vv;
+        }
+        ke *= 0.5 * m;
+        float4 p = make_float4((float)xn[0], (float)xn[1], (float)xn[2], pos4[i].w);
+        pos4_next[i] = p;
+        check_moved(p, io.pos_old[i], kp, io.st);
+    }
+    write_partials(ke, 0.0, 0.0, 0, io.partials, sh);
+    if (md_last_block(io.counter)) {
+        finalize(kp, tp, 0, gridDim.x, io.partials, io.st, io.rec, io.rec_cap, sh);
+        if (threadIdx.x == 0) {
+            set_condition(io);
+            *io.counter = 0;
+        }
+    }
+}
+
+template <int KIND>
+void fused_dispatch(md_ctx *c, const md_kparams &kp, const pair_consts &pc, const thermo_par &tp,
+                    const step_io &io)
+{
+    long long threads = (long long)kp.n * c->pair_tpa;
+    int nb = (int)((threads + 127) / 128);
+    const float2 *lj = (const float2 *)c->lj_dev;
+    switch (c->pair_tpa) {
+#define MD_FUSED_CASE(T)                                                                         \
+    case T:                                                                                      \
+        k_pair_leapfrog<KIND, T, (T >= 32 ? 1 : (T >= 16 ? 2 : (T >= 8 ? 4 : 8)))>              \
+            <<<nb, 128, 0, c->stream>>>(kp, pc, tp, io, c->pos4, c->pos4_alt, c->type, c->nl,    \
+                                        c->nl_n, lj, c->f, c->vir, c->x, c->v, c->mass);         \
+        break;
+        MD_FUSED_CASE(1)
+        MD_FUSED_CASE(2)
+        MD_FUSED_CASE(4)
+        MD_FUSED_CASE(8)
+        MD_FUSED_CASE(16)
+        MD_FUSED_CASE(32)
+#undef MD_FUSED_CASE
+    default:
+        break;
+    }
+}
+
+}  // namespace
+
+bool md_can_fuse(const md_ctx *c)
+{
+    return c->integrator == MD_LEAPFROG && !c->has_bonds && !c->has_angles;
+}
+
+void launch_pair_leapfrog(md_ctx *c, const md_kparams &kp, unsigned long long cond, int has_cond)
+{
+    pair_consts pc = make_pair_consts(c);
+    thermo_par tp = make_tp(c, 0);
+    step_io io = make_io(c, cond, has_cond);
+    if (c->lkspace == 0) fused_dispatch<0>(c, kp, pc, tp, io);
+    else fused_dispatch<1>(c, kp, pc, tp, io);
+    /* the updated positions are now the current ones */
+    float4 *t = c->pos4;
+    c->pos4 = c->pos4_alt;
+    c->pos4_alt = t;
+}

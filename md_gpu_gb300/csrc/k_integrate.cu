@@ -21,136 +21,9 @@
  *   G = (2 KE - ndf k T0) / Q,  Q = ndf k T0 tau^2,
  * with the conserved quantity KE + PE + Q xi^2/2 + ndf k T0 eta.
  */
-#include "md_device.cuh"
+#include "md_thermo.cuh"
 
 namespace {
-
-constexpr double RGAS = 8.314e-3;   /* kJ/mol/K, as integrator.cu:155 (1000/8.314) */
-
-struct thermo_par {
-    double t0, tau, q_nh;
-    int ndf, berendsen, nh, energy;
-};
-
-/* Per-step bookkeeping buffers and the graph condition to set. */
-struct step_io {
-    md_devstate *st;
-    double *partials;
-    md_thermo *rec;
-    int rec_cap;
-    unsigned *counter;
-    const float4 *pos_old;
-    cudaGraphConditionalHandle cond;
-    int has_cond;
-};
-
-/* Sum of a double over the block; result valid in thread 0. */
-__device__ __forceinline__ double block_sum(double v, double *sh)
-{
-    for (int o = 16; o > 0; o >>= 1) v += __shfl_down_sync(0xffffffffu, v, o);
-    int w = threadIdx.x >> 5, l = threadIdx.x & 31;
-    if (l == 0) sh[w] = v;
-    __syncthreads();
-    double r = 0.0;
-    if (threadIdx.x == 0)
-        for (int k = 0; k < (int)(blockDim.x >> 5); k++) r += sh[k];
-    __syncthreads();
-    return r;
-}
-
-__device__ __forceinline__ double wrap(double x, double L)
-{
-    return x - L * trunc(x * 2.0 / L);
-}
-
-__device__ __forceinline__ void write_partials(double ke, double pe, double w, int energy,
-                                               double *partials, double *sh)
-{
-    double a = block_sum(ke, sh);
-    if (threadIdx.x == 0) partials[blockIdx.x] = a;
-    if (energy) {
-        double b = block_sum(pe, sh);
-        double c = block_sum(w, sh);
-        if (threadIdx.x == 0) {
-            partials[gridDim.x + blockIdx.x] = b;
-            partials[2 * gridDim.x + blockIdx.x] = c;
-        }
-    }
-}
-
-/* Fixed-order totals of the block partials, then (thread 0) temperature,
- * thermostat bookkeeping and the step record.  mode 0 leapfrog, 1 VV / NH,
- * 2 observe only (no step, the Berendsen reference temperature kept). */
-__device__ void finalize(const md_kparams &kp, const thermo_par &tp, int mode, int npart,
-                         const double *partials, md_devstate *st, md_thermo *rec, int rec_cap,
-                         double *sh)
-{
-    double a = 0.0, b = 0.0, c = 0.0;
-    for (int k = threadIdx.x; k < npart; k += blockDim.x) {
-        a += __ldcg(partials + k);
-        if (tp.energy) { b += __ldcg(partials + npart + k); c += __ldcg(partials + 2 * npart + k); }
-    }
-    double ke = block_sum(a, sh);
-    double pe = tp.energy ? block_sum(b, sh) : 0.0;
-    double w = tp.energy ? block_sum(c, sh) : 0.0;
-    if (threadIdx.x != 0) return;
-    volatile md_devstate *vs = st;
-    double kt = RGAS * tp.t0;
-    double lam = 1.0;
-    if (mode == 0 && tp.berendsen) lam = sqrt(1.0 + kp.dt / tp.tau * (tp.t0 / vs->temper - 1.0));
-    double xi = vs->xi, eta = vs->eta;
-    if (mode == 1) {
-        st->vscale = 1.0;
-        if (tp.nh) {
-            xi = vs->xi_a;
-            eta = vs->eta_a;
-            xi += 0.25 * kp.dt * (2.0 * ke - tp.ndf * kt) / tp.q_nh;
-            double s2 = exp(-0.5 * kp.dt * xi);
-            ke *= s2 * s2;
-            eta += 0.5 * kp.dt * xi;
-            xi += 0.25 * kp.dt * (2.0 * ke - tp.ndf * kt) / tp.q_nh;
-            st->vscale = s2;
-            st->xi = xi;
-            st->eta = eta;
-        }
-    }
-    double temper = 2.0 * ke / (tp.ndf * RGAS);
-    st->ke = ke;
-    if (tp.energy) { st->pe = pe; st->virial = w / 6.0; }
-    /* observing the state does not move the Berendsen reference temperature:
-     * the first step uses T = T0 (integrator.cu:77) */
-    if (mode == 2) return;
-    st->temper = temper;
-    st->lambda = lam;
-    long long step = vs->step;
-    md_thermo r;
-    r.step = step;
-    r.ke = ke;
-    r.temper = temper;
-    r.pe = tp.energy ? pe : 0.0;
-    r.virial = tp.energy ? w / 6.0 : 0.0;
-    r.conserved = tp.energy ? ke + pe + (tp.nh ? 0.5 * tp.q_nh * xi * xi + tp.ndf * kt * eta : 0.0) : 0.0;
-    r.xi = xi;
-    r.lambda = lam;
-    r.builds = vs->builds;
-    r.flags = tp.energy ? 1 : 0;
-    rec[step % rec_cap] = r;
-    st->step = step + 1;
-}
-
-__device__ __forceinline__ void check_moved(float4 p, float4 old, const md_kparams &kp,
-                                            md_devstate *st)
-{
-    if (md_rsq_exact(p, old, kp) >= kp.rmaxdif) st->update = 1;
-}
-
-__device__ __forceinline__ void set_condition(const step_io &io)
-{
-    if (io.has_cond) {
-        volatile md_devstate *vs = io.st;
-        cudaGraphSetConditional(io.cond, vs->update ? 1u : 0u);
-    }
-}
 
 /* Leapfrog update + list check + KE partials; the last block finalises. */
 __global__ void __launch_bounds__(256) k_leapfrog(md_kparams kp, thermo_par tp, step_io io,
@@ -324,35 +197,6 @@ __global__ void k_scatter_in(md_kparams kp, int what, md_devstate *st,
     } else {
         for (int d = 0; d < 3; d++) v[d * P + s] = in[3 * (size_t)o + d];
     }
-}
-
-thermo_par make_tp(const md_ctx *c, int energy)
-{
-    thermo_par tp;
-    tp.t0 = c->temper_0;
-    tp.tau = c->tau_t > 0 ? c->tau_t : 100.0;
-    tp.ndf = 3 * c->n - 3;
-    if (tp.ndf < 1) tp.ndf = 1;
-    tp.q_nh = tp.ndf * RGAS * tp.t0 * tp.tau * tp.tau;
-    if (tp.q_nh <= 0) tp.q_nh = 1.0;
-    tp.berendsen = (c->enstype == 1 && c->integrator == MD_LEAPFROG) ? 1 : 0;
-    tp.nh = (c->integrator == MD_NH) ? 1 : 0;
-    tp.energy = energy;
-    return tp;
-}
-
-step_io make_io(md_ctx *c, unsigned long long cond, int has_cond)
-{
-    step_io io;
-    io.st = c->st;
-    io.partials = c->partials;
-    io.rec = c->rec;
-    io.rec_cap = c->rec_cap;
-    io.counter = &c->st->blocks_done;
-    io.pos_old = c->pos_old;
-    io.cond = (cudaGraphConditionalHandle)cond;
-    io.has_cond = has_cond;
-    return io;
 }
 
 }  // namespace

@@ -245,7 +245,7 @@ md_status fail(md_ctx *c, md_status s, const std::string &msg)
 
 void free_device(md_ctx *c)
 {
-    void *ptrs[] = {c->x, c->v, c->mass, c->pos4, c->pos_old, c->type, c->perm, c->iperm, c->f,
+    void *ptrs[] = {c->x, c->v, c->mass, c->pos4, c->pos4_alt, c->pos_old, c->type, c->perm, c->iperm, c->f,
                     c->vir, c->epot, c->nl, c->nl_n, c->excl_orig, c->excl_s, c->cell_rank, c->cell_lin,
                     c->cell_count, c->cell_start, c->cell_fill, c->key, c->src, c->tmp_d, c->tmp4,
                     c->tmp_i, c->bl_o, c->bl_on, c->al_o, c->al_on, c->bl_s, c->bl_sn, c->al_s,
@@ -285,8 +285,12 @@ void enqueue_steps(md_ctx *c, int nsteps, int energy_first)
         int energy = (energy_first && k == 0) ? 1 : 0;
         if (c->integrator == MD_LEAPFROG) {
             launch_rebuild(c, kp, false);
-            launch_forces(c, kp, energy != 0, MD_TERM_ALL);
-            launch_leapfrog(c, kp, energy, 0, 0);
+            if (!energy && md_can_fuse(c)) {
+                launch_pair_leapfrog(c, kp, 0, 0);
+            } else {
+                launch_forces(c, kp, energy != 0, MD_TERM_ALL);
+                launch_leapfrog(c, kp, energy, 0, 0);
+            }
         } else {
             launch_vv_first(c, kp, 0, 0);
             launch_rebuild(c, kp, false);
@@ -352,15 +356,26 @@ md_status capture_graph(md_ctx *c, int nsteps, int energy_first)
         return fail(c, MD_ERR_CUDA, std::string("graph capture: ") + cudaGetErrorString(e));
     }
     md_status s = MD_OK;
+    const float4 *start_pos4 = c->pos4;
     if (c->integrator == MD_LEAPFROG) launch_set_condition(c, (unsigned long long)h[0]);
+    int fused = 0;
     for (int k = 0; k < nsteps && s == MD_OK; k++) {
         int energy = (energy_first && k == 0) ? 1 : 0;
         if (c->integrator == MD_LEAPFROG) {
             s = capture_rebuild_node(c, kp, h[k]);
             if (s != MD_OK) break;
-            launch_forces(c, kp, energy != 0, MD_TERM_ALL);
             int next = k + 1 < nsteps;
-            launch_leapfrog(c, kp, energy, next ? (unsigned long long)h[k + 1] : 0ull, next);
+            unsigned long long hn = next ? (unsigned long long)h[k + 1] : 0ull;
+            /* an even number of fused steps brings the position buffers back
+             * to where the graph started */
+            bool fuse = !energy && md_can_fuse(c) && (next || (fused & 1));
+            if (fuse) {
+                launch_pair_leapfrog(c, kp, hn, next);
+                fused++;
+            } else {
+                launch_forces(c, kp, energy != 0, MD_TERM_ALL);
+                launch_leapfrog(c, kp, energy, hn, next);
+            }
         } else {
             launch_vv_first(c, kp, (unsigned long long)h[k], 1);
             s = capture_rebuild_node(c, kp, h[k]);
@@ -371,6 +386,11 @@ md_status capture_graph(md_ctx *c, int nsteps, int energy_first)
     }
     cudaGraph_t out = nullptr;
     e = cudaStreamEndCapture(c->stream, &out);
+    if (c->pos4 != start_pos4) {   /* capture failed part way: restore the buffers */
+        float4 *t = c->pos4;
+        c->pos4 = c->pos4_alt;
+        c->pos4_alt = t;
+    }
     if (s != MD_OK) {
         cudaGraphDestroy(g);
         return s;
@@ -384,6 +404,7 @@ md_status capture_graph(md_ctx *c, int nsteps, int energy_first)
     if (e != cudaSuccess) return fail(c, MD_ERR_CUDA, std::string("graph instantiate: ") + cudaGetErrorString(e));
     c->gsteps = nsteps;
     c->genergy = energy_first;
+    c->gpos4 = c->pos4;
     return MD_OK;
 }
 
@@ -645,7 +666,7 @@ md_status md_create(const md_system_desc *d, void *stream, md_ctx **out)
     cudaError_t e = cudaSuccess;
 #define MD_ALLOC(ptr, cnt) if (e == cudaSuccess) e = dalloc(&(ptr), (cnt))
     MD_ALLOC(c->x, 3 * P); MD_ALLOC(c->v, 3 * P); MD_ALLOC(c->mass, P);
-    MD_ALLOC(c->pos4, P); MD_ALLOC(c->pos_old, P);
+    MD_ALLOC(c->pos4, P); MD_ALLOC(c->pos4_alt, P); MD_ALLOC(c->pos_old, P);
     MD_ALLOC(c->type, P); MD_ALLOC(c->perm, P); MD_ALLOC(c->iperm, P);
     MD_ALLOC(c->f, 3 * P); MD_ALLOC(c->vir, P); MD_ALLOC(c->epot, P);
     MD_ALLOC(c->nl_n, P);
@@ -657,7 +678,9 @@ md_status md_create(const md_system_desc *d, void *stream, md_ctx **out)
     MD_ALLOC(c->bl_o, 4 * P); MD_ALLOC(c->bl_on, P); MD_ALLOC(c->al_o, 4 * P); MD_ALLOC(c->al_on, P);
     MD_ALLOC(c->bl_s, 4 * P); MD_ALLOC(c->bl_sn, P); MD_ALLOC(c->al_s, 4 * P); MD_ALLOC(c->al_sn, P);
     c->npart = (int)(P / 256);
-    MD_ALLOC(c->partials, 3 * (size_t)c->npart + 8);
+    /* block partials of the integrators (256 threads) and of the fused step
+     * (128 threads, up to 32 per atom) */
+    MD_ALLOC(c->partials, 3 * (P / 4 + 256) + 8);
     MD_ALLOC(c->st, 1);
     c->rec_cap = 4096;
     MD_ALLOC(c->rec, c->rec_cap);
@@ -940,7 +963,7 @@ md_status md_step(md_ctx *c, int nsteps, int energy_every)
             continue;
         }
         int en = energy_every > 0 ? 1 : 0;
-        if (!c->gexec || c->gsteps != g || c->genergy != en) {
+        if (!c->gexec || c->gsteps != g || c->genergy != en || c->gpos4 != c->pos4) {
             md_status s = capture_graph(c, g, en);
             if (s != MD_OK) return s;
         }
@@ -1061,8 +1084,9 @@ md_status md_get_info(md_ctx *c, md_info *out)
     out->max_neighbors = *std::max_element(cnt.begin(), cnt.begin() + c->n);
     /* in a step graph without a rebuild: pair, bonded (if any), integrator
      * (leapfrog: one kernel; VV: two); a rebuild adds 9 kernels */
-    out->kernels_per_step = 1 + ((c->has_bonds || c->has_angles) ? 1 : 0) +
-                            (c->integrator == MD_LEAPFROG ? 1 : 2);
+    out->kernels_per_step = md_can_fuse(c) ? 1
+                                           : 1 + ((c->has_bonds || c->has_angles) ? 1 : 0) +
+                                                 (c->integrator == MD_LEAPFROG ? 1 : 2);
     return MD_OK;
 }
 

@@ -101,6 +101,7 @@ struct md_ctx {
     int device = 0;
     double *x = nullptr, *v = nullptr, *mass = nullptr;   /* sorted order */
     float4 *pos4 = nullptr, *pos_old = nullptr;
+    float4 *pos4_alt = nullptr;     /* second position buffer of the fused step */
     int *type = nullptr, *perm = nullptr, *iperm = nullptr;
     long long *f = nullptr;                               /* 3*pitch, SoA */
     float *vir = nullptr, *epot = nullptr;
@@ -132,6 +133,7 @@ struct md_ctx {
     cudaGraphExec_t gexec = nullptr;
     int gsteps = 0;
     int genergy = 0;
+    const float4 *gpos4 = nullptr; /* position buffer current when the graph was captured */
     long long host_step = 0;       /* steps run so far (mirrors st->step) */
     double *io_dev = nullptr;      /* 4*pitch doubles for host transfers */
     int pair_tpa = 8;    /* threads per atom in the pair kernel */
@@ -161,6 +163,11 @@ void launch_vv_second(md_ctx *c, const md_kparams &kp, int energy);
 void launch_thermo_from_state(md_ctx *c, const md_kparams &kp, int energy);
 void launch_gather_out(md_ctx *c, const md_kparams &kp, int what, void *dst);
 void launch_scatter_in(md_ctx *c, const md_kparams &kp, int what, const void *src);
+/* ---- launchers (k_fused.cu) ---- */
+/* Leapfrog systems without bonded terms step with one fused kernel. */
+bool md_can_fuse(const md_ctx *c);
+/* Pair forces + leapfrog + check in one kernel; swaps pos4 and pos4_alt. */
+void launch_pair_leapfrog(md_ctx *c, const md_kparams &kp, unsigned long long cond, int has_cond);
 
 #define MD_CUDA_TRY(c, expr)                                                   \
     do {                                                                       \

@@ -1,0 +1,211 @@
+/*
+ * md_pair.cuh -- the per-pair force law shared by the pair kernels.
+ *
+ * pair_forces.cu:34-205: for each listed j inside rc,
+ *   Wolf:  ff = qfac qi qj ([2a/sqrt(pi) r + P5(t) t] e^{-a^2 r^2} / r - W) / r^2,
+ *          t = 1/(1 + p a r), P5 = A&S 7.1.26 (simulation.h:39-44),
+ *   RF:    ff = qfac qi qj (1/r - k_rf r^2) / r^2,
+ *   + LJ:  ff += lj1 r^-14 - lj2 r^-8,
+ * F_i += ff d, w_i += ff r^2.
+ */
+#ifndef MD_PAIR_CUH
+#define MD_PAIR_CUH
+
+#include "md_internal.h"
+
+namespace {
+
+#define A1 0.254829592f
+#define A2 -0.284496736f
+#define A3 1.421413741f
+#define A4 -1.453152027f
+#define A5 1.061405429f
+#define QFAC 1389.35427611722f
+
+struct pair_consts {
+    float ucc;     /* Coulomb energy shift at rc */
+    float rc6i;    /* rc^-6 */
+    float rcinv;   /* 1/rc */
+};
+
+/* Round to nearest even for |t| < 2^22 with two FP32 adds (no conversion
+ * instruction): the minimum-image shift rint(d / L). */
+__device__ __forceinline__ float rint_small(float t)
+{
+    const float M = 12582912.0f;   /* 1.5 * 2^23 */
+    return __fsub_rn(__fadd_rn(t, M), M);
+}
+
+/* The hardware approximations (PTX ISA ex2/rsqrt/rcp .approx.ftz): relative
+ * errors ~2^-22, well inside the 1e-5 force tolerance; arguments here are
+ * never denormal. */
+__device__ __forceinline__ float ex2_approx(float x)
+{
+    float y;
+    asm("ex2.approx.ftz.f32 %0, %1;" : "=f"(y) : "f"(x));
+    return y;
+}
+__device__ __forceinline__ float rsqrt_approx(float x)
+{
+    float y;
+    asm("rsqrt.approx.ftz.f32 %0, %1;" : "=f"(y) : "f"(x));
+    return y;
+}
+__device__ __forceinline__ float rcp_approx(float x)
+{
+    float y;
+    asm("rcp.approx.ftz.f32 %0, %1;" : "=f"(y) : "f"(x));
+    return y;
+}
+
+struct pair_acc {
+    float fx, fy, fz, fw, fe;
+};
+
+/* One pair: F_i += ff d, w_i += ff r^2 (pair_forces.cu:165-200 / :74-120). */
+template <int KIND, bool ENERGY>
+__device__ __forceinline__ void pair_term(const md_kparams &kp, const pair_consts &pc, float4 pi,
+                                          float qi, float4 pj, float2 l, bool valid, pair_acc &a)
+{
+    float dx = pi.x - pj.x, dy = pi.y - pj.y, dz = pi.z - pj.z;
+    dx -= kp.box[0] * rint_small(dx * kp.boxi[0]);
+    dy -= kp.box[1] * rint_small(dy * kp.boxi[1]);
+    dz -= kp.box[2] * rint_small(dz * kp.boxi[2]);
+    float rsq = dx * dx + dy * dy + dz * dz;
+    float ri = rsqrt_approx(rsq);
+    float ri2 = ri * ri;
+    float qq = qi * pj.w;
+    float ff, uc = 0.0f;
+    if (KIND == 1) {
+        float r = rsq * ri;
+        float t = rcp_approx(1.0f + kp.palfa * r);
+        float poly = ((((A5 * t + A4) * t + A3) * t + A2) * t + A1) * t;
+        float ex = ex2_approx(kp.alfasq * rsq);
+        ff = ((kp.spiialfa * r + poly) * ex * ri - kp.wolf) * qq;
+        if (ENERGY) uc = qq * (poly * ex * ri - pc.ucc + kp.wolf * __logf(r * pc.rcinv));
+    } else {
+        ff = qq * (ri - kp.reacf * rsq);
+        if (ENERGY) uc = qq * (ri + 0.5f * kp.reacf * rsq - pc.ucc);
+    }
+    float ri6 = ri2 * ri2 * ri2;
+    ff = ff * ri2 + (l.x * ri6 - l.y) * ri6 * ri2;
+    /* list padding entries point at the atom itself: r = 0 is skipped */
+    bool in = valid && rsq <= kp.rcutsq && rsq > 0.0f;
+    ff = in ? ff : 0.0f;
+    a.fx += ff * dx;
+    a.fy += ff * dy;
+    a.fz += ff * dz;
+    a.fw += ff * rsq;
+    if (ENERGY) {
+        float ulj = l.x * (1.0f / 12.0f) * (ri6 * ri6 - pc.rc6i * pc.rc6i) -
+                    l.y * (1.0f / 6.0f) * (ri6 - pc.rc6i);
+        a.fe += in ? 0.5f * (uc + ulj) : 0.0f;
+    }
+}
+
+
+struct pair_total {
+    long long fx, fy, fz;   /* int64 fixed point, valid in lane 0 of the atom's group */
+    float fw, fe;
+};
+
+/* Pair forces of atom ii from its list: TPA lanes per atom, lane l takes the
+ * entries l, l+TPA, ... in batches of B (TPA*B divides 32, the padding
+ * quantum of the list rows, so no entry needs a bounds test).  The loads are
+ * software pipelined: while batch t is computed, the positions of batch t+1
+ * and the list entries of batch t+2 are in flight.  Each lane sums in FP32
+ * and converts its sum to int64 once; lane sums are combined with integer
+ * shuffles (exact), so the result depends only on TPA.  Every lane of the
+ * warp must call this (the shuffles use the full mask). */
+template <int KIND, int TPA, int B, bool ENERGY>
+__device__ __forceinline__ pair_total pair_sum(const md_kparams &kp, const pair_consts &pc, int ii,
+                                               bool active, int lane,
+                                               const float4 *__restrict__ pos4,
+                                               const int *__restrict__ type,
+                                               const unsigned *__restrict__ nl,
+                                               const int *__restrict__ nl_n, const float2 *lj)
+{
+    static_assert(MD_LIST_QUANTUM % (TPA * B) == 0, "batch must divide the list padding");
+    const float4 pi = pos4[ii];
+    const int cnt = active ? nl_n[ii] : 0;
+    const int nb = ((cnt + MD_LIST_QUANTUM - 1) / MD_LIST_QUANTUM) * (MD_LIST_QUANTUM / (TPA * B));
+    const float2 *ljrow = lj + type[ii] * MD_MAXTYPE;
+    const float qi = QFAC * pi.w;
+    pair_acc acc = {0.0f, 0.0f, 0.0f, 0.0f, 0.0f};
+    const unsigned *lp = nl + (size_t)ii * kp.cap + lane;
+    unsigned e0[B], e1[B];
+    float4 p0[B];
+    if (nb > 0) {
+#pragma unroll
+        for (int b = 0; b < B; b++) e0[b] = __ldg(lp + b * TPA);
+#pragma unroll
+        for (int b = 0; b < B; b++) p0[b] = __ldg(pos4 + (e0[b] & MD_INDEX_MASK));
+    }
+    if (nb > 1) {
+#pragma unroll
+        for (int b = 0; b < B; b++) e1[b] = __ldg(lp + (B + b) * TPA);
+    }
+#pragma unroll 2
+    for (int t = 0; t < nb; t++) {
+        float4 p1[B];
+        unsigned e2[B];
+        if (t + 1 < nb) {
+#pragma unroll
+            for (int b = 0; b < B; b++) p1[b] = __ldg(pos4 + (e1[b] & MD_INDEX_MASK));
+        }
+        if (t + 2 < nb) {
+#pragma unroll
+            for (int b = 0; b < B; b++) e2[b] = __ldg(lp + ((t + 2) * B + b) * TPA);
+        }
+#pragma unroll
+        for (int b = 0; b < B; b++)
+            pair_term<KIND, ENERGY>(kp, pc, pi, qi, p0[b], ljrow[e0[b] >> MD_TYPE_SHIFT], true, acc);
+#pragma unroll
+        for (int b = 0; b < B; b++) {
+            e0[b] = e1[b];
+            p0[b] = p1[b];
+            e1[b] = e2[b];
+        }
+    }
+    pair_total r;
+    r.fx = __float2ll_rn(acc.fx * 4294967296.0f);
+    r.fy = __float2ll_rn(acc.fy * 4294967296.0f);
+    r.fz = __float2ll_rn(acc.fz * 4294967296.0f);
+    r.fw = acc.fw;
+    r.fe = acc.fe;
+    if (TPA > 1) {
+        const unsigned mask = 0xffffffffu;
+#pragma unroll
+        for (int off = TPA / 2; off > 0; off >>= 1) {
+            r.fx += __shfl_down_sync(mask, r.fx, off, TPA);
+            r.fy += __shfl_down_sync(mask, r.fy, off, TPA);
+            r.fz += __shfl_down_sync(mask, r.fz, off, TPA);
+            r.fw += __shfl_down_sync(mask, r.fw, off, TPA);
+            if (ENERGY) r.fe += __shfl_down_sync(mask, r.fe, off, TPA);
+        }
+    }
+    return r;
+}
+
+inline pair_consts make_pair_consts(const md_ctx *c)
+{
+    pair_consts pc;
+    double rc = sqrt((double)c->rcutsq);
+    pc.rcinv = (float)(1.0 / rc);
+    pc.rc6i = (float)(1.0 / (rc * rc * rc * rc * rc * rc));
+    if (c->lkspace == 1) {
+        double a = c->alfa, x = a * rc;
+        double t = 1.0 / (1.0 + (double)0.3275911f * x);
+        double poly = ((((double)A5 * t + (double)A4) * t + (double)A3) * t + (double)A2) * t + (double)A1;
+        pc.ucc = (float)(poly * t * exp(-x * x) / rc);
+    } else if (c->lkspace == 0) {
+        pc.ucc = (float)(1.0 / rc + 0.5 * (double)c->reacf * rc * rc);
+    } else {
+        pc.ucc = 0.0f;
+    }
+    return pc;
+}
+
+}  // namespace
+
+#endif
