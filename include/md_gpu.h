@@ -175,6 +175,9 @@ md_status md_autotune(md_ctx *ctx, int *pair_tpa, int *list_tpa);
  * 1-2 bonded pairs): bit b of mask[a] excludes every pair of types a and b
  * from the neighbour list (made symmetric); ntype entries.  Rebuilds the list. */
 md_status md_set_type_exclusions(md_ctx *ctx, const unsigned *mask);
+/* md_step launches each step's kernels eagerly instead of replaying a
+ * captured graph when use_graphs is 0 (for profilers and debugging). */
+md_status md_set_graphs(md_ctx *ctx, int use_graphs);
 /* Milliseconds of device time of the last md_step call (CUDA events). */
 md_status md_last_step_ms(md_ctx *ctx, float *ms);
 /* The pair-force kernel alone, nrep launches on the context's stream between

@@ -947,10 +947,10 @@ md_status md_step(md_ctx *c, int nsteps, int energy_every)
     while (left > 0) {
         int aligned = energy_every > 0 ? (int)(c->host_step % energy_every == 0) : 1;
         int g = energy_every > 0 ? energy_every : std::min(nsteps, 32);
-        if (!aligned || left < g) {
+        if (!aligned || left < g || !c->use_graphs) {
             /* eager steps up to the next aligned step / the remainder */
             int k = left;
-            if (energy_every > 0 && !aligned) {
+            if (energy_every > 0 && !aligned && c->use_graphs) {
                 long long next = (c->host_step / energy_every + 1) * energy_every;
                 k = (int)std::min<long long>(left, next - c->host_step);
             }
@@ -1151,6 +1151,13 @@ md_status md_autotune(md_ctx *c, int *pair_tpa, int *list_tpa)
     }
     if (pair_tpa) *pair_tpa = bp;
     if (list_tpa) *list_tpa = bl;
+    return MD_OK;
+}
+
+md_status md_set_graphs(md_ctx *c, int use_graphs)
+{
+    if (!c) return MD_ERR_ARG;
+    c->use_graphs = use_graphs ? 1 : 0;
     return MD_OK;
 }
 

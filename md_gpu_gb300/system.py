@@ -101,6 +101,7 @@ def library(path: Optional[str] = None):
     L.md_time_rebuild.argtypes = [vp, C.c_int, C.POINTER(C.c_float)]
     L.md_autotune.argtypes = [vp, C.POINTER(C.c_int), C.POINTER(C.c_int)]
     L.md_set_type_exclusions.argtypes = [vp, vp]
+    L.md_set_graphs.argtypes = [vp, C.c_int]
     L.md_ref_kinetic_energy_noalloc.argtypes = [vp, C.c_int, vp, vp]
     _lib = L
     return L
@@ -324,6 +325,10 @@ class MDSystem:
         """mask[a] bit b: exclude all pairs of types a and b (0-based)."""
         m = np.ascontiguousarray(mask, np.uint32)
         _check(library().md_set_type_exclusions(self._ctx, m.ctypes.data), self._ctx)
+
+    def set_graphs(self, use_graphs=True):
+        """Replay captured step graphs (default) or launch eagerly."""
+        _check(library().md_set_graphs(self._ctx, 1 if use_graphs else 0), self._ctx)
 
     def set_tuning(self, pair_tpa, list_tpa):
         _check(library().md_set_tuning(self._ctx, pair_tpa, list_tpa), self._ctx)
