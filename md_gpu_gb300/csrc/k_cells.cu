@@ -115,6 +115,7 @@ __global__ void k_cell_order(md_kparams kp, const md_devstate *st, int always, i
 __global__ void k_permute(md_kparams kp, const md_devstate *st, int always,
                           const int *__restrict__ src, const double *__restrict__ x,
                           const double *__restrict__ v, const double *__restrict__ mass,
+                          const double *__restrict__ minv,
                           const float4 *__restrict__ pos4, const int *__restrict__ perm,
                           const int *__restrict__ type, double *tmp_d, float4 *tmp4, int *tmp_i)
 {
@@ -127,6 +128,7 @@ __global__ void k_permute(md_kparams kp, const md_devstate *st, int always,
         tmp_d[(3 + d) * P + s] = v[d * P + o];
     }
     tmp_d[6 * P + s] = mass[o];
+    tmp_d[7 * P + s] = minv[o];
     tmp4[s] = pos4[o];
     tmp_i[s] = perm[o];
     tmp_i[P + s] = type[o];
@@ -135,7 +137,7 @@ __global__ void k_permute(md_kparams kp, const md_devstate *st, int always,
 __global__ void k_copyback(md_kparams kp, const md_devstate *st, int always,
                            const double *__restrict__ tmp_d, const float4 *__restrict__ tmp4,
                            const int *__restrict__ tmp_i, double *x, double *v, double *mass,
-                           float4 *pos4, int *perm, int *iperm, int *type)
+                           double *minv, float4 *pos4, int *perm, int *iperm, int *type)
 {
     if (!always && !st->update) return;
     int s = blockIdx.x * blockDim.x + threadIdx.x;
@@ -146,6 +148,7 @@ __global__ void k_copyback(md_kparams kp, const md_devstate *st, int always,
         v[d * P + s] = tmp_d[(3 + d) * P + s];
     }
     mass[s] = tmp_d[6 * P + s];
+    minv[s] = tmp_d[7 * P + s];
     pos4[s] = tmp4[s];
     int o = tmp_i[s];
     perm[s] = o;
@@ -455,10 +458,10 @@ void launch_rebuild(md_ctx *c, const md_kparams &kp, bool unconditional)
     k_cell_scatter<<<nb, 256, 0, s>>>(kp, c->st, always, c->key, c->cell_start, c->cell_fill, c->src);
     k_cell_order<<<(c->ncells + 255) / 256, 256, 0, s>>>(kp, c->st, always, c->ncells,
                                                           c->cell_start, c->perm, c->src);
-    k_permute<<<nb, 256, 0, s>>>(kp, c->st, always, c->src, c->x, c->v, c->mass, c->pos4, c->perm,
-                                 c->type, c->tmp_d, c->tmp4, c->tmp_i);
+    k_permute<<<nb, 256, 0, s>>>(kp, c->st, always, c->src, c->x, c->v, c->mass, c->minv, c->pos4,
+                                 c->perm, c->type, c->tmp_d, c->tmp4, c->tmp_i);
     k_copyback<<<nb, 256, 0, s>>>(kp, c->st, always, c->tmp_d, c->tmp4, c->tmp_i, c->x, c->v,
-                                  c->mass, c->pos4, c->perm, c->iperm, c->type);
+                                  c->mass, c->minv, c->pos4, c->perm, c->iperm, c->type);
     k_remap<<<nb, 256, 0, s>>>(kp, c->st, always, c->perm, c->iperm, c->excl_orig, c->excl_s,
                                c->bl_o, c->bl_on, c->bl_s, c->bl_sn, c->al_o, c->al_on, c->al_s,
                                c->al_sn, c->has_bonds, c->has_angles);

@@ -21,10 +21,13 @@ __global__ void __launch_bounds__(128) k_pair_leapfrog(
     md_kparams kp, pair_consts pc, thermo_par tp, step_io io, const float4 *__restrict__ pos4,
     float4 *__restrict__ pos4_next, const int *__restrict__ type, const unsigned *__restrict__ nl,
     const int *__restrict__ nl_n, const float2 *__restrict__ ljtab, long long *f, float *vir,
-    double *x, double *v, const double *__restrict__ mass)
+    double *x, double *v, const double *__restrict__ mass, const double *__restrict__ minv)
 {
+    constexpr int NA = 128 / TPA;   /* atoms per block */
     __shared__ float2 lj[MD_MAXTYPE * MD_MAXTYPE];
     __shared__ double sh[8];
+    __shared__ long long s_f[NA][3];
+    __shared__ float s_x[NA][3];
     if (threadIdx.x < MD_MAXTYPE * MD_MAXTYPE) lj[threadIdx.x] = ljtab[threadIdx.x];
     __syncthreads();
     int gt = blockIdx.x * blockDim.x + threadIdx.x;
@@ -32,31 +35,46 @@ __global__ void __launch_bounds__(128) k_pair_leapfrog(
     bool active = i < kp.n;
     pair_total t = pair_sum<KIND, TPA, B, false>(kp, pc, active ? i : 0, active, lane, pos4, type,
                                                  nl, nl_n, lj);
-    double ke = 0.0;
-    if (active && lane == 0) {
-        const size_t P = (size_t)kp.pitch;
-        f[i] = t.fx;
-        f[P + i] = t.fy;
-        f[2 * P + i] = t.fz;
-        vir[i] = t.fw;
-        double lam = 1.0;
-        if (tp.berendsen) lam = sqrt(1.0 + kp.dt / tp.tau * (tp.t0 / io.st->temper - 1.0));
-        const long long fi[3] = {t.fx, t.fy, t.fz};
-        double m = mass[i], dtm = kp.dt / m;
-        double xn[3];
-        for (int d = 0; d < 3; d++) {
-            double F = (double)fi[d] * FX_INV;
-            double vv = (v[d * P + i] + F * dtm) * lam;
-            v[d * P + i] = vv;
-            double xx = wrap(x[d * P + i] + vv * kp.dt, kp.boxd[d]);
-            x[d * P + i] = xx;
-            xn[d] = xx;
-            ke += vv * vv;
+    const size_t P = (size_t)kp.pitch;
+    if (lane == 0) {
+        int a = threadIdx.x / TPA;
+        s_f[a][0] = t.fx;
+        s_f[a][1] = t.fy;
+        s_f[a][2] = t.fz;
+        if (active) {
+            f[i] = t.fx;
+            f[P + i] = t.fy;
+            f[2 * P + i] = t.fz;
+            vir[i] = t.fw;
         }
-        ke *= 0.5 * m;
-        float4 p = make_float4((float)xn[0], (float)xn[1], (float)xn[2], pos4[i].w);
-        pos4_next[i] = p;
-        check_moved(p, io.pos_old[i], kp, io.st);
+    }
+    __syncthreads();
+    /* FP64 leapfrog of the block's atoms spread over all threads, one
+     * (atom, axis) per thread: full warps on the FP64 pipe */
+    const int i0 = blockIdx.x * NA;
+    const double lam = tp.berendsen ? io.st->lam_next : 1.0;
+    double ke = 0.0;
+    for (int k = threadIdx.x; k < 3 * NA; k += blockDim.x) {
+        int a = k / 3, d = k - 3 * a, ia = i0 + a;
+        if (ia < kp.n) {
+            double F = (double)s_f[a][d] * FX_INV;
+            double vv = (v[d * P + ia] + F * (kp.dt * minv[ia])) * lam;
+            v[d * P + ia] = vv;
+            double xx = wrap(x[d * P + ia] + vv * kp.dt, kp.boxd[d], kp.box2i[d]);
+            x[d * P + ia] = xx;
+            s_x[a][d] = (float)xx;
+            ke += 0.5 * mass[ia] * vv * vv;
+        }
+    }
+    __syncthreads();
+    if (threadIdx.x < NA) {
+        int ia = i0 + threadIdx.x;
+        if (ia < kp.n) {
+            float4 p = make_float4(s_x[threadIdx.x][0], s_x[threadIdx.x][1], s_x[threadIdx.x][2],
+                                   pos4[ia].w);
+            pos4_next[ia] = p;
+            check_moved(p, io.pos_old[ia], kp, io.st);
+        }
     }
     write_partials(ke, 0.0, 0.0, 0, io.partials, sh);
     if (md_last_block(io.counter)) {
@@ -80,7 +98,7 @@ void fused_dispatch(md_ctx *c, const md_kparams &kp, const pair_consts &pc, cons
     case T:                                                                                      \
         k_pair_leapfrog<KIND, T, (T >= 32 ? 1 : (T >= 16 ? 2 : (T >= 8 ? 4 : 8)))>              \
             <<<nb, 128, 0, c->stream>>>(kp, pc, tp, io, c->pos4, c->pos4_alt, c->type, c->nl,    \
-                                        c->nl_n, lj, c->f, c->vir, c->x, c->v, c->mass);         \
+                                        c->nl_n, lj, c->f, c->vir, c->x, c->v, c->mass, c->minv); \
         break;
         MD_FUSED_CASE(1)
         MD_FUSED_CASE(2)

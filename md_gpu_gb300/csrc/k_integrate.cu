@@ -28,7 +28,8 @@ namespace {
 /* Leapfrog update + list check + KE partials; the last block finalises. */
 __global__ void __launch_bounds__(256) k_leapfrog(md_kparams kp, thermo_par tp, step_io io,
                                                   double *x, double *v,
-                                                  const double *__restrict__ mass, float4 *pos4,
+                                                  const double *__restrict__ mass,
+                                                  const double *__restrict__ minv, float4 *pos4,
                                                   const long long *__restrict__ f,
                                                   const float *__restrict__ epot,
                                                   const float *__restrict__ vir)
@@ -36,17 +37,16 @@ __global__ void __launch_bounds__(256) k_leapfrog(md_kparams kp, thermo_par tp, 
     __shared__ double sh[8];
     int s = blockIdx.x * blockDim.x + threadIdx.x;
     const int P = kp.pitch;
-    double lam = 1.0;
-    if (tp.berendsen) lam = sqrt(1.0 + kp.dt / tp.tau * (tp.t0 / io.st->temper - 1.0));
+    const double lam = tp.berendsen ? io.st->lam_next : 1.0;
     double ke = 0.0, pe = 0.0, w = 0.0;
     if (s < kp.n) {
-        double m = mass[s], dtm = kp.dt / m;
+        double m = mass[s], dtm = kp.dt * minv[s];
         double xn[3];
         for (int d = 0; d < 3; d++) {
             double F = (double)f[d * P + s] * FX_INV;
             double vv = (v[d * P + s] + F * dtm) * lam;
             v[d * P + s] = vv;
-            double xx = wrap(x[d * P + s] + vv * kp.dt, kp.boxd[d]);
+            double xx = wrap(x[d * P + s] + vv * kp.dt, kp.boxd[d], kp.box2i[d]);
             x[d * P + s] = xx;
             xn[d] = xx;
             ke += vv * vv;
@@ -72,32 +72,23 @@ __global__ void __launch_bounds__(256) k_leapfrog(md_kparams kp, thermo_par tp, 
  * list check; the last block sets the rebuild condition. */
 __global__ void __launch_bounds__(256) k_vv_first(md_kparams kp, thermo_par tp, step_io io,
                                                   double *x, double *v,
-                                                  const double *__restrict__ mass, float4 *pos4,
+                                                  const double *__restrict__ minv, float4 *pos4,
                                                   const long long *__restrict__ f)
 {
     int s = blockIdx.x * blockDim.x + threadIdx.x;
     const int P = kp.pitch;
     md_devstate *st = io.st;
-    double scale = st->vscale;
-    if (tp.nh) {
-        /* every thread evaluates the same scalar update; one thread stores it */
-        double kt = RGAS * tp.t0, ke = st->ke, xi = st->xi, eta = st->eta;
-        xi += 0.25 * kp.dt * (2.0 * ke - tp.ndf * kt) / tp.q_nh;
-        double s1 = exp(-0.5 * kp.dt * xi);
-        ke *= s1 * s1;
-        eta += 0.5 * kp.dt * xi;
-        xi += 0.25 * kp.dt * (2.0 * ke - tp.ndf * kt) / tp.q_nh;
-        scale *= s1;
-        if (s == 0) { st->xi_a = xi; st->eta_a = eta; }
-    }
+    /* pending thermostat factor and, for NH, the first half step of this
+     * step, both prepared by the previous step's reduction */
+    const double scale = st->kick_scale;
     if (s < kp.n) {
-        double m = mass[s], hdtm = 0.5 * kp.dt / m;
+        double hdtm = 0.5 * kp.dt * minv[s];
         double xn[3];
         for (int d = 0; d < 3; d++) {
             double F = (double)f[d * P + s] * FX_INV;
             double vv = v[d * P + s] * scale + F * hdtm;
             v[d * P + s] = vv;
-            double xx = wrap(x[d * P + s] + vv * kp.dt, kp.boxd[d]);
+            double xx = wrap(x[d * P + s] + vv * kp.dt, kp.boxd[d], kp.box2i[d]);
             x[d * P + s] = xx;
             xn[d] = xx;
         }
@@ -120,6 +111,7 @@ __global__ void __launch_bounds__(256) k_vv_first(md_kparams kp, thermo_par tp, 
 __global__ void __launch_bounds__(256) k_vv_second(md_kparams kp, thermo_par tp, int kick,
                                                    step_io io, double *v,
                                                    const double *__restrict__ mass,
+                                                   const double *__restrict__ minv,
                                                    const long long *__restrict__ f,
                                                    const float *__restrict__ epot,
                                                    const float *__restrict__ vir)
@@ -130,7 +122,7 @@ __global__ void __launch_bounds__(256) k_vv_second(md_kparams kp, thermo_par tp,
     double ke = 0.0, pe = 0.0, w = 0.0;
     double scale = kick ? 1.0 : io.st->vscale;
     if (s < kp.n) {
-        double m = mass[s], hdtm = 0.5 * kp.dt / m;
+        double m = mass[s], hdtm = 0.5 * kp.dt * minv[s];
         for (int d = 0; d < 3; d++) {
             double vv = v[d * P + s];
             if (kick) {
@@ -205,28 +197,28 @@ void launch_leapfrog(md_ctx *c, const md_kparams &kp, int energy, unsigned long 
 {
     int nb = (kp.n + 255) / 256;
     k_leapfrog<<<nb, 256, 0, c->stream>>>(kp, make_tp(c, energy), make_io(c, cond, has_cond), c->x,
-                                          c->v, c->mass, c->pos4, c->f, c->epot, c->vir);
+                                          c->v, c->mass, c->minv, c->pos4, c->f, c->epot, c->vir);
 }
 
 void launch_vv_first(md_ctx *c, const md_kparams &kp, unsigned long long cond, int has_cond)
 {
     int nb = (kp.n + 255) / 256;
     k_vv_first<<<nb, 256, 0, c->stream>>>(kp, make_tp(c, 0), make_io(c, cond, has_cond), c->x,
-                                          c->v, c->mass, c->pos4, c->f);
+                                          c->v, c->minv, c->pos4, c->f);
 }
 
 void launch_vv_second(md_ctx *c, const md_kparams &kp, int energy)
 {
     int nb = (kp.n + 255) / 256;
     k_vv_second<<<nb, 256, 0, c->stream>>>(kp, make_tp(c, energy), 1, make_io(c, 0, 0), c->v,
-                                           c->mass, c->f, c->epot, c->vir);
+                                           c->mass, c->minv, c->f, c->epot, c->vir);
 }
 
 void launch_thermo_from_state(md_ctx *c, const md_kparams &kp, int energy)
 {
     int nb = (kp.n + 255) / 256;
     k_vv_second<<<nb, 256, 0, c->stream>>>(kp, make_tp(c, energy), 0, make_io(c, 0, 0), c->v,
-                                           c->mass, c->f, c->epot, c->vir);
+                                           c->mass, c->minv, c->f, c->epot, c->vir);
 }
 
 void launch_gather_out(md_ctx *c, const md_kparams &kp, int what, void *dst)

@@ -245,7 +245,7 @@ md_status fail(md_ctx *c, md_status s, const std::string &msg)
 
 void free_device(md_ctx *c)
 {
-    void *ptrs[] = {c->x, c->v, c->mass, c->pos4, c->pos4_alt, c->pos_old, c->type, c->perm, c->iperm, c->f,
+    void *ptrs[] = {c->x, c->v, c->mass, c->minv, c->pos4, c->pos4_alt, c->pos_old, c->type, c->perm, c->iperm, c->f,
                     c->vir, c->epot, c->nl, c->nl_n, c->excl_orig, c->excl_s, c->cell_rank, c->cell_lin,
                     c->cell_count, c->cell_start, c->cell_fill, c->key, c->src, c->tmp_d, c->tmp4,
                     c->tmp_i, c->bl_o, c->bl_on, c->al_o, c->al_on, c->bl_s, c->bl_sn, c->al_s,
@@ -453,6 +453,7 @@ md_kparams md_make_kparams(const md_ctx *c)
         kp.box[d] = c->box[d];
         kp.boxi[d] = c->boxi[d];
         kp.boxd[d] = (double)c->box[d];
+        kp.box2i[d] = 2.0 / (double)c->box[d];
         kp.ncell[d] = c->ncell[d];
         kp.binlen[d] = c->binlen[d];
         kp.stencil[d] = c->stencil[d];
@@ -665,7 +666,7 @@ md_status md_create(const md_system_desc *d, void *stream, md_ctx **out)
     const size_t P = c->pitch;
     cudaError_t e = cudaSuccess;
 #define MD_ALLOC(ptr, cnt) if (e == cudaSuccess) e = dalloc(&(ptr), (cnt))
-    MD_ALLOC(c->x, 3 * P); MD_ALLOC(c->v, 3 * P); MD_ALLOC(c->mass, P);
+    MD_ALLOC(c->x, 3 * P); MD_ALLOC(c->v, 3 * P); MD_ALLOC(c->mass, P); MD_ALLOC(c->minv, P);
     MD_ALLOC(c->pos4, P); MD_ALLOC(c->pos4_alt, P); MD_ALLOC(c->pos_old, P);
     MD_ALLOC(c->type, P); MD_ALLOC(c->perm, P); MD_ALLOC(c->iperm, P);
     MD_ALLOC(c->f, 3 * P); MD_ALLOC(c->vir, P); MD_ALLOC(c->epot, P);
@@ -674,7 +675,7 @@ md_status md_create(const md_system_desc *d, void *stream, md_ctx **out)
     MD_ALLOC(c->cell_rank, c->ncells); MD_ALLOC(c->cell_lin, c->ncells); MD_ALLOC(c->cell_count, c->ncells);
     MD_ALLOC(c->cell_start, c->ncells + 1); MD_ALLOC(c->cell_fill, c->ncells);
     MD_ALLOC(c->key, P); MD_ALLOC(c->src, P);
-    MD_ALLOC(c->tmp_d, 7 * P); MD_ALLOC(c->tmp4, P); MD_ALLOC(c->tmp_i, 3 * P);
+    MD_ALLOC(c->tmp_d, 8 * P); MD_ALLOC(c->tmp4, P); MD_ALLOC(c->tmp_i, 3 * P);
     MD_ALLOC(c->bl_o, 4 * P); MD_ALLOC(c->bl_on, P); MD_ALLOC(c->al_o, 4 * P); MD_ALLOC(c->al_on, P);
     MD_ALLOC(c->bl_s, 4 * P); MD_ALLOC(c->bl_sn, P); MD_ALLOC(c->al_s, 4 * P); MD_ALLOC(c->al_sn, P);
     c->npart = (int)(P / 256);
@@ -700,7 +701,7 @@ md_status md_create(const md_system_desc *d, void *stream, md_ctx **out)
     cudaEventCreate(&c->ev0);
     cudaEventCreate(&c->ev1);
     /* host staging in sorted order = original order before the first build */
-    std::vector<double> hx(3 * P, 0.0), hv(3 * P, 0.0), hm(P, 1.0);
+    std::vector<double> hx(3 * P, 0.0), hv(3 * P, 0.0), hm(P, 1.0), hmi(P, 1.0);
     std::vector<float4> hp(P, make_float4(0, 0, 0, 0));
     std::vector<int> ht(P, 0), hperm(P), hiperm(P);
     std::vector<uint4> hex(P, make_uint4(MD_EXCL_NONE, MD_EXCL_NONE, MD_EXCL_NONE, MD_EXCL_NONE));
@@ -710,6 +711,7 @@ md_status md_create(const md_system_desc *d, void *stream, md_ctx **out)
             hv[k * P + i] = d->vel ? d->vel[3 * i + k] : 0.0;
         }
         hm[i] = c->type_mass[c->itype[i]];
+        hmi[i] = 1.0 / hm[i];
         hp[i] = make_float4(d->pos[3 * i], d->pos[3 * i + 1], d->pos[3 * i + 2], c->charge[i]);
         ht[i] = c->itype[i];
         hex[i] = make_uint4(c->excl_host[4 * i], c->excl_host[4 * i + 1], c->excl_host[4 * i + 2],
@@ -732,6 +734,8 @@ md_status md_create(const md_system_desc *d, void *stream, md_ctx **out)
     hs.temper = c->temper_0;   /* integrator.cu:77 */
     hs.vscale = 1.0;
     hs.lambda = 1.0;
+    hs.lam_next = 1.0;     /* T_prev = T0 on the first step (integrator.cu:77) */
+    hs.kick_scale = 1.0;
     std::vector<int> zeros(c->ncells, 0);
     auto up = [&](void *dst, const void *srcp, size_t bytes) {
         if (e == cudaSuccess) e = cudaMemcpy(dst, srcp, bytes, cudaMemcpyHostToDevice);
@@ -739,6 +743,7 @@ md_status md_create(const md_system_desc *d, void *stream, md_ctx **out)
     up(c->x, hx.data(), sizeof(double) * 3 * P);
     up(c->v, hv.data(), sizeof(double) * 3 * P);
     up(c->mass, hm.data(), sizeof(double) * P);
+    up(c->minv, hmi.data(), sizeof(double) * P);
     up(c->pos4, hp.data(), sizeof(float4) * P);
     up(c->type, ht.data(), sizeof(int) * P);
     up(c->perm, hperm.data(), sizeof(int) * P);

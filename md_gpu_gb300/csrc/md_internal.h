@@ -54,6 +54,8 @@ struct md_devstate {
     double xi_a, eta_a;  /* the same after the first thermostat half step of a step */
     double vscale;       /* velocity scale pending from the last thermostat half step */
     double lambda;       /* last Berendsen scale */
+    double lam_next;     /* Berendsen scale of the next leapfrog step */
+    double kick_scale;   /* velocity scale applied by the next VV first half (NH: s2*s1) */
     unsigned blocks_done; /* blocks finished in the current reduction kernel */
 };
 
@@ -62,6 +64,7 @@ struct md_kparams {
     int n, pitch, cap, ntype;
     float box[3], boxi[3];
     double boxd[3];
+    double box2i[3];  /* 2/L, for the wrap x -= L trunc(2x/L) */
     float rcutsq, reacf, rskinsq, rmaxdif;
     float palfa, spiialfa, alfasq, wolf;
     int lkspace;
@@ -100,6 +103,7 @@ struct md_ctx {
     bool own_stream = false;
     int device = 0;
     double *x = nullptr, *v = nullptr, *mass = nullptr;   /* sorted order */
+    double *minv = nullptr;                               /* 1/mass, sorted order */
     float4 *pos4 = nullptr, *pos_old = nullptr;
     float4 *pos4_alt = nullptr;     /* second position buffer of the fused step */
     int *type = nullptr, *perm = nullptr, *iperm = nullptr;
@@ -111,7 +115,7 @@ struct md_ctx {
     int *cell_rank = nullptr, *cell_count = nullptr, *cell_start = nullptr, *cell_fill = nullptr;
     int *cell_lin = nullptr;                              /* rank -> linear cell index */
     int *key = nullptr, *src = nullptr;
-    double *tmp_d = nullptr;                              /* 7*pitch scratch for permutation */
+    double *tmp_d = nullptr;                              /* 8*pitch scratch for permutation */
     float4 *tmp4 = nullptr;
     int *tmp_i = nullptr;                                 /* 3*pitch */
     /* bonded lists: original-space CSR (fixed) and sorted-space per-atom slots */

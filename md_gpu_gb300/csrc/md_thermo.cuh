@@ -42,9 +42,24 @@ __device__ __forceinline__ double block_sum(double v, double *sh)
     return r;
 }
 
-__device__ __forceinline__ double wrap(double x, double L)
+/* x -= L trunc(2x/L) (nve_leapfrog.cu:52-56) with 2/L precomputed. */
+__device__ __forceinline__ double wrap(double x, double L, double two_over_l)
 {
-    return x - L * trunc(x * 2.0 / L);
+    return x - L * trunc(x * two_over_l);
+}
+
+/* First thermostat half step of the next VV step (NH): from KE (already
+ * scaled by the pending factor) and xi, eta; returns the factor s1. */
+__device__ __forceinline__ double nh_half_a(const md_kparams &kp, const thermo_par &tp, double ke,
+                                            double &xi, double &eta)
+{
+    double kt = RGAS * tp.t0;
+    xi += 0.25 * kp.dt * (2.0 * ke - tp.ndf * kt) / tp.q_nh;
+    double s1 = exp(-0.5 * kp.dt * xi);
+    ke *= s1 * s1;
+    eta += 0.5 * kp.dt * xi;
+    xi += 0.25 * kp.dt * (2.0 * ke - tp.ndf * kt) / tp.q_nh;
+    return s1;
 }
 
 __device__ __forceinline__ void write_partials(double ke, double pe, double w, int energy,
@@ -80,8 +95,7 @@ __device__ void finalize(const md_kparams &kp, const thermo_par &tp, int mode, i
     if (threadIdx.x != 0) return;
     volatile md_devstate *vs = st;
     double kt = RGAS * tp.t0;
-    double lam = 1.0;
-    if (mode == 0 && tp.berendsen) lam = sqrt(1.0 + kp.dt / tp.tau * (tp.t0 / vs->temper - 1.0));
+    double lam = (mode == 0 && tp.berendsen) ? vs->lam_next : 1.0;
     double xi = vs->xi, eta = vs->eta;
     if (mode == 1) {
         st->vscale = 1.0;
@@ -101,11 +115,23 @@ __device__ void finalize(const md_kparams &kp, const thermo_par &tp, int mode, i
     double temper = 2.0 * ke / (tp.ndf * RGAS);
     st->ke = ke;
     if (tp.energy) { st->pe = pe; st->virial = w / 6.0; }
+    if (tp.nh && mode != 0) {
+        /* the next step's first thermostat half step, from this state */
+        double xa = xi, ea = eta;
+        double s1 = nh_half_a(kp, tp, ke, xa, ea);
+        st->xi_a = xa;
+        st->eta_a = ea;
+        st->kick_scale = vs->vscale * s1;
+    } else if (mode != 0) {
+        st->kick_scale = vs->vscale;
+    }
     /* observing the state does not move the Berendsen reference temperature:
      * the first step uses T = T0 (integrator.cu:77) */
     if (mode == 2) return;
     st->temper = temper;
     st->lambda = lam;
+    /* integrator.cu:146-147 for the next step, from this step's temperature */
+    st->lam_next = tp.berendsen ? sqrt(1.0 + kp.dt / tp.tau * (tp.t0 / temper - 1.0)) : 1.0;
     long long step = vs->step;
     md_thermo r;
     r.step = step;
