@@ -169,7 +169,10 @@ md_status md_get_cell_ranks(md_ctx *ctx, int *rank);
 md_status md_set_tuning(md_ctx *ctx, int pair_tpa, int list_tpa);
 /* Autotuner: times the pair kernel for 2/4/8/16 threads per atom and the list
  * builders (warp per cell, 4/8/16 threads per atom) on the current state and
- * keeps the fastest of each; returns the choice. */
+ * keeps the fastest of each; returns the choice.  For leapfrog systems
+ * without bonded terms it also times the step with the pair kernel and the
+ * integrator fused into one kernel against separate kernels, by running
+ * steps: the system then advances by 192 steps. */
 md_status md_autotune(md_ctx *ctx, int *pair_tpa, int *list_tpa);
 /* Per-type exclusions (no counterpart in the reference, which excludes only
  * 1-2 bonded pairs): bit b of mask[a] excludes every pair of types a and b

@@ -116,7 +116,7 @@ void fused_dispatch(md_ctx *c, const md_kparams &kp, const pair_consts &pc, cons
 
 bool md_can_fuse(const md_ctx *c)
 {
-    return c->integrator == MD_LEAPFROG && !c->has_bonds && !c->has_angles;
+    return c->fuse_step && c->integrator == MD_LEAPFROG && !c->has_bonds && !c->has_angles;
 }
 
 void launch_pair_leapfrog(md_ctx *c, const md_kparams &kp, unsigned long long cond, int has_cond)

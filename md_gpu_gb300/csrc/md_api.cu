@@ -1130,7 +1130,8 @@ md_status md_autotune(md_ctx *c, int *pair_tpa, int *list_tpa)
     const int pt[] = {2, 4, 8, 16};
     const int lt[] = {0, 4, 8, 16};
     float best = 1e30f;
-    int bp = c->pair_tpa, bl = c->list_tpa;
+    int bp = c->pair_tpa, bl = c->list_tpa, bf = 0;
+    c->fuse_step = 0;
     for (int t : pt) {
         c->pair_tpa = t;
         float ms = 0.0f, m2 = 0.0f;
@@ -1140,6 +1141,21 @@ md_status md_autotune(md_ctx *c, int *pair_tpa, int *list_tpa)
         if (m2 < best) { best = m2; bp = t; }
     }
     c->pair_tpa = bp;
+    /* leapfrog systems without bonded terms: separate or fused pair and
+     * integrator kernels, timed as they run (the system advances 192 steps) */
+    c->fuse_step = 1;
+    if (md_can_fuse(c)) {
+        float tm[2] = {0.0f, 0.0f};
+        for (int fz = 0; fz < 2; fz++) {
+            c->fuse_step = fz;
+            md_status s = md_step(c, 32, 0);
+            if (s == MD_OK) s = md_step(c, 64, 0);
+            if (s == MD_OK) s = md_last_step_ms(c, &tm[fz]);
+            if (s != MD_OK) return s;
+        }
+        bf = tm[1] < tm[0] ? 1 : 0;
+    }
+    c->fuse_step = bf;
     best = 1e30f;
     for (int t : lt) {
         c->list_tpa = t;

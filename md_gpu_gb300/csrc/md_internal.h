@@ -139,6 +139,7 @@ struct md_ctx {
     int genergy = 0;
     const float4 *gpos4 = nullptr; /* position buffer current when the graph was captured */
     int use_graphs = 1;            /* 0: launch every step's kernels eagerly */
+    int fuse_step = 0;             /* 1: fused pair+leapfrog kernel where applicable */
     long long host_step = 0;       /* steps run so far (mirrors st->step) */
     double *io_dev = nullptr;      /* 4*pitch doubles for host transfers */
     int pair_tpa = 8;    /* threads per atom in the pair kernel */
