@@ -93,6 +93,24 @@ const char *md_status_string(md_status s);
 /* Copies the last error message of ctx (may be NULL for global errors). */
 md_status md_last_error(const md_ctx *ctx, char *buf, int len);
 
+/* Many independent systems ("replicas", e.g. uneven sizes and per-replica
+ * force fields) in one context, advanced together: every stage of a step is
+ * one launch over all replicas, and md_step replays one captured graph for
+ * the whole batch.  No counterpart in the reference, which runs one system
+ * per process.  descs[r] describes replica r exactly as md_create would take
+ * it; replicas must share lkspace, integrator, enstype, dt and tau_t, and
+ * have no bonds or angles (MD_ERR_UNSUPPORTED).  Box, cutoff, skin, alpha,
+ * LJ table, masses, charges and temperature are per replica.  Host arrays of
+ * the context (positions, velocities, forces, energies, neighbour lists,
+ * order) hold the replicas' atoms concatenated in replica order; the
+ * neighbour list of a replica holds only its own atoms.  md_get_thermo
+ * returns the batch totals (temperature over all degrees of freedom);
+ * md_get_replica_thermo the per-replica values.  nrep == 1 is md_create. */
+md_status md_create_batch(const md_system_desc *descs, int nrep, void *stream, md_ctx **out);
+/* Per-replica state after the last step of a batch (out[r], r < nrep and
+ * < the batch's replica count; synchronises the stream). */
+md_status md_get_replica_thermo(md_ctx *ctx, md_thermo *out, int nrep);
+
 /* SimulationInit + config_init + forces_init + neighborlist_init +
  * integrate_init (simulation.cu:40, runGPU.cu:53-60): reads <base>.inp,
  * <base>.fld and <base>.cfg in the reference grammar, uploads the system
@@ -165,7 +183,7 @@ md_status md_get_order(md_ctx *ctx, int *perm);
 md_status md_get_cell_ranks(md_ctx *ctx, int *rank);
 /* Tuning knobs: threads per atom of the pair kernel (1, 2, 4, 8, 16, 32) and
  * the list builder (0 = one warp per cell, the default; or 1..32 threads per
- * atom).  Every setting builds the identical list. */
+ * atom; batches take 0 only).  Every setting builds the identical list. */
 md_status md_set_tuning(md_ctx *ctx, int pair_tpa, int list_tpa);
 /* Autotuner: times the pair kernel for 2/4/8/16 threads per atom and the list
  * builders (warp per cell, 4/8/16 threads per atom) on the current state and

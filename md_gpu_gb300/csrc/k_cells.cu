@@ -15,15 +15,6 @@
 
 namespace {
 
-/* (x + L/2) / bin truncated and clamped: the binning rule of the reference's
- * sketch (neighborlist_kernel_o.cu:20-25) with IEEE add and divide. */
-__device__ __forceinline__ int cell_of(float x, float box, float binlen, int nc)
-{
-    float s = __fdiv_rn(__fadd_rn(x, box / 2.0f), binlen);
-    int c = (s <= 0.0f) ? 0 : (int)s;
-    return c >= nc ? nc - 1 : c;
-}
-
 __global__ void k_check(md_kparams kp, const float4 *__restrict__ pos4,
                         const float4 *__restrict__ pos_old, md_devstate *st)
 {
@@ -47,6 +38,68 @@ __global__ void k_cell_key(md_kparams kp, const md_devstate *st, int always,
     int r = cell_rank[cx + kp.ncell[0] * (cy + kp.ncell[1] * cz)];
     key[i] = r;
     atomicAdd(&cell_count[r], 1);
+}
+
+/* The same for a batch: each atom is tested with its replica's box and skin. */
+__global__ void k_check_b(int n, const md_rep *__restrict__ reps, const int *__restrict__ arep,
+                          const float4 *__restrict__ pos4, const float4 *__restrict__ pos_old,
+                          md_devstate *st, int *rep_upd)
+{
+    int i = blockIdx.x * blockDim.x + threadIdx.x;
+    if (i >= n) return;
+    const int r = arep[i];
+    const md_rep &R = reps[r];
+    if (md_rsq_box(pos4[i], pos_old[i], R.box, R.boxi) >= R.rmaxdif) {
+        st->update = 1;
+        rep_upd[r] = 1;
+    }
+}
+
+/* Cell keys of a batch: the replica's cell grid, ranks offset by its first
+ * cell, so every replica's cells (and atoms) stay one contiguous range.  A
+ * replica that is not being rebuilt keeps the keys of its last build, so
+ * its atoms keep their order (and their list rows stay valid). */
+__global__ void k_cell_key_b(int n, const md_rep *__restrict__ reps, const int *__restrict__ arep,
+                             const md_devstate *st, int always, const int *__restrict__ rep_upd,
+                             const int *__restrict__ skey, const float4 *__restrict__ pos4,
+                             const int *__restrict__ cell_rank, int *key, int *cell_count)
+{
+    if (!always && !st->update) return;
+    int i = blockIdx.x * blockDim.x + threadIdx.x;
+    if (i >= n) return;
+    const int rep = arep[i];
+    int r;
+    if (rep_upd[rep]) {
+        const md_rep &R = reps[rep];
+        float4 p = pos4[i];
+        int cx = cell_of(p.x, R.box[0], R.binlen[0], R.ncell[0]);
+        int cy = cell_of(p.y, R.box[1], R.binlen[1], R.ncell[1]);
+        int cz = cell_of(p.z, R.box[2], R.binlen[2], R.ncell[2]);
+        r = cell_rank[R.cell0 + cx + R.ncell[0] * (cy + R.ncell[1] * cz)];
+    } else {
+        r = skey[i];
+    }
+    key[i] = r;
+    atomicAdd(&cell_count[r], 1);
+}
+
+/* Rebuild every replica of a batch (forced builds). */
+__global__ void k_flag_all(int *rep_upd, int nrep)
+{
+    int r = blockIdx.x * blockDim.x + threadIdx.x;
+    if (r < nrep) rep_upd[r] = 1;
+}
+
+/* Ends a rebuild of a batch: counts the rebuilt replicas' builds and clears
+ * the requests. */
+__global__ void k_clear_update_b(md_devstate *st, int *rep_upd, md_repstate *repst, int nrep)
+{
+    int r = blockIdx.x * blockDim.x + threadIdx.x;
+    if (r == 0) st->update = 0;
+    if (r < nrep && rep_upd[r]) {
+        repst[r].builds += 1;
+        rep_upd[r] = 0;
+    }
 }
 
 /* Exclusive scan of the cell counts (one block), then zero the counters for
@@ -117,7 +170,8 @@ __global__ void k_permute(md_kparams kp, const md_devstate *st, int always,
                           const double *__restrict__ v, const double *__restrict__ mass,
                           const double *__restrict__ minv,
                           const float4 *__restrict__ pos4, const int *__restrict__ perm,
-                          const int *__restrict__ type, double *tmp_d, float4 *tmp4, int *tmp_i)
+                          const int *__restrict__ type, const int *__restrict__ key,
+                          double *tmp_d, float4 *tmp4, int *tmp_i)
 {
     if (!always && !st->update) return;
     int s = blockIdx.x * blockDim.x + threadIdx.x;
@@ -132,12 +186,14 @@ __global__ void k_permute(md_kparams kp, const md_devstate *st, int always,
     tmp4[s] = pos4[o];
     tmp_i[s] = perm[o];
     tmp_i[P + s] = type[o];
+    if (key) tmp_i[2 * P + s] = key[o];
 }
 
 __global__ void k_copyback(md_kparams kp, const md_devstate *st, int always,
                            const double *__restrict__ tmp_d, const float4 *__restrict__ tmp4,
                            const int *__restrict__ tmp_i, double *x, double *v, double *mass,
-                           double *minv, float4 *pos4, int *perm, int *iperm, int *type)
+                           double *minv, float4 *pos4, int *perm, int *iperm, int *type,
+                           int *skey)
 {
     if (!always && !st->update) return;
     int s = blockIdx.x * blockDim.x + threadIdx.x;
@@ -154,6 +210,7 @@ __global__ void k_copyback(md_kparams kp, const md_devstate *st, int always,
     perm[s] = o;
     iperm[o] = s;
     type[s] = tmp_i[P + s];
+    if (skey) skey[s] = tmp_i[2 * P + s];
 }
 
 /* Exclusions and bonded lists re-expressed in the new sorted indices. */
@@ -291,12 +348,21 @@ constexpr int CW_WARPS = 4;
 constexpr int CW_MAXI = 32;
 constexpr int CW_MAXST = 128;
 
+/* Cell geometry seen by one warp: the system's, or in a batch the replica's
+ * that owns the cell. */
+struct cell_geom {
+    float L[3], Li[3], rskinsq;
+    int nc[3], sten[3], shift, lin0;
+};
+
+template <bool BATCH>
 __global__ void __launch_bounds__(CW_WARPS * 32) k_build_cells(
     md_kparams kp, md_devstate *st, int always, int ncells, const float4 *__restrict__ pos4,
     const int *__restrict__ type, const uint4 *__restrict__ excl_s,
     const int *__restrict__ cell_rank, const int *__restrict__ cell_lin,
     const int *__restrict__ cell_start, const unsigned *__restrict__ type_mask, unsigned *nl,
-    int *nl_n, float4 *pos_old)
+    int *nl_n, float4 *pos_old, const md_rep *__restrict__ reps, const int *__restrict__ crep,
+    const int *__restrict__ rep_upd)
 {
     if (!always && !st->update) return;
     __shared__ float4 s_p[CW_WARPS][CW_MAXI];
@@ -310,13 +376,28 @@ __global__ void __launch_bounds__(CW_WARPS * 32) k_build_cells(
     if (r >= ncells) return;
     const int ib = cell_start[r], ie = cell_start[r + 1];
     if (ib == ie) return;
+    cell_geom G;
+    if (BATCH) {
+        const int rr = crep[r];
+        if (!rep_upd[rr]) return;   /* this replica keeps its list */
+        const md_rep &R = reps[rr];
+        for (int d = 0; d < 3; d++) {
+            G.L[d] = R.box[d]; G.Li[d] = R.boxi[d]; G.nc[d] = R.ncell[d]; G.sten[d] = R.stencil[d];
+        }
+        G.rskinsq = R.rskinsq; G.shift = R.cell_shift; G.lin0 = R.cell0;
+    } else {
+        for (int d = 0; d < 3; d++) {
+            G.L[d] = kp.box[d]; G.Li[d] = kp.boxi[d]; G.nc[d] = kp.ncell[d]; G.sten[d] = kp.stencil[d];
+        }
+        G.rskinsq = kp.rskinsq; G.shift = kp.cell_shift; G.lin0 = 0;
+    }
     const int lin = cell_lin[r];
-    const int nx = kp.ncell[0], ny = kp.ncell[1], nz = kp.ncell[2];
+    const int nx = G.nc[0], ny = G.nc[1], nz = G.nc[2];
     const int c3[3] = {lin % nx, (lin / nx) % ny, lin / (nx * ny)};
     int lo[3], len[3];
     for (int d = 0; d < 3; d++) {
-        if (kp.stencil[d] < 0) { lo[d] = 0; len[d] = kp.ncell[d]; }
-        else { lo[d] = c3[d] - kp.stencil[d]; len[d] = 2 * kp.stencil[d] + 1; }
+        if (G.sten[d] < 0) { lo[d] = 0; len[d] = G.nc[d]; }
+        else { lo[d] = c3[d] - G.sten[d]; len[d] = 2 * G.sten[d] + 1; }
     }
     const int nst = len[0] * len[1] * len[2];   /* <= 125 with cells of side >= rl/2 */
     /* stencil ranges in traversal order (z outer, x inner); lane k takes k, k+32, ... */
@@ -334,7 +415,7 @@ __global__ void __launch_bounds__(CW_WARPS * 32) k_build_cells(
             int cx = xx < 0 ? xx + nx : (xx >= nx ? xx - nx : xx);
             int cy = yy < 0 ? yy + ny : (yy >= ny ? yy - ny : yy);
             int cz = zz < 0 ? zz + nz : (zz >= nz ? zz - nz : zz);
-            int r2 = cell_rank[cx + nx * (cy + ny * cz)];
+            int r2 = cell_rank[G.lin0 + cx + nx * (cy + ny * cz)];
             jb = cell_start[r2];
             cnt = cell_start[r2 + 1] - jb;
         }
@@ -353,7 +434,7 @@ __global__ void __launch_bounds__(CW_WARPS * 32) k_build_cells(
     if (lane == 0) s_pre[w][nst] = run;
     const int total = run;
     const unsigned lt = (1u << lane) - 1u;
-    const float L0 = kp.box[0], L1 = kp.box[1], L2 = kp.box[2];
+    const float L0 = G.L[0], L1 = G.L[1], L2 = G.L[2];
     __syncwarp();
     for (int i0 = ib; i0 < ie; i0 += CW_MAXI) {
         const int ni = min(CW_MAXI, ie - i0);
@@ -395,16 +476,16 @@ __global__ void __launch_bounds__(CW_WARPS * 32) k_build_cells(
             for (int a = 0; a < ni; a++) {
                 float4 p = s_p[w][a];
                 float rsq;
-                if (kp.cell_shift) {
+                if (G.shift) {
                     /* fl(fl(px - qx) - u) is the reference's fl(d - fl(L rint(d/L))) */
                     float dx = __fsub_rn(__fsub_rn(p.x, q.x), ux);
                     float dy = __fsub_rn(__fsub_rn(p.y, q.y), uy);
                     float dz = __fsub_rn(__fsub_rn(p.z, q.z), uz);
                     rsq = __fadd_rn(__fadd_rn(__fmul_rn(dx, dx), __fmul_rn(dy, dy)), __fmul_rn(dz, dz));
                 } else {
-                    rsq = md_rsq_exact(p, q, kp);
+                    rsq = md_rsq_box(p, q, G.L, G.Li);
                 }
-                bool ok = vj && rsq < kp.rskinsq && j != i0 + a;
+                bool ok = vj && rsq < G.rskinsq && j != i0 + a;
                 if ((excl_bits >> a) & 1u) {
                     uint4 ex = s_ex[w][a];
                     ok = ok && uj != ex.x && uj != ex.y && uj != ex.z && uj != ex.w &&
@@ -444,27 +525,52 @@ __global__ void __launch_bounds__(CW_WARPS * 32) k_build_cells(
 void launch_check(md_ctx *c, const md_kparams &kp)
 {
     int nb = (kp.n + 255) / 256;
+    if (c->nrep > 1) {
+        k_check_b<<<nb, 256, 0, c->stream>>>(kp.n, c->reps_dev, c->arep, c->pos4, c->pos_old, c->st,
+                                             c->rep_upd);
+        return;
+    }
     k_check<<<nb, 256, 0, c->stream>>>(kp, c->pos4, c->pos_old, c->st);
 }
 
-void launch_rebuild(md_ctx *c, const md_kparams &kp, bool unconditional)
+void launch_rebuild(md_ctx *c, const md_kparams &kp, bool unconditional, bool all_replicas)
 {
     int always = unconditional ? 1 : 0;
     int nb = (kp.n + 255) / 256;
     cudaStream_t s = c->stream;
-    k_cell_key<<<nb, 256, 0, s>>>(kp, c->st, always, c->pos4, c->cell_rank, c->key, c->cell_count);
+    const bool batch = c->nrep > 1;
+    const int rb = (c->nrep + 255) / 256;
+    if (batch && all_replicas) k_flag_all<<<rb, 256, 0, s>>>(c->rep_upd, c->nrep);
+    if (batch)
+        k_cell_key_b<<<nb, 256, 0, s>>>(kp.n, c->reps_dev, c->arep, c->st, always, c->rep_upd,
+                                        c->skey, c->pos4, c->cell_rank, c->key, c->cell_count);
+    else
+        k_cell_key<<<nb, 256, 0, s>>>(kp, c->st, always, c->pos4, c->cell_rank, c->key, c->cell_count);
     k_cell_scan<<<1, 1024, 0, s>>>(kp, c->st, always, c->ncells, c->cell_count, c->cell_start,
                                    c->cell_fill);
     k_cell_scatter<<<nb, 256, 0, s>>>(kp, c->st, always, c->key, c->cell_start, c->cell_fill, c->src);
     k_cell_order<<<(c->ncells + 255) / 256, 256, 0, s>>>(kp, c->st, always, c->ncells,
                                                           c->cell_start, c->perm, c->src);
     k_permute<<<nb, 256, 0, s>>>(kp, c->st, always, c->src, c->x, c->v, c->mass, c->minv, c->pos4,
-                                 c->perm, c->type, c->tmp_d, c->tmp4, c->tmp_i);
+                                 c->perm, c->type, batch ? c->key : nullptr, c->tmp_d, c->tmp4,
+                                 c->tmp_i);
     k_copyback<<<nb, 256, 0, s>>>(kp, c->st, always, c->tmp_d, c->tmp4, c->tmp_i, c->x, c->v,
-                                  c->mass, c->minv, c->pos4, c->perm, c->iperm, c->type);
-    k_remap<<<nb, 256, 0, s>>>(kp, c->st, always, c->perm, c->iperm, c->excl_orig, c->excl_s,
-                               c->bl_o, c->bl_on, c->bl_s, c->bl_sn, c->al_o, c->al_on, c->al_s,
-                               c->al_sn, c->has_bonds, c->has_angles);
+                                  c->mass, c->minv, c->pos4, c->perm, c->iperm, c->type,
+                                  batch ? c->skey : nullptr);
+    /* a batch has no exclusions or bonded lists to re-express */
+    if (!batch)
+        k_remap<<<nb, 256, 0, s>>>(kp, c->st, always, c->perm, c->iperm, c->excl_orig, c->excl_s,
+                                   c->bl_o, c->bl_on, c->bl_s, c->bl_sn, c->al_o, c->al_on, c->al_s,
+                                   c->al_sn, c->has_bonds, c->has_angles);
+    if (batch) {
+        /* at most 5 stencil cells per axis (cells of side >= rl/2): <= 125 */
+        k_build_cells<true><<<(c->ncells + CW_WARPS - 1) / CW_WARPS, CW_WARPS * 32, 0, s>>>(
+            kp, c->st, always, c->ncells, c->pos4, c->type, c->excl_s, c->cell_rank, c->cell_lin,
+            c->cell_start, c->type_mask_dev, c->nl, c->nl_n, c->pos_old, c->reps_dev, c->crep,
+            c->rep_upd);
+        k_clear_update_b<<<rb, 256, 0, s>>>(c->st, c->rep_upd, c->repst, c->nrep);
+        return;
+    }
     int ltpa = c->list_tpa;
     if (ltpa == 0) {   /* the warp-per-cell builder keeps up to 128 stencil cells in shared memory */
         int nst = 1;
@@ -475,9 +581,9 @@ void launch_rebuild(md_ctx *c, const md_kparams &kp, bool unconditional)
     int lb = (int)((threads + 255) / 256);
     switch (ltpa) {
     case 0:
-        k_build_cells<<<(c->ncells + CW_WARPS - 1) / CW_WARPS, CW_WARPS * 32, 0, s>>>(
+        k_build_cells<false><<<(c->ncells + CW_WARPS - 1) / CW_WARPS, CW_WARPS * 32, 0, s>>>(
             kp, c->st, always, c->ncells, c->pos4, c->type, c->excl_s, c->cell_rank, c->cell_lin,
-            c->cell_start, c->type_mask_dev, c->nl, c->nl_n, c->pos_old);
+            c->cell_start, c->type_mask_dev, c->nl, c->nl_n, c->pos_old, nullptr, nullptr, nullptr);
         break;
 #define MD_LIST_CASE(T)                                                                            \
     case T:                                                                                        \

@@ -36,7 +36,7 @@ __global__ void __launch_bounds__(128) k_pair(md_kparams kp, pair_consts pc,
     int gt = blockIdx.x * blockDim.x + threadIdx.x;
     int i = gt / TPA, lane = gt % TPA;
     bool active = i < kp.n;
-    pair_total t = pair_sum<KIND, TPA, B, ENERGY>(kp, pc, active ? i : 0, active, lane, pos4, type,
+    pair_total t = pair_sum<KIND, TPA, B, ENERGY>(geom_kp{kp, pc}, kp.cap, active ? i : 0, active, lane, pos4, type,
                                                   nl, nl_n, lj);
     const size_t P = (size_t)kp.pitch;
     if (active && lane == 0) {
@@ -151,6 +151,10 @@ void pair_dispatch(md_ctx *c, const md_kparams &kp, const pair_consts &pc)
 
 void launch_forces(md_ctx *c, const md_kparams &kp, bool energy, int terms)
 {
+    if (c->nrep > 1) {
+        launch_forces_b(c, kp, energy, terms);
+        return;
+    }
     pair_consts pc = make_pair_consts(c);
     if (terms & MD_TERM_PAIR) {
         if (c->lkspace == 0) {

@@ -33,7 +33,7 @@ __global__ void __launch_bounds__(128) k_pair_leapfrog(
     int gt = blockIdx.x * blockDim.x + threadIdx.x;
     int i = gt / TPA, lane = gt % TPA;
     bool active = i < kp.n;
-    pair_total t = pair_sum<KIND, TPA, B, false>(kp, pc, active ? i : 0, active, lane, pos4, type,
+    pair_total t = pair_sum<KIND, TPA, B, false>(geom_kp{kp, pc}, kp.cap, active ? i : 0, active, lane, pos4, type,
                                                  nl, nl_n, lj);
     const size_t P = (size_t)kp.pitch;
     if (lane == 0) {
@@ -116,7 +116,8 @@ void fused_dispatch(md_ctx *c, const md_kparams &kp, const pair_consts &pc, cons
 
 bool md_can_fuse(const md_ctx *c)
 {
-    return c->fuse_step && c->integrator == MD_LEAPFROG && !c->has_bonds && !c->has_angles;
+    return c->fuse_step && c->nrep == 1 && c->integrator == MD_LEAPFROG && !c->has_bonds &&
+           !c->has_angles;
 }
 
 void launch_pair_leapfrog(md_ctx *c, const md_kparams &kp, unsigned long long cond, int has_cond)

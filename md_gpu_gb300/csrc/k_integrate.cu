@@ -21,6 +21,8 @@
  *   G = (2 KE - ndf k T0) / Q,  Q = ndf k T0 tau^2,
  * with the conserved quantity KE + PE + Q xi^2/2 + ndf k T0 eta.
  */
+#include <algorithm>
+
 #include "md_thermo.cuh"
 
 namespace {
@@ -146,6 +148,7 @@ __global__ void __launch_bounds__(256) k_vv_second(md_kparams kp, thermo_par tp,
 /* Original-order output: what 0 positions (3), 1 velocities (3, pending NH
  * scale applied), 2 forces + sum ff r^2 (4), 3 per-atom energy (1). */
 __global__ void k_gather_out(md_kparams kp, int what, const md_devstate *st,
+                             const md_repstate *__restrict__ repst, const int *__restrict__ arep,
                              const int *__restrict__ perm, const double *__restrict__ x,
                              const double *__restrict__ v, const long long *__restrict__ f,
                              const float *__restrict__ vir, const float *__restrict__ epot,
@@ -158,7 +161,7 @@ __global__ void k_gather_out(md_kparams kp, int what, const md_devstate *st,
     if (what == 0) {
         for (int d = 0; d < 3; d++) out[3 * (size_t)o + d] = x[d * P + s];
     } else if (what == 1) {
-        double sc = st->vscale;
+        double sc = repst ? repst[arep[s]].vscale : st->vscale;
         for (int d = 0; d < 3; d++) out[3 * (size_t)o + d] = v[d * P + s] * sc;
     } else if (what == 2) {
         for (int d = 0; d < 3; d++) out[4 * (size_t)o + d] = (double)f[d * P + s] * FX_INV;
@@ -169,12 +172,13 @@ __global__ void k_gather_out(md_kparams kp, int what, const md_devstate *st,
 }
 
 /* Original-order input: what 0 positions (also refreshes pos4), 1 velocities. */
-__global__ void k_scatter_in(md_kparams kp, int what, md_devstate *st,
-                             const int *__restrict__ iperm, const double *__restrict__ in,
+__global__ void k_scatter_in(md_kparams kp, int what, md_devstate *st, md_repstate *repst,
+                             int nrep, const int *__restrict__ iperm, const double *__restrict__ in,
                              double *x, double *v, float4 *pos4)
 {
     int o = blockIdx.x * blockDim.x + threadIdx.x;
     if (o == 0 && what == 1) st->vscale = 1.0;
+    if (repst && o < nrep && what == 1) repst[o].vscale = 1.0;
     if (o >= kp.n) return;
     const int P = kp.pitch;
     int s = iperm[o];
@@ -195,6 +199,11 @@ __global__ void k_scatter_in(md_kparams kp, int what, md_devstate *st,
 
 void launch_leapfrog(md_ctx *c, const md_kparams &kp, int energy, unsigned long long cond, int has_cond)
 {
+    if (c->nrep > 1) {
+        launch_leapfrog_b(c, kp, energy, cond, has_cond);
+        return;
+    }
+
     int nb = (kp.n + 255) / 256;
     k_leapfrog<<<nb, 256, 0, c->stream>>>(kp, make_tp(c, energy), make_io(c, cond, has_cond), c->x,
                                           c->v, c->mass, c->minv, c->pos4, c->f, c->epot, c->vir);
@@ -202,6 +211,11 @@ void launch_leapfrog(md_ctx *c, const md_kparams &kp, int energy, unsigned long 
 
 void launch_vv_first(md_ctx *c, const md_kparams &kp, unsigned long long cond, int has_cond)
 {
+    if (c->nrep > 1) {
+        launch_vv_first_b(c, kp, cond, has_cond);
+        return;
+    }
+
     int nb = (kp.n + 255) / 256;
     k_vv_first<<<nb, 256, 0, c->stream>>>(kp, make_tp(c, 0), make_io(c, cond, has_cond), c->x,
                                           c->v, c->minv, c->pos4, c->f);
@@ -209,6 +223,11 @@ void launch_vv_first(md_ctx *c, const md_kparams &kp, unsigned long long cond, i
 
 void launch_vv_second(md_ctx *c, const md_kparams &kp, int energy)
 {
+    if (c->nrep > 1) {
+        launch_vv_second_b(c, kp, energy, 1);
+        return;
+    }
+
     int nb = (kp.n + 255) / 256;
     k_vv_second<<<nb, 256, 0, c->stream>>>(kp, make_tp(c, energy), 1, make_io(c, 0, 0), c->v,
                                            c->mass, c->minv, c->f, c->epot, c->vir);
@@ -216,6 +235,11 @@ void launch_vv_second(md_ctx *c, const md_kparams &kp, int energy)
 
 void launch_thermo_from_state(md_ctx *c, const md_kparams &kp, int energy)
 {
+    if (c->nrep > 1) {
+        launch_vv_second_b(c, kp, energy, 0);
+        return;
+    }
+
     int nb = (kp.n + 255) / 256;
     k_vv_second<<<nb, 256, 0, c->stream>>>(kp, make_tp(c, energy), 0, make_io(c, 0, 0), c->v,
                                            c->mass, c->minv, c->f, c->epot, c->vir);
@@ -224,13 +248,16 @@ void launch_thermo_from_state(md_ctx *c, const md_kparams &kp, int energy)
 void launch_gather_out(md_ctx *c, const md_kparams &kp, int what, void *dst)
 {
     int nb = (kp.n + 255) / 256;
-    k_gather_out<<<nb, 256, 0, c->stream>>>(kp, what, c->st, c->perm, c->x, c->v, c->f, c->vir,
-                                            c->epot, (double *)dst);
+    k_gather_out<<<nb, 256, 0, c->stream>>>(kp, what, c->st, c->nrep > 1 ? c->repst : nullptr,
+                                            c->arep, c->perm, c->x, c->v, c->f, c->vir, c->epot,
+                                            (double *)dst);
 }
 
 void launch_scatter_in(md_ctx *c, const md_kparams &kp, int what, const void *src)
 {
     int nb = (kp.n + 255) / 256;
-    k_scatter_in<<<nb, 256, 0, c->stream>>>(kp, what, c->st, c->iperm, (const double *)src, c->x,
-                                            c->v, c->pos4);
+    int nbs = std::max(nb, (c->nrep + 255) / 256);
+    k_scatter_in<<<nbs, 256, 0, c->stream>>>(kp, what, c->st, c->nrep > 1 ? c->repst : nullptr,
+                                             c->nrep, c->iperm, (const double *)src, c->x, c->v,
+                                             c->pos4);
 }

@@ -48,9 +48,9 @@ extern "C" md_status md_time_rebuild(md_ctx *c, int nrep, float *ms_per_build)
 {
     if (!c || nrep <= 0 || !ms_per_build) return MD_ERR_ARG;
     md_kparams kp = md_make_kparams(c);
-    launch_rebuild(c, kp, true);   /* warm */
+    launch_rebuild(c, kp, true, true);   /* warm */
     MD_CUDA_TRY(c, cudaEventRecord(c->ev0, c->stream));
-    for (int r = 0; r < nrep; r++) launch_rebuild(c, kp, true);
+    for (int r = 0; r < nrep; r++) launch_rebuild(c, kp, true, true);
     MD_CUDA_TRY(c, cudaEventRecord(c->ev1, c->stream));
     MD_CUDA_TRY(c, cudaEventSynchronize(c->ev1));
     float ms = 0.0f;

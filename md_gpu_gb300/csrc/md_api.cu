@@ -250,7 +250,8 @@ void free_device(md_ctx *c)
                     c->cell_count, c->cell_start, c->cell_fill, c->key, c->src, c->tmp_d, c->tmp4,
                     c->tmp_i, c->bl_o, c->bl_on, c->al_o, c->al_on, c->bl_s, c->bl_sn, c->al_s,
                     c->al_sn, c->partials, c->st, c->rec, c->lj_dev, c->bonded_par,
-                    c->type_mask_dev, c->io_dev};
+                    c->type_mask_dev, c->io_dev, c->reps_dev, c->repst, c->arep, c->crep,
+                    c->ljr_dev, c->grid_tab, c->rep_upd, c->skey};
     for (void *p : ptrs)
         if (p) cudaFree(p);
 }
@@ -284,7 +285,7 @@ void enqueue_steps(md_ctx *c, int nsteps, int energy_first)
     for (int k = 0; k < nsteps; k++) {
         int energy = (energy_first && k == 0) ? 1 : 0;
         if (c->integrator == MD_LEAPFROG) {
-            launch_rebuild(c, kp, false);
+            launch_rebuild(c, kp, false, false);
             if (!energy && md_can_fuse(c)) {
                 launch_pair_leapfrog(c, kp, 0, 0);
             } else {
@@ -293,7 +294,7 @@ void enqueue_steps(md_ctx *c, int nsteps, int energy_first)
             }
         } else {
             launch_vv_first(c, kp, 0, 0);
-            launch_rebuild(c, kp, false);
+            launch_rebuild(c, kp, false, false);
             launch_forces(c, kp, energy != 0, MD_TERM_ALL);
             launch_vv_second(c, kp, energy);
         }
@@ -322,7 +323,7 @@ md_status capture_rebuild_node(md_ctx *c, const md_kparams &kp, cudaGraphConditi
                                                  cudaStreamCaptureModeThreadLocal));
     cudaStream_t keep = c->stream;
     c->stream = c->stream2;
-    launch_rebuild(c, kp, true);
+    launch_rebuild(c, kp, true, false);
     c->stream = keep;
     cudaGraph_t out = nullptr;
     MD_CUDA_TRY(c, cudaStreamEndCapture(c->stream2, &out));
@@ -411,7 +412,7 @@ md_status capture_graph(md_ctx *c, int nsteps, int energy_first)
 md_status initial_build(md_ctx *c)
 {
     md_kparams kp = md_make_kparams(c);
-    launch_rebuild(c, kp, true);
+    launch_rebuild(c, kp, true, true);
     md_status s = check_overflow_and_sync(c);
     if (s == MD_ERR_LIST_OVERFLOW) {
         md_devstate h;
@@ -422,7 +423,7 @@ md_status initial_build(md_ctx *c)
         int zero = 0;
         MD_CUDA_TRY(c, cudaMemcpy(&c->st->list_overflow, &zero, sizeof(int), cudaMemcpyHostToDevice));
         kp = md_make_kparams(c);
-        launch_rebuild(c, kp, true);
+        launch_rebuild(c, kp, true, true);
         s = check_overflow_and_sync(c);
     }
     return s;
@@ -437,9 +438,241 @@ md_status refresh_state(md_ctx *c)
     return check_overflow_and_sync(c);
 }
 
+/* Cells of side >= rl/2 along each axis, the stencil (cells within rl; -1 =
+ * every cell when the stencil would wrap onto itself) and the cells' ranks
+ * along a 3-D Hilbert curve. */
+struct cell_grid {
+    int ncell[3], stencil[3], ncells;
+    float binlen[3];
+    std::vector<int> rank;   /* linear cell index -> Hilbert rank */
+    std::vector<int> lin;    /* Hilbert rank -> linear cell index */
+};
+
+void make_cell_grid(const float box[3], float rl, cell_grid &g)
+{
+    int bits = 1;
+    for (int k = 0; k < 3; k++) {
+        int nc = (int)floorf(box[k] / (0.5f * rl * 1.0001f));
+        nc = std::max(1, std::min(nc, 1024));
+        g.ncell[k] = nc;
+        g.binlen[k] = box[k] / (float)nc;
+        int sten = (int)ceilf(rl / g.binlen[k]);
+        g.stencil[k] = (2 * sten + 1 >= nc) ? -1 : sten;
+        while ((1 << bits) < nc) bits++;
+    }
+    g.ncells = g.ncell[0] * g.ncell[1] * g.ncell[2];
+    std::vector<std::pair<unsigned long long, int>> hk(g.ncells);
+    for (int z = 0; z < g.ncell[2]; z++)
+        for (int y = 0; y < g.ncell[1]; y++)
+            for (int x = 0; x < g.ncell[0]; x++) {
+                int lin = x + g.ncell[0] * (y + g.ncell[1] * z);
+                hk[lin] = std::make_pair(hilbert3(x, y, z, bits), lin);
+            }
+    std::sort(hk.begin(), hk.end());
+    g.rank.assign(g.ncells, 0);
+    g.lin.assign(g.ncells, 0);
+    for (int r = 0; r < g.ncells; r++) {
+        g.rank[hk[r].second] = r;
+        g.lin[r] = hk[r].second;
+    }
+}
+
+/* Host staging of everything uploaded at creation, in the initial (original)
+ * atom order, pitch-sized. */
+struct host_stage {
+    std::vector<double> x, v, m, mi;
+    std::vector<float4> p4;
+    std::vector<int> type;
+    std::vector<uint4> excl;
+    std::vector<int> cell_rank, cell_lin;
+    std::vector<int2> blo;      /* bonded lists (empty for batches) */
+    std::vector<int> blon;
+    std::vector<int4> alo;
+    std::vector<int> alon;
+    std::vector<float> ljh, bp;
+    /* batches */
+    std::vector<int> arep, crep;
+    std::vector<float2> ljr;
+    std::vector<int2> grid;
+    std::vector<md_repstate> repst;
+
+    void init(size_t P)
+    {
+        x.assign(3 * P, 0.0);
+        v.assign(3 * P, 0.0);
+        m.assign(P, 1.0);
+        mi.assign(P, 1.0);
+        p4.assign(P, make_float4(0, 0, 0, 0));
+        type.assign(P, 0);
+        excl.assign(P, make_uint4(MD_EXCL_NONE, MD_EXCL_NONE, MD_EXCL_NONE, MD_EXCL_NONE));
+        ljh.assign(2 * MD_MAXTYPE * MD_MAXTYPE, 0.0f);
+        bp.assign(4 * MD_MAXTYPE, 0.0f);
+    }
+};
+
+/* Streams, device memory, upload, first list build and force evaluation of
+ * a context whose host fields are set; frees everything on failure. */
+md_status setup_device(md_ctx *c, void *stream, host_stage &h, md_ctx **out)
+{
+    if (stream) {
+        c->stream = (cudaStream_t)stream;
+    } else {
+        if (cudaStreamCreateWithFlags(&c->stream, cudaStreamNonBlocking) != cudaSuccess) {
+            md_status s = fail(c, MD_ERR_CUDA, "stream creation failed");
+            delete c;
+            return s;
+        }
+        c->own_stream = true;
+    }
+    if (cudaStreamCreateWithFlags(&c->stream2, cudaStreamNonBlocking) != cudaSuccess) {
+        md_status s = fail(c, MD_ERR_CUDA, "stream creation failed");
+        if (c->own_stream) cudaStreamDestroy(c->stream);
+        delete c;
+        return s;
+    }
+    cudaGetDevice(&c->device);
+    const size_t P = c->pitch;
+    const int n = c->n;
+    const bool batch = c->nrep > 1;
+    /* block partials of the integrators (256 threads; one grid per replica
+     * in a batch) and of the fused step (128 threads, up to 32 per atom) */
+    size_t npart = 3 * (P / 4 + 256) + 8;
+    if (batch) npart = std::max(npart, 3 * (size_t)c->grid_cnt[md_grid_index(256)] + 8);
+    cudaError_t e = cudaSuccess;
+#define MD_ALLOC(ptr, cnt) if (e == cudaSuccess) e = dalloc(&(ptr), (cnt))
+    MD_ALLOC(c->x, 3 * P); MD_ALLOC(c->v, 3 * P); MD_ALLOC(c->mass, P); MD_ALLOC(c->minv, P);
+    MD_ALLOC(c->pos4, P); MD_ALLOC(c->pos4_alt, P); MD_ALLOC(c->pos_old, P);
+    MD_ALLOC(c->type, P); MD_ALLOC(c->perm, P); MD_ALLOC(c->iperm, P);
+    MD_ALLOC(c->f, 3 * P); MD_ALLOC(c->vir, P); MD_ALLOC(c->epot, P);
+    MD_ALLOC(c->nl_n, P);
+    MD_ALLOC(c->excl_orig, P); MD_ALLOC(c->excl_s, P);
+    MD_ALLOC(c->cell_rank, c->ncells); MD_ALLOC(c->cell_lin, c->ncells); MD_ALLOC(c->cell_count, c->ncells);
+    MD_ALLOC(c->cell_start, c->ncells + 1); MD_ALLOC(c->cell_fill, c->ncells);
+    MD_ALLOC(c->key, P); MD_ALLOC(c->src, P);
+    MD_ALLOC(c->tmp_d, 8 * P); MD_ALLOC(c->tmp4, P); MD_ALLOC(c->tmp_i, 3 * P);
+    MD_ALLOC(c->bl_o, 4 * P); MD_ALLOC(c->bl_on, P); MD_ALLOC(c->al_o, 4 * P); MD_ALLOC(c->al_on, P);
+    MD_ALLOC(c->bl_s, 4 * P); MD_ALLOC(c->bl_sn, P); MD_ALLOC(c->al_s, 4 * P); MD_ALLOC(c->al_sn, P);
+    c->npart = (int)(P / 256);
+    MD_ALLOC(c->partials, npart);
+    MD_ALLOC(c->st, 1);
+    c->rec_cap = 4096;
+    MD_ALLOC(c->rec, c->rec_cap);
+    MD_ALLOC(c->lj_dev, 2 * MD_MAXTYPE * MD_MAXTYPE);
+    MD_ALLOC(c->bonded_par, 4 * MD_MAXTYPE);
+    MD_ALLOC(c->type_mask_dev, MD_MAXTYPE);
+    MD_ALLOC(c->io_dev, 4 * P);
+    if (batch) {
+        MD_ALLOC(c->reps_dev, c->nrep); MD_ALLOC(c->repst, c->nrep);
+        MD_ALLOC(c->arep, P); MD_ALLOC(c->crep, c->ncells);
+        MD_ALLOC(c->rep_upd, c->nrep); MD_ALLOC(c->skey, P);
+        MD_ALLOC(c->ljr_dev, (size_t)MD_MAXTYPE * MD_MAXTYPE * c->nrep);
+        MD_ALLOC(c->grid_tab, h.grid.size());
+    }
+#undef MD_ALLOC
+    if (e != cudaSuccess) {
+        md_status s = fail(c, MD_ERR_CUDA, std::string("device allocation: ") + cudaGetErrorString(e));
+        free_device(c);
+        if (c->own_stream) cudaStreamDestroy(c->stream);
+        cudaStreamDestroy(c->stream2);
+        delete c;
+        return s;
+    }
+    cudaEventCreate(&c->ev0);
+    cudaEventCreate(&c->ev1);
+    std::vector<int> hperm(P);
+    for (size_t i = 0; i < P; i++) hperm[i] = (int)i;
+    md_devstate hs;
+    memset(&hs, 0, sizeof(hs));
+    hs.temper = c->temper_0;   /* integrator.cu:77 */
+    hs.vscale = 1.0;
+    hs.lambda = 1.0;
+    hs.lam_next = 1.0;     /* T_prev = T0 on the first step (integrator.cu:77) */
+    hs.kick_scale = 1.0;
+    std::vector<int> zeros(c->ncells, 0);
+    auto up = [&](void *dst, const void *srcp, size_t bytes) {
+        if (e == cudaSuccess && bytes > 0) e = cudaMemcpy(dst, srcp, bytes, cudaMemcpyHostToDevice);
+    };
+    up(c->x, h.x.data(), sizeof(double) * 3 * P);
+    up(c->v, h.v.data(), sizeof(double) * 3 * P);
+    up(c->mass, h.m.data(), sizeof(double) * P);
+    up(c->minv, h.mi.data(), sizeof(double) * P);
+    up(c->pos4, h.p4.data(), sizeof(float4) * P);
+    up(c->type, h.type.data(), sizeof(int) * P);
+    up(c->perm, hperm.data(), sizeof(int) * P);
+    up(c->iperm, hperm.data(), sizeof(int) * P);
+    up(c->excl_orig, h.excl.data(), sizeof(uint4) * P);
+    /* batches never remap exclusions (they have none): the sorted copy is set once */
+    if (batch) up(c->excl_s, h.excl.data(), sizeof(uint4) * P);
+    up(c->cell_rank, h.cell_rank.data(), sizeof(int) * c->ncells);
+    up(c->cell_lin, h.cell_lin.data(), sizeof(int) * c->ncells);
+    up(c->cell_count, zeros.data(), sizeof(int) * c->ncells);
+    up(c->cell_fill, zeros.data(), sizeof(int) * c->ncells);
+    if (!h.blo.empty()) {
+        up(c->bl_o, h.blo.data(), sizeof(int2) * 4 * n);
+        up(c->bl_on, h.blon.data(), sizeof(int) * n);
+        up(c->al_o, h.alo.data(), sizeof(int4) * 4 * n);
+        up(c->al_on, h.alon.data(), sizeof(int) * n);
+    } else {
+        if (e == cudaSuccess) e = cudaMemset(c->bl_on, 0, sizeof(int) * P);
+        if (e == cudaSuccess) e = cudaMemset(c->al_on, 0, sizeof(int) * P);
+    }
+    up(c->lj_dev, h.ljh.data(), sizeof(float) * h.ljh.size());
+    up(c->bonded_par, h.bp.data(), sizeof(float) * h.bp.size());
+    up(c->type_mask_dev, c->type_excl_mask, sizeof(unsigned) * MD_MAXTYPE);
+    up(c->st, &hs, sizeof(hs));
+    if (batch) {
+        up(c->reps_dev, c->reps.data(), sizeof(md_rep) * c->nrep);
+        up(c->repst, h.repst.data(), sizeof(md_repstate) * c->nrep);
+        up(c->arep, h.arep.data(), sizeof(int) * P);
+        up(c->crep, h.crep.data(), sizeof(int) * c->ncells);
+        up(c->ljr_dev, h.ljr.data(), sizeof(float2) * h.ljr.size());
+        up(c->grid_tab, h.grid.data(), sizeof(int2) * h.grid.size());
+        if (e == cudaSuccess) e = cudaMemset(c->rep_upd, 0, sizeof(int) * c->nrep);
+        if (e == cudaSuccess) e = cudaMemset(c->skey, 0, sizeof(int) * P);
+    }
+    if (e == cudaSuccess) e = cudaMemset(c->f, 0, sizeof(long long) * 3 * P);
+    if (e == cudaSuccess) e = cudaMemset(c->vir, 0, sizeof(float) * P);
+    if (e == cudaSuccess) e = cudaMemset(c->epot, 0, sizeof(float) * P);
+    if (e == cudaSuccess) e = cudaMemset(c->bl_sn, 0, sizeof(int) * P);
+    if (e == cudaSuccess) e = cudaMemset(c->al_sn, 0, sizeof(int) * P);
+    if (e == cudaSuccess) e = cudaMemset(c->nl_n, 0, sizeof(int) * P);
+    if (e != cudaSuccess) {
+        md_status s = fail(c, MD_ERR_CUDA, std::string("upload: ") + cudaGetErrorString(e));
+        md_destroy(c);
+        return s;
+    }
+    md_status s = alloc_list(c, (c->nmaxlist + 31) / 32 * 32);
+    if (s == MD_OK) s = initial_build(c);
+    if (s == MD_OK) s = refresh_state(c);
+    if (s != MD_OK) {
+        g_last_error = c->last_error;
+        md_destroy(c);
+        return s;
+    }
+    *out = c;
+    return MD_OK;
+}
+
 }  // namespace
 
 void md_set_global_error(const std::string &msg) { g_last_error = msg; }
+
+int md_cell_shift(const int stencil[3], const float binlen[3], const float box[3])
+{
+    for (int d = 0; d < 3; d++)
+        if (stencil[d] < 0 || (stencil[d] + 1) * (double)binlen[d] >= 0.49 * (double)box[d]) return 0;
+    return 1;
+}
+
+int md_ndf(const md_ctx *c)
+{
+    if (c->nrep > 1) {
+        long long s = 0;
+        for (const md_rep &r : c->reps) s += r.ndf;
+        return (int)s;
+    }
+    return std::max(1, 3 * c->n - 3);
+}
 
 md_kparams md_make_kparams(const md_ctx *c)
 {
@@ -458,12 +691,7 @@ md_kparams md_make_kparams(const md_ctx *c)
         kp.binlen[d] = c->binlen[d];
         kp.stencil[d] = c->stencil[d];
     }
-    /* The image of a stencil cell gives the reference's rint(d/L) exactly when
-     * every candidate pair is well inside half a box: |d| <= (S+1) bin < 0.49 L. */
-    kp.cell_shift = 1;
-    for (int d = 0; d < 3; d++)
-        if (c->stencil[d] < 0 || (c->stencil[d] + 1) * (double)c->binlen[d] >= 0.49 * (double)c->box[d])
-            kp.cell_shift = 0;
+    kp.cell_shift = md_cell_shift(c->stencil, c->binlen, c->box);
     kp.rcutsq = c->rcutsq;
     kp.reacf = c->reacf;
     kp.rskinsq = c->rskinsq;
@@ -623,168 +851,262 @@ md_status md_create(const md_system_desc *d, void *stream, md_ctx **out)
     c->has_angles = c->angles.empty() ? 0 : 1;
 
     /* cells of side >= rl/2 and their Hilbert ranks */
-    int bits = 1;
+    cell_grid g;
+    make_cell_grid(c->box, rl, g);
     for (int k = 0; k < 3; k++) {
-        int nc = (int)floorf(c->box[k] / (0.5f * rl * 1.0001f));
-        nc = std::max(1, std::min(nc, 1024));
-        c->ncell[k] = nc;
-        c->binlen[k] = c->box[k] / (float)nc;
-        int sten = (int)ceilf(rl / c->binlen[k]);
-        c->stencil[k] = (2 * sten + 1 >= nc) ? -1 : sten;
-        while ((1 << bits) < nc) bits++;
+        c->ncell[k] = g.ncell[k];
+        c->binlen[k] = g.binlen[k];
+        c->stencil[k] = g.stencil[k];
     }
-    c->ncells = c->ncell[0] * c->ncell[1] * c->ncell[2];
-    std::vector<std::pair<unsigned long long, int>> hk(c->ncells);
-    for (int z = 0; z < c->ncell[2]; z++)
-        for (int y = 0; y < c->ncell[1]; y++)
-            for (int x = 0; x < c->ncell[0]; x++) {
-                int lin = x + c->ncell[0] * (y + c->ncell[1] * z);
-                hk[lin] = std::make_pair(hilbert3(x, y, z, bits), lin);
-            }
-    std::sort(hk.begin(), hk.end());
-    std::vector<int> rank(c->ncells);
-    for (int r = 0; r < c->ncells; r++) rank[hk[r].second] = r;
+    c->ncells = g.ncells;
 
-    /* device memory */
-    if (stream) {
-        c->stream = (cudaStream_t)stream;
-    } else {
-        if (cudaStreamCreateWithFlags(&c->stream, cudaStreamNonBlocking) != cudaSuccess) {
-            md_status s = fail(c, MD_ERR_CUDA, "stream creation failed");
+    /* host staging in sorted order = original order before the first build */
+    host_stage h;
+    h.init(c->pitch);
+    const size_t P = c->pitch;
+    for (int i = 0; i < n; i++) {
+        for (int k = 0; k < 3; k++) {
+            h.x[k * P + i] = d->pos[3 * i + k];
+            h.v[k * P + i] = d->vel ? d->vel[3 * i + k] : 0.0;
+        }
+        h.m[i] = c->type_mass[c->itype[i]];
+        h.mi[i] = 1.0 / h.m[i];
+        h.p4[i] = make_float4(d->pos[3 * i], d->pos[3 * i + 1], d->pos[3 * i + 2], c->charge[i]);
+        h.type[i] = c->itype[i];
+        h.excl[i] = make_uint4(c->excl_host[4 * i], c->excl_host[4 * i + 1], c->excl_host[4 * i + 2],
+                               c->excl_host[4 * i + 3]);
+    }
+    h.cell_rank = std::move(g.rank);
+    h.cell_lin = std::move(g.lin);
+    h.blo = std::move(blo);
+    h.blon = std::move(blon);
+    h.alo = std::move(alo);
+    h.alon = std::move(alon);
+    for (int a = 0; a < c->ntype; a++)
+        for (int b = 0; b < c->ntype; b++) {
+            h.ljh[2 * (a * MD_MAXTYPE + b)] = c->lj1[a * c->ntype + b];
+            h.ljh[2 * (a * MD_MAXTYPE + b) + 1] = c->lj2[a * c->ntype + b];
+        }
+    for (int k = 0; k < MD_MAXTYPE; k++) {
+        h.bp[k] = c->bnd1[k]; h.bp[MD_MAXTYPE + k] = c->bnd2[k];
+        h.bp[2 * MD_MAXTYPE + k] = c->ang1[k]; h.bp[3 * MD_MAXTYPE + k] = c->ang2[k];
+    }
+    return setup_device(c, stream, h, out);
+}
+
+md_status md_create_batch(const md_system_desc *descs, int nrep, void *stream, md_ctx **out)
+{
+    if (!descs || !out || nrep < 1) return fail(nullptr, MD_ERR_ARG, "md_create_batch: null argument");
+    if (nrep == 1) return md_create(descs, stream, out);
+    const md_system_desc &d0 = descs[0];
+    long long ntot = 0;
+    int ntype = 1, nmax = 0;
+    for (int r = 0; r < nrep; r++) {
+        const md_system_desc *d = descs + r;
+        std::string at = " (replica " + std::to_string(r) + ")";
+        if (d->natom <= 0 || d->ntype < 1 || d->ntype > MD_MAXTYPE || !d->itype || !d->charge ||
+            !d->pos || !d->type_mass || !d->lj1 || !d->lj2)
+            return fail(nullptr, MD_ERR_ARG, "md_create_batch: missing or invalid descriptor fields" + at);
+        if (d->nbonds > 0 || d->nangle > 0)
+            return fail(nullptr, MD_ERR_UNSUPPORTED, "md_create_batch: bonded terms in a batch" + at);
+        if (d->lkspace < 0 || d->lkspace > 2 || d->rcutsq <= 0 || d->skin < 0 || d->dt <= 0 ||
+            d->integrator < 0 || d->integrator > 2 || d->enstype < 0 || d->enstype > 1)
+            return fail(nullptr, MD_ERR_ARG, "md_create_batch: invalid run parameters" + at);
+        if (d->lkspace != d0.lkspace || d->integrator != d0.integrator || d->enstype != d0.enstype ||
+            d->dt != d0.dt || d->tau_t != d0.tau_t)
+            return fail(nullptr, MD_ERR_ARG,
+                        "md_create_batch: replicas must share lkspace, integrator, ensemble, dt and tau_t" + at);
+        for (int i = 0; i < d->natom; i++)
+            if (d->itype[i] < 0 || d->itype[i] >= d->ntype)
+                return fail(nullptr, MD_ERR_ARG, "md_create_batch: atom type out of range" + at);
+        float rl = sqrtf(d->rcutsq) + d->skin;
+        for (int k = 0; k < 3; k++)
+            if (2.0f * rl > d->box[k])
+                return fail(nullptr, MD_ERR_BOX, "md_create_batch: cutoff + skin exceeds half the box" + at);
+        ntot += d->natom;
+        ntype = std::max(ntype, d->ntype);
+        nmax = std::max(nmax, d->nmaxlist > 0 ? d->nmaxlist : 64);
+    }
+    if (ntot >= (long long)MD_INDEX_MASK)
+        return fail(nullptr, MD_ERR_ARG, "md_create_batch: too many atoms");
+    md_ctx *c = new (std::nothrow) md_ctx();
+    if (!c) return fail(nullptr, MD_ERR_ARG, "out of host memory");
+    const int n = (int)ntot;
+    c->nrep = nrep;
+    c->n = n;
+    c->ntype = ntype;
+    c->pitch = ((n + 255) / 256) * 256;
+    for (int k = 0; k < 3; k++) {
+        c->box[k] = d0.box[k];
+        c->boxi[k] = (float)(1.0 / (double)d0.box[k]);
+    }
+    c->lkspace = d0.lkspace;
+    c->rcutsq = d0.rcutsq;
+    c->reacf = d0.lkspace == 0 ? d0.reacf : 0.0f;
+    c->alfa = d0.alfa;
+    c->skin = d0.skin;
+    c->nmaxlist = nmax;
+    c->enstype = d0.enstype;
+    c->temper_0 = d0.temper_0;
+    c->dt = d0.dt;
+    c->tau_t = d0.tau_t > 0 ? d0.tau_t : 100.0f;
+    c->integrator = d0.integrator;
+    if (c->lkspace > 0) wolf_consts(c->alfa, c->rcutsq, c->wc);
+    if (c->lkspace != 1) c->wc[3] = 0.0f;
+    c->rskinsq = (float)pow((double)(c->skin + sqrtf(c->rcutsq)), 2.0);
+    c->rmaxdif = c->skin * c->skin / 4.0f;
+    memset(c->lj1, 0, sizeof(c->lj1));
+    memset(c->lj2, 0, sizeof(c->lj2));
+    memset(c->bnd1, 0, sizeof(c->bnd1));
+    memset(c->bnd2, 0, sizeof(c->bnd2));
+    memset(c->ang1, 0, sizeof(c->ang1));
+    memset(c->ang2, 0, sizeof(c->ang2));
+    memset(c->type_mass, 0, sizeof(c->type_mass));
+    c->list_tpa = 0;   /* batches build their lists one warp per cell */
+
+    host_stage h;
+    const size_t P = c->pitch;
+    h.init(P);
+    h.arep.assign(P, nrep - 1);
+    h.ljr.assign((size_t)MD_MAXTYPE * MD_MAXTYPE * nrep, make_float2(0.0f, 0.0f));
+    h.repst.resize(nrep);
+    c->reps.resize(nrep);
+    c->rep_natom.resize(nrep);
+    c->itype.resize(n);
+    c->charge.resize(n);
+    int atom0 = 0, cell0 = 0;
+    const double tau = c->tau_t;
+    for (int r = 0; r < nrep; r++) {
+        const md_system_desc *d = descs + r;
+        md_rep &R = c->reps[r];
+        memset(&R, 0, sizeof(R));
+        for (int k = 0; k < 3; k++) {
+            R.box[k] = d->box[k];
+            R.boxi[k] = (float)(1.0 / (double)d->box[k]);   /* simulation.cu:290-292 */
+            R.boxd[k] = (double)d->box[k];
+            R.box2i[k] = 2.0 / (double)d->box[k];
+        }
+        R.rcutsq = d->rcutsq;
+        R.reacf = d->lkspace == 0 ? d->reacf : 0.0f;
+        float wc[4] = {0.0f, 0.0f, 0.0f, 0.0f};
+        if (d->lkspace > 0) wolf_consts(d->alfa, d->rcutsq, wc);
+        R.palfa = wc[0];
+        R.spiialfa = wc[1];
+        R.alfasq = wc[2];
+        R.wolf = d->lkspace == 1 ? wc[3] : 0.0f;
+        R.rskinsq = (float)pow((double)(d->skin + sqrtf(d->rcutsq)), 2.0);   /* neighborlist.cu:35 */
+        R.rmaxdif = d->skin * d->skin / 4.0f;                                 /* neighborlist.cu:36 */
+        md_shift_consts(d->lkspace, d->rcutsq, d->alfa, R.reacf, &R.ucc, &R.rc6i, &R.rcinv);
+        cell_grid g;
+        make_cell_grid(d->box, sqrtf(d->rcutsq) + d->skin, g);
+        for (int k = 0; k < 3; k++) {
+            R.ncell[k] = g.ncell[k];
+            R.stencil[k] = g.stencil[k];
+            R.binlen[k] = g.binlen[k];
+        }
+        R.cell_shift = md_cell_shift(R.stencil, R.binlen, R.box);
+        int nst = 1;   /* the warp-per-cell builder holds up to 128 stencil cells */
+        for (int k = 0; k < 3; k++) nst *= R.stencil[k] < 0 ? R.ncell[k] : 2 * R.stencil[k] + 1;
+        if (nst > 128) {
+            md_status s = fail(c, MD_ERR_UNSUPPORTED, "md_create_batch: stencil too large");
             delete c;
             return s;
         }
-        c->own_stream = true;
-    }
-    if (cudaStreamCreateWithFlags(&c->stream2, cudaStreamNonBlocking) != cudaSuccess) {
-        md_status s = fail(c, MD_ERR_CUDA, "stream creation failed");
-        if (c->own_stream) cudaStreamDestroy(c->stream);
-        delete c;
-        return s;
-    }
-    cudaGetDevice(&c->device);
-    const size_t P = c->pitch;
-    cudaError_t e = cudaSuccess;
-#define MD_ALLOC(ptr, cnt) if (e == cudaSuccess) e = dalloc(&(ptr), (cnt))
-    MD_ALLOC(c->x, 3 * P); MD_ALLOC(c->v, 3 * P); MD_ALLOC(c->mass, P); MD_ALLOC(c->minv, P);
-    MD_ALLOC(c->pos4, P); MD_ALLOC(c->pos4_alt, P); MD_ALLOC(c->pos_old, P);
-    MD_ALLOC(c->type, P); MD_ALLOC(c->perm, P); MD_ALLOC(c->iperm, P);
-    MD_ALLOC(c->f, 3 * P); MD_ALLOC(c->vir, P); MD_ALLOC(c->epot, P);
-    MD_ALLOC(c->nl_n, P);
-    MD_ALLOC(c->excl_orig, P); MD_ALLOC(c->excl_s, P);
-    MD_ALLOC(c->cell_rank, c->ncells); MD_ALLOC(c->cell_lin, c->ncells); MD_ALLOC(c->cell_count, c->ncells);
-    MD_ALLOC(c->cell_start, c->ncells + 1); MD_ALLOC(c->cell_fill, c->ncells);
-    MD_ALLOC(c->key, P); MD_ALLOC(c->src, P);
-    MD_ALLOC(c->tmp_d, 8 * P); MD_ALLOC(c->tmp4, P); MD_ALLOC(c->tmp_i, 3 * P);
-    MD_ALLOC(c->bl_o, 4 * P); MD_ALLOC(c->bl_on, P); MD_ALLOC(c->al_o, 4 * P); MD_ALLOC(c->al_on, P);
-    MD_ALLOC(c->bl_s, 4 * P); MD_ALLOC(c->bl_sn, P); MD_ALLOC(c->al_s, 4 * P); MD_ALLOC(c->al_sn, P);
-    c->npart = (int)(P / 256);
-    /* block partials of the integrators (256 threads) and of the fused step
-     * (128 threads, up to 32 per atom) */
-    MD_ALLOC(c->partials, 3 * (P / 4 + 256) + 8);
-    MD_ALLOC(c->st, 1);
-    c->rec_cap = 4096;
-    MD_ALLOC(c->rec, c->rec_cap);
-    MD_ALLOC(c->lj_dev, 2 * MD_MAXTYPE * MD_MAXTYPE);
-    MD_ALLOC(c->bonded_par, 4 * MD_MAXTYPE);
-    MD_ALLOC(c->type_mask_dev, MD_MAXTYPE);
-    MD_ALLOC(c->io_dev, 4 * P);
-#undef MD_ALLOC
-    if (e != cudaSuccess) {
-        md_status s = fail(c, MD_ERR_CUDA, std::string("device allocation: ") + cudaGetErrorString(e));
-        free_device(c);
-        if (c->own_stream) cudaStreamDestroy(c->stream);
-        cudaStreamDestroy(c->stream2);
-        delete c;
-        return s;
-    }
-    cudaEventCreate(&c->ev0);
-    cudaEventCreate(&c->ev1);
-    /* host staging in sorted order = original order before the first build */
-    std::vector<double> hx(3 * P, 0.0), hv(3 * P, 0.0), hm(P, 1.0), hmi(P, 1.0);
-    std::vector<float4> hp(P, make_float4(0, 0, 0, 0));
-    std::vector<int> ht(P, 0), hperm(P), hiperm(P);
-    std::vector<uint4> hex(P, make_uint4(MD_EXCL_NONE, MD_EXCL_NONE, MD_EXCL_NONE, MD_EXCL_NONE));
-    for (int i = 0; i < n; i++) {
-        for (int k = 0; k < 3; k++) {
-            hx[k * P + i] = d->pos[3 * i + k];
-            hv[k * P + i] = d->vel ? d->vel[3 * i + k] : 0.0;
+        R.cell0 = cell0;
+        R.ncells = g.ncells;
+        R.atom0 = atom0;
+        R.natom = d->natom;
+        R.ndf = std::max(1, 3 * d->natom - 3);
+        R.t0 = d->temper_0;
+        R.q_nh = R.ndf * 8.314e-3 * R.t0 * tau * tau;
+        if (R.q_nh <= 0) R.q_nh = 1.0;
+        c->rep_natom[r] = d->natom;
+        /* cells: global rank = cell0 + Hilbert rank inside the replica */
+        for (int k = 0; k < g.ncells; k++) {
+            h.cell_rank.push_back(cell0 + g.rank[k]);
+            h.cell_lin.push_back(g.lin[k]);
+            h.crep.push_back(r);
         }
-        hm[i] = c->type_mass[c->itype[i]];
-        hmi[i] = 1.0 / hm[i];
-        hp[i] = make_float4(d->pos[3 * i], d->pos[3 * i + 1], d->pos[3 * i + 2], c->charge[i]);
-        ht[i] = c->itype[i];
-        hex[i] = make_uint4(c->excl_host[4 * i], c->excl_host[4 * i + 1], c->excl_host[4 * i + 2],
-                            c->excl_host[4 * i + 3]);
-    }
-    for (size_t i = 0; i < P; i++) { hperm[i] = (int)i; hiperm[i] = (int)i; }
-    std::vector<float> ljh(2 * MD_MAXTYPE * MD_MAXTYPE, 0.0f);
-    for (int a = 0; a < c->ntype; a++)
-        for (int b = 0; b < c->ntype; b++) {
-            ljh[2 * (a * MD_MAXTYPE + b)] = c->lj1[a * c->ntype + b];
-            ljh[2 * (a * MD_MAXTYPE + b) + 1] = c->lj2[a * c->ntype + b];
+        for (int a = 0; a < d->ntype; a++)
+            for (int b = 0; b < d->ntype; b++)
+                h.ljr[(size_t)r * MD_MAXTYPE * MD_MAXTYPE + a * MD_MAXTYPE + b] =
+                    make_float2(d->lj1[a * d->ntype + b], d->lj2[a * d->ntype + b]);
+        for (int i = 0; i < d->natom; i++) {
+            int gi = atom0 + i;
+            for (int k = 0; k < 3; k++) {
+                h.x[k * P + gi] = d->pos[3 * i + k];
+                h.v[k * P + gi] = d->vel ? d->vel[3 * i + k] : 0.0;
+            }
+            h.m[gi] = d->type_mass[d->itype[i]];
+            h.mi[gi] = 1.0 / h.m[gi];
+            h.p4[gi] = make_float4(d->pos[3 * i], d->pos[3 * i + 1], d->pos[3 * i + 2], d->charge[i]);
+            h.type[gi] = d->itype[i];
+            h.arep[gi] = r;
+            c->itype[gi] = d->itype[i];
+            c->charge[gi] = d->charge[i];
         }
-    std::vector<float> bp(4 * MD_MAXTYPE);
-    for (int k = 0; k < MD_MAXTYPE; k++) {
-        bp[k] = c->bnd1[k]; bp[MD_MAXTYPE + k] = c->bnd2[k];
-        bp[2 * MD_MAXTYPE + k] = c->ang1[k]; bp[3 * MD_MAXTYPE + k] = c->ang2[k];
+        md_repstate &S = h.repst[r];
+        memset(&S, 0, sizeof(S));
+        S.temper = R.t0;
+        S.vscale = S.lambda = S.lam_next = S.kick_scale = 1.0;
+        atom0 += d->natom;
+        cell0 += g.ncells;
     }
-    md_devstate hs;
-    memset(&hs, 0, sizeof(hs));
-    hs.temper = c->temper_0;   /* integrator.cu:77 */
-    hs.vscale = 1.0;
-    hs.lambda = 1.0;
-    hs.lam_next = 1.0;     /* T_prev = T0 on the first step (integrator.cu:77) */
-    hs.kick_scale = 1.0;
-    std::vector<int> zeros(c->ncells, 0);
-    auto up = [&](void *dst, const void *srcp, size_t bytes) {
-        if (e == cudaSuccess) e = cudaMemcpy(dst, srcp, bytes, cudaMemcpyHostToDevice);
-    };
-    up(c->x, hx.data(), sizeof(double) * 3 * P);
-    up(c->v, hv.data(), sizeof(double) * 3 * P);
-    up(c->mass, hm.data(), sizeof(double) * P);
-    up(c->minv, hmi.data(), sizeof(double) * P);
-    up(c->pos4, hp.data(), sizeof(float4) * P);
-    up(c->type, ht.data(), sizeof(int) * P);
-    up(c->perm, hperm.data(), sizeof(int) * P);
-    up(c->iperm, hiperm.data(), sizeof(int) * P);
-    up(c->excl_orig, hex.data(), sizeof(uint4) * P);
-    up(c->cell_rank, rank.data(), sizeof(int) * c->ncells);
-    {
-        std::vector<int> lin(c->ncells);
-        for (int r = 0; r < c->ncells; r++) lin[r] = hk[r].second;
-        up(c->cell_lin, lin.data(), sizeof(int) * c->ncells);
+    c->ncells = cell0;
+    for (int k = 0; k < 3; k++) {
+        c->ncell[k] = c->reps[0].ncell[k];
+        c->binlen[k] = c->reps[0].binlen[k];
+        c->stencil[k] = c->reps[0].stencil[k];
     }
-    up(c->cell_count, zeros.data(), sizeof(int) * c->ncells);
-    up(c->cell_fill, zeros.data(), sizeof(int) * c->ncells);
-    up(c->bl_o, blo.data(), sizeof(int2) * 4 * n);
-    up(c->bl_on, blon.data(), sizeof(int) * n);
-    up(c->al_o, alo.data(), sizeof(int4) * 4 * n);
-    up(c->al_on, alon.data(), sizeof(int) * n);
-    up(c->lj_dev, ljh.data(), sizeof(float) * ljh.size());
-    up(c->bonded_par, bp.data(), sizeof(float) * bp.size());
-    up(c->type_mask_dev, c->type_excl_mask, sizeof(unsigned) * MD_MAXTYPE);
-    up(c->st, &hs, sizeof(hs));
-    if (e == cudaSuccess) e = cudaMemset(c->f, 0, sizeof(long long) * 3 * P);
-    if (e == cudaSuccess) e = cudaMemset(c->vir, 0, sizeof(float) * P);
-    if (e == cudaSuccess) e = cudaMemset(c->epot, 0, sizeof(float) * P);
-    if (e == cudaSuccess) e = cudaMemset(c->bl_sn, 0, sizeof(int) * P);
-    if (e == cudaSuccess) e = cudaMemset(c->al_sn, 0, sizeof(int) * P);
-    if (e == cudaSuccess) e = cudaMemset(c->nl_n, 0, sizeof(int) * P);
-    if (e != cudaSuccess) {
-        md_status s = fail(c, MD_ERR_CUDA, std::string("upload: ") + cudaGetErrorString(e));
-        md_destroy(c);
-        return s;
+    /* replica-aligned grids of 4 .. 256 atoms per block */
+    for (int k = 0; k < MD_NGRID; k++) {
+        const int A = 4 << k;
+        c->grid_off[k] = (int)h.grid.size();
+        for (int r = 0; r < nrep; r++) {
+            md_rep &R = c->reps[r];
+            if (A == 256) R.blk0 = (int)h.grid.size() - c->grid_off[k];
+            for (int j = 0; j < R.natom; j += A) h.grid.push_back(make_int2(r, R.atom0 + j));
+            if (A == 256) R.nblk = (int)h.grid.size() - c->grid_off[k] - R.blk0;
+        }
+        c->grid_cnt[k] = (int)h.grid.size() - c->grid_off[k];
     }
-    md_status s = alloc_list(c, (c->nmaxlist + 31) / 32 * 32);
-    if (s == MD_OK) s = initial_build(c);
-    if (s == MD_OK) s = refresh_state(c);
-    if (s != MD_OK) {
-        g_last_error = c->last_error;
-        md_destroy(c);
-        return s;
+    return setup_device(c, stream, h, out);
+}
+
+md_status md_get_replica_thermo(md_ctx *c, md_thermo *out, int nrep)
+{
+    if (!c || !out || nrep < 1) return MD_ERR_ARG;
+    if (c->nrep == 1) return md_get_thermo(c, out);
+    MD_CUDA_TRY(c, cudaStreamSynchronize(c->stream));
+    md_devstate h;
+    MD_CUDA_TRY(c, cudaMemcpy(&h, c->st, sizeof(h), cudaMemcpyDeviceToHost));
+    int k = std::min(nrep, c->nrep);
+    std::vector<md_repstate> rs(k);
+    MD_CUDA_TRY(c, cudaMemcpy(rs.data(), c->repst, sizeof(md_repstate) * k, cudaMemcpyDeviceToHost));
+    int flags = 0;
+    if (h.step > 0) {
+        md_thermo last;
+        MD_CUDA_TRY(c, cudaMemcpy(&last, c->rec + (h.step - 1) % c->rec_cap, sizeof(md_thermo),
+                                  cudaMemcpyDeviceToHost));
+        flags = last.flags;
     }
-    *out = c;
+    const bool nh = c->integrator == MD_NH;
+    for (int r = 0; r < k; r++) {
+        const md_rep &R = c->reps[r];
+        md_thermo &o = out[r];
+        memset(&o, 0, sizeof(o));
+        o.step = h.step > 0 ? h.step - 1 : 0;
+        o.ke = rs[r].ke;
+        o.temper = 2.0 * rs[r].ke / (R.ndf * 8.314e-3);
+        o.pe = rs[r].pe;
+        o.virial = rs[r].virial;
+        o.conserved = rs[r].ke + rs[r].pe +
+                      (nh ? 0.5 * R.q_nh * rs[r].xi * rs[r].xi + R.ndf * 8.314e-3 * R.t0 * rs[r].eta : 0.0);
+        o.xi = rs[r].xi;
+        o.lambda = rs[r].lambda;
+        o.builds = rs[r].builds;
+        o.flags = flags;
+    }
     return MD_OK;
 }
 
@@ -905,7 +1227,7 @@ md_status md_update_neighbors(md_ctx *c, int force)
     if (force) return initial_build(c);
     MD_CUDA_TRY(c, cudaMemsetAsync(&c->st->update, 0, sizeof(int), c->stream));
     launch_check(c, kp);
-    launch_rebuild(c, kp, false);
+    launch_rebuild(c, kp, false, false);
     return check_overflow_and_sync(c);
 }
 
@@ -1000,7 +1322,7 @@ md_status md_get_thermo(md_ctx *c, md_thermo *out)
     if (h.step == 0) {
         memset(out, 0, sizeof(*out));
         out->ke = h.ke;
-        out->temper = 2.0 * h.ke / (std::max(1, 3 * c->n - 3) * 8.314e-3);
+        out->temper = 2.0 * h.ke / (md_ndf(c) * 8.314e-3);
         out->pe = h.pe;
         out->virial = h.virial;
         out->conserved = h.ke + h.pe;
@@ -1050,6 +1372,7 @@ md_status md_run_host(md_ctx *c, double *pos3, double *vel3, int nsteps, int ene
 md_status md_write_cfg(md_ctx *c, const char *path)
 {
     if (!c || !path) return MD_ERR_ARG;
+    if (c->nrep > 1) return fail(c, MD_ERR_UNSUPPORTED, "md_write_cfg: a batch holds several boxes");
     std::vector<double> p(3 * (size_t)c->n), v(3 * (size_t)c->n);
     md_status s = md_get_positions(c, p.data());
     if (s == MD_OK) s = md_get_velocities(c, v.data());
@@ -1158,6 +1481,7 @@ md_status md_autotune(md_ctx *c, int *pair_tpa, int *list_tpa)
     c->fuse_step = bf;
     best = 1e30f;
     for (int t : lt) {
+        if (c->nrep > 1 && t != 0) continue;   /* batches build one warp per cell */
         c->list_tpa = t;
         float ms = 0.0f, m2 = 0.0f;
         md_status s = md_time_rebuild(c, 2, &ms);
@@ -1187,6 +1511,8 @@ md_status md_set_tuning(md_ctx *c, int pair_tpa, int list_tpa)
     if (!c) return MD_ERR_ARG;
     auto ok = [](int t) { return t == 1 || t == 2 || t == 4 || t == 8 || t == 16 || t == 32; };
     if (!ok(pair_tpa) || !(list_tpa == 0 || ok(list_tpa))) return MD_ERR_ARG;
+    if (c->nrep > 1 && list_tpa != 0)
+        return fail(c, MD_ERR_ARG, "md_set_tuning: a batch builds its lists one warp per cell");
     c->pair_tpa = pair_tpa;
     c->list_tpa = list_tpa;
     if (c->gexec) {

@@ -10,15 +10,30 @@
  * neighborlist.cu:268-283 (and :167-174) write it: no FMA contraction, so the
  * neighbour set and the rebuild decision are bit-identical to the reference's
  * on the same positions. */
-__device__ __forceinline__ float md_rsq_exact(float4 a, float4 b, const md_kparams &kp)
+__device__ __forceinline__ float md_rsq_box(float4 a, float4 b, const float *box,
+                                            const float *boxi)
 {
     float dx = __fsub_rn(a.x, b.x);
     float dy = __fsub_rn(a.y, b.y);
     float dz = __fsub_rn(a.z, b.z);
-    dx = __fsub_rn(dx, __fmul_rn(kp.box[0], rintf(__fmul_rn(dx, kp.boxi[0]))));
-    dy = __fsub_rn(dy, __fmul_rn(kp.box[1], rintf(__fmul_rn(dy, kp.boxi[1]))));
-    dz = __fsub_rn(dz, __fmul_rn(kp.box[2], rintf(__fmul_rn(dz, kp.boxi[2]))));
+    dx = __fsub_rn(dx, __fmul_rn(box[0], rintf(__fmul_rn(dx, boxi[0]))));
+    dy = __fsub_rn(dy, __fmul_rn(box[1], rintf(__fmul_rn(dy, boxi[1]))));
+    dz = __fsub_rn(dz, __fmul_rn(box[2], rintf(__fmul_rn(dz, boxi[2]))));
     return __fadd_rn(__fadd_rn(__fmul_rn(dx, dx), __fmul_rn(dy, dy)), __fmul_rn(dz, dz));
+}
+
+__device__ __forceinline__ float md_rsq_exact(float4 a, float4 b, const md_kparams &kp)
+{
+    return md_rsq_box(a, b, kp.box, kp.boxi);
+}
+
+/* (x + L/2) / bin truncated and clamped: the binning rule of the reference's
+ * sketch (neighborlist_kernel_o.cu:20-25) with IEEE add and divide. */
+__device__ __forceinline__ int cell_of(float x, float box, float binlen, int nc)
+{
+    float s = __fdiv_rn(__fadd_rn(x, box / 2.0f), binlen);
+    int c = (s <= 0.0f) ? 0 : (int)s;
+    return c >= nc ? nc - 1 : c;
 }
 
 /* True in every thread of the block that finishes last (threadfence

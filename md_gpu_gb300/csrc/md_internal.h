@@ -23,6 +23,7 @@
 #define MD_INTERNAL_H
 
 #include <cuda_runtime.h>
+#include <math.h>
 #include <stdint.h>
 
 #include <string>
@@ -74,6 +75,48 @@ struct md_kparams {
     int cell_shift;   /* 1: a stencil cell's periodic image fixes the min-image shift */
     double dt;
 };
+
+/* One replica of a batch: its geometry, cutoffs, cell grid and thermostat
+ * constants.  A batch keeps every replica's atoms in one contiguous range
+ * (the same range in the original and in the sorted order, since a build
+ * only reorders atoms inside their replica's cells) and its cells in one
+ * contiguous range of ranks. */
+struct md_rep {
+    float box[3], boxi[3];
+    double boxd[3], box2i[3];
+    float rcutsq, rskinsq, rmaxdif, reacf;
+    float palfa, spiialfa, alfasq, wolf;
+    float ucc, rc6i, rcinv;
+    int ncell[3], stencil[3];
+    float binlen[3];
+    int cell_shift;
+    int cell0, ncells;   /* first cell rank (= offset of its cell_rank table), cell count */
+    int atom0, natom;
+    int blk0, nblk;      /* its blocks of the 256-atom integrator grid */
+    int ndf;
+    double t0, q_nh;
+};
+
+/* Per-replica thermodynamic state of a batch (the fields md_devstate holds
+ * for a single system). */
+struct md_repstate {
+    double temper, ke, pe, virial;
+    double xi, eta, xi_a, eta_a;
+    double vscale, lambda, lam_next, kick_scale;
+    int builds;          /* neighbour-list builds of this replica */
+    int pad;
+};
+
+/* Replica-aligned launch grids of a batch: for A atoms per block (A = 4 ..
+ * 256, powers of two) block b covers atoms [tab[b].y, min(tab[b].y + A, end
+ * of replica tab[b].x)). */
+#define MD_NGRID 7
+inline int md_grid_index(int atoms_per_block)
+{
+    int k = 0;
+    while ((4 << k) < atoms_per_block) k++;
+    return k;
+}
 
 struct md_ctx {
     /* ---- host copy of the run ---- */
@@ -145,17 +188,65 @@ struct md_ctx {
     int pair_tpa = 8;    /* threads per atom in the pair kernel */
     int list_tpa = 0;    /* list build: 0 = one warp per cell, else threads per atom */
 
+    /* batches of replicas (nrep > 1; md_create_batch) */
+    int nrep = 1;
+    std::vector<md_rep> reps;
+    std::vector<int> rep_natom;
+    md_rep *reps_dev = nullptr;
+    md_repstate *repst = nullptr;
+    int *arep = nullptr;          /* atom -> replica (the same in both orders) */
+    int *rep_upd = nullptr;       /* per replica: an atom moved >= skin/2 since its last build */
+    int *skey = nullptr;          /* cell rank of every sorted atom at the last build */
+    int *crep = nullptr;          /* cell rank -> replica */
+    float2 *ljr_dev = nullptr;    /* nrep x 64 (lj1, lj2) */
+    int2 *grid_tab = nullptr;     /* the MD_NGRID replica-aligned grids, concatenated */
+    int grid_off[MD_NGRID] = {0}, grid_cnt[MD_NGRID] = {0};
+
     /* timing of the last md_step call (CUDA events on the stream) */
     cudaEvent_t ev0 = nullptr, ev1 = nullptr;
 };
 
 md_kparams md_make_kparams(const md_ctx *c);
+/* 1 when a stencil cell's periodic image gives the reference's min-image
+ * shift exactly: every candidate pair lies well inside half a box,
+ * |d| <= (S+1) bin < 0.49 L on every axis. */
+int md_cell_shift(const int stencil[3], const float binlen[3], const float box[3]);
+/* Degrees of freedom of the temperature: 3N - 3 per system (integrator.cu:155). */
+int md_ndf(const md_ctx *c);
+
+/* Constants of the consistent potentials at the cutoff: the Coulomb shift
+ * ucc (Wolf: erfc(a rc)/rc with A&S 7.1.26; reaction field: 1/rc + k rc^2/2),
+ * rc^-6 and 1/rc, computed in FP64 and rounded once. */
+inline void md_shift_consts(int lkspace, float rcutsq, float alfa, float reacf, float *ucc,
+                            float *rc6i, float *rcinv)
+{
+    double rc = sqrt((double)rcutsq);
+    *rcinv = (float)(1.0 / rc);
+    *rc6i = (float)(1.0 / (rc * rc * rc * rc * rc * rc));
+    if (lkspace == 1) {
+        const double a1 = (double)0.254829592f, a2 = (double)-0.284496736f,
+                     a3 = (double)1.421413741f, a4 = (double)-1.453152027f,
+                     a5 = (double)1.061405429f;
+        double x = (double)alfa * rc;
+        double t = 1.0 / (1.0 + (double)0.3275911f * x);
+        double poly = ((((a5 * t + a4) * t + a3) * t + a2) * t + a1);
+        *ucc = (float)(poly * t * exp(-x * x) / rc);
+    } else if (lkspace == 0) {
+        *ucc = (float)(1.0 / rc + 0.5 * (double)reacf * rc * rc);
+    } else {
+        *ucc = 0.0f;
+    }
+}
 /* Message returned by md_last_error(NULL, ...). */
 void md_set_global_error(const std::string &msg);
 
 /* ---- launchers (k_cells.cu) ---- */
 void launch_check(md_ctx *c, const md_kparams &kp);
-void launch_rebuild(md_ctx *c, const md_kparams &kp, bool unconditional);
+/* unconditional: build without looking at the device's rebuild request (the
+ * body of a graph's conditional rebuild node, or a forced build).  In a
+ * batch only the replicas whose atoms moved are rebuilt, unless
+ * all_replicas is set (forced builds). */
+void launch_rebuild(md_ctx *c, const md_kparams &kp, bool unconditional, bool all_replicas);
 void launch_set_condition(md_ctx *c, unsigned long long handle);
 /* ---- launchers (k_forces.cu) ---- */
 void launch_forces(md_ctx *c, const md_kparams &kp, bool energy, int terms);
@@ -174,6 +265,14 @@ void launch_scatter_in(md_ctx *c, const md_kparams &kp, int what, const void *sr
 bool md_can_fuse(const md_ctx *c);
 /* Pair forces + leapfrog + check in one kernel; swaps pos4 and pos4_alt. */
 void launch_pair_leapfrog(md_ctx *c, const md_kparams &kp, unsigned long long cond, int has_cond);
+
+/* ---- launchers of batches (k_batch.cu); the launchers above forward to
+ * these when c->nrep > 1 (the list kernels of a batch live in k_cells.cu) ---- */
+void launch_forces_b(md_ctx *c, const md_kparams &kp, bool energy, int terms);
+void launch_leapfrog_b(md_ctx *c, const md_kparams &kp, int energy, unsigned long long cond,
+                       int has_cond);
+void launch_vv_first_b(md_ctx *c, const md_kparams &kp, unsigned long long cond, int has_cond);
+void launch_vv_second_b(md_ctx *c, const md_kparams &kp, int energy, int kick);
 
 #define MD_CUDA_TRY(c, expr)                                                   \
     do {                                                                       \

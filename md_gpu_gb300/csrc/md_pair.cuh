@@ -62,15 +62,49 @@ struct pair_acc {
     float fx, fy, fz, fw, fe;
 };
 
+/* Geometry and force-law constants seen by an atom.  geom_kp reads them
+ * from the kernel parameters (a single system); geom_reg holds a copy in
+ * registers (one replica of a batch). */
+struct geom_kp {
+    const md_kparams &kp;
+    const pair_consts &pc;
+    __device__ __forceinline__ float L(int d) const { return kp.box[d]; }
+    __device__ __forceinline__ float Li(int d) const { return kp.boxi[d]; }
+    __device__ __forceinline__ float rcsq() const { return kp.rcutsq; }
+    __device__ __forceinline__ float reacf() const { return kp.reacf; }
+    __device__ __forceinline__ float palfa() const { return kp.palfa; }
+    __device__ __forceinline__ float spiialfa() const { return kp.spiialfa; }
+    __device__ __forceinline__ float alfasq() const { return kp.alfasq; }
+    __device__ __forceinline__ float wolf() const { return kp.wolf; }
+    __device__ __forceinline__ float ucc() const { return pc.ucc; }
+    __device__ __forceinline__ float rc6i() const { return pc.rc6i; }
+    __device__ __forceinline__ float rcinv() const { return pc.rcinv; }
+};
+
+struct geom_reg {
+    float L_[3], Li_[3], rcsq_, reacf_, palfa_, spiialfa_, alfasq_, wolf_, ucc_, rc6i_, rcinv_;
+    __device__ __forceinline__ float L(int d) const { return L_[d]; }
+    __device__ __forceinline__ float Li(int d) const { return Li_[d]; }
+    __device__ __forceinline__ float rcsq() const { return rcsq_; }
+    __device__ __forceinline__ float reacf() const { return reacf_; }
+    __device__ __forceinline__ float palfa() const { return palfa_; }
+    __device__ __forceinline__ float spiialfa() const { return spiialfa_; }
+    __device__ __forceinline__ float alfasq() const { return alfasq_; }
+    __device__ __forceinline__ float wolf() const { return wolf_; }
+    __device__ __forceinline__ float ucc() const { return ucc_; }
+    __device__ __forceinline__ float rc6i() const { return rc6i_; }
+    __device__ __forceinline__ float rcinv() const { return rcinv_; }
+};
+
 /* One pair: F_i += ff d, w_i += ff r^2 (pair_forces.cu:165-200 / :74-120). */
-template <int KIND, bool ENERGY>
-__device__ __forceinline__ void pair_term(const md_kparams &kp, const pair_consts &pc, float4 pi,
-                                          float qi, float4 pj, float2 l, bool valid, pair_acc &a)
+template <int KIND, bool ENERGY, class G>
+__device__ __forceinline__ void pair_term(const G &g, float4 pi, float qi, float4 pj, float2 l,
+                                          bool valid, pair_acc &a)
 {
     float dx = pi.x - pj.x, dy = pi.y - pj.y, dz = pi.z - pj.z;
-    dx -= kp.box[0] * rint_small(dx * kp.boxi[0]);
-    dy -= kp.box[1] * rint_small(dy * kp.boxi[1]);
-    dz -= kp.box[2] * rint_small(dz * kp.boxi[2]);
+    dx -= g.L(0) * rint_small(dx * g.Li(0));
+    dy -= g.L(1) * rint_small(dy * g.Li(1));
+    dz -= g.L(2) * rint_small(dz * g.Li(2));
     float rsq = dx * dx + dy * dy + dz * dz;
     float ri = rsqrt_approx(rsq);
     float ri2 = ri * ri;
@@ -78,31 +112,30 @@ __device__ __forceinline__ void pair_term(const md_kparams &kp, const pair_const
     float ff, uc = 0.0f;
     if (KIND == 1) {
         float r = rsq * ri;
-        float t = rcp_approx(1.0f + kp.palfa * r);
+        float t = rcp_approx(1.0f + g.palfa() * r);
         float poly = ((((A5 * t + A4) * t + A3) * t + A2) * t + A1) * t;
-        float ex = ex2_approx(kp.alfasq * rsq);
-        ff = ((kp.spiialfa * r + poly) * ex * ri - kp.wolf) * qq;
-        if (ENERGY) uc = qq * (poly * ex * ri - pc.ucc + kp.wolf * __logf(r * pc.rcinv));
+        float ex = ex2_approx(g.alfasq() * rsq);
+        ff = ((g.spiialfa() * r + poly) * ex * ri - g.wolf()) * qq;
+        if (ENERGY) uc = qq * (poly * ex * ri - g.ucc() + g.wolf() * __logf(r * g.rcinv()));
     } else {
-        ff = qq * (ri - kp.reacf * rsq);
-        if (ENERGY) uc = qq * (ri + 0.5f * kp.reacf * rsq - pc.ucc);
+        ff = qq * (ri - g.reacf() * rsq);
+        if (ENERGY) uc = qq * (ri + 0.5f * g.reacf() * rsq - g.ucc());
     }
     float ri6 = ri2 * ri2 * ri2;
     ff = ff * ri2 + (l.x * ri6 - l.y) * ri6 * ri2;
     /* list padding entries point at the atom itself: r = 0 is skipped */
-    bool in = valid && rsq <= kp.rcutsq && rsq > 0.0f;
+    bool in = valid && rsq <= g.rcsq() && rsq > 0.0f;
     ff = in ? ff : 0.0f;
     a.fx += ff * dx;
     a.fy += ff * dy;
     a.fz += ff * dz;
     a.fw += ff * rsq;
     if (ENERGY) {
-        float ulj = l.x * (1.0f / 12.0f) * (ri6 * ri6 - pc.rc6i * pc.rc6i) -
-                    l.y * (1.0f / 6.0f) * (ri6 - pc.rc6i);
+        float ulj = l.x * (1.0f / 12.0f) * (ri6 * ri6 - g.rc6i() * g.rc6i()) -
+                    l.y * (1.0f / 6.0f) * (ri6 - g.rc6i());
         a.fe += in ? 0.5f * (uc + ulj) : 0.0f;
     }
 }
-
 
 struct pair_total {
     long long fx, fy, fz;   /* int64 fixed point, valid in lane 0 of the atom's group */
@@ -117,9 +150,8 @@ struct pair_total {
  * and converts its sum to int64 once; lane sums are combined with integer
  * shuffles (exact), so the result depends only on TPA.  Every lane of the
  * warp must call this (the shuffles use the full mask). */
-template <int KIND, int TPA, int B, bool ENERGY>
-__device__ __forceinline__ pair_total pair_sum(const md_kparams &kp, const pair_consts &pc, int ii,
-                                               bool active, int lane,
+template <int KIND, int TPA, int B, bool ENERGY, class G>
+__device__ __forceinline__ pair_total pair_sum(const G &g, int cap, int ii, bool active, int lane,
                                                const float4 *__restrict__ pos4,
                                                const int *__restrict__ type,
                                                const unsigned *__restrict__ nl,
@@ -132,7 +164,7 @@ __device__ __forceinline__ pair_total pair_sum(const md_kparams &kp, const pair_
     const float2 *ljrow = lj + type[ii] * MD_MAXTYPE;
     const float qi = QFAC * pi.w;
     pair_acc acc = {0.0f, 0.0f, 0.0f, 0.0f, 0.0f};
-    const unsigned *lp = nl + (size_t)ii * kp.cap + lane;
+    const unsigned *lp = nl + (size_t)ii * cap + lane;
     unsigned e0[B], e1[B];
     float4 p0[B];
     if (nb > 0) {
@@ -159,7 +191,7 @@ __device__ __forceinline__ pair_total pair_sum(const md_kparams &kp, const pair_
         }
 #pragma unroll
         for (int b = 0; b < B; b++)
-            pair_term<KIND, ENERGY>(kp, pc, pi, qi, p0[b], ljrow[e0[b] >> MD_TYPE_SHIFT], true, acc);
+            pair_term<KIND, ENERGY>(g, pi, qi, p0[b], ljrow[e0[b] >> MD_TYPE_SHIFT], true, acc);
 #pragma unroll
         for (int b = 0; b < B; b++) {
             e0[b] = e1[b];
@@ -190,19 +222,7 @@ __device__ __forceinline__ pair_total pair_sum(const md_kparams &kp, const pair_
 inline pair_consts make_pair_consts(const md_ctx *c)
 {
     pair_consts pc;
-    double rc = sqrt((double)c->rcutsq);
-    pc.rcinv = (float)(1.0 / rc);
-    pc.rc6i = (float)(1.0 / (rc * rc * rc * rc * rc * rc));
-    if (c->lkspace == 1) {
-        double a = c->alfa, x = a * rc;
-        double t = 1.0 / (1.0 + (double)0.3275911f * x);
-        double poly = ((((double)A5 * t + (double)A4) * t + (double)A3) * t + (double)A2) * t + (double)A1;
-        pc.ucc = (float)(poly * t * exp(-x * x) / rc);
-    } else if (c->lkspace == 0) {
-        pc.ucc = (float)(1.0 / rc + 0.5 * (double)c->reacf * rc * rc);
-    } else {
-        pc.ucc = 0.0f;
-    }
+    md_shift_consts(c->lkspace, c->rcutsq, c->alfa, c->reacf, &pc.ucc, &pc.rc6i, &pc.rcinv);
     return pc;
 }
 

@@ -50,15 +50,15 @@ __device__ __forceinline__ double wrap(double x, double L, double two_over_l)
 
 /* First thermostat half step of the next VV step (NH): from KE (already
  * scaled by the pending factor) and xi, eta; returns the factor s1. */
-__device__ __forceinline__ double nh_half_a(const md_kparams &kp, const thermo_par &tp, double ke,
+__device__ __forceinline__ double nh_half_a(double dt, const thermo_par &tp, double ke,
                                             double &xi, double &eta)
 {
     double kt = RGAS * tp.t0;
-    xi += 0.25 * kp.dt * (2.0 * ke - tp.ndf * kt) / tp.q_nh;
-    double s1 = exp(-0.5 * kp.dt * xi);
+    xi += 0.25 * dt * (2.0 * ke - tp.ndf * kt) / tp.q_nh;
+    double s1 = exp(-0.5 * dt * xi);
     ke *= s1 * s1;
-    eta += 0.5 * kp.dt * xi;
-    xi += 0.25 * kp.dt * (2.0 * ke - tp.ndf * kt) / tp.q_nh;
+    eta += 0.5 * dt * xi;
+    xi += 0.25 * dt * (2.0 * ke - tp.ndf * kt) / tp.q_nh;
     return s1;
 }
 
@@ -77,9 +77,85 @@ __device__ __forceinline__ void write_partials(double ke, double pe, double w, i
     }
 }
 
+/* Thermostat bookkeeping of one system after a step, from its FP64 totals
+ * (ke before any pending thermostat scale, pe, w = sum ff r^2).  S is
+ * md_devstate (a single system) or md_repstate (one replica of a batch): both
+ * hold the same thermostat fields.  mode 0 leapfrog, 1 VV / NH, 2 observe
+ * only (no step; the Berendsen reference temperature kept).  Returns the
+ * kinetic energy after the thermostat and sets *xi_out, *eta_out, *lam_out. */
+template <class S>
+__device__ double thermo_advance(double dt, const thermo_par &tp, int mode, double ke, double pe,
+                                 double w, S *st, double *xi_out, double *eta_out, double *lam_out)
+{
+    volatile S *vs = st;
+    double kt = RGAS * tp.t0;
+    double lam = (mode == 0 && tp.berendsen) ? vs->lam_next : 1.0;
+    double xi = vs->xi, eta = vs->eta;
+    if (mode == 1) {
+        st->vscale = 1.0;
+        if (tp.nh) {
+            xi = vs->xi_a;
+            eta = vs->eta_a;
+            xi += 0.25 * dt * (2.0 * ke - tp.ndf * kt) / tp.q_nh;
+            double s2 = exp(-0.5 * dt * xi);
+            ke *= s2 * s2;
+            eta += 0.5 * dt * xi;
+            xi += 0.25 * dt * (2.0 * ke - tp.ndf * kt) / tp.q_nh;
+            st->vscale = s2;
+            st->xi = xi;
+            st->eta = eta;
+        }
+    }
+    st->ke = ke;
+    if (tp.energy) { st->pe = pe; st->virial = w / 6.0; }
+    if (tp.nh && mode != 0) {
+        /* the next step's first thermostat half step, from this state */
+        double xa = xi, ea = eta;
+        double s1 = nh_half_a(dt, tp, ke, xa, ea);
+        st->xi_a = xa;
+        st->eta_a = ea;
+        st->kick_scale = vs->vscale * s1;
+    } else if (mode != 0) {
+        st->kick_scale = vs->vscale;
+    }
+    *xi_out = xi;
+    *eta_out = eta;
+    *lam_out = lam;
+    /* observing the state does not move the Berendsen reference temperature:
+     * the first step uses T = T0 (integrator.cu:77) */
+    if (mode == 2) return ke;
+    double temper = 2.0 * ke / (tp.ndf * RGAS);
+    st->temper = temper;
+    st->lambda = lam;
+    /* integrator.cu:146-147 for the next step, from this step's temperature */
+    st->lam_next = tp.berendsen ? sqrt(1.0 + dt / tp.tau * (tp.t0 / temper - 1.0)) : 1.0;
+    return ke;
+}
+
+/* Appends the step record and advances the step counter (thread 0). */
+__device__ void write_record(const thermo_par &tp, int ndf, double ke, double pe, double w,
+                             double extra, double xi, double lam, md_devstate *st, md_thermo *rec,
+                             int rec_cap)
+{
+    volatile md_devstate *vs = st;
+    long long step = vs->step;
+    md_thermo r;
+    r.step = step;
+    r.ke = ke;
+    r.temper = 2.0 * ke / (ndf * RGAS);
+    r.pe = tp.energy ? pe : 0.0;
+    r.virial = tp.energy ? w / 6.0 : 0.0;
+    r.conserved = tp.energy ? ke + pe + extra : 0.0;
+    r.xi = xi;
+    r.lambda = lam;
+    r.builds = vs->builds;
+    r.flags = tp.energy ? 1 : 0;
+    rec[step % rec_cap] = r;
+    st->step = step + 1;
+}
+
 /* Fixed-order totals of the block partials, then (thread 0) temperature,
- * thermostat bookkeeping and the step record.  mode 0 leapfrog, 1 VV / NH,
- * 2 observe only (no step, the Berendsen reference temperature kept). */
+ * thermostat bookkeeping and the step record (mode as thermo_advance). */
 __device__ void finalize(const md_kparams &kp, const thermo_par &tp, int mode, int npart,
                          const double *partials, md_devstate *st, md_thermo *rec, int rec_cap,
                          double *sh)
@@ -93,59 +169,11 @@ __device__ void finalize(const md_kparams &kp, const thermo_par &tp, int mode, i
     double pe = tp.energy ? block_sum(b, sh) : 0.0;
     double w = tp.energy ? block_sum(c, sh) : 0.0;
     if (threadIdx.x != 0) return;
-    volatile md_devstate *vs = st;
-    double kt = RGAS * tp.t0;
-    double lam = (mode == 0 && tp.berendsen) ? vs->lam_next : 1.0;
-    double xi = vs->xi, eta = vs->eta;
-    if (mode == 1) {
-        st->vscale = 1.0;
-        if (tp.nh) {
-            xi = vs->xi_a;
-            eta = vs->eta_a;
-            xi += 0.25 * kp.dt * (2.0 * ke - tp.ndf * kt) / tp.q_nh;
-            double s2 = exp(-0.5 * kp.dt * xi);
-            ke *= s2 * s2;
-            eta += 0.5 * kp.dt * xi;
-            xi += 0.25 * kp.dt * (2.0 * ke - tp.ndf * kt) / tp.q_nh;
-            st->vscale = s2;
-            st->xi = xi;
-            st->eta = eta;
-        }
-    }
-    double temper = 2.0 * ke / (tp.ndf * RGAS);
-    st->ke = ke;
-    if (tp.energy) { st->pe = pe; st->virial = w / 6.0; }
-    if (tp.nh && mode != 0) {
-        /* the next step's first thermostat half step, from this state */
-        double xa = xi, ea = eta;
-        double s1 = nh_half_a(kp, tp, ke, xa, ea);
-        st->xi_a = xa;
-        st->eta_a = ea;
-        st->kick_scale = vs->vscale * s1;
-    } else if (mode != 0) {
-        st->kick_scale = vs->vscale;
-    }
-    /* observing the state does not move the Berendsen reference temperature:
-     * the first step uses T = T0 (integrator.cu:77) */
+    double xi, eta, lam;
+    ke = thermo_advance(kp.dt, tp, mode, ke, pe, w, st, &xi, &eta, &lam);
     if (mode == 2) return;
-    st->temper = temper;
-    st->lambda = lam;
-    /* integrator.cu:146-147 for the next step, from this step's temperature */
-    st->lam_next = tp.berendsen ? sqrt(1.0 + kp.dt / tp.tau * (tp.t0 / temper - 1.0)) : 1.0;
-    long long step = vs->step;
-    md_thermo r;
-    r.step = step;
-    r.ke = ke;
-    r.temper = temper;
-    r.pe = tp.energy ? pe : 0.0;
-    r.virial = tp.energy ? w / 6.0 : 0.0;
-    r.conserved = tp.energy ? ke + pe + (tp.nh ? 0.5 * tp.q_nh * xi * xi + tp.ndf * kt * eta : 0.0) : 0.0;
-    r.xi = xi;
-    r.lambda = lam;
-    r.builds = vs->builds;
-    r.flags = tp.energy ? 1 : 0;
-    rec[step % rec_cap] = r;
-    st->step = step + 1;
+    double extra = tp.nh ? 0.5 * tp.q_nh * xi * xi + tp.ndf * RGAS * tp.t0 * eta : 0.0;
+    write_record(tp, tp.ndf, ke, pe, w, extra, xi, lam, st, rec, rec_cap);
 }
 
 __device__ __forceinline__ void check_moved(float4 p, float4 old, const md_kparams &kp,
@@ -168,8 +196,7 @@ inline thermo_par make_tp(const md_ctx *c, int energy)
     thermo_par tp;
     tp.t0 = c->temper_0;
     tp.tau = c->tau_t > 0 ? c->tau_t : 100.0;
-    tp.ndf = 3 * c->n - 3;
-    if (tp.ndf < 1) tp.ndf = 1;
+    tp.ndf = md_ndf(c);
     tp.q_nh = tp.ndf * RGAS * tp.t0 * tp.tau * tp.tau;
     if (tp.q_nh <= 0) tp.q_nh = 1.0;
     tp.berendsen = (c->enstype == 1 && c->integrator == MD_LEAPFROG) ? 1 : 0;

@@ -25,3 +25,27 @@ def aggregate_rate(atom_steps: float, elapsed_ms: float, world: int, device=None
     dist.all_reduce(a, op=dist.ReduceOp.SUM)
     dist.all_reduce(t, op=dist.ReduceOp.MAX)
     return float(a.item()) / (float(t.item()) * 1e-3), float(t.item())
+
+
+def equilibrate_batch(replicas, temp: float = 1200.0,
+                      stages=((0.5, 10.0, 400), (2.0, 100.0, 200))):
+    """Relax and thermalise a list of MDSystem.from_arrays keyword dicts as
+    one batch: Berendsen leapfrog NVT stages (dt fs, tau fs, steps) at `temp`.
+    Replicas generated on a compressed lattice start far from equilibrium;
+    this melts them before a production run.  Returns copies of the dicts
+    with positions and velocities replaced by the final state."""
+    import numpy as np
+
+    from .system import MD_LEAPFROG, MDSystem
+    cur = [dict(r) for r in replicas]
+    for dt, tau, n in stages:
+        spec = [dict(r, integrator=MD_LEAPFROG, enstype=1, temper_0=temp, dt=dt, tau_t=tau)
+                for r in cur]
+        with MDSystem.from_batch(spec) as b:
+            b.step(int(n))
+            X, V = b.positions(), b.velocities()
+            slices = b.replica_slices()
+        for r, sl in zip(cur, slices):
+            r["pos"] = X[sl].astype(np.float32)
+            r["vel"] = V[sl].astype(np.float32)
+    return cur

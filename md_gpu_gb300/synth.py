@@ -109,8 +109,9 @@ def nacl_params(eps_scale=(1.0, 1.0), sig_scale=(1.0, 1.0)):
     sC, eC = NACL_LJ["Cl"]
     sN *= sig_scale[0]; sC *= sig_scale[1]
     eN *= KCAL * eps_scale[0]; eC *= KCAL * eps_scale[1]
-    return [(1, 1, "LJ", sN, eN), (1, 2, "LJ", 0.5 * (sN + sC), float(np.sqrt(eN * eC))),
-            (2, 2, "LJ", sC, eC)]
+    return [(1, 1, "LJ", float(sN), float(eN)),
+            (1, 2, "LJ", float(0.5 * (sN + sC)), float(np.sqrt(eN * eC))),
+            (2, 2, "LJ", float(sC), float(eC))]
 
 
 def nacl_rocksalt(ncell: int = 20, seed: int = 1, temp: float = 1200.0, density: float = 1.5,
@@ -153,6 +154,115 @@ def nacl_rocksalt(ncell: int = 20, seed: int = 1, temp: float = 1200.0, density:
         bonds=np.zeros((0, 3), np.int64), angles=np.zeros((0, 4), np.int64),
         box=box, itype=itype, charge=charge,
         pos=_centre(pos, box), vel=_maxwell(rng, masses, temp))
+
+
+def nacl_replica(natom: int, seed: int = 1, temp: float = 1200.0, density: float = 1.5,
+                 rc: float = 12.0, skin: float = 1.0, alpha: float = 0.2, dt: float = 2.0,
+                 nsteps: int = 2000, nmaxlist: int = 416, eps_scale=(1.0, 1.0),
+                 sig_scale=(1.0, 1.0), charge_scale: float = 1.0, integrator: str = "vv",
+                 ensemble: str = "nve", jitter: float = 0.25) -> System:
+    """NaCl-like replica of any even size.  natom ions at `density` g/cm^3
+    occupy a random half-Na / half-Cl subset of the sites of a simple-cubic
+    lattice with alternating site types (rocksalt) of m^3 >= natom sites,
+    m even; ions are displaced by up to +-jitter A.  The cutoff is clamped to
+    rc <= L/2 (1 - 1e-3) - skin so that cutoff + skin stays inside half the
+    box (the minimum-image convention of the force and list kernels) for the
+    smallest replicas; the clamped value is what the .inp carries."""
+    natom = int(natom)
+    if natom < 2 or natom % 2:
+        raise ValueError("natom must be even and >= 2")
+    mNa, mCl = 22.98977, 35.4527
+    rho = density / ((mNa + mCl) / 2.0) * AVOGADRO * 1e-24
+    L = (natom / rho) ** (1.0 / 3.0)
+    m = int(np.ceil(natom ** (1.0 / 3.0) - 1e-9))
+    m += m % 2
+    a = L / m
+    g = np.stack(np.meshgrid(*[np.arange(m)] * 3, indexing="ij"), -1).reshape(-1, 3)
+    odd = g.sum(1) % 2 == 1
+    rng = np.random.default_rng(seed)
+    na_sites = rng.choice(np.flatnonzero(~odd), natom // 2, replace=False)
+    cl_sites = rng.choice(np.flatnonzero(odd), natom // 2, replace=False)
+    sites = np.empty(natom, np.int64)
+    sites[0::2] = np.sort(na_sites)
+    sites[1::2] = np.sort(cl_sites)
+    pos = (g[sites] + 0.5) * a - 0.5 * L + rng.uniform(-jitter, jitter, (natom, 3))
+    itype = np.empty(natom, np.int64)
+    itype[0::2] = 1
+    itype[1::2] = 2
+    charge = np.where(itype == 1, 1.0, -1.0) * charge_scale
+    masses = np.where(itype == 1, mNa, mCl)
+    box = np.full(3, L)
+    rc_eff = min(rc, 0.5 * L * (1.0 - 1e-3) - skin)
+    inp = dict(ensemble=ensemble, temper=temp, times=(0, nsteps, max(1, nsteps // 10), dt),
+               cutoff=(rc_eff, 1), alfa=alpha, skin=(skin, nmaxlist), rdel=0.02,
+               integrator=integrator)
+    return System(
+        name="nacl", inp=inp,
+        types=[("Na", mNa, 1.0), ("Cl", mCl, -1.0)],
+        vdw=nacl_params(eps_scale=eps_scale, sig_scale=sig_scale),
+        bond_types=[], angle_types=[],
+        bonds=np.zeros((0, 3), np.int64), angles=np.zeros((0, 4), np.int64),
+        box=box, itype=itype, charge=charge,
+        pos=_centre(pos, box), vel=_maxwell(rng, masses, temp))
+
+
+def replica_batch(nrep: int = 512, nmin: int = 256, nmax: int = 8192, seed: int = 1,
+                  spread: float = 0.1, **kw) -> List[System]:
+    """Uneven NaCl-like replicas: N uniform in [nmin, nmax] (rounded down to
+    even), each with its own eps and sigma per type and charge scale drawn
+    uniformly within +-spread of the molten-NaCl values; 1.5 g/cm^3, 1200 K."""
+    rng = np.random.default_rng(seed)
+    out = []
+    for r in range(nrep):
+        n = int(rng.integers(nmin, nmax + 1))
+        n -= n % 2
+        es = tuple(rng.uniform(1 - spread, 1 + spread, 2))
+        ss = tuple(rng.uniform(1 - spread, 1 + spread, 2))
+        qs = float(rng.uniform(1 - spread, 1 + spread))
+        out.append(nacl_replica(n, seed=seed * 1000003 + r, eps_scale=es, sig_scale=ss,
+                                charge_scale=qs, **kw))
+    return out
+
+
+def to_arrays(sys_: System) -> Dict[str, object]:
+    """Keyword arguments of MDSystem.from_arrays for a system, with the unit
+    conversions and float rounding of the reference's parser
+    (simulation.cu:58-316): masses g/mol * 1e4, lj1 = 48 eps sigma^12,
+    lj2 = 24 eps sigma^6, rc^2 in float, angles in rad."""
+    f32 = np.float32
+    p = sys_.inp
+    nt = len(sys_.types)
+    mass = np.array([f32(np.float64(f32(m)) * 10000.0) for (_, m, _) in sys_.types], f32)
+    lj1 = np.zeros((nt, nt), f32)
+    lj2 = np.zeros((nt, nt), f32)
+    for (i, j, form, a, b) in sys_.vdw:
+        a32, b32 = f32(a), f32(b)
+        if form == "LJ":
+            l1 = f32(np.float64(f32(48.0) * b32) * np.float64(a32) ** 12)
+            l2 = f32(np.float64(f32(24.0) * b32) * np.float64(a32) ** 6)
+        else:
+            l1, l2 = f32(12.0) * a32, f32(6.0) * b32
+        lj1[i - 1, j - 1] = lj1[j - 1, i - 1] = l1
+        lj2[i - 1, j - 1] = lj2[j - 1, i - 1] = l2
+    rc, lk = p["cutoff"]
+    rc32 = f32(rc)
+    integ = {"leapfrog": 0, "vv": 1, "nh": 2}[p.get("integrator", "leapfrog")]
+    if len(sys_.bonds) or len(sys_.angles):
+        raise ValueError("to_arrays: bonded systems are read from files")
+    if lk == 0:
+        eps = f32(p.get("reacf", 1.0))
+        num = f32(2.0) * (eps - f32(1.0)) / (f32(2.0) * eps + f32(1.0))
+        reacf, alfa = f32(np.float64(num) / np.float64(rc32) ** 3), f32(0.0)
+    else:
+        reacf, alfa = f32(0.0), f32(p["alfa"]) if lk == 1 else f32(3.09 / np.float64(rc32))
+    return dict(box=sys_.box.astype(f32), itype=(sys_.itype - 1).astype(np.int32),
+                charge=sys_.charge.astype(f32), pos=sys_.pos.astype(f32), vel=sys_.vel.astype(f32),
+                type_mass=mass, lj1=lj1, lj2=lj2, lkspace=lk, rcutsq=float(rc32 * rc32),
+                reacf=float(reacf), alfa=float(alfa), skin=float(f32(p["skin"][0])),
+                nmaxlist=int(p["skin"][1]), dt=float(f32(p["times"][3])),
+                enstype=1 if p["ensemble"] == "nvt" else 0,
+                temper_0=float(f32(p.get("temper", 0.0))), tau_t=float(f32(p.get("tau_t", 100.0))),
+                integrator=integ)
 
 
 def water_grid(nside: int = 32, seed: int = 1, temp: float = 300.0, rc: float = 10.0,

@@ -62,6 +62,48 @@ class Info(C.Structure):
                 ("builds", C.c_int), ("max_neighbors", C.c_int), ("kernels_per_step", C.c_int)]
 
 
+def _make_desc(keep, *, box, itype, charge, pos, vel, type_mass, lj1, lj2, lkspace, rcutsq,
+               skin, nmaxlist, dt, reacf=0.0, alfa=0.0, enstype=0, temper_0=0.0, tau_t=100.0,
+               integrator=MD_LEAPFROG, bonds=None, bnd1=None, bnd2=None, angles=None,
+               ang1=None, ang2=None) -> SystemDesc:
+    """An md_system_desc over numpy copies of the arrays (kept alive in `keep`)."""
+
+    def f32(a):
+        a = np.ascontiguousarray(a, np.float32)
+        keep.append(a)
+        return _ptr(a, C.c_float)
+
+    def i32(a):
+        a = np.ascontiguousarray(a, np.int32)
+        keep.append(a)
+        return _ptr(a, C.c_int)
+
+    n = int(np.asarray(itype).shape[0])
+    ntype = int(np.asarray(type_mass).shape[0])
+    d = SystemDesc()
+    d.natom, d.ntype = n, ntype
+    for k in range(3):
+        d.box[k] = float(box[k])
+    d.itype, d.charge = i32(itype), f32(charge)
+    d.pos = f32(np.asarray(pos).reshape(-1))
+    d.vel = f32(np.asarray(vel).reshape(-1)) if vel is not None else None
+    d.type_mass = f32(type_mass)
+    d.lj1, d.lj2 = f32(np.asarray(lj1).reshape(-1)), f32(np.asarray(lj2).reshape(-1))
+    pad8 = lambda a: np.pad(np.asarray(a, np.float32), (0, 8 - len(a)))
+    if bonds is not None and len(bonds):
+        d.nbonds = len(bonds)
+        d.bonds = i32(np.asarray(bonds).reshape(-1))
+        d.bnd1, d.bnd2 = f32(pad8(bnd1)), f32(pad8(bnd2))
+    if angles is not None and len(angles):
+        d.nangle = len(angles)
+        d.angles = i32(np.asarray(angles).reshape(-1))
+        d.ang1, d.ang2 = f32(pad8(ang1)), f32(pad8(ang2))
+    d.lkspace, d.rcutsq, d.reacf, d.alfa = lkspace, rcutsq, reacf, alfa
+    d.skin, d.nmaxlist, d.enstype, d.temper_0 = skin, nmaxlist, enstype, temper_0
+    d.dt, d.tau_t, d.integrator = dt, tau_t, integrator
+    return d
+
+
 _lib = None
 
 
@@ -103,6 +145,8 @@ def library(path: Optional[str] = None):
     L.md_set_type_exclusions.argtypes = [vp, vp]
     L.md_set_graphs.argtypes = [vp, C.c_int]
     L.md_ref_kinetic_energy_noalloc.argtypes = [vp, C.c_int, vp, vp]
+    L.md_create_batch.argtypes = [C.POINTER(SystemDesc), C.c_int, vp, C.POINTER(vp)]
+    L.md_get_replica_thermo.argtypes = [vp, C.POINTER(Thermo), C.c_int]
     _lib = L
     return L
 
@@ -154,45 +198,47 @@ class MDSystem:
         """Arrays in the reference's in-memory conventions: itype 0-based,
         masses g/mol*1e4 per type, lj tables ntype x ntype, bonds (type,i,j)
         and angles (type,i,j,k) 0-based, bnd1/ang1 = 2k, ang2 in rad."""
-        L = library()
         keep = []
-
-        def f32(a):
-            a = np.ascontiguousarray(a, np.float32)
-            keep.append(a)
-            return _ptr(a, C.c_float)
-
-        def i32(a):
-            a = np.ascontiguousarray(a, np.int32)
-            keep.append(a)
-            return _ptr(a, C.c_int)
-
-        n = int(np.asarray(itype).shape[0])
-        ntype = int(np.asarray(type_mass).shape[0])
-        d = SystemDesc()
-        d.natom, d.ntype = n, ntype
-        for k in range(3):
-            d.box[k] = float(box[k])
-        d.itype, d.charge = i32(itype), f32(charge)
-        d.pos = f32(np.asarray(pos).reshape(-1))
-        d.vel = f32(np.asarray(vel).reshape(-1)) if vel is not None else None
-        d.type_mass = f32(type_mass)
-        d.lj1, d.lj2 = f32(np.asarray(lj1).reshape(-1)), f32(np.asarray(lj2).reshape(-1))
-        pad8 = lambda a: np.pad(np.asarray(a, np.float32), (0, 8 - len(a)))
-        if bonds is not None and len(bonds):
-            d.nbonds = len(bonds)
-            d.bonds = i32(np.asarray(bonds).reshape(-1))
-            d.bnd1, d.bnd2 = f32(pad8(bnd1)), f32(pad8(bnd2))
-        if angles is not None and len(angles):
-            d.nangle = len(angles)
-            d.angles = i32(np.asarray(angles).reshape(-1))
-            d.ang1, d.ang2 = f32(pad8(ang1)), f32(pad8(ang2))
-        d.lkspace, d.rcutsq, d.reacf, d.alfa = lkspace, rcutsq, reacf, alfa
-        d.skin, d.nmaxlist, d.enstype, d.temper_0 = skin, nmaxlist, enstype, temper_0
-        d.dt, d.tau_t, d.integrator = dt, tau_t, integrator
+        d = _make_desc(keep, box=box, itype=itype, charge=charge, pos=pos, vel=vel,
+                       type_mass=type_mass, lj1=lj1, lj2=lj2, lkspace=lkspace, rcutsq=rcutsq,
+                       skin=skin, nmaxlist=nmaxlist, dt=dt, reacf=reacf, alfa=alfa,
+                       enstype=enstype, temper_0=temper_0, tau_t=tau_t, integrator=integrator,
+                       bonds=bonds, bnd1=bnd1, bnd2=bnd2, angles=angles, ang1=ang1, ang2=ang2)
         ctx = C.c_void_p()
-        _check(L.md_create(C.byref(d), stream, C.byref(ctx)))
-        return cls(ctx, n)
+        _check(library().md_create(C.byref(d), stream, C.byref(ctx)))
+        return cls(ctx, d.natom)
+
+    @classmethod
+    def from_batch(cls, replicas, stream=None) -> "MDSystem":
+        """A batch of independent replicas (md_create_batch): `replicas` is a
+        list of from_arrays keyword dicts.  Positions, velocities, forces and
+        energies of the result hold the replicas' atoms concatenated in
+        order (see replica_slices); thermo() gives batch totals and
+        replica_thermo() the per-replica values."""
+        keep = []
+        descs = (SystemDesc * len(replicas))()
+        sizes = []
+        for k, kw in enumerate(replicas):
+            descs[k] = _make_desc(keep, **kw)
+            sizes.append(descs[k].natom)
+        ctx = C.c_void_p()
+        _check(library().md_create_batch(descs, len(replicas), stream, C.byref(ctx)))
+        sim = cls(ctx, int(sum(sizes)))
+        sim.replica_sizes = sizes
+        return sim
+
+    def replica_slices(self):
+        """Atom ranges of the replicas in the concatenated host arrays."""
+        sizes = getattr(self, "replica_sizes", [self.natom])
+        off = np.concatenate([[0], np.cumsum(sizes)])
+        return [slice(int(off[k]), int(off[k + 1])) for k in range(len(sizes))]
+
+    def replica_thermo(self):
+        """Per-replica thermodynamic state after the last step."""
+        n = len(getattr(self, "replica_sizes", [self.natom]))
+        buf = (Thermo * n)()
+        _check(library().md_get_replica_thermo(self._ctx, buf, n), self._ctx)
+        return [buf[i].as_dict() for i in range(n)]
 
     def close(self):
         if self._ctx:

@@ -86,9 +86,8 @@ def rows_canonical(nn, nm, n, width):
     return out
 
 
-def system_from_case(case, integrator=None, nmaxlist=None, tau_t=100.0, stream=None):
-    """The same inputs the oracle sees, uploaded through the C ABI."""
-    from md_gpu_gb300 import MDSystem
+def case_arrays(case, integrator=None, nmaxlist=None, tau_t=100.0):
+    """MDSystem.from_arrays keyword arguments for the inputs the oracle sees."""
     p = case.params
     nt = case.fld.ntype
     bonds = case.bonds.copy()
@@ -101,15 +100,20 @@ def system_from_case(case, integrator=None, nmaxlist=None, tau_t=100.0, stream=N
     lj1 = np.ctypeslib.as_array(case.fld.lj1)[:nt * nt].astype(np.float32)
     lj2 = np.ctypeslib.as_array(case.fld.lj2)[:nt * nt].astype(np.float32)
     arr = lambda k: np.ctypeslib.as_array(getattr(case.fld, k)).astype(np.float32)
-    return MDSystem.from_arrays(
+    return dict(
         box=case.box, itype=case.itype, charge=case.q, pos=case.pos, vel=case.vel, type_mass=tm,
         lj1=lj1, lj2=lj2, lkspace=p.lkspace, rcutsq=p.rcutsq, reacf=p.reacf, alfa=p.alfa,
         skin=p.skin, nmaxlist=nmaxlist or p.nmaxlist, dt=p.dt, enstype=p.enstype,
         temper_0=p.temper_0, tau_t=tau_t,
         integrator=p.integrator if integrator is None else integrator,
         bonds=bonds if len(bonds) else None, bnd1=arr("bnd1"), bnd2=arr("bnd2"),
-        angles=angles if len(angles) else None, ang1=arr("ang1"), ang2=arr("ang2"),
-        stream=stream)
+        angles=angles if len(angles) else None, ang1=arr("ang1"), ang2=arr("ang2"))
+
+
+def system_from_case(case, integrator=None, nmaxlist=None, tau_t=100.0, stream=None):
+    """The same inputs the oracle sees, uploaded through the C ABI."""
+    from md_gpu_gb300 import MDSystem
+    return MDSystem.from_arrays(stream=stream, **case_arrays(case, integrator, nmaxlist, tau_t))
 
 
 def oracle_state(case):

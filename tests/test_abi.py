@@ -87,3 +87,41 @@ def test_too_many_bonds(lib):
         with pytest.raises(MDError) as e:
             MDSystem.from_files(base)
         assert e.value.status == 6
+
+
+def test_batch_rejects_bad_replicas(lib):
+    """md_create_batch validates every replica on the host: bonded terms are
+    not batched (7), replicas must share dt / integrator (1), and each
+    replica's cutoff + skin must fit half its box (8)."""
+    import numpy as np
+    a = synth.to_arrays(synth.nacl_replica(600, seed=1))
+    b = synth.to_arrays(synth.nacl_replica(800, seed=2))
+    bad_dt = dict(b, dt=1.0)
+    with pytest.raises(MDError) as e:
+        MDSystem.from_batch([a, bad_dt])
+    assert e.value.status == 1
+    small = dict(b, box=np.full(3, 20.0, np.float32))
+    with pytest.raises(MDError) as e:
+        MDSystem.from_batch([a, small])
+    assert e.value.status == 8
+    bonded = dict(b, bonds=np.array([[0, 0, 1]]), bnd1=[100.0], bnd2=[2.8])
+    with pytest.raises(MDError) as e:
+        MDSystem.from_batch([a, bonded])
+    assert e.value.status == 7
+
+
+def test_replica_batch_generator():
+    """Uneven replica sizes in range, even, neutral; the cutoff is clamped so
+    cutoff + skin fits half of every box."""
+    import numpy as np
+    reps = synth.replica_batch(24, seed=5)
+    sizes = [r.natom for r in reps]
+    assert min(sizes) >= 256 and max(sizes) <= 8192 and all(n % 2 == 0 for n in sizes)
+    assert len(set(sizes)) > 12
+    for r in reps:
+        rc = r.inp["cutoff"][0]
+        assert 2 * (rc + r.inp["skin"][0]) < r.box[0]
+        assert abs(r.charge.sum()) < 1e-9
+        assert np.all(np.abs(r.pos) <= 0.5 * r.box[0])
+    small = synth.nacl_replica(256, seed=1)
+    assert small.inp["cutoff"][0] < 12.0
