@@ -56,31 +56,58 @@ __global__ void k_check_b(int n, const md_rep *__restrict__ reps, const int *__r
 }
 
 /* Cell keys of a batch: the replica's cell grid, ranks offset by its first
- * cell, so every replica's cells (and atoms) stay one contiguous range.  A
- * replica that is not being rebuilt keeps the keys of its last build, so
- * its atoms keep their order (and their list rows stay valid). */
+ * cell, so every replica's cells (and atoms) stay one contiguous range.
+ * Only replicas with a rebuild request are re-binned; every other replica
+ * keeps its order, cell ranges and list rows untouched by all build passes. */
 __global__ void k_cell_key_b(int n, const md_rep *__restrict__ reps, const int *__restrict__ arep,
                              const md_devstate *st, int always, const int *__restrict__ rep_upd,
-                             const int *__restrict__ skey, const float4 *__restrict__ pos4,
-                             const int *__restrict__ cell_rank, int *key, int *cell_count)
+                             const float4 *__restrict__ pos4, const int *__restrict__ cell_rank,
+                             int *key, int *cell_count)
 {
     if (!always && !st->update) return;
     int i = blockIdx.x * blockDim.x + threadIdx.x;
     if (i >= n) return;
     const int rep = arep[i];
-    int r;
-    if (rep_upd[rep]) {
-        const md_rep &R = reps[rep];
-        float4 p = pos4[i];
-        int cx = cell_of(p.x, R.box[0], R.binlen[0], R.ncell[0]);
-        int cy = cell_of(p.y, R.box[1], R.binlen[1], R.ncell[1]);
-        int cz = cell_of(p.z, R.box[2], R.binlen[2], R.ncell[2]);
-        r = cell_rank[R.cell0 + cx + R.ncell[0] * (cy + R.ncell[1] * cz)];
-    } else {
-        r = skey[i];
-    }
+    if (!rep_upd[rep]) return;
+    const md_rep &R = reps[rep];
+    float4 p = pos4[i];
+    int cx = cell_of(p.x, R.box[0], R.binlen[0], R.ncell[0]);
+    int cy = cell_of(p.y, R.box[1], R.binlen[1], R.ncell[1]);
+    int cz = cell_of(p.z, R.box[2], R.binlen[2], R.ncell[2]);
+    int r = cell_rank[R.cell0 + cx + R.ncell[0] * (cy + R.ncell[1] * cz)];
     key[i] = r;
     atomicAdd(&cell_count[r], 1);
+}
+
+/* Per-replica exclusive scan of the cell counts, one warp per replica being
+ * rebuilt: its cells start at its first atom.  Counters are zeroed for the
+ * next build. */
+__global__ void k_cell_scan_b(const md_devstate *st, int always, int nrep,
+                              const md_rep *__restrict__ reps, const int *__restrict__ rep_upd,
+                              int *cell_count, int *cell_start, int *cell_fill)
+{
+    if (!always && !st->update) return;
+    const int r = (blockIdx.x * blockDim.x + threadIdx.x) >> 5, lane = threadIdx.x & 31;
+    if (r >= nrep || !rep_upd[r]) return;
+    const md_rep &R = reps[r];
+    int run = R.atom0;
+    for (int k0 = 0; k0 < R.ncells; k0 += 32) {
+        const int k = k0 + lane;
+        const int c = R.cell0 + k;
+        int cnt = k < R.ncells ? cell_count[c] : 0;
+        int incl = cnt;
+        for (int o = 1; o < 32; o <<= 1) {
+            int v = __shfl_up_sync(0xffffffffu, incl, o);
+            if (lane >= o) incl += v;
+        }
+        if (k < R.ncells) {
+            cell_start[c] = run + incl - cnt;
+            cell_count[c] = 0;
+            cell_fill[c] = 0;
+        }
+        run += __shfl_sync(0xffffffffu, incl, 31);
+    }
+    if (lane == 0) cell_start[R.cell0 + R.ncells] = run;   /* = the next replica's first atom */
 }
 
 /* Rebuild every replica of a batch (forced builds). */
@@ -90,12 +117,16 @@ __global__ void k_flag_all(int *rep_upd, int nrep)
     if (r < nrep) rep_upd[r] = 1;
 }
 
-/* Ends a rebuild of a batch: counts the rebuilt replicas' builds and clears
- * the requests. */
-__global__ void k_clear_update_b(md_devstate *st, int *rep_upd, md_repstate *repst, int nrep)
+/* Ends a rebuild of a batch: counts the build and the rebuilt replicas'
+ * builds and clears the requests. */
+__global__ void k_clear_update_b(md_devstate *st, int always, int *rep_upd, md_repstate *repst,
+                                 int nrep)
 {
     int r = blockIdx.x * blockDim.x + threadIdx.x;
-    if (r == 0) st->update = 0;
+    if (r == 0) {
+        if (always || st->update) st->builds += 1;
+        st->update = 0;
+    }
     if (r < nrep && rep_upd[r]) {
         repst[r].builds += 1;
         rep_upd[r] = 0;
@@ -133,13 +164,17 @@ __global__ void k_cell_scan(md_kparams kp, md_devstate *st, int always, int ncel
     if (t == 0) st->builds += 1;
 }
 
+/* In a batch (arep, rep_upd non-null) the passes below touch only the atoms
+ * and cells of replicas being rebuilt. */
 __global__ void k_cell_scatter(md_kparams kp, const md_devstate *st, int always,
                                const int *__restrict__ key, const int *__restrict__ cell_start,
-                               int *cell_fill, int *src)
+                               int *cell_fill, int *src, const int *__restrict__ arep,
+                               const int *__restrict__ rep_upd)
 {
     if (!always && !st->update) return;
     int i = blockIdx.x * blockDim.x + threadIdx.x;
     if (i >= kp.n) return;
+    if (arep && !rep_upd[arep[i]]) return;
     int r = key[i];
     src[cell_start[r] + atomicAdd(&cell_fill[r], 1)] = i;
 }
@@ -148,11 +183,12 @@ __global__ void k_cell_scatter(md_kparams kp, const md_devstate *st, int always,
  * function of the positions alone. */
 __global__ void k_cell_order(md_kparams kp, const md_devstate *st, int always, int ncells,
                              const int *__restrict__ cell_start, const int *__restrict__ perm,
-                             int *src)
+                             int *src, const int *__restrict__ crep, const int *__restrict__ rep_upd)
 {
     if (!always && !st->update) return;
     int c = blockIdx.x * blockDim.x + threadIdx.x;
     if (c >= ncells) return;
+    if (crep && !rep_upd[crep[c]]) return;
     int b = cell_start[c], e = cell_start[c + 1];
     for (int k = b + 1; k < e; k++) {
         int a = src[k], ka = perm[a];
@@ -170,12 +206,13 @@ __global__ void k_permute(md_kparams kp, const md_devstate *st, int always,
                           const double *__restrict__ v, const double *__restrict__ mass,
                           const double *__restrict__ minv,
                           const float4 *__restrict__ pos4, const int *__restrict__ perm,
-                          const int *__restrict__ type, const int *__restrict__ key,
-                          double *tmp_d, float4 *tmp4, int *tmp_i)
+                          const int *__restrict__ type, double *tmp_d, float4 *tmp4, int *tmp_i,
+                          const int *__restrict__ arep, const int *__restrict__ rep_upd)
 {
     if (!always && !st->update) return;
     int s = blockIdx.x * blockDim.x + threadIdx.x;
     if (s >= kp.n) return;
+    if (arep && !rep_upd[arep[s]]) return;   /* atoms stay inside their replica's range */
     int o = src[s], P = kp.pitch;
     for (int d = 0; d < 3; d++) {
         tmp_d[d * P + s] = x[d * P + o];
@@ -186,18 +223,18 @@ __global__ void k_permute(md_kparams kp, const md_devstate *st, int always,
     tmp4[s] = pos4[o];
     tmp_i[s] = perm[o];
     tmp_i[P + s] = type[o];
-    if (key) tmp_i[2 * P + s] = key[o];
 }
 
 __global__ void k_copyback(md_kparams kp, const md_devstate *st, int always,
                            const double *__restrict__ tmp_d, const float4 *__restrict__ tmp4,
                            const int *__restrict__ tmp_i, double *x, double *v, double *mass,
                            double *minv, float4 *pos4, int *perm, int *iperm, int *type,
-                           int *skey)
+                           const int *__restrict__ arep, const int *__restrict__ rep_upd)
 {
     if (!always && !st->update) return;
     int s = blockIdx.x * blockDim.x + threadIdx.x;
     if (s >= kp.n) return;
+    if (arep && !rep_upd[arep[s]]) return;
     int P = kp.pitch;
     for (int d = 0; d < 3; d++) {
         x[d * P + s] = tmp_d[d * P + s];
@@ -210,7 +247,6 @@ __global__ void k_copyback(md_kparams kp, const md_devstate *st, int always,
     perm[s] = o;
     iperm[o] = s;
     type[s] = tmp_i[P + s];
-    if (skey) skey[s] = tmp_i[2 * P + s];
 }
 
 /* Exclusions and bonded lists re-expressed in the new sorted indices. */
@@ -540,23 +576,30 @@ void launch_rebuild(md_ctx *c, const md_kparams &kp, bool unconditional, bool al
     cudaStream_t s = c->stream;
     const bool batch = c->nrep > 1;
     const int rb = (c->nrep + 255) / 256;
-    if (batch && all_replicas) k_flag_all<<<rb, 256, 0, s>>>(c->rep_upd, c->nrep);
-    if (batch)
+    const int *arep = batch ? c->arep : nullptr;
+    const int *crep = batch ? c->crep : nullptr;
+    if (batch) {
+        if (all_replicas) k_flag_all<<<rb, 256, 0, s>>>(c->rep_upd, c->nrep);
         k_cell_key_b<<<nb, 256, 0, s>>>(kp.n, c->reps_dev, c->arep, c->st, always, c->rep_upd,
-                                        c->skey, c->pos4, c->cell_rank, c->key, c->cell_count);
-    else
+                                        c->pos4, c->cell_rank, c->key, c->cell_count);
+        k_cell_scan_b<<<(c->nrep + 7) / 8, 256, 0, s>>>(c->st, always, c->nrep, c->reps_dev,
+                                                        c->rep_upd, c->cell_count, c->cell_start,
+                                                        c->cell_fill);
+    } else {
         k_cell_key<<<nb, 256, 0, s>>>(kp, c->st, always, c->pos4, c->cell_rank, c->key, c->cell_count);
-    k_cell_scan<<<1, 1024, 0, s>>>(kp, c->st, always, c->ncells, c->cell_count, c->cell_start,
-                                   c->cell_fill);
-    k_cell_scatter<<<nb, 256, 0, s>>>(kp, c->st, always, c->key, c->cell_start, c->cell_fill, c->src);
+        k_cell_scan<<<1, 1024, 0, s>>>(kp, c->st, always, c->ncells, c->cell_count, c->cell_start,
+                                       c->cell_fill);
+    }
+    k_cell_scatter<<<nb, 256, 0, s>>>(kp, c->st, always, c->key, c->cell_start, c->cell_fill, c->src,
+                                      arep, c->rep_upd);
     k_cell_order<<<(c->ncells + 255) / 256, 256, 0, s>>>(kp, c->st, always, c->ncells,
-                                                          c->cell_start, c->perm, c->src);
+                                                          c->cell_start, c->perm, c->src, crep,
+                                                          c->rep_upd);
     k_permute<<<nb, 256, 0, s>>>(kp, c->st, always, c->src, c->x, c->v, c->mass, c->minv, c->pos4,
-                                 c->perm, c->type, batch ? c->key : nullptr, c->tmp_d, c->tmp4,
-                                 c->tmp_i);
+                                 c->perm, c->type, c->tmp_d, c->tmp4, c->tmp_i, arep, c->rep_upd);
     k_copyback<<<nb, 256, 0, s>>>(kp, c->st, always, c->tmp_d, c->tmp4, c->tmp_i, c->x, c->v,
-                                  c->mass, c->minv, c->pos4, c->perm, c->iperm, c->type,
-                                  batch ? c->skey : nullptr);
+                                  c->mass, c->minv, c->pos4, c->perm, c->iperm, c->type, arep,
+                                  c->rep_upd);
     /* a batch has no exclusions or bonded lists to re-express */
     if (!batch)
         k_remap<<<nb, 256, 0, s>>>(kp, c->st, always, c->perm, c->iperm, c->excl_orig, c->excl_s,
@@ -568,7 +611,7 @@ void launch_rebuild(md_ctx *c, const md_kparams &kp, bool unconditional, bool al
             kp, c->st, always, c->ncells, c->pos4, c->type, c->excl_s, c->cell_rank, c->cell_lin,
             c->cell_start, c->type_mask_dev, c->nl, c->nl_n, c->pos_old, c->reps_dev, c->crep,
             c->rep_upd);
-        k_clear_update_b<<<rb, 256, 0, s>>>(c->st, c->rep_upd, c->repst, c->nrep);
+        k_clear_update_b<<<rb, 256, 0, s>>>(c->st, always, c->rep_upd, c->repst, c->nrep);
         return;
     }
     int ltpa = c->list_tpa;

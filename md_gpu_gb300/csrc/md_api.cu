@@ -251,7 +251,7 @@ void free_device(md_ctx *c)
                     c->tmp_i, c->bl_o, c->bl_on, c->al_o, c->al_on, c->bl_s, c->bl_sn, c->al_s,
                     c->al_sn, c->partials, c->st, c->rec, c->lj_dev, c->bonded_par,
                     c->type_mask_dev, c->io_dev, c->reps_dev, c->repst, c->arep, c->crep,
-                    c->ljr_dev, c->grid_tab, c->rep_upd, c->skey};
+                    c->ljr_dev, c->grid_tab, c->rep_upd};
     for (void *p : ptrs)
         if (p) cudaFree(p);
 }
@@ -564,7 +564,7 @@ md_status setup_device(md_ctx *c, void *stream, host_stage &h, md_ctx **out)
     if (batch) {
         MD_ALLOC(c->reps_dev, c->nrep); MD_ALLOC(c->repst, c->nrep);
         MD_ALLOC(c->arep, P); MD_ALLOC(c->crep, c->ncells);
-        MD_ALLOC(c->rep_upd, c->nrep); MD_ALLOC(c->skey, P);
+        MD_ALLOC(c->rep_upd, c->nrep);
         MD_ALLOC(c->ljr_dev, (size_t)MD_MAXTYPE * MD_MAXTYPE * c->nrep);
         MD_ALLOC(c->grid_tab, h.grid.size());
     }
@@ -628,7 +628,6 @@ md_status setup_device(md_ctx *c, void *stream, host_stage &h, md_ctx **out)
         up(c->ljr_dev, h.ljr.data(), sizeof(float2) * h.ljr.size());
         up(c->grid_tab, h.grid.data(), sizeof(int2) * h.grid.size());
         if (e == cudaSuccess) e = cudaMemset(c->rep_upd, 0, sizeof(int) * c->nrep);
-        if (e == cudaSuccess) e = cudaMemset(c->skey, 0, sizeof(int) * P);
     }
     if (e == cudaSuccess) e = cudaMemset(c->f, 0, sizeof(long long) * 3 * P);
     if (e == cudaSuccess) e = cudaMemset(c->vir, 0, sizeof(float) * P);

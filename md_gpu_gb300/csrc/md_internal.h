@@ -196,7 +196,6 @@ struct md_ctx {
     md_repstate *repst = nullptr;
     int *arep = nullptr;          /* atom -> replica (the same in both orders) */
     int *rep_upd = nullptr;       /* per replica: an atom moved >= skin/2 since its last build */
-    int *skey = nullptr;          /* cell rank of every sorted atom at the last build */
     int *crep = nullptr;          /* cell rank -> replica */
     float2 *ljr_dev = nullptr;    /* nrep x 64 (lj1, lj2) */
     int2 *grid_tab = nullptr;     /* the MD_NGRID replica-aligned grids, concatenated */
