@@ -4,8 +4,14 @@ rc 12 A, skin 1 A, Berendsen leapfrog NVT at 1200 K, dt 2 fs) on one GB300.
 
 One bench "step" is one segment of --md-steps MD steps (list check and
 rebuilds at their natural rate, forces, integration) run through md_step as
-captured CUDA graphs.  L2 is flushed (512 MB write) before every timed segment;
-inside a segment the ~80 MB working set stays resident, as in any MD run.
+captured CUDA graphs (32 steps per graph).  L2 is flushed (512 MB write)
+before every timed segment; inside a segment the ~80 MB working set stays
+resident, as in any MD run.
+
+The same line carries, under "batched_replicas", the batch workload: 512
+NaCl-like replicas of 256..8192 ions (own eps/sigma per type and charge scale
+within +-10%), velocity Verlet NVE at dt 2 fs, advanced together by
+md_create_batch (one launch per stage, one graph for the batch).
 
     python bench.py [--gpus N] [--steps K] [--warmup W] [--impl ours|reference]
 
@@ -142,6 +148,49 @@ def run_reference(args):
     print(json.dumps(line), flush=True)
 
 
+def batch_leg(args, flush):
+    """Throughput of the 512-replica batch (atom-steps/s over all replicas)."""
+    import torch
+
+    from md_gpu_gb300 import MDSystem, synth
+    from md_gpu_gb300.replicas import equilibrate_batch
+    reps = synth.replica_batch(args.nrep, seed=1)
+    arrs = equilibrate_batch([synth.to_arrays(r) for r in reps])
+    sizes = [r.natom for r in reps]
+    with MDSystem.from_batch(arrs) as b:
+        pt, _ = b.autotune()
+        b.step(args.md_steps)
+        builds0 = b.info()["builds"]
+        rb0 = [t["builds"] for t in b.replica_thermo()]
+        ms = []
+        for _ in range(args.batch_segments):
+            flush.zero_()
+            torch.cuda.synchronize()
+            b.step(args.md_steps)
+            ms.append(b.last_step_ms())
+        info = b.info()
+        th = b.replica_thermo()
+        pair_ms = b.time_pair(20)
+    steps = args.md_steps * len(ms)
+    rebuilt = sum(t["builds"] for t in th) - sum(rb0)
+    return {
+        "workload": (f"{args.nrep} NaCl-like replicas, N uniform in [256, 8192] (seed 1), 1.5 g/cm^3, "
+                     "eps/sigma per type and charge scale uniform within +-10% of the molten-NaCl "
+                     "values, Wolf alpha 0.2/A, rc 12 A (clamped to L/2 - skin for the smallest boxes), "
+                     "skin 1 A, velocity Verlet NVE dt 2 fs, melted first by Berendsen leapfrog "
+                     "(400 steps dt 0.5 fs tau 10 fs, 200 steps dt 2 fs tau 100 fs) at 1200 K"),
+        "value": sum(sizes) * steps / (sum(ms) * 1e-3), "unit": UNIT,
+        "natom": int(sum(sizes)), "nrep": len(sizes), "min_natom": int(min(sizes)),
+        "max_natom": int(max(sizes)), "md_steps": steps, "ms_per_md_step": sum(ms) / steps,
+        "pair_ms": pair_ms, "pair_threads_per_atom": pt,
+        "batch_rebuild_events": info["builds"] - builds0,
+        "replica_rebuilds_per_replica_step": rebuilt / (len(sizes) * steps),
+        "temperature_K": {"min": min(t["temper"] for t in th), "mean": float(np.mean([t["temper"] for t in th])),
+                          "max": max(t["temper"] for t in th)},
+        "l2": "flushed (512 MB write) before every timed segment",
+    }
+
+
 def run_ours(args):
     import torch
     rank, world, local = rank_info()
@@ -166,6 +215,8 @@ def run_ours(args):
     n = sim.natom
     flush = torch.empty(512 * 1024 * 1024, dtype=torch.uint8, device="cuda")
     tuned = sim.autotune() if not args.no_autotune else None
+    if args.eager:
+        sim.set_graphs(False)
 
     for _ in range(args.warmup):
         sim.step(args.md_steps)
@@ -231,12 +282,16 @@ def run_ours(args):
                "h2d_bytes_per_step": 2 * 3 * n * 8,
                "d2h_bytes_per_step": 2 * 3 * n * 8 + args.md_steps * 72,
                "call": "md_run_host (upload pos/vel, list build, md_steps steps, download records + pos/vel)"}
+        if args.nrep > 0:
+            extra_batch = batch_leg(args, flush)
         cpu_v, cpu_dt, cores = cpu_reference_sample(base, 1, 0, args.ref_md_steps)
         extra = {"roofline": roof, "e2e": e2e, "force_rms_rel_err_vs_fp64": err,
                  "cpu_baseline": {"value": cpu_v, "unit": UNIT, "cores": cores, "kind": "port",
                                   "sample": f"{args.ref_md_steps} MD steps of the same system (one O(N^2) "
                                             "list build, then rebuilds on the skin/2 criterion), oracle "
                                             "FP32 restatement, OpenMP"}}
+        if args.nrep > 0:
+            extra["batched_replicas"] = extra_batch
     line = {"metric": METRIC, "value": value, "unit": UNIT, "n_gpus": world, "steps": args.steps,
             "warmup": args.warmup, "ms_per_step": total_ms / args.steps, "higher_is_better": True,
             "scaling": "weak", "vs_baseline": None, "dtype": "f32",
@@ -249,8 +304,11 @@ def run_ours(args):
                        "pair_threads_per_atom": info["pair_tpa"],
                        "list_builder": "warp per cell" if info["list_tpa"] == 0
                        else f"{info['list_tpa']} threads per atom",
-                       "autotuned": tuned is not None},
-            "gpu_launches": info["kernels_per_step"] * args.md_steps * args.steps,
+                       "autotuned": tuned is not None,
+                       "launch": "eager (profiling)" if args.eager else "CUDA graphs, 32 steps each"},
+            "gpu_launches": (args.steps * (args.md_steps // 32 * info["kernels_per_graph"] +
+                                           args.md_steps * info["kernels_per_step"]) +
+                             builds * info["kernels_per_rebuild"]),
             "clocks": clocks}
     line.update(extra)
     if rank == 0:
@@ -266,13 +324,18 @@ def main():
     ap.add_argument("--steps", type=int, default=20)
     ap.add_argument("--warmup", type=int, default=3)
     ap.add_argument("--impl", choices=["ours", "reference"], default="ours")
-    ap.add_argument("--md-steps", type=int, default=100)
+    ap.add_argument("--md-steps", type=int, default=128, help="MD steps per bench step (multiple of 32)")
+    ap.add_argument("--nrep", type=int, default=512, help="replicas of the batch leg (0: skip it)")
+    ap.add_argument("--batch-segments", type=int, default=4)
     ap.add_argument("--ref-md-steps", type=int, default=10)
     ap.add_argument("--ncell", type=int, default=20)
     ap.add_argument("--no-autotune", action="store_true")
+    ap.add_argument("--eager", action="store_true",
+                    help="launch every step's kernels eagerly instead of replaying graphs (for profilers)")
     args = ap.parse_args()
     if args.warmup < 3 and args.impl == "ours":
         args.warmup = 3
+    args.md_steps = max(32, (args.md_steps + 31) // 32 * 32)
     if args.impl == "reference":
         run_reference(args)
     else:

@@ -174,7 +174,9 @@ typedef struct {
     int pair_threads_per_atom, list_threads_per_atom;
     int builds;
     int max_neighbors;
-    int kernels_per_step;   /* kernel launches of one md_step step */
+    int kernels_per_step;   /* kernel launches of one md_step step without a rebuild */
+    int kernels_per_rebuild; /* kernels a list rebuild adds to a step */
+    int kernels_per_graph;  /* kernels a step graph runs besides its steps (condition set-up) */
 } md_info;
 md_status md_get_info(md_ctx *ctx, md_info *out);
 /* Sorted -> original index map of the current atom order. */

@@ -72,43 +72,38 @@ __global__ void __launch_bounds__(128) k_pair_b(int cap, int pitch, const int2 *
 }
 
 /* Per-replica FP64 totals from the block partials (each replica's blocks
- * are one contiguous range of the 256-atom grid), one warp per replica in a
- * fixed order, then each replica's thermostat bookkeeping and the batch's
- * step record (sums over replicas).  Runs in the last block to finish. */
+ * are one contiguous range of the MD_LA-atom grid), one thread per replica
+ * summing its blocks in order, then each replica's thermostat bookkeeping
+ * and the batch's step record (sums over replicas, fixed order).  Runs in
+ * the last block to finish. */
 __device__ void finalize_b(const md_kparams &kp, const thermo_par &tp, int mode, int nrep,
                            const md_rep *__restrict__ reps, md_repstate *repst,
                            const double *partials, int npart, md_devstate *st, md_thermo *rec,
                            int rec_cap, double *sh)
 {
-    const int w = threadIdx.x >> 5, lane = threadIdx.x & 31, nw = blockDim.x >> 5;
     double tke = 0.0, tpe = 0.0, tw = 0.0, tex = 0.0;
-    for (int r = w; r < nrep; r += nw) {
+    for (int r = threadIdx.x; r < nrep; r += blockDim.x) {
         const md_rep &R = reps[r];
         double a = 0.0, b = 0.0, c = 0.0;
-        for (int k = lane; k < R.nblk; k += 32) {
+        for (int k = 0; k < R.nblk; k++) {
             a += __ldcg(partials + R.blk0 + k);
             if (tp.energy) {
                 b += __ldcg(partials + npart + R.blk0 + k);
                 c += __ldcg(partials + 2 * npart + R.blk0 + k);
             }
         }
-        for (int o = 16; o > 0; o >>= 1) {
-            a += __shfl_down_sync(0xffffffffu, a, o);
-            b += __shfl_down_sync(0xffffffffu, b, o);
-            c += __shfl_down_sync(0xffffffffu, c, o);
-        }
-        if (lane == 0) {
-            thermo_par t = tp;
-            t.t0 = R.t0;
-            t.ndf = R.ndf;
-            t.q_nh = R.q_nh;
-            double xi, eta, lam;
-            double ke = thermo_advance(kp.dt, t, mode, a, b, c, repst + r, &xi, &eta, &lam);
-            tke += ke;
-            tpe += b;
-            tw += c;
-            if (t.nh) tex += 0.5 * t.q_nh * xi * xi + t.ndf * RGAS * t.t0 * eta;
-        }
+        thermo_par t = tp;
+        t.t0 = R.t0;
+        t.ndf = R.ndf;
+        t.q_nh = R.q_nh;
+        t.inv_ndfr = R.inv_ndfr;
+        t.inv_q = R.inv_q;
+        double xi, eta, lam;
+        double ke = thermo_advance(kp.dt, t, mode, a, b, c, repst + r, &xi, &eta, &lam);
+        tke += ke;
+        tpe += b;
+        tw += c;
+        if (t.nh) tex += 0.5 * t.q_nh * xi * xi + t.ndf * RGAS * t.t0 * eta;
     }
     const double KE = block_sum(tke, sh);
     const double PE = block_sum(tpe, sh);
@@ -121,52 +116,55 @@ __device__ void finalize_b(const md_kparams &kp, const thermo_par &tp, int mode,
         st->virial = W / 6.0;
     }
     if (mode == 2) return;
-    st->temper = 2.0 * KE / (tp.ndf * RGAS);
-    write_record(tp, tp.ndf, KE, PE, W, EX, 0.0, 1.0, st, rec, rec_cap);
+    st->temper = 2.0 * KE * tp.inv_ndfr;
+    write_record(tp, tp.inv_ndfr, KE, PE, W, EX, 0.0, 1.0, st, rec, rec_cap);
 }
 
-/* Leapfrog of a batch (k_leapfrog per replica): Berendsen scale, box and
- * skin of the block's replica. */
-__global__ void __launch_bounds__(256) k_leapfrog_b(md_kparams kp, thermo_par tp, step_io io,
-                                                    int nrep, const int2 *__restrict__ tab,
-                                                    const md_rep *__restrict__ reps,
-                                                    md_repstate *repst, int *rep_upd, double *x,
-                                                    double *v, const double *__restrict__ mass,
-                                                    const double *__restrict__ minv, float4 *pos4,
-                                                    const long long *__restrict__ f,
-                                                    const float *__restrict__ epot,
-                                                    const float *__restrict__ vir)
+/* Leapfrog of a batch (k_leapfrog per replica, one thread per (atom, axis)):
+ * Berendsen scale, box and skin of the block's replica. */
+__global__ void __launch_bounds__(3 * MD_LA) k_leapfrog_b(md_kparams kp, thermo_par tp,
+                                                         step_io io, int nrep,
+                                                         const int2 *__restrict__ tab,
+                                                         const md_rep *__restrict__ reps,
+                                                         md_repstate *repst, int *rep_upd,
+                                                         double *x, double *v,
+                                                         const double *__restrict__ mass,
+                                                         const double *__restrict__ kick,
+                                                         float4 *pos4,
+                                                         const long long *__restrict__ f,
+                                                         const float *__restrict__ epot,
+                                                         const float *__restrict__ vir)
 {
-    __shared__ double sh[8];
+    __shared__ double sh[3 * MD_LA / 32];
+    __shared__ float s_x[3][MD_LA];
     const int2 bt = tab[blockIdx.x];
     const md_rep &R = reps[bt.x];
-    const int s = bt.y + threadIdx.x;
-    const int P = kp.pitch;
-    const double lam = tp.berendsen ? repst[bt.x].lam_next : 1.0;
-    double ke = 0.0, pe = 0.0, w = 0.0;
-    if (s < R.atom0 + R.natom) {
-        double m = mass[s], dtm = kp.dt * minv[s];
-        double xn[3];
-        for (int d = 0; d < 3; d++) {
-            double F = (double)f[d * P + s] * FX_INV;
-            double vv = (v[d * P + s] + F * dtm) * lam;
-            v[d * P + s] = vv;
-            double xx = wrap(x[d * P + s] + vv * kp.dt, R.boxd[d], R.box2i[d]);
-            x[d * P + s] = xx;
-            xn[d] = xx;
-            ke += vv * vv;
-        }
-        ke *= 0.5 * m;
-        float4 p = pos4[s];
-        p = make_float4((float)xn[0], (float)xn[1], (float)xn[2], p.w);
+    const int d = threadIdx.x / MD_LA, a = threadIdx.x - d * MD_LA;
+    const int s = bt.y + a;
+    const bool act = s < R.atom0 + R.natom;
+    const size_t o = (size_t)d * kp.pitch + s;
+    double ke2 = 0.0, pe = 0.0, w = 0.0;
+    if (act) {
+        const axis_par ax = axis_of(d, R.wlim, R.boxd, R.box2i);
+        double vv = v[o] + (double)f[o] * kick[s];
+        if (tp.berendsen) vv *= repst[bt.x].lam_next;
+        v[o] = vv;
+        double xx = x[o] + vv * kp.dt;
+        s_x[d][a] = wrap(xx, ax.lim, ax.L, ax.two_over_l);
+        x[o] = xx;
+        ke2 = mass[s] * (vv * vv);
+        if (d == 0 && tp.energy) { pe = epot[s]; w = vir[s]; }
+    }
+    __syncthreads();
+    if (d == 0 && act) {
+        float4 p = make_float4(s_x[0][a], s_x[1][a], s_x[2][a], pos4[s].w);
         pos4[s] = p;
         if (md_rsq_box(p, io.pos_old[s], R.box, R.boxi) >= R.rmaxdif) {
             io.st->update = 1;
             rep_upd[bt.x] = 1;
         }
-        if (tp.energy) { pe = epot[s]; w = vir[s]; }
     }
-    write_partials(ke, pe, w, tp.energy, io.partials, sh);
+    write_partials(ke2, pe, w, tp.energy, io.partials, sh);
     if (md_last_block(io.counter)) {
         finalize_b(kp, tp, 0, nrep, reps, repst, io.partials, gridDim.x, io.st, io.rec, io.rec_cap, sh);
         if (threadIdx.x == 0) {
@@ -177,32 +175,36 @@ __global__ void __launch_bounds__(256) k_leapfrog_b(md_kparams kp, thermo_par tp
 }
 
 /* Velocity Verlet first half of a batch (k_vv_first per replica). */
-__global__ void __launch_bounds__(256) k_vv_first_b(md_kparams kp, step_io io,
-                                                    const int2 *__restrict__ tab,
-                                                    const md_rep *__restrict__ reps,
-                                                    const md_repstate *__restrict__ repst,
-                                                    int *rep_upd, double *x, double *v,
-                                                    const double *__restrict__ minv, float4 *pos4,
-                                                    const long long *__restrict__ f)
+__global__ void __launch_bounds__(3 * MD_LA) k_vv_first_b(md_kparams kp, step_io io,
+                                                         const int2 *__restrict__ tab,
+                                                         const md_rep *__restrict__ reps,
+                                                         const md_repstate *__restrict__ repst,
+                                                         int *rep_upd, double *x, double *v,
+                                                         const double *__restrict__ kick,
+                                                         float4 *pos4,
+                                                         const long long *__restrict__ f)
 {
+    __shared__ float s_x[3][MD_LA];
     const int2 bt = tab[blockIdx.x];
     const md_rep &R = reps[bt.x];
-    const int s = bt.y + threadIdx.x;
-    const int P = kp.pitch;
+    const int d = threadIdx.x / MD_LA, a = threadIdx.x - d * MD_LA;
+    const int s = bt.y + a;
+    const bool act = s < R.atom0 + R.natom;
+    const size_t o = (size_t)d * kp.pitch + s;
     const double scale = repst[bt.x].kick_scale;
-    if (s < R.atom0 + R.natom) {
-        double hdtm = 0.5 * kp.dt * minv[s];
-        double xn[3];
-        for (int d = 0; d < 3; d++) {
-            double F = (double)f[d * P + s] * FX_INV;
-            double vv = v[d * P + s] * scale + F * hdtm;
-            v[d * P + s] = vv;
-            double xx = wrap(x[d * P + s] + vv * kp.dt, R.boxd[d], R.box2i[d]);
-            x[d * P + s] = xx;
-            xn[d] = xx;
-        }
-        float4 p = pos4[s];
-        p = make_float4((float)xn[0], (float)xn[1], (float)xn[2], p.w);
+    if (act) {
+        const axis_par ax = axis_of(d, R.wlim, R.boxd, R.box2i);
+        double vv = v[o];
+        if (scale != 1.0) vv *= scale;
+        vv += (double)f[o] * (0.5 * kick[s]);
+        v[o] = vv;
+        double xx = x[o] + vv * kp.dt;
+        s_x[d][a] = wrap(xx, ax.lim, ax.L, ax.two_over_l);
+        x[o] = xx;
+    }
+    __syncthreads();
+    if (d == 0 && act) {
+        float4 p = make_float4(s_x[0][a], s_x[1][a], s_x[2][a], pos4[s].w);
         pos4[s] = p;
         if (md_rsq_box(p, io.pos_old[s], R.box, R.boxi) >= R.rmaxdif) {
             io.st->update = 1;
@@ -217,45 +219,41 @@ __global__ void __launch_bounds__(256) k_vv_first_b(md_kparams kp, step_io io,
     }
 }
 
-/* Velocity Verlet second half of a batch (k_vv_second per replica); kick = 0
- * observes the state only. */
-__global__ void __launch_bounds__(256) k_vv_second_b(md_kparams kp, thermo_par tp, int kick,
-                                                     step_io io, int nrep,
-                                                     const int2 *__restrict__ tab,
-                                                     const md_rep *__restrict__ reps,
-                                                     md_repstate *repst, double *v,
-                                                     const double *__restrict__ mass,
-                                                     const double *__restrict__ minv,
-                                                     const long long *__restrict__ f,
-                                                     const float *__restrict__ epot,
-                                                     const float *__restrict__ vir)
+/* Velocity Verlet second half of a batch (k_vv_second per replica); do_kick
+ * = 0 observes the state only. */
+__global__ void __launch_bounds__(3 * MD_LA) k_vv_second_b(md_kparams kp, thermo_par tp,
+                                                          int do_kick, step_io io, int nrep,
+                                                          const int2 *__restrict__ tab,
+                                                          const md_rep *__restrict__ reps,
+                                                          md_repstate *repst, double *v,
+                                                          const double *__restrict__ mass,
+                                                          const double *__restrict__ kick,
+                                                          const long long *__restrict__ f,
+                                                          const float *__restrict__ epot,
+                                                          const float *__restrict__ vir)
 {
-    __shared__ double sh[8];
+    __shared__ double sh[3 * MD_LA / 32];
     const int2 bt = tab[blockIdx.x];
     const md_rep &R = reps[bt.x];
-    const int s = bt.y + threadIdx.x;
-    const int P = kp.pitch;
-    double ke = 0.0, pe = 0.0, w = 0.0;
-    const double scale = kick ? 1.0 : repst[bt.x].vscale;
+    const int d = threadIdx.x / MD_LA, a = threadIdx.x - d * MD_LA;
+    const int s = bt.y + a;
+    const size_t o = (size_t)d * kp.pitch + s;
+    double ke2 = 0.0, pe = 0.0, w = 0.0;
     if (s < R.atom0 + R.natom) {
-        double m = mass[s], hdtm = 0.5 * kp.dt * minv[s];
-        for (int d = 0; d < 3; d++) {
-            double vv = v[d * P + s];
-            if (kick) {
-                vv += (double)f[d * P + s] * FX_INV * hdtm;
-                v[d * P + s] = vv;
-            } else {
-                vv *= scale;
-            }
-            ke += vv * vv;
+        double vv = v[o];
+        if (do_kick) {
+            vv += (double)f[o] * (0.5 * kick[s]);
+            v[o] = vv;
+        } else {
+            vv *= repst[bt.x].vscale;
         }
-        ke *= 0.5 * m;
-        if (tp.energy) { pe = epot[s]; w = vir[s]; }
+        ke2 = mass[s] * (vv * vv);
+        if (d == 0 && tp.energy) { pe = epot[s]; w = vir[s]; }
     }
-    write_partials(ke, pe, w, tp.energy, io.partials, sh);
+    write_partials(ke2, pe, w, tp.energy, io.partials, sh);
     if (md_last_block(io.counter)) {
-        finalize_b(kp, tp, kick ? 1 : 2, nrep, reps, repst, io.partials, gridDim.x, io.st, io.rec,
-                   io.rec_cap, sh);
+        finalize_b(kp, tp, do_kick ? 1 : 2, nrep, reps, repst, io.partials, gridDim.x, io.st,
+                   io.rec, io.rec_cap, sh);
         if (threadIdx.x == 0) *io.counter = 0;
     }
 }
@@ -285,8 +283,8 @@ void pair_dispatch_b(md_ctx *c, const md_kparams &kp)
     }
 }
 
-inline const int2 *grid256(const md_ctx *c) { return c->grid_tab + c->grid_off[md_grid_index(256)]; }
-inline int grid256_blocks(const md_ctx *c) { return c->grid_cnt[md_grid_index(256)]; }
+inline const int2 *grid_int(const md_ctx *c) { return c->grid_tab + c->grid_off[md_grid_index(MD_LA)]; }
+inline int grid_int_blocks(const md_ctx *c) { return c->grid_cnt[md_grid_index(MD_LA)]; }
 
 }  // namespace
 
@@ -310,22 +308,22 @@ void launch_forces_b(md_ctx *c, const md_kparams &kp, bool energy, int terms)
 void launch_leapfrog_b(md_ctx *c, const md_kparams &kp, int energy, unsigned long long cond,
                        int has_cond)
 {
-    k_leapfrog_b<<<grid256_blocks(c), 256, 0, c->stream>>>(
-        kp, make_tp(c, energy), make_io(c, cond, has_cond), c->nrep, grid256(c), c->reps_dev,
-        c->repst, c->rep_upd, c->x, c->v, c->mass, c->minv, c->pos4, c->f, c->epot, c->vir);
+    k_leapfrog_b<<<grid_int_blocks(c), 3 * MD_LA, 0, c->stream>>>(
+        kp, make_tp(c, energy), make_io(c, cond, has_cond), c->nrep, grid_int(c), c->reps_dev,
+        c->repst, c->rep_upd, c->x, c->v, c->mass, c->kick, c->pos4, c->f, c->epot, c->vir);
 }
 
 void launch_vv_first_b(md_ctx *c, const md_kparams &kp, unsigned long long cond, int has_cond)
 {
-    k_vv_first_b<<<grid256_blocks(c), 256, 0, c->stream>>>(kp, make_io(c, cond, has_cond),
-                                                           grid256(c), c->reps_dev, c->repst,
-                                                           c->rep_upd, c->x, c->v, c->minv, c->pos4,
+    k_vv_first_b<<<grid_int_blocks(c), 3 * MD_LA, 0, c->stream>>>(kp, make_io(c, cond, has_cond),
+                                                           grid_int(c), c->reps_dev, c->repst,
+                                                           c->rep_upd, c->x, c->v, c->kick, c->pos4,
                                                            c->f);
 }
 
 void launch_vv_second_b(md_ctx *c, const md_kparams &kp, int energy, int kick)
 {
-    k_vv_second_b<<<grid256_blocks(c), 256, 0, c->stream>>>(
-        kp, make_tp(c, energy), kick, make_io(c, 0, 0), c->nrep, grid256(c), c->reps_dev,
-        c->repst, c->v, c->mass, c->minv, c->f, c->epot, c->vir);
+    k_vv_second_b<<<grid_int_blocks(c), 3 * MD_LA, 0, c->stream>>>(
+        kp, make_tp(c, energy), kick, make_io(c, 0, 0), c->nrep, grid_int(c), c->reps_dev,
+        c->repst, c->v, c->mass, c->kick, c->f, c->epot, c->vir);
 }

@@ -204,7 +204,7 @@ __global__ void k_cell_order(md_kparams kp, const md_devstate *st, int always, i
 __global__ void k_permute(md_kparams kp, const md_devstate *st, int always,
                           const int *__restrict__ src, const double *__restrict__ x,
                           const double *__restrict__ v, const double *__restrict__ mass,
-                          const double *__restrict__ minv,
+                          const double *__restrict__ kick,
                           const float4 *__restrict__ pos4, const int *__restrict__ perm,
                           const int *__restrict__ type, double *tmp_d, float4 *tmp4, int *tmp_i,
                           const int *__restrict__ arep, const int *__restrict__ rep_upd)
@@ -219,7 +219,7 @@ __global__ void k_permute(md_kparams kp, const md_devstate *st, int always,
         tmp_d[(3 + d) * P + s] = v[d * P + o];
     }
     tmp_d[6 * P + s] = mass[o];
-    tmp_d[7 * P + s] = minv[o];
+    tmp_d[7 * P + s] = kick[o];
     tmp4[s] = pos4[o];
     tmp_i[s] = perm[o];
     tmp_i[P + s] = type[o];
@@ -228,7 +228,7 @@ __global__ void k_permute(md_kparams kp, const md_devstate *st, int always,
 __global__ void k_copyback(md_kparams kp, const md_devstate *st, int always,
                            const double *__restrict__ tmp_d, const float4 *__restrict__ tmp4,
                            const int *__restrict__ tmp_i, double *x, double *v, double *mass,
-                           double *minv, float4 *pos4, int *perm, int *iperm, int *type,
+                           double *kick, float4 *pos4, int *perm, int *iperm, int *type,
                            const int *__restrict__ arep, const int *__restrict__ rep_upd)
 {
     if (!always && !st->update) return;
@@ -241,7 +241,7 @@ __global__ void k_copyback(md_kparams kp, const md_devstate *st, int always,
         v[d * P + s] = tmp_d[(3 + d) * P + s];
     }
     mass[s] = tmp_d[6 * P + s];
-    minv[s] = tmp_d[7 * P + s];
+    kick[s] = tmp_d[7 * P + s];
     pos4[s] = tmp4[s];
     int o = tmp_i[s];
     perm[s] = o;
@@ -595,10 +595,10 @@ void launch_rebuild(md_ctx *c, const md_kparams &kp, bool unconditional, bool al
     k_cell_order<<<(c->ncells + 255) / 256, 256, 0, s>>>(kp, c->st, always, c->ncells,
                                                           c->cell_start, c->perm, c->src, crep,
                                                           c->rep_upd);
-    k_permute<<<nb, 256, 0, s>>>(kp, c->st, always, c->src, c->x, c->v, c->mass, c->minv, c->pos4,
+    k_permute<<<nb, 256, 0, s>>>(kp, c->st, always, c->src, c->x, c->v, c->mass, c->kick, c->pos4,
                                  c->perm, c->type, c->tmp_d, c->tmp4, c->tmp_i, arep, c->rep_upd);
     k_copyback<<<nb, 256, 0, s>>>(kp, c->st, always, c->tmp_d, c->tmp4, c->tmp_i, c->x, c->v,
-                                  c->mass, c->minv, c->pos4, c->perm, c->iperm, c->type, arep,
+                                  c->mass, c->kick, c->pos4, c->perm, c->iperm, c->type, arep,
                                   c->rep_upd);
     /* a batch has no exclusions or bonded lists to re-express */
     if (!batch)

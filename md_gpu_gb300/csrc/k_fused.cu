@@ -21,7 +21,7 @@ __global__ void __launch_bounds__(128) k_pair_leapfrog(
     md_kparams kp, pair_consts pc, thermo_par tp, step_io io, const float4 *__restrict__ pos4,
     float4 *__restrict__ pos4_next, const int *__restrict__ type, const unsigned *__restrict__ nl,
     const int *__restrict__ nl_n, const float2 *__restrict__ ljtab, long long *f, float *vir,
-    double *x, double *v, const double *__restrict__ mass, const double *__restrict__ minv)
+    double *x, double *v, const double *__restrict__ mass, const double *__restrict__ kick)
 {
     constexpr int NA = 128 / TPA;   /* atoms per block */
     __shared__ float2 lj[MD_MAXTYPE * MD_MAXTYPE];
@@ -53,17 +53,17 @@ __global__ void __launch_bounds__(128) k_pair_leapfrog(
      * (atom, axis) per thread: full warps on the FP64 pipe */
     const int i0 = blockIdx.x * NA;
     const double lam = tp.berendsen ? io.st->lam_next : 1.0;
-    double ke = 0.0;
+    double ke2 = 0.0;
     for (int k = threadIdx.x; k < 3 * NA; k += blockDim.x) {
         int a = k / 3, d = k - 3 * a, ia = i0 + a;
         if (ia < kp.n) {
-            double F = (double)s_f[a][d] * FX_INV;
-            double vv = (v[d * P + ia] + F * (kp.dt * minv[ia])) * lam;
+            double vv = v[d * P + ia] + (double)s_f[a][d] * kick[ia];
+            if (tp.berendsen) vv *= lam;
             v[d * P + ia] = vv;
-            double xx = wrap(x[d * P + ia] + vv * kp.dt, kp.boxd[d], kp.box2i[d]);
+            double xx = x[d * P + ia] + vv * kp.dt;
+            s_x[a][d] = wrap(xx, kp.wlim[d], kp.boxd[d], kp.box2i[d]);
             x[d * P + ia] = xx;
-            s_x[a][d] = (float)xx;
-            ke += 0.5 * mass[ia] * vv * vv;
+            ke2 += mass[ia] * vv * vv;
         }
     }
     __syncthreads();
@@ -76,7 +76,7 @@ __global__ void __launch_bounds__(128) k_pair_leapfrog(
             check_moved(p, io.pos_old[ia], kp, io.st);
         }
     }
-    write_partials(ke, 0.0, 0.0, 0, io.partials, sh);
+    write_partials(ke2, 0.0, 0.0, 0, io.partials, sh);
     if (md_last_block(io.counter)) {
         finalize(kp, tp, 0, gridDim.x, io.partials, io.st, io.rec, io.rec_cap, sh);
         if (threadIdx.x == 0) {
@@ -98,7 +98,7 @@ void fused_dispatch(md_ctx *c, const md_kparams &kp, const pair_consts &pc, cons
     case T:                                                                                      \
         k_pair_leapfrog<KIND, T, (T >= 32 ? 1 : (T >= 16 ? 2 : (T >= 8 ? 4 : 8)))>              \
             <<<nb, 128, 0, c->stream>>>(kp, pc, tp, io, c->pos4, c->pos4_alt, c->type, c->nl,    \
-                                        c->nl_n, lj, c->f, c->vir, c->x, c->v, c->mass, c->minv); \
+                                        c->nl_n, lj, c->f, c->vir, c->x, c->v, c->mass, c->kick); \
         break;
         MD_FUSED_CASE(1)
         MD_FUSED_CASE(2)

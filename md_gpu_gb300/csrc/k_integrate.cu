@@ -27,40 +27,49 @@
 
 namespace {
 
-/* Leapfrog update + list check + KE partials; the last block finalises. */
-__global__ void __launch_bounds__(256) k_leapfrog(md_kparams kp, thermo_par tp, step_io io,
-                                                  double *x, double *v,
-                                                  const double *__restrict__ mass,
-                                                  const double *__restrict__ minv, float4 *pos4,
-                                                  const long long *__restrict__ f,
-                                                  const float *__restrict__ epot,
-                                                  const float *__restrict__ vir)
+/* The integrators run one thread per (atom, axis): MD_LA atoms per block,
+ * axis = threadIdx.x / MD_LA, so each axis streams a contiguous run of the
+ * SoA arrays and the FP64 chains of one atom run in three threads (the FP64
+ * pipe is slow and deep here: more independent chains hide its latency).
+ * The new FP32 positions meet in shared memory, where one thread per atom
+ * writes pos4 and performs the list check.
+ *
+ * Leapfrog update + list check + KE partials; the last block finalises.
+ * kick[s] = dt/m * 2^-32 turns the fixed-point force into the velocity
+ * change directly (the same product as F dt/m, rounded once). */
+__global__ void __launch_bounds__(3 * MD_LA) k_leapfrog(md_kparams kp, thermo_par tp, step_io io,
+                                                       double *x, double *v,
+                                                       const double *__restrict__ mass,
+                                                       const double *__restrict__ kick,
+                                                       float4 *pos4,
+                                                       const long long *__restrict__ f,
+                                                       const float *__restrict__ epot,
+                                                       const float *__restrict__ vir)
 {
-    __shared__ double sh[8];
-    int s = blockIdx.x * blockDim.x + threadIdx.x;
-    const int P = kp.pitch;
-    const double lam = tp.berendsen ? io.st->lam_next : 1.0;
-    double ke = 0.0, pe = 0.0, w = 0.0;
+    __shared__ double sh[3 * MD_LA / 32];
+    __shared__ float s_x[3][MD_LA];
+    const int d = threadIdx.x / MD_LA, a = threadIdx.x - d * MD_LA;
+    const int s = blockIdx.x * MD_LA + a;
+    const size_t o = (size_t)d * kp.pitch + s;
+    double ke2 = 0.0, pe = 0.0, w = 0.0;
     if (s < kp.n) {
-        double m = mass[s], dtm = kp.dt * minv[s];
-        double xn[3];
-        for (int d = 0; d < 3; d++) {
-            double F = (double)f[d * P + s] * FX_INV;
-            double vv = (v[d * P + s] + F * dtm) * lam;
-            v[d * P + s] = vv;
-            double xx = wrap(x[d * P + s] + vv * kp.dt, kp.boxd[d], kp.box2i[d]);
-            x[d * P + s] = xx;
-            xn[d] = xx;
-            ke += vv * vv;
-        }
-        ke *= 0.5 * m;
-        float4 p = pos4[s];
-        p = make_float4((float)xn[0], (float)xn[1], (float)xn[2], p.w);
+        const axis_par ax = axis_of(d, kp.wlim, kp.boxd, kp.box2i);
+        double vv = v[o] + (double)f[o] * kick[s];
+        if (tp.berendsen) vv *= io.st->lam_next;
+        v[o] = vv;
+        double xx = x[o] + vv * kp.dt;
+        s_x[d][a] = wrap(xx, ax.lim, ax.L, ax.two_over_l);
+        x[o] = xx;
+        ke2 = mass[s] * (vv * vv);
+        if (d == 0 && tp.energy) { pe = epot[s]; w = vir[s]; }
+    }
+    __syncthreads();
+    if (d == 0 && s < kp.n) {
+        float4 p = make_float4(s_x[0][a], s_x[1][a], s_x[2][a], pos4[s].w);
         pos4[s] = p;
         check_moved(p, io.pos_old[s], kp, io.st);
-        if (tp.energy) { pe = epot[s]; w = vir[s]; }
     }
-    write_partials(ke, pe, w, tp.energy, io.partials, sh);
+    write_partials(ke2, pe, w, tp.energy, io.partials, sh);
     if (md_last_block(io.counter)) {
         finalize(kp, tp, 0, gridDim.x, io.partials, io.st, io.rec, io.rec_cap, sh);
         if (threadIdx.x == 0) {
@@ -72,30 +81,33 @@ __global__ void __launch_bounds__(256) k_leapfrog(md_kparams kp, thermo_par tp, 
 
 /* Velocity Verlet first half: thermostat half step (NH), half kick, drift,
  * list check; the last block sets the rebuild condition. */
-__global__ void __launch_bounds__(256) k_vv_first(md_kparams kp, thermo_par tp, step_io io,
-                                                  double *x, double *v,
-                                                  const double *__restrict__ minv, float4 *pos4,
-                                                  const long long *__restrict__ f)
+__global__ void __launch_bounds__(3 * MD_LA) k_vv_first(md_kparams kp, thermo_par tp, step_io io,
+                                                       double *x, double *v,
+                                                       const double *__restrict__ kick,
+                                                       float4 *pos4,
+                                                       const long long *__restrict__ f)
 {
-    int s = blockIdx.x * blockDim.x + threadIdx.x;
-    const int P = kp.pitch;
+    __shared__ float s_x[3][MD_LA];
+    const int d = threadIdx.x / MD_LA, a = threadIdx.x - d * MD_LA;
+    const int s = blockIdx.x * MD_LA + a;
+    const size_t o = (size_t)d * kp.pitch + s;
     md_devstate *st = io.st;
     /* pending thermostat factor and, for NH, the first half step of this
      * step, both prepared by the previous step's reduction */
     const double scale = st->kick_scale;
     if (s < kp.n) {
-        double hdtm = 0.5 * kp.dt * minv[s];
-        double xn[3];
-        for (int d = 0; d < 3; d++) {
-            double F = (double)f[d * P + s] * FX_INV;
-            double vv = v[d * P + s] * scale + F * hdtm;
-            v[d * P + s] = vv;
-            double xx = wrap(x[d * P + s] + vv * kp.dt, kp.boxd[d], kp.box2i[d]);
-            x[d * P + s] = xx;
-            xn[d] = xx;
-        }
-        float4 p = pos4[s];
-        p = make_float4((float)xn[0], (float)xn[1], (float)xn[2], p.w);
+        const axis_par ax = axis_of(d, kp.wlim, kp.boxd, kp.box2i);
+        double vv = v[o];
+        if (scale != 1.0) vv *= scale;
+        vv += (double)f[o] * (0.5 * kick[s]);
+        v[o] = vv;
+        double xx = x[o] + vv * kp.dt;
+        s_x[d][a] = wrap(xx, ax.lim, ax.L, ax.two_over_l);
+        x[o] = xx;
+    }
+    __syncthreads();
+    if (d == 0 && s < kp.n) {
+        float4 p = make_float4(s_x[0][a], s_x[1][a], s_x[2][a], pos4[s].w);
         pos4[s] = p;
         check_moved(p, io.pos_old[s], kp, st);
     }
@@ -108,39 +120,35 @@ __global__ void __launch_bounds__(256) k_vv_first(md_kparams kp, thermo_par tp, 
 }
 
 /* Velocity Verlet second half kick and KE (PE, virial) partials; the last
- * block finalises.  kick = 0: observe the state only (pending NH scale
+ * block finalises.  do_kick = 0: observe the state only (pending NH scale
  * applied), mode 2. */
-__global__ void __launch_bounds__(256) k_vv_second(md_kparams kp, thermo_par tp, int kick,
-                                                   step_io io, double *v,
-                                                   const double *__restrict__ mass,
-                                                   const double *__restrict__ minv,
-                                                   const long long *__restrict__ f,
-                                                   const float *__restrict__ epot,
-                                                   const float *__restrict__ vir)
+__global__ void __launch_bounds__(3 * MD_LA) k_vv_second(md_kparams kp, thermo_par tp, int do_kick,
+                                                        step_io io, double *v,
+                                                        const double *__restrict__ mass,
+                                                        const double *__restrict__ kick,
+                                                        const long long *__restrict__ f,
+                                                        const float *__restrict__ epot,
+                                                        const float *__restrict__ vir)
 {
-    __shared__ double sh[8];
-    int s = blockIdx.x * blockDim.x + threadIdx.x;
-    const int P = kp.pitch;
-    double ke = 0.0, pe = 0.0, w = 0.0;
-    double scale = kick ? 1.0 : io.st->vscale;
+    __shared__ double sh[3 * MD_LA / 32];
+    const int d = threadIdx.x / MD_LA, a = threadIdx.x - d * MD_LA;
+    const int s = blockIdx.x * MD_LA + a;
+    const size_t o = (size_t)d * kp.pitch + s;
+    double ke2 = 0.0, pe = 0.0, w = 0.0;
     if (s < kp.n) {
-        double m = mass[s], hdtm = 0.5 * kp.dt * minv[s];
-        for (int d = 0; d < 3; d++) {
-            double vv = v[d * P + s];
-            if (kick) {
-                vv += (double)f[d * P + s] * FX_INV * hdtm;
-                v[d * P + s] = vv;
-            } else {
-                vv *= scale;
-            }
-            ke += vv * vv;
+        double vv = v[o];
+        if (do_kick) {
+            vv += (double)f[o] * (0.5 * kick[s]);
+            v[o] = vv;
+        } else {
+            vv *= io.st->vscale;
         }
-        ke *= 0.5 * m;
-        if (tp.energy) { pe = epot[s]; w = vir[s]; }
+        ke2 = mass[s] * (vv * vv);
+        if (d == 0 && tp.energy) { pe = epot[s]; w = vir[s]; }
     }
-    write_partials(ke, pe, w, tp.energy, io.partials, sh);
+    write_partials(ke2, pe, w, tp.energy, io.partials, sh);
     if (md_last_block(io.counter)) {
-        finalize(kp, tp, kick ? 1 : 2, gridDim.x, io.partials, io.st, io.rec, io.rec_cap, sh);
+        finalize(kp, tp, do_kick ? 1 : 2, gridDim.x, io.partials, io.st, io.rec, io.rec_cap, sh);
         if (threadIdx.x == 0) *io.counter = 0;
     }
 }
@@ -204,9 +212,9 @@ void launch_leapfrog(md_ctx *c, const md_kparams &kp, int energy, unsigned long 
         return;
     }
 
-    int nb = (kp.n + 255) / 256;
-    k_leapfrog<<<nb, 256, 0, c->stream>>>(kp, make_tp(c, energy), make_io(c, cond, has_cond), c->x,
-                                          c->v, c->mass, c->minv, c->pos4, c->f, c->epot, c->vir);
+    int nb = (kp.n + MD_LA - 1) / MD_LA;
+    k_leapfrog<<<nb, 3 * MD_LA, 0, c->stream>>>(kp, make_tp(c, energy), make_io(c, cond, has_cond), c->x,
+                                          c->v, c->mass, c->kick, c->pos4, c->f, c->epot, c->vir);
 }
 
 void launch_vv_first(md_ctx *c, const md_kparams &kp, unsigned long long cond, int has_cond)
@@ -216,9 +224,9 @@ void launch_vv_first(md_ctx *c, const md_kparams &kp, unsigned long long cond, i
         return;
     }
 
-    int nb = (kp.n + 255) / 256;
-    k_vv_first<<<nb, 256, 0, c->stream>>>(kp, make_tp(c, 0), make_io(c, cond, has_cond), c->x,
-                                          c->v, c->minv, c->pos4, c->f);
+    int nb = (kp.n + MD_LA - 1) / MD_LA;
+    k_vv_first<<<nb, 3 * MD_LA, 0, c->stream>>>(kp, make_tp(c, 0), make_io(c, cond, has_cond), c->x,
+                                          c->v, c->kick, c->pos4, c->f);
 }
 
 void launch_vv_second(md_ctx *c, const md_kparams &kp, int energy)
@@ -228,9 +236,9 @@ void launch_vv_second(md_ctx *c, const md_kparams &kp, int energy)
         return;
     }
 
-    int nb = (kp.n + 255) / 256;
-    k_vv_second<<<nb, 256, 0, c->stream>>>(kp, make_tp(c, energy), 1, make_io(c, 0, 0), c->v,
-                                           c->mass, c->minv, c->f, c->epot, c->vir);
+    int nb = (kp.n + MD_LA - 1) / MD_LA;
+    k_vv_second<<<nb, 3 * MD_LA, 0, c->stream>>>(kp, make_tp(c, energy), 1, make_io(c, 0, 0), c->v,
+                                           c->mass, c->kick, c->f, c->epot, c->vir);
 }
 
 void launch_thermo_from_state(md_ctx *c, const md_kparams &kp, int energy)
@@ -240,9 +248,9 @@ void launch_thermo_from_state(md_ctx *c, const md_kparams &kp, int energy)
         return;
     }
 
-    int nb = (kp.n + 255) / 256;
-    k_vv_second<<<nb, 256, 0, c->stream>>>(kp, make_tp(c, energy), 0, make_io(c, 0, 0), c->v,
-                                           c->mass, c->minv, c->f, c->epot, c->vir);
+    int nb = (kp.n + MD_LA - 1) / MD_LA;
+    k_vv_second<<<nb, 3 * MD_LA, 0, c->stream>>>(kp, make_tp(c, energy), 0, make_io(c, 0, 0), c->v,
+                                           c->mass, c->kick, c->f, c->epot, c->vir);
 }
 
 void launch_gather_out(md_ctx *c, const md_kparams &kp, int what, void *dst)

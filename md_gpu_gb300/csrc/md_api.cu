@@ -245,7 +245,7 @@ md_status fail(md_ctx *c, md_status s, const std::string &msg)
 
 void free_device(md_ctx *c)
 {
-    void *ptrs[] = {c->x, c->v, c->mass, c->minv, c->pos4, c->pos4_alt, c->pos_old, c->type, c->perm, c->iperm, c->f,
+    void *ptrs[] = {c->x, c->v, c->mass, c->kick, c->pos4, c->pos4_alt, c->pos_old, c->type, c->perm, c->iperm, c->f,
                     c->vir, c->epot, c->nl, c->nl_n, c->excl_orig, c->excl_s, c->cell_rank, c->cell_lin,
                     c->cell_count, c->cell_start, c->cell_fill, c->key, c->src, c->tmp_d, c->tmp4,
                     c->tmp_i, c->bl_o, c->bl_on, c->al_o, c->al_on, c->bl_s, c->bl_sn, c->al_s,
@@ -480,7 +480,7 @@ void make_cell_grid(const float box[3], float rl, cell_grid &g)
 /* Host staging of everything uploaded at creation, in the initial (original)
  * atom order, pitch-sized. */
 struct host_stage {
-    std::vector<double> x, v, m, mi;
+    std::vector<double> x, v, m, mi;   /* mi: the kick factor dt/m * 2^-32 */
     std::vector<float4> p4;
     std::vector<int> type;
     std::vector<uint4> excl;
@@ -537,10 +537,10 @@ md_status setup_device(md_ctx *c, void *stream, host_stage &h, md_ctx **out)
     /* block partials of the integrators (256 threads; one grid per replica
      * in a batch) and of the fused step (128 threads, up to 32 per atom) */
     size_t npart = 3 * (P / 4 + 256) + 8;
-    if (batch) npart = std::max(npart, 3 * (size_t)c->grid_cnt[md_grid_index(256)] + 8);
+    if (batch) npart = std::max(npart, 3 * (size_t)c->grid_cnt[md_grid_index(MD_LA)] + 8);
     cudaError_t e = cudaSuccess;
 #define MD_ALLOC(ptr, cnt) if (e == cudaSuccess) e = dalloc(&(ptr), (cnt))
-    MD_ALLOC(c->x, 3 * P); MD_ALLOC(c->v, 3 * P); MD_ALLOC(c->mass, P); MD_ALLOC(c->minv, P);
+    MD_ALLOC(c->x, 3 * P); MD_ALLOC(c->v, 3 * P); MD_ALLOC(c->mass, P); MD_ALLOC(c->kick, P);
     MD_ALLOC(c->pos4, P); MD_ALLOC(c->pos4_alt, P); MD_ALLOC(c->pos_old, P);
     MD_ALLOC(c->type, P); MD_ALLOC(c->perm, P); MD_ALLOC(c->iperm, P);
     MD_ALLOC(c->f, 3 * P); MD_ALLOC(c->vir, P); MD_ALLOC(c->epot, P);
@@ -595,7 +595,7 @@ md_status setup_device(md_ctx *c, void *stream, host_stage &h, md_ctx **out)
     up(c->x, h.x.data(), sizeof(double) * 3 * P);
     up(c->v, h.v.data(), sizeof(double) * 3 * P);
     up(c->mass, h.m.data(), sizeof(double) * P);
-    up(c->minv, h.mi.data(), sizeof(double) * P);
+    up(c->kick, h.mi.data(), sizeof(double) * P);
     up(c->pos4, h.p4.data(), sizeof(float4) * P);
     up(c->type, h.type.data(), sizeof(int) * P);
     up(c->perm, hperm.data(), sizeof(int) * P);
@@ -686,6 +686,7 @@ md_kparams md_make_kparams(const md_ctx *c)
         kp.boxi[d] = c->boxi[d];
         kp.boxd[d] = (double)c->box[d];
         kp.box2i[d] = 2.0 / (double)c->box[d];
+        kp.wlim[d] = 0.4999f * c->box[d];
         kp.ncell[d] = c->ncell[d];
         kp.binlen[d] = c->binlen[d];
         kp.stencil[d] = c->stencil[d];
@@ -869,7 +870,7 @@ md_status md_create(const md_system_desc *d, void *stream, md_ctx **out)
             h.v[k * P + i] = d->vel ? d->vel[3 * i + k] : 0.0;
         }
         h.m[i] = c->type_mass[c->itype[i]];
-        h.mi[i] = 1.0 / h.m[i];
+        h.mi[i] = ((double)c->dt * (1.0 / h.m[i])) * FX_INV;
         h.p4[i] = make_float4(d->pos[3 * i], d->pos[3 * i + 1], d->pos[3 * i + 2], c->charge[i]);
         h.type[i] = c->itype[i];
         h.excl[i] = make_uint4(c->excl_host[4 * i], c->excl_host[4 * i + 1], c->excl_host[4 * i + 2],
@@ -984,6 +985,7 @@ md_status md_create_batch(const md_system_desc *descs, int nrep, void *stream, m
             R.boxi[k] = (float)(1.0 / (double)d->box[k]);   /* simulation.cu:290-292 */
             R.boxd[k] = (double)d->box[k];
             R.box2i[k] = 2.0 / (double)d->box[k];
+            R.wlim[k] = 0.4999f * d->box[k];
         }
         R.rcutsq = d->rcutsq;
         R.reacf = d->lkspace == 0 ? d->reacf : 0.0f;
@@ -1019,6 +1021,8 @@ md_status md_create_batch(const md_system_desc *descs, int nrep, void *stream, m
         R.t0 = d->temper_0;
         R.q_nh = R.ndf * 8.314e-3 * R.t0 * tau * tau;
         if (R.q_nh <= 0) R.q_nh = 1.0;
+        R.inv_ndfr = 1.0 / (R.ndf * 8.314e-3);
+        R.inv_q = 1.0 / R.q_nh;
         c->rep_natom[r] = d->natom;
         /* cells: global rank = cell0 + Hilbert rank inside the replica */
         for (int k = 0; k < g.ncells; k++) {
@@ -1037,7 +1041,7 @@ md_status md_create_batch(const md_system_desc *descs, int nrep, void *stream, m
                 h.v[k * P + gi] = d->vel ? d->vel[3 * i + k] : 0.0;
             }
             h.m[gi] = d->type_mass[d->itype[i]];
-            h.mi[gi] = 1.0 / h.m[gi];
+            h.mi[gi] = ((double)d->dt * (1.0 / h.m[gi])) * FX_INV;
             h.p4[gi] = make_float4(d->pos[3 * i], d->pos[3 * i + 1], d->pos[3 * i + 2], d->charge[i]);
             h.type[gi] = d->itype[i];
             h.arep[gi] = r;
@@ -1063,9 +1067,9 @@ md_status md_create_batch(const md_system_desc *descs, int nrep, void *stream, m
         c->grid_off[k] = (int)h.grid.size();
         for (int r = 0; r < nrep; r++) {
             md_rep &R = c->reps[r];
-            if (A == 256) R.blk0 = (int)h.grid.size() - c->grid_off[k];
+            if (A == MD_LA) R.blk0 = (int)h.grid.size() - c->grid_off[k];
             for (int j = 0; j < R.natom; j += A) h.grid.push_back(make_int2(r, R.atom0 + j));
-            if (A == 256) R.nblk = (int)h.grid.size() - c->grid_off[k] - R.blk0;
+            if (A == MD_LA) R.nblk = (int)h.grid.size() - c->grid_off[k] - R.blk0;
         }
         c->grid_cnt[k] = (int)h.grid.size() - c->grid_off[k];
     }
@@ -1414,6 +1418,11 @@ md_status md_get_info(md_ctx *c, md_info *out)
     out->kernels_per_step = md_can_fuse(c) ? 1
                                            : 1 + ((c->has_bonds || c->has_angles) ? 1 : 0) +
                                                  (c->integrator == MD_LEAPFROG ? 1 : 2);
+    /* single system: key, scan, scatter, order, permute, copyback, remap,
+     * list, clear; batch: key, scan, scatter, order, permute, copyback,
+     * list, clear */
+    out->kernels_per_rebuild = c->nrep > 1 ? 8 : 9;
+    out->kernels_per_graph = c->integrator == MD_LEAPFROG ? 1 : 0;
     return MD_OK;
 }
 

@@ -73,6 +73,7 @@ struct md_kparams {
     float binlen[3];
     int stencil[3];   /* cell range per axis: +-stencil, or -1 = all cells */
     int cell_shift;   /* 1: a stencil cell's periodic image fixes the min-image shift */
+    float wlim[3];    /* 0.4999 L: |x| below it needs no periodic wrap */
     double dt;
 };
 
@@ -84,6 +85,7 @@ struct md_kparams {
 struct md_rep {
     float box[3], boxi[3];
     double boxd[3], box2i[3];
+    float wlim[3];
     float rcutsq, rskinsq, rmaxdif, reacf;
     float palfa, spiialfa, alfasq, wolf;
     float ucc, rc6i, rcinv;
@@ -92,9 +94,9 @@ struct md_rep {
     int cell_shift;
     int cell0, ncells;   /* first cell rank (= offset of its cell_rank table), cell count */
     int atom0, natom;
-    int blk0, nblk;      /* its blocks of the 256-atom integrator grid */
+    int blk0, nblk;      /* its blocks of the MD_LA-atom integrator grid */
     int ndf;
-    double t0, q_nh;
+    double t0, q_nh, inv_ndfr, inv_q;   /* 1/(ndf R), 1/Q */
 };
 
 /* Per-replica thermodynamic state of a batch (the fields md_devstate holds
@@ -111,6 +113,8 @@ struct md_repstate {
  * 256, powers of two) block b covers atoms [tab[b].y, min(tab[b].y + A, end
  * of replica tab[b].x)). */
 #define MD_NGRID 7
+/* Integrator blocks: MD_LA atoms x 3 axes, one thread per (atom, axis). */
+#define MD_LA 128
 inline int md_grid_index(int atoms_per_block)
 {
     int k = 0;
@@ -146,7 +150,7 @@ struct md_ctx {
     bool own_stream = false;
     int device = 0;
     double *x = nullptr, *v = nullptr, *mass = nullptr;   /* sorted order */
-    double *minv = nullptr;                               /* 1/mass, sorted order */
+    double *kick = nullptr;   /* dt/m * 2^-32: fixed-point force -> velocity change of one step */
     float4 *pos4 = nullptr, *pos_old = nullptr;
     float4 *pos4_alt = nullptr;     /* second position buffer of the fused step */
     int *type = nullptr, *perm = nullptr, *iperm = nullptr;

@@ -13,6 +13,9 @@ constexpr double RGAS = 8.314e-3;   /* kJ/mol/K, as integrator.cu:155 (1000/8.31
 
 struct thermo_par {
     double t0, tau, q_nh;
+    double inv_ndfr;   /* 1 / (ndf R): temperature from 2 KE */
+    double inv_q;      /* 1 / Q (Nose-Hoover mass) */
+    double dt_tau;     /* dt / tau (Berendsen) */
     int ndf, berendsen, nh, energy;
 };
 
@@ -42,10 +45,19 @@ __device__ __forceinline__ double block_sum(double v, double *sh)
     return r;
 }
 
-/* x -= L trunc(2x/L) (nve_leapfrog.cu:52-56) with 2/L precomputed. */
-__device__ __forceinline__ double wrap(double x, double L, double two_over_l)
+/* x -= L trunc(2x/L) (nve_leapfrog.cu:52-56) with 2/L precomputed; returns
+ * the FP32 copy of the result.  An atom whose FP32 position lies inside
+ * +-0.4999 L is inside +-L/2 in FP64 as well, where trunc gives 0: only atoms
+ * near or past the boundary pay for the FP64 product and trunc (the FP64
+ * pipe is the scarce one here), and the result is the same in every case. */
+__device__ __forceinline__ float wrap(double &x, float lim, double L, double two_over_l)
 {
-    return x - L * trunc(x * two_over_l);
+    float xf = (float)x;
+    if (!(fabsf(xf) < lim)) {
+        x = x - L * trunc(x * two_over_l);
+        xf = (float)x;
+    }
+    return xf;
 }
 
 /* First thermostat half step of the next VV step (NH): from KE (already
@@ -54,18 +66,20 @@ __device__ __forceinline__ double nh_half_a(double dt, const thermo_par &tp, dou
                                             double &xi, double &eta)
 {
     double kt = RGAS * tp.t0;
-    xi += 0.25 * dt * (2.0 * ke - tp.ndf * kt) / tp.q_nh;
+    xi += 0.25 * dt * (2.0 * ke - tp.ndf * kt) * tp.inv_q;
     double s1 = exp(-0.5 * dt * xi);
     ke *= s1 * s1;
     eta += 0.5 * dt * xi;
-    xi += 0.25 * dt * (2.0 * ke - tp.ndf * kt) / tp.q_nh;
+    xi += 0.25 * dt * (2.0 * ke - tp.ndf * kt) * tp.inv_q;
     return s1;
 }
 
-__device__ __forceinline__ void write_partials(double ke, double pe, double w, int energy,
+/* Block partials of the reductions: ke2 is twice the kinetic energy (m v^2;
+ * halved once per block, exactly), pe the potential energy, w sum ff r^2. */
+__device__ __forceinline__ void write_partials(double ke2, double pe, double w, int energy,
                                                double *partials, double *sh)
 {
-    double a = block_sum(ke, sh);
+    double a = 0.5 * block_sum(ke2, sh);
     if (threadIdx.x == 0) partials[blockIdx.x] = a;
     if (energy) {
         double b = block_sum(pe, sh);
@@ -96,11 +110,11 @@ __device__ double thermo_advance(double dt, const thermo_par &tp, int mode, doub
         if (tp.nh) {
             xi = vs->xi_a;
             eta = vs->eta_a;
-            xi += 0.25 * dt * (2.0 * ke - tp.ndf * kt) / tp.q_nh;
+            xi += 0.25 * dt * (2.0 * ke - tp.ndf * kt) * tp.inv_q;
             double s2 = exp(-0.5 * dt * xi);
             ke *= s2 * s2;
             eta += 0.5 * dt * xi;
-            xi += 0.25 * dt * (2.0 * ke - tp.ndf * kt) / tp.q_nh;
+            xi += 0.25 * dt * (2.0 * ke - tp.ndf * kt) * tp.inv_q;
             st->vscale = s2;
             st->xi = xi;
             st->eta = eta;
@@ -124,16 +138,16 @@ __device__ double thermo_advance(double dt, const thermo_par &tp, int mode, doub
     /* observing the state does not move the Berendsen reference temperature:
      * the first step uses T = T0 (integrator.cu:77) */
     if (mode == 2) return ke;
-    double temper = 2.0 * ke / (tp.ndf * RGAS);
+    double temper = 2.0 * ke * tp.inv_ndfr;
     st->temper = temper;
     st->lambda = lam;
     /* integrator.cu:146-147 for the next step, from this step's temperature */
-    st->lam_next = tp.berendsen ? sqrt(1.0 + dt / tp.tau * (tp.t0 / temper - 1.0)) : 1.0;
+    st->lam_next = tp.berendsen ? sqrt(1.0 + tp.dt_tau * (tp.t0 / temper - 1.0)) : 1.0;
     return ke;
 }
 
 /* Appends the step record and advances the step counter (thread 0). */
-__device__ void write_record(const thermo_par &tp, int ndf, double ke, double pe, double w,
+__device__ void write_record(const thermo_par &tp, double inv_ndfr, double ke, double pe, double w,
                              double extra, double xi, double lam, md_devstate *st, md_thermo *rec,
                              int rec_cap)
 {
@@ -142,7 +156,7 @@ __device__ void write_record(const thermo_par &tp, int ndf, double ke, double pe
     md_thermo r;
     r.step = step;
     r.ke = ke;
-    r.temper = 2.0 * ke / (ndf * RGAS);
+    r.temper = 2.0 * ke * inv_ndfr;
     r.pe = tp.energy ? pe : 0.0;
     r.virial = tp.energy ? w / 6.0 : 0.0;
     r.conserved = tp.energy ? ke + pe + extra : 0.0;
@@ -173,7 +187,23 @@ __device__ void finalize(const md_kparams &kp, const thermo_par &tp, int mode, i
     ke = thermo_advance(kp.dt, tp, mode, ke, pe, w, st, &xi, &eta, &lam);
     if (mode == 2) return;
     double extra = tp.nh ? 0.5 * tp.q_nh * xi * xi + tp.ndf * RGAS * tp.t0 * eta : 0.0;
-    write_record(tp, tp.ndf, ke, pe, w, extra, xi, lam, st, rec, rec_cap);
+    write_record(tp, tp.inv_ndfr, ke, pe, w, extra, xi, lam, st, rec, rec_cap);
+}
+
+/* Per-axis constants of an integrator thread (the axis is a runtime value:
+ * selects instead of indexing the parameter arrays). */
+struct axis_par {
+    double L, two_over_l;
+    float lim;
+};
+__device__ __forceinline__ axis_par axis_of(int d, const float *wlim, const double *boxd,
+                                            const double *box2i)
+{
+    axis_par a;
+    a.L = d == 0 ? boxd[0] : (d == 1 ? boxd[1] : boxd[2]);
+    a.two_over_l = d == 0 ? box2i[0] : (d == 1 ? box2i[1] : box2i[2]);
+    a.lim = d == 0 ? wlim[0] : (d == 1 ? wlim[1] : wlim[2]);
+    return a;
 }
 
 __device__ __forceinline__ void check_moved(float4 p, float4 old, const md_kparams &kp,
@@ -199,6 +229,9 @@ inline thermo_par make_tp(const md_ctx *c, int energy)
     tp.ndf = md_ndf(c);
     tp.q_nh = tp.ndf * RGAS * tp.t0 * tp.tau * tp.tau;
     if (tp.q_nh <= 0) tp.q_nh = 1.0;
+    tp.inv_ndfr = 1.0 / (tp.ndf * RGAS);
+    tp.inv_q = 1.0 / tp.q_nh;
+    tp.dt_tau = (double)c->dt / tp.tau;
     tp.berendsen = (c->enstype == 1 && c->integrator == MD_LEAPFROG) ? 1 : 0;
     tp.nh = (c->integrator == MD_NH) ? 1 : 0;
     tp.energy = energy;

@@ -59,7 +59,8 @@ class Info(C.Structure):
     _fields_ = [("natom", C.c_int), ("pitch", C.c_int), ("capacity", C.c_int),
                 ("ncell", C.c_int * 3), ("stencil", C.c_int * 3), ("binlen", C.c_float * 3),
                 ("pair_threads_per_atom", C.c_int), ("list_threads_per_atom", C.c_int),
-                ("builds", C.c_int), ("max_neighbors", C.c_int), ("kernels_per_step", C.c_int)]
+                ("builds", C.c_int), ("max_neighbors", C.c_int), ("kernels_per_step", C.c_int),
+                ("kernels_per_rebuild", C.c_int), ("kernels_per_graph", C.c_int)]
 
 
 def _make_desc(keep, *, box, itype, charge, pos, vel, type_mass, lj1, lj2, lkspace, rcutsq,
@@ -327,7 +328,9 @@ class MDSystem:
                 "ncell": list(i.ncell), "stencil": list(i.stencil), "binlen": list(i.binlen),
                 "pair_tpa": i.pair_threads_per_atom, "list_tpa": i.list_threads_per_atom,
                 "builds": i.builds, "max_neighbors": i.max_neighbors,
-                "kernels_per_step": i.kernels_per_step}
+                "kernels_per_step": i.kernels_per_step,
+                "kernels_per_rebuild": i.kernels_per_rebuild,
+                "kernels_per_graph": i.kernels_per_graph}
 
     def neighbor_list(self, nmax):
         """Reference layout (neighborlist.cu:284): (nnlist[pitch*nmax], nnlist_max[pitch])."""

@@ -167,8 +167,10 @@ def test_batch_autotune_and_graph_replays(cases):
         assert gu.rms_rel(a.forces()[:, :3], f0[:, :3]) <= 1e-6
         a.set_tuning(pt, 0)
         b.set_tuning(pt, 0)
-        a.set_positions(b.positions())
-        a.set_velocities(b.velocities())
+        # both start from forces evaluated with the same tuning
+        for s in (a, b):
+            s.set_positions(b.positions())
+            s.set_velocities(b.velocities())
         b.set_graphs(False)
         a.step(64)
         b.step(64)
