@@ -380,3 +380,88 @@ def md_plain_run(case: Case, x, v, nsteps, integrator, state=None, records=True)
     fld.bonds = C.POINTER(C.c_int)()
     fld.angles = C.POINTER(C.c_int)()
     return st, (rec[:nsteps] if rec is not None else None)
+
+
+# ---- adjoint of velocity-Verlet NVE (FP64, all pairs; small N) ----
+
+class AdjCfg(C.Structure):
+    _fields_ = [("natom", C.c_int), ("ntype", C.c_int), ("nsteps", C.c_int),
+                ("box", C.c_double * 3), ("rcutsq", C.c_double), ("alfa", C.c_double),
+                ("dt", C.c_double), ("w_pe", C.c_double), ("w_rdf", C.c_double),
+                ("rdf_a", C.c_int), ("rdf_b", C.c_int), ("nbins", C.c_int),
+                ("rdf_dr", C.c_double), ("rdf_sigma", C.c_double)]
+
+
+@dataclasses.dataclass
+class AdjProblem:
+    """One system and loss for the FP64 adjoint: arrays in FP64, masses per
+    atom in g/mol*1e4, LJ tables ntype x ntype, charges q (scale 1)."""
+
+    box: np.ndarray
+    itype: np.ndarray
+    q: np.ndarray
+    mass: np.ndarray
+    lj1: np.ndarray
+    lj2: np.ndarray
+    x0: np.ndarray
+    v0: np.ndarray
+    rcutsq: float
+    alfa: float
+    dt: float
+    nsteps: int
+    w_pe: float = 1.0
+    w_rdf: float = 1.0
+    rdf_a: int = 0
+    rdf_b: int = 1
+    nbins: int = 200
+    rdf_dr: float = 0.05
+    rdf_sigma: float = 0.05
+
+    def cfg(self):
+        c = AdjCfg()
+        c.natom, c.ntype, c.nsteps = len(self.itype), int(np.asarray(self.lj1).shape[0]), self.nsteps
+        for k in range(3):
+            c.box[k] = float(self.box[k])
+        c.rcutsq, c.alfa, c.dt = self.rcutsq, self.alfa, self.dt
+        c.w_pe, c.w_rdf = self.w_pe, self.w_rdf
+        c.rdf_a, c.rdf_b, c.nbins = self.rdf_a, self.rdf_b, self.nbins
+        c.rdf_dr, c.rdf_sigma = self.rdf_dr, self.rdf_sigma
+        return c
+
+    def _arrays(self, lj1=None, lj2=None, q=None):
+        d = lambda a: np.ascontiguousarray(a, np.float64)
+        return (np.ascontiguousarray(self.itype, np.int32), d(self.q if q is None else q), d(self.mass),
+                d(self.lj1 if lj1 is None else lj1).reshape(-1), d(self.lj2 if lj2 is None else lj2).reshape(-1),
+                d(self.x0).reshape(-1), d(self.v0).reshape(-1))
+
+
+def adj_loss(prob: AdjProblem, target=None, lj1=None, lj2=None, q=None):
+    """Loss of the FP64 forward run; returns (loss, gbar, mean PE)."""
+    L = lib()
+    L.orc_adj_loss.restype = C.c_double
+    c = prob.cfg()
+    it, qq, m, l1, l2, x0, v0 = prob._arrays(lj1, lj2, q)
+    tg = None if target is None else np.ascontiguousarray(target, np.float64)
+    g = np.zeros(prob.nbins)
+    pe = C.c_double()
+    loss = L.orc_adj_loss(C.byref(c), _p(it, C.c_int), _p(qq, C.c_double), _p(m, C.c_double),
+                          _p(l1, C.c_double), _p(l2, C.c_double), _p(x0, C.c_double), _p(v0, C.c_double),
+                          _p(tg, C.c_double) if tg is not None else None, _p(g, C.c_double), C.byref(pe))
+    return loss, g, pe.value
+
+
+def adj_grad(prob: AdjProblem, target=None):
+    """Loss and its FP64 adjoint gradient: (loss, dlj1[nt,nt], dlj2[nt,nt], dlns, gbar)."""
+    L = lib()
+    L.orc_adj_grad.restype = C.c_double
+    c = prob.cfg()
+    it, qq, m, l1, l2, x0, v0 = prob._arrays()
+    nt = c.ntype
+    tg = None if target is None else np.ascontiguousarray(target, np.float64)
+    d1, d2, g = np.zeros(nt * nt), np.zeros(nt * nt), np.zeros(prob.nbins)
+    ds = C.c_double()
+    loss = L.orc_adj_grad(C.byref(c), _p(it, C.c_int), _p(qq, C.c_double), _p(m, C.c_double),
+                          _p(l1, C.c_double), _p(l2, C.c_double), _p(x0, C.c_double), _p(v0, C.c_double),
+                          _p(tg, C.c_double) if tg is not None else None, _p(d1, C.c_double),
+                          _p(d2, C.c_double), C.byref(ds), _p(g, C.c_double))
+    return loss, d1.reshape(nt, nt), d2.reshape(nt, nt), ds.value, g

@@ -1205,3 +1205,303 @@ int orc_md_plain_run(const orc_params *p, const orc_ffield *f, int n, double *x,
     free(excl); free(p4); free(f4); free(ep); free(fr);
     return 0;
 }
+
+
+/* ====================================================================== */
+/* Adjoint of velocity-Verlet NVE (FP64, all pairs).                      */
+/*                                                                        */
+/* Forward, per step: v_h = v + c F(x); x' = x + dt v_h; v' = v_h + c F(x'),  */
+/* c = dt/(2 m).  With P = dL/dx and u_m = dL/dv_h(m), reverse mode gives */
+/*   u_m  = u_{m+1} + dt P_{m+1}            (u_K = 0)                      */
+/*   P_m  = P_{m+1} + dO_m/dx_m + f_m c J(x_m) u_m                          */
+/*   dL/dtheta += f_m c (dF(x_m)/dtheta) . u_m                             */
+/* with f_m = 2 for 1 <= m <= K-1 (F(x_m) enters two half kicks, both with */
+/* the same adjoint vector u_m) and f_0 = 1; J = dF/dx is symmetric:       */
+/* (J w)_i = sum_j [ff (w_i - w_j) + g (d.(w_i - w_j)) d], g = (dff/dr)/r. */
+/* ====================================================================== */
+
+typedef struct {
+    double rc, rcsq, alpha, spi, W, ec_c, p, rc6i, rc12i;
+} adjmodel;
+
+static void adjmodel_init(adjmodel *m, double rcutsq, double alfa)
+{
+    m->rcsq = rcutsq;
+    m->rc = sqrt(rcutsq);
+    m->alpha = alfa;
+    m->p = (double)ORC_PEX * alfa;
+    m->spi = 2.0 / sqrt(3.14159265358979323846) * alfa;
+    double ec = erfc_as(alfa * m->rc);
+    m->W = ec / m->rc + m->spi * exp(-alfa * alfa * rcutsq);
+    m->ec_c = ec / m->rc;
+    double rc2i = 1.0 / rcutsq;
+    m->rc6i = rc2i * rc2i * rc2i;
+    m->rc12i = m->rc6i * m->rc6i;
+}
+
+typedef struct {
+    double ff, g, ffc, uc, ulj1, ulj2, flj1, flj2;
+} adjterm;
+
+/* Force factor ff (F_i = ff d), g = (dff/dr)/r, the Coulomb parts for the
+ * charge-scale derivative, and the derivatives of u and ff with respect to
+ * lj1 and lj2; qq includes qfac. */
+static inline void adj_pair(const adjmodel *m, double rsq, double qq, double l1, double l2,
+                            adjterm *o)
+{
+    double r = sqrt(rsq), ri = 1.0 / r, ri2 = ri * ri;
+    double a = m->alpha;
+    double t = 1.0 / (1.0 + m->p * r);
+    double P = ((((double)ORC_A5 * t + (double)ORC_A4) * t + (double)ORC_A3) * t + (double)ORC_A2) * t + (double)ORC_A1;
+    double dPt = (((5.0 * (double)ORC_A5 * t + 4.0 * (double)ORC_A4) * t + 3.0 * (double)ORC_A3) * t +
+                  2.0 * (double)ORC_A2) * t + (double)ORC_A1;   /* d(tP)/dt */
+    double e = exp(-a * a * rsq);
+    double E = P * t * e;                                     /* A&S erfc(a r) */
+    double dE = dPt * (-m->p * t * t) * e + P * t * (-2.0 * a * a * r) * e;
+    double h = m->spi * e + E * ri;
+    double dh = m->spi * (-2.0 * a * a * r) * e + dE * ri - E * ri2;
+    double fc = qq * (h - m->W) * ri2;
+    double dfc = qq * (dh * ri2 - 2.0 * (h - m->W) * ri2 * ri);
+    double ri6 = ri2 * ri2 * ri2, ri8 = ri6 * ri2, ri14 = ri6 * ri8;
+    double flj = l1 * ri14 - l2 * ri8;
+    double dflj = -14.0 * l1 * ri14 * ri + 8.0 * l2 * ri8 * ri;
+    o->ff = fc + flj;
+    o->g = (dfc + dflj) * ri;
+    o->ffc = fc;
+    o->uc = qq * (E * ri - m->ec_c + m->W * log(r / m->rc));
+    o->ulj1 = (ri6 * ri6 - m->rc12i) / 12.0;
+    o->ulj2 = -(ri6 - m->rc6i) / 6.0;
+    o->flj1 = ri14;
+    o->flj2 = -ri8;
+}
+
+static inline void adj_delta(const double *x, int i, int j, const double *L, double d[3])
+{
+    for (int k = 0; k < 3; k++) {
+        d[k] = x[3 * i + k] - x[3 * j + k];
+        d[k] -= L[k] * rint(d[k] / L[k]);
+    }
+}
+
+/* Forces and potential energy at x (all pairs inside rc). */
+static double adj_forces(const orc_adj_cfg *c, const adjmodel *m, const int *itype, const double *q,
+                         const double *lj1, const double *lj2, const double *x, double *F)
+{
+    const int n = c->natom, nt = c->ntype;
+    const double qfac = (double)ORC_QFAC;
+    double U = 0.0;
+#pragma omp parallel for reduction(+ : U) schedule(dynamic, 16)
+    for (int i = 0; i < n; i++) {
+        double f0 = 0, f1 = 0, f2 = 0;
+        for (int j = 0; j < n; j++) {
+            if (j == i) continue;
+            double d[3];
+            adj_delta(x, i, j, c->box, d);
+            double rsq = d[0] * d[0] + d[1] * d[1] + d[2] * d[2];
+            if (rsq > m->rcsq) continue;
+            int t = itype[i] * nt + itype[j];
+            adjterm o;
+            adj_pair(m, rsq, qfac * q[i] * q[j], lj1[t], lj2[t], &o);
+            f0 += o.ff * d[0]; f1 += o.ff * d[1]; f2 += o.ff * d[2];
+            U += 0.5 * (o.uc + lj1[t] * o.ulj1 + lj2[t] * o.ulj2);
+        }
+        F[3 * i] = f0; F[3 * i + 1] = f1; F[3 * i + 2] = f2;
+    }
+    return U;
+}
+
+static double adj_rdf_norm(const orc_adj_cfg *c, const int *itype, int b)
+{
+    int na = 0, nb = 0;
+    for (int i = 0; i < c->natom; i++) {
+        na += itype[i] == c->rdf_a;
+        nb += itype[i] == c->rdf_b;
+    }
+    double V = c->box[0] * c->box[1] * c->box[2];
+    double rb = (b + 0.5) * c->rdf_dr;
+    return V / ((double)na * (double)nb * 4.0 * 3.14159265358979323846 * rb * rb);
+}
+
+/* Adds the smoothed RDF of frame x to g (nbins). */
+static void adj_rdf_add(const orc_adj_cfg *c, const int *itype, const double *x, const double *norm,
+                        double *g)
+{
+    const int n = c->natom, nb = c->nbins;
+    const double s = c->rdf_sigma, rmax = nb * c->rdf_dr + 5.0 * s;
+    const double kn = 1.0 / (sqrt(2.0 * 3.14159265358979323846) * s);
+    for (int i = 0; i < n; i++) {
+        if (itype[i] != c->rdf_a) continue;
+        for (int j = 0; j < n; j++) {
+            if (j == i || itype[j] != c->rdf_b) continue;
+            double d[3];
+            adj_delta(x, i, j, c->box, d);
+            double r = sqrt(d[0] * d[0] + d[1] * d[1] + d[2] * d[2]);
+            if (r >= rmax) continue;
+            for (int b = 0; b < nb; b++) {
+                double y = (b + 0.5) * c->rdf_dr - r;
+                if (fabs(y) > 5.0 * s) continue;
+                g[b] += norm[b] * kn * exp(-0.5 * y * y / (s * s));
+            }
+        }
+    }
+}
+
+/* Gradient of sum_b e_b g_b(x) with respect to x, added to G. */
+static void adj_rdf_grad(const orc_adj_cfg *c, const int *itype, const double *x, const double *norm,
+                         const double *e, double *G)
+{
+    const int n = c->natom, nb = c->nbins;
+    const double s = c->rdf_sigma, rmax = nb * c->rdf_dr + 5.0 * s;
+    const double kn = 1.0 / (sqrt(2.0 * 3.14159265358979323846) * s);
+    for (int i = 0; i < n; i++) {
+        if (itype[i] != c->rdf_a) continue;
+        for (int j = 0; j < n; j++) {
+            if (j == i || itype[j] != c->rdf_b) continue;
+            double d[3];
+            adj_delta(x, i, j, c->box, d);
+            double r = sqrt(d[0] * d[0] + d[1] * d[1] + d[2] * d[2]);
+            if (r >= rmax) continue;
+            double coef = 0.0;   /* sum_b e_b dg_b/dr */
+            for (int b = 0; b < nb; b++) {
+                double y = (b + 0.5) * c->rdf_dr - r;
+                if (fabs(y) > 5.0 * s) continue;
+                coef += e[b] * norm[b] * kn * exp(-0.5 * y * y / (s * s)) * y / (s * s);
+            }
+            for (int k = 0; k < 3; k++) {
+                G[3 * i + k] += coef * d[k] / r;
+                G[3 * j + k] -= coef * d[k] / r;
+            }
+        }
+    }
+}
+
+/* The forward trajectory: frames (K+1) x 3N, mean PE, gbar. */
+static void adj_forward(const orc_adj_cfg *c, const adjmodel *m, const int *itype, const double *q,
+                        const double *mass, const double *lj1, const double *lj2, const double *x0,
+                        const double *v0, double *frames, double *pe_mean, double *gbar,
+                        const double *norm)
+{
+    const int n = c->natom, K = c->nsteps;
+    double *x = (double *)malloc(sizeof(double) * 3 * n), *v = (double *)malloc(sizeof(double) * 3 * n);
+    double *F = (double *)malloc(sizeof(double) * 3 * n);
+    memcpy(x, x0, sizeof(double) * 3 * n);
+    memcpy(v, v0, sizeof(double) * 3 * n);
+    for (int b = 0; b < c->nbins; b++) gbar[b] = 0.0;
+    double usum = adj_forces(c, m, itype, q, lj1, lj2, x, F);
+    adj_rdf_add(c, itype, x, norm, gbar);
+    if (frames) memcpy(frames, x, sizeof(double) * 3 * n);
+    for (int s = 0; s < K; s++) {
+        for (int i = 0; i < n; i++)
+            for (int k = 0; k < 3; k++) {
+                v[3 * i + k] += 0.5 * c->dt / mass[i] * F[3 * i + k];
+                x[3 * i + k] += c->dt * v[3 * i + k];
+                x[3 * i + k] -= c->box[k] * trunc(2.0 * x[3 * i + k] / c->box[k]);
+            }
+        usum += adj_forces(c, m, itype, q, lj1, lj2, x, F);
+        for (int i = 0; i < n; i++)
+            for (int k = 0; k < 3; k++) v[3 * i + k] += 0.5 * c->dt / mass[i] * F[3 * i + k];
+        adj_rdf_add(c, itype, x, norm, gbar);
+        if (frames) memcpy(frames + (size_t)3 * n * (s + 1), x, sizeof(double) * 3 * n);
+    }
+    for (int b = 0; b < c->nbins; b++) gbar[b] /= (K + 1);
+    *pe_mean = usum / (K + 1);
+    free(x); free(v); free(F);
+}
+
+double orc_adj_loss(const orc_adj_cfg *c, const int *itype, const double *q, const double *mass,
+                    const double *lj1, const double *lj2, const double *x0, const double *v0,
+                    const double *target, double *gbar_out, double *pe_mean_out)
+{
+    adjmodel m;
+    adjmodel_init(&m, c->rcutsq, c->alfa);
+    double *norm = (double *)calloc((size_t)c->nbins + 1, sizeof(double));
+    double *gbar = (double *)malloc(sizeof(double) * c->nbins);
+    for (int b = 0; b < c->nbins; b++) norm[b] = adj_rdf_norm(c, itype, b);
+    double pe = 0.0;
+    adj_forward(c, &m, itype, q, mass, lj1, lj2, x0, v0, NULL, &pe, gbar, norm);
+    double L = c->w_pe * pe / c->natom;
+    for (int b = 0; b < c->nbins; b++) {
+        double t = target ? target[b] : 0.0;
+        L += c->w_rdf * (gbar[b] - t) * (gbar[b] - t);
+    }
+    if (gbar_out) memcpy(gbar_out, gbar, sizeof(double) * c->nbins);
+    if (pe_mean_out) *pe_mean_out = pe;
+    free(norm); free(gbar);
+    return L;
+}
+
+double orc_adj_grad(const orc_adj_cfg *c, const int *itype, const double *q, const double *mass,
+                    const double *lj1, const double *lj2, const double *x0, const double *v0,
+                    const double *target, double *dlj1, double *dlj2, double *dlns,
+                    double *gbar_out)
+{
+    const int n = c->natom, K = c->nsteps, nt = c->ntype, nb = c->nbins;
+    adjmodel m;
+    adjmodel_init(&m, c->rcutsq, c->alfa);
+    double *norm = (double *)calloc((size_t)nb + 1, sizeof(double));
+    double *gbar = (double *)malloc(sizeof(double) * nb);
+    double *e = (double *)malloc(sizeof(double) * nb);
+    double *frames = (double *)malloc(sizeof(double) * 3 * n * (size_t)(K + 1));
+    double *P = (double *)calloc(3 * (size_t)n, sizeof(double));
+    double *U = (double *)calloc(3 * (size_t)n, sizeof(double));
+    double *w = (double *)malloc(sizeof(double) * 3 * n);
+    double *F = (double *)malloc(sizeof(double) * 3 * n);
+    for (int b = 0; b < nb; b++) norm[b] = adj_rdf_norm(c, itype, b);
+    double pe = 0.0;
+    adj_forward(c, &m, itype, q, mass, lj1, lj2, x0, v0, frames, &pe, gbar, norm);
+    double L = c->w_pe * pe / n;
+    for (int b = 0; b < nb; b++) {
+        double t = target ? target[b] : 0.0;
+        L += c->w_rdf * (gbar[b] - t) * (gbar[b] - t);
+        e[b] = c->w_rdf * 2.0 * (gbar[b] - t) / (K + 1);
+    }
+    for (int k = 0; k < nt * nt; k++) { dlj1[k] = 0.0; dlj2[k] = 0.0; }
+    *dlns = 0.0;
+    const double wpe = c->w_pe / ((double)(K + 1) * n);
+    const double qfac = (double)ORC_QFAC;
+    for (int mfr = K; mfr >= 0; mfr--) {
+        const double *x = frames + (size_t)3 * n * mfr;
+        if (mfr < K) {
+            double fac = mfr >= 1 ? 2.0 : 1.0;
+            for (int i = 0; i < 3 * n; i++) {
+                U[i] += c->dt * P[i];
+                w[i] = fac * 0.5 * c->dt / mass[i / 3] * U[i];
+            }
+        }
+        /* observable gradient (PE: -F; RDF) and, below the last frame, J w
+         * and the parameter terms; explicit dU/dtheta for every frame */
+        adj_forces(c, &m, itype, q, lj1, lj2, x, F);
+        for (int i = 0; i < 3 * n; i++) P[i] -= wpe * F[i];
+        adj_rdf_grad(c, itype, x, norm, e, P);
+        for (int i = 0; i < n; i++)
+            for (int j = i + 1; j < n; j++) {
+                double d[3];
+                adj_delta(x, i, j, c->box, d);
+                double rsq = d[0] * d[0] + d[1] * d[1] + d[2] * d[2];
+                if (rsq > m.rcsq) continue;
+                int tij = itype[i] * nt + itype[j], tji = itype[j] * nt + itype[i];
+                adjterm o;
+                adj_pair(&m, rsq, qfac * q[i] * q[j], lj1[tij], lj2[tij], &o);
+                /* explicit derivative of the mean PE (each table entry carries half a pair) */
+                dlj1[tij] += 0.5 * wpe * o.ulj1; dlj1[tji] += 0.5 * wpe * o.ulj1;
+                dlj2[tij] += 0.5 * wpe * o.ulj2; dlj2[tji] += 0.5 * wpe * o.ulj2;
+                *dlns += wpe * 2.0 * o.uc;
+                if (mfr == K) continue;
+                double dwi = d[0] * w[3 * i] + d[1] * w[3 * i + 1] + d[2] * w[3 * i + 2];
+                double dwj = d[0] * w[3 * j] + d[1] * w[3 * j + 1] + d[2] * w[3 * j + 2];
+                double dd = dwi - dwj;
+                for (int k = 0; k < 3; k++) {
+                    double jw = o.ff * (w[3 * i + k] - w[3 * j + k]) + o.g * dd * d[k];
+                    P[3 * i + k] += jw;
+                    P[3 * j + k] -= jw;
+                }
+                /* dynamics term: row i uses entry (ti,tj) with d.w_i, row j entry (tj,ti) with -d.w_j */
+                dlj1[tij] += o.flj1 * dwi; dlj1[tji] -= o.flj1 * dwj;
+                dlj2[tij] += o.flj2 * dwi; dlj2[tji] -= o.flj2 * dwj;
+                *dlns += 2.0 * o.ffc * dd;
+            }
+    }
+    if (gbar_out) memcpy(gbar_out, gbar, sizeof(double) * nb);
+    free(norm); free(gbar); free(e); free(frames); free(P); free(U); free(w); free(F);
+    return L;
+}

@@ -183,6 +183,39 @@ int orc_md_plain_run(const orc_params *p, const orc_ffield *f, int n, double *x,
                      const int *itype, const float *q, const double *m, const float box[3],
                      int nsteps, int integrator, double *state_io, double *rec_out);
 
+/* ---- adjoint of velocity-Verlet NVE (no reference counterpart) ----
+ * One system, FP64, all pairs inside rc (O(N^2) per frame, small N only),
+ * LJ + Wolf Coulomb with A&S 7.1.26 erfc.  Frames m = 0..K are the initial
+ * configuration and the K steps.  Loss
+ *   L = w_pe <U>/N + w_rdf sum_b (gbar_b - t_b)^2,
+ * <U> the frame average of the consistent potential energy, gbar the frame
+ * average of the Gaussian-smoothed RDF of type pair (rdf_a, rdf_b):
+ *   g_b = V/(N_a N_b 4 pi r_b^2) sum_{i in a, j in b} K(r_b - r_ij),
+ *   r_b = (b + 1/2) dr, K a normalised Gaussian of width sigma.
+ * Gradients are with respect to every LJ table entry lj1[a*nt+b], lj2[...]
+ * (as used by the row of an atom of type a) and to the log of a common
+ * charge scale (charges q -> s q at s = 1). */
+typedef struct {
+    int natom, ntype, nsteps;
+    double box[3];
+    double rcutsq, alfa, dt;
+    double w_pe, w_rdf;
+    int rdf_a, rdf_b, nbins;
+    double rdf_dr, rdf_sigma;
+} orc_adj_cfg;
+
+/* Forward run only: the loss; gbar (nbins) and the mean PE when non-NULL.
+ * target may be NULL (zero). */
+double orc_adj_loss(const orc_adj_cfg *c, const int *itype, const double *q, const double *mass,
+                    const double *lj1, const double *lj2, const double *x0, const double *v0,
+                    const double *target, double *gbar, double *pe_mean);
+/* Forward run and the discrete adjoint: returns the loss and writes dlj1,
+ * dlj2 (ntype*ntype) and dlns (1). */
+double orc_adj_grad(const orc_adj_cfg *c, const int *itype, const double *q, const double *mass,
+                    const double *lj1, const double *lj2, const double *x0, const double *v0,
+                    const double *target, double *dlj1, double *dlj2, double *dlns,
+                    double *gbar);
+
 int orc_num_threads(void);
 
 #ifdef __cplusplus
