@@ -1289,10 +1289,10 @@ static double adj_forces(const orc_adj_cfg *c, const adjmodel *m, const int *ity
 {
     const int n = c->natom, nt = c->ntype;
     const double qfac = (double)ORC_QFAC;
-    double U = 0.0;
-#pragma omp parallel for reduction(+ : U) schedule(dynamic, 16)
+    double *ui = (double *)calloc((size_t)n + 1, sizeof(double));
+#pragma omp parallel for schedule(dynamic, 16)
     for (int i = 0; i < n; i++) {
-        double f0 = 0, f1 = 0, f2 = 0;
+        double f0 = 0, f1 = 0, f2 = 0, U = 0.0;
         for (int j = 0; j < n; j++) {
             if (j == i) continue;
             double d[3];
@@ -1306,7 +1306,11 @@ static double adj_forces(const orc_adj_cfg *c, const adjmodel *m, const int *ity
             U += 0.5 * (o.uc + lj1[t] * o.ulj1 + lj2[t] * o.ulj2);
         }
         F[3 * i] = f0; F[3 * i + 1] = f1; F[3 * i + 2] = f2;
+        ui[i] = U;
     }
+    double U = 0.0;   /* fixed order: the result does not depend on the thread count */
+    for (int i = 0; i < n; i++) U += ui[i];
+    free(ui);
     return U;
 }
 
