@@ -11,7 +11,9 @@ resident, as in any MD run.
 The same line carries, under "batched_replicas", the batch workload: 512
 NaCl-like replicas of 256..8192 ions (own eps/sigma per type and charge scale
 within +-10%), velocity Verlet NVE at dt 2 fs, advanced together by
-md_create_batch (one launch per stage, one graph for the batch).
+md_create_batch (one launch per stage, one graph for the batch); and under
+"adjoint", gradients per second of a trajectory loss of 64 x 8000-ion NaCl
+over 2000 velocity-Verlet steps (md_adjoint_run, checkpoints every 50 steps).
 
     python bench.py [--gpus N] [--steps K] [--warmup W] [--impl ours|reference]
 
@@ -191,6 +193,62 @@ def batch_leg(args, flush):
     }
 
 
+def adjoint_leg(args):
+    """Differentiable MD: gradients of <U>/N + RDF loss of 64 x 8000-ion NaCl
+    over 2000 VV steps w.r.t. (eps_Na, sigma_Na, eps_Cl, sigma_Cl, charge
+    scale), by the library's adjoint with checkpoints every 50 steps."""
+    import torch
+
+    from md_gpu_gb300 import MDSystem, params, synth
+    nrep, natom, K = args.adj_nrep, args.adj_natom, args.adj_steps
+    eps = np.array([synth.NACL_LJ["Na"][1], synth.NACL_LJ["Cl"][1]]) * synth.KCAL
+    sig = np.array([synth.NACL_LJ["Na"][0], synth.NACL_LJ["Cl"][0]])
+
+    def batch(scale):
+        l1, l2 = params.lb_tables(eps * scale, sig * scale)
+        out = []
+        for r in range(nrep):
+            a = synth.to_arrays(synth.nacl_replica(natom, seed=7000 + r, integrator="vv", ensemble="nve"))
+            a.update(lj1=l1.astype(np.float32), lj2=l2.astype(np.float32),
+                     charge=(a["charge"] * scale).astype(np.float32))
+            out.append(a)
+        return out
+
+    kw = dict(checkpoint=50, nbins=200, dr=0.05, sigma=0.05)
+    with MDSystem.from_batch(batch(1.05)) as b:
+        target = b.adjoint(K, gradient=False, **kw)["gbar"]
+    with MDSystem.from_batch(batch(1.0)) as b:
+        torch.cuda.synchronize()
+        t0 = time.perf_counter()
+        fwd = b.adjoint(K, gradient=False, target=target, **kw)
+        t_fwd = time.perf_counter() - t0
+    with MDSystem.from_batch(batch(1.0)) as b:
+        torch.cuda.synchronize()
+        t0 = time.perf_counter()
+        out = b.adjoint(K, gradient=True, target=target, **kw)
+        t_adj = time.perf_counter() - t0
+    grads = []
+    for r in range(nrep):
+        de, ds = params.lb_chain(out["dlj1"][r], out["dlj2"][r], eps, sig)
+        grads.append([de[0], ds[0], de[1], ds[1], out["dlns"][r]])
+    grads = np.array(grads)
+    n_grads = grads.size
+    return {
+        "workload": (f"{nrep} replicas of {natom}-ion molten NaCl (LJ + Wolf, rc 12 A), {K} velocity-Verlet "
+                     "NVE steps at dt 2 fs from 1200 K; loss = <U>/N + sum_b (gbar_b - target_b)^2 of the "
+                     "Gaussian-smoothed Na-Cl RDF (200 bins of 0.05 A, sigma 0.05 A), target from the same "
+                     "run at eps, sigma and charges +5%; gradients w.r.t. eps_Na, sigma_Na, eps_Cl, "
+                     "sigma_Cl and the charge scale; checkpoints every 50 steps"),
+        "value": n_grads / t_adj, "unit": "param-grads/s", "seconds": t_adj,
+        "forward_seconds": t_fwd,
+        "central_difference_equivalent": {
+            "value": n_grads / (10 * t_fwd), "unit": "param-grads/s",
+            "note": "10 forward runs of the same batch (two per parameter), FP32 forward"},
+        "loss_mean": float(out["loss"].mean()), "loss_forward_only_mean": float(fwd["loss"].mean()),
+        "grad_mean": grads.mean(0).tolist(),
+    }
+
+
 def run_ours(args):
     import torch
     rank, world, local = rank_info()
@@ -284,6 +342,7 @@ def run_ours(args):
                "call": "md_run_host (upload pos/vel, list build, md_steps steps, download records + pos/vel)"}
         if args.nrep > 0:
             extra_batch = batch_leg(args, flush)
+        extra_adj = adjoint_leg(args) if args.adj_nrep > 0 else None
         cpu_v, cpu_dt, cores = cpu_reference_sample(base, 1, 0, args.ref_md_steps)
         extra = {"roofline": roof, "e2e": e2e, "force_rms_rel_err_vs_fp64": err,
                  "cpu_baseline": {"value": cpu_v, "unit": UNIT, "cores": cores, "kind": "port",
@@ -292,6 +351,8 @@ def run_ours(args):
                                             "FP32 restatement, OpenMP"}}
         if args.nrep > 0:
             extra["batched_replicas"] = extra_batch
+        if extra_adj is not None:
+            extra["adjoint"] = extra_adj
     line = {"metric": METRIC, "value": value, "unit": UNIT, "n_gpus": world, "steps": args.steps,
             "warmup": args.warmup, "ms_per_step": total_ms / args.steps, "higher_is_better": True,
             "scaling": "weak", "vs_baseline": None, "dtype": "f32",
@@ -327,6 +388,9 @@ def main():
     ap.add_argument("--md-steps", type=int, default=128, help="MD steps per bench step (multiple of 32)")
     ap.add_argument("--nrep", type=int, default=512, help="replicas of the batch leg (0: skip it)")
     ap.add_argument("--batch-segments", type=int, default=4)
+    ap.add_argument("--adj-nrep", type=int, default=64, help="replicas of the adjoint leg (0: skip it)")
+    ap.add_argument("--adj-natom", type=int, default=8000)
+    ap.add_argument("--adj-steps", type=int, default=2000)
     ap.add_argument("--ref-md-steps", type=int, default=10)
     ap.add_argument("--ncell", type=int, default=20)
     ap.add_argument("--no-autotune", action="store_true")

@@ -105,11 +105,40 @@ md_status md_last_error(const md_ctx *ctx, char *buf, int len);
  * order) hold the replicas' atoms concatenated in replica order; the
  * neighbour list of a replica holds only its own atoms.  md_get_thermo
  * returns the batch totals (temperature over all degrees of freedom);
- * md_get_replica_thermo the per-replica values.  nrep == 1 is md_create. */
+ * md_get_replica_thermo the per-replica values.  A batch of one replica is
+ * a batch context (the adjoint, md_adjoint_run, takes batch contexts). */
 md_status md_create_batch(const md_system_desc *descs, int nrep, void *stream, md_ctx **out);
 /* Per-replica state after the last step of a batch (out[r], r < nrep and
  * < the batch's replica count; synchronises the stream). */
 md_status md_get_replica_thermo(md_ctx *ctx, md_thermo *out, int nrep);
+
+/* Differentiable trajectories (no counterpart in the reference).  For a
+ * batch context with velocity Verlet NVE, md_adjoint_run runs nsteps steps
+ * from the current state and evaluates per replica the loss
+ *   L = w_pe <U>/N + w_rdf sum_b (gbar_b - target_b)^2,
+ * <U> the average potential energy over the nsteps + 1 frames, gbar the
+ * frame average of the Na-Cl-style RDF of atom types (rdf_a, rdf_b) smoothed
+ * by Gaussians of width rdf_sigma on nbins bins of width rdf_dr (centres at
+ * (b + 1/2) rdf_dr; the range plus 5 sigma must lie inside every replica's
+ * cutoff).  With gradient != 0 it also returns dL/d lj1[a][b] and
+ * dL/d lj2[a][b] (8x8 per replica, entry a*8+b as used by atoms of type a;
+ * the derivative for a symmetric pair parameter is the sum of the (a,b) and
+ * (b,a) entries) and dL/d ln s for a common charge scale s, by the discrete
+ * adjoint of the integrator with (x, v) checkpoints every `checkpoint` steps
+ * and recompute.  The context is left at the end of the trajectory.
+ * target: nrep*nbins (NULL = 0); loss: nrep; gbar: nrep*nbins (may be NULL);
+ * dlj1, dlj2: nrep*64; dlns: nrep. */
+typedef struct {
+    int nsteps;         /* steps of the trajectory (frames 0..nsteps) */
+    int checkpoint;     /* steps between checkpoints (recompute segment) */
+    int gradient;       /* 0: forward pass only (loss, gbar) */
+    double w_pe, w_rdf; /* loss weights */
+    int rdf_a, rdf_b;   /* atom types of the RDF pair (0-based) */
+    int nbins;          /* <= 512 */
+    double rdf_dr, rdf_sigma;   /* A */
+} md_adjoint_cfg;
+md_status md_adjoint_run(md_ctx *ctx, const md_adjoint_cfg *cfg, const double *target, double *loss,
+                         double *gbar, double *dlj1, double *dlj2, double *dlns);
 
 /* SimulationInit + config_init + forces_init + neighborlist_init +
  * integrate_init (simulation.cu:40, runGPU.cu:53-60): reads <base>.inp,

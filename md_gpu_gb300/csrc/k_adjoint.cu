@@ -1,0 +1,562 @@
+/*
+ * k_adjoint.cu -- gradients of trajectory-averaged observables of a batch
+ * of replicas (velocity Verlet NVE) by the discrete adjoint, with
+ * checkpoint-and-recompute.  No counterpart in the reference.
+ *
+ * Loss per replica (frames m = 0..K: the start and every step):
+ *   L = w_pe <U>/N + w_rdf sum_b (gbar_b - t_b)^2,
+ *   g_b(x) = V/(N_a N_b 4 pi r_b^2) sum_{i in a, j in b} K(r_b - r_ij),
+ * K a normalised Gaussian of width sigma, r_b = (b + 1/2) dr, gbar the frame
+ * average.  Gradients: every LJ table entry lj1[a][b], lj2[a][b] (as used by
+ * the rows of atoms of type a) and the log of a common charge scale.
+ *
+ * Forward per step: v_h = v + c F(x); x' = x + dt v_h; v' = v_h + c F(x'),
+ * c = dt/(2m).  Reverse mode with P = dL/dx and u_m = dL/dv_h(m):
+ *   u_m = u_{m+1} + dt P_{m+1}                         (u_K = 0)
+ *   P_m = P_{m+1} + dO_m/dx_m + f_m J(x_m) (c u_m)
+ *   dL/dtheta += f_m (dF(x_m)/dtheta) . (c u_m) + dO_m/dtheta,
+ * f_m = 2 for 0 < m < K (F(x_m) enters two half kicks with the same adjoint
+ * vector), f_0 = 1; J = dF/dx is symmetric, for a pair potential
+ *   (J w)_i = sum_j [ff (w_i - w_j) + g (d.(w_i - w_j)) d],  g = (dff/dr)/r.
+ * The pair terms differentiate the force law the dynamics use (A&S 7.1.26
+ * erfc included), in FP32; the adjoint state P, u is FP64 in the original
+ * atom order, and every sum is taken in a fixed order (block slots, then
+ * replicas), so the gradient is deterministic.
+ *
+ * Checkpoints: (x, v) every C steps in the forward run.  The backward run
+ * recomputes one segment of C steps at a time from its checkpoint, keeping
+ * its positions, and sweeps the frames of the segment backwards.  Both runs
+ * force a list build at every checkpoint frame, so the recomputed
+ * trajectory is bit-identical to the forward one.
+ */
+#include <math.h>
+
+#include <algorithm>
+#include <vector>
+
+#include "md_pair.cuh"
+#include "md_thermo.cuh"
+
+namespace {
+
+constexpr int ADJ_TPA = 4;            /* lanes per atom in the adjoint pair kernels */
+constexpr int ADJ_MAXBINS = 512;
+constexpr double ADJ_HFIX = 1048576.0; /* 2^20: fixed point of the RDF kernel values */
+
+struct adj_par {
+    int cap, pitch, nbins, rdf_a, rdf_b, with_w;
+    float dr, sigma, inv_2s2, kn, rmaxsq, rdf_fac;
+    float wpe_k;   /* w_pe / (K + 1): the PE weight of one frame, per atom over N */
+};
+
+/* A row's per-neighbour-type parameter slots: lj1 terms, lj2 terms, then
+ * the charge scale. */
+template <int NT>
+struct adj_slots {
+    float p1[NT], p2[NT], ps;
+};
+
+/* RDF histogram of one frame: rows of type a, neighbours of type b inside
+ * rmax; kernel values in fixed point (2^-20) summed with integer atomics in
+ * shared memory, then into the replica's histogram. */
+__global__ void __launch_bounds__(MD_LA * ADJ_TPA) k_adj_rdf(adj_par ap, const int2 *__restrict__ tab,
+                                                           const md_rep *__restrict__ reps,
+                                                           const float4 *__restrict__ pos4,
+                                                           const int *__restrict__ type,
+                                                           const unsigned *__restrict__ nl,
+                                                           const int *__restrict__ nl_n,
+                                                           unsigned long long *hist)
+{
+    __shared__ unsigned long long sh[ADJ_MAXBINS];
+    for (int k = threadIdx.x; k < ap.nbins; k += blockDim.x) sh[k] = 0ull;
+    __syncthreads();
+    const int2 bt = tab[blockIdx.x];
+    const md_rep &R = reps[bt.x];
+    const geom_reg g = rep_geom(R);
+    const int a = threadIdx.x / ADJ_TPA, lane = threadIdx.x % ADJ_TPA;
+    const int i = bt.y + a;
+    if (i < R.atom0 + R.natom && type[i] == ap.rdf_a) {
+        const float4 pi = pos4[i];
+        const int cnt = nl_n[i];
+        const float reach = 5.0f * ap.sigma;
+        for (int k = lane; k < cnt; k += ADJ_TPA) {
+            const unsigned e = nl[(size_t)i * ap.cap + k];
+            if ((int)(e >> MD_TYPE_SHIFT) != ap.rdf_b) continue;
+            const float4 pj = pos4[e & MD_INDEX_MASK];
+            float dx = pi.x - pj.x, dy = pi.y - pj.y, dz = pi.z - pj.z;
+            dx -= g.L(0) * rint_small(dx * g.Li(0));
+            dy -= g.L(1) * rint_small(dy * g.Li(1));
+            dz -= g.L(2) * rint_small(dz * g.Li(2));
+            const float rsq = dx * dx + dy * dy + dz * dz;
+            if (rsq >= ap.rmaxsq || rsq == 0.0f) continue;
+            const float r = sqrtf(rsq);
+            int b0 = (int)ceilf((r - reach) / ap.dr - 0.5f), b1 = (int)floorf((r + reach) / ap.dr - 0.5f);
+            b0 = max(b0, 0);
+            b1 = min(b1, ap.nbins - 1);
+            for (int b = b0; b <= b1; b++) {
+                const float y = ((float)b + 0.5f) * ap.dr - r;
+                const float kv = ap.kn * __expf(-y * y * ap.inv_2s2);
+                atomicAdd(&sh[b], (unsigned long long)__float2uint_rn(kv * (float)ADJ_HFIX));
+            }
+        }
+    }
+    __syncthreads();
+    for (int k = threadIdx.x; k < ap.nbins; k += blockDim.x)
+        if (sh[k]) atomicAdd(&hist[(size_t)bt.x * ap.nbins + k], sh[k]);
+}
+
+/* Per-replica sum of the frame's potential energies (from the last
+ * velocity-Verlet reduction), one thread per replica. */
+__global__ void k_adj_pe(int nrep, const md_repstate *__restrict__ repst, double *pe_sum)
+{
+    int r = blockIdx.x * blockDim.x + threadIdx.x;
+    if (r < nrep) pe_sum[r] += repst[r].pe;
+}
+
+/* u += dt P (not at the last frame), w = f_m c u with c = dt/(2m) =
+ * kick/2 * 2^32; sorted-order w4, original-order P and u (3 per atom). */
+__global__ void k_adj_w(int n, double dt, int update, double fac, const int *__restrict__ perm,
+                        const double *__restrict__ kick, double *U, const double *__restrict__ Pv,
+                        float4 *w4)
+{
+    int s = blockIdx.x * blockDim.x + threadIdx.x;
+    if (s >= n) return;
+    const size_t o = 3 * (size_t)perm[s];
+    const double c = fac * 0.5 * kick[s] * FX_SCALE;
+    double u[3];
+    for (int d = 0; d < 3; d++) {
+        u[d] = U[o + d];
+        if (update) {
+            u[d] += dt * Pv[o + d];
+            U[o + d] = u[d];
+        }
+    }
+    w4[s] = make_float4((float)(c * u[0]), (float)(c * u[1]), (float)(c * u[2]), 0.0f);
+}
+
+/* P += G (sorted-order G, original-order P). */
+__global__ void k_adj_acc(int n, int pitch, const int *__restrict__ perm, const double *__restrict__ G,
+                          double *Pv)
+{
+    int s = blockIdx.x * blockDim.x + threadIdx.x;
+    if (s >= n) return;
+    const size_t o = 3 * (size_t)perm[s];
+    for (int d = 0; d < 3; d++) Pv[o + d] += G[(size_t)d * pitch + s];
+}
+
+/* The adjoint pair kernel of one frame: per atom i (ADJ_TPA lanes over its
+ * list row) G_i = J(x) w |_i - wpe F_i + d(sum_b e_b g_b)/dx_i, and the
+ * row's parameter slots; the block reduces its rows into (type, slot) sums
+ * in a fixed order.  ebn[b] = e_b norm_b kn / sigma^2 of the replica. */
+template <int KIND, int NT>
+__global__ void __launch_bounds__(MD_LA * ADJ_TPA) k_adj_back(
+    adj_par ap, const int2 *__restrict__ tab, const md_rep *__restrict__ reps,
+    const float2 *__restrict__ ljr, const float *__restrict__ ebn, const float4 *__restrict__ pos4,
+    const int *__restrict__ type, const unsigned *__restrict__ nl, const int *__restrict__ nl_n,
+    const float4 *__restrict__ w4, double *G, double *part)
+{
+    constexpr int NS = 2 * NT + 1;           /* slots of a row */
+    constexpr int NB = 2 * NT * NT + 1;      /* slots of a block: (type, slot) */
+    __shared__ float2 lj[MD_MAXTYPE * MD_MAXTYPE];
+    __shared__ float sb[ADJ_MAXBINS];
+    __shared__ float s_val[MD_LA][NS];
+    __shared__ int s_type[MD_LA];
+    const int2 bt = tab[blockIdx.x];
+    const md_rep &R = reps[bt.x];
+    if (threadIdx.x < MD_MAXTYPE * MD_MAXTYPE)
+        lj[threadIdx.x] = ljr[bt.x * MD_MAXTYPE * MD_MAXTYPE + threadIdx.x];
+    for (int k = threadIdx.x; k < ap.nbins; k += blockDim.x) sb[k] = ebn[(size_t)bt.x * ap.nbins + k];
+    const geom_reg g = rep_geom(R);
+    const float wpe = ap.wpe_k / (float)R.natom;
+    const float W = R.wolf, A = R.palfa;
+    const float spi = R.spiialfa;
+    const float alsq = -R.alfasq * 0.69314718f;   /* alpha^2 (alfasq = -alpha^2 / ln 2) */
+    __syncthreads();
+    const int a = threadIdx.x / ADJ_TPA, lane = threadIdx.x % ADJ_TPA;
+    const int i = bt.y + a;
+    const bool active = i < R.atom0 + R.natom;
+    const int ii = active ? i : bt.y;
+    const float4 pi = pos4[ii];
+    const int ti = type[ii];
+    const float qi = QFAC * pi.w;
+    const float4 wi = ap.with_w ? w4[ii] : make_float4(0.f, 0.f, 0.f, 0.f);
+    const bool ra = ti == ap.rdf_a, rb = ti == ap.rdf_b;
+    const float reach = 5.0f * ap.sigma;
+    float gx = 0.f, gy = 0.f, gz = 0.f;
+    adj_slots<NT> sl;
+#pragma unroll
+    for (int k = 0; k < NT; k++) { sl.p1[k] = 0.f; sl.p2[k] = 0.f; }
+    sl.ps = 0.f;
+    const int cnt = active ? nl_n[ii] : 0;
+    for (int k = lane; k < cnt; k += ADJ_TPA) {
+        const unsigned e = nl[(size_t)ii * ap.cap + k];
+        const int j = (int)(e & MD_INDEX_MASK), tj = (int)(e >> MD_TYPE_SHIFT);
+        const float4 pj = pos4[j];
+        float dx = pi.x - pj.x, dy = pi.y - pj.y, dz = pi.z - pj.z;
+        dx -= g.L(0) * rint_small(dx * g.Li(0));
+        dy -= g.L(1) * rint_small(dy * g.Li(1));
+        dz -= g.L(2) * rint_small(dz * g.Li(2));
+        const float rsq = dx * dx + dy * dy + dz * dz;
+        if (rsq > g.rcsq() || rsq == 0.0f) continue;
+        const float r = sqrtf(rsq), ri = 1.0f / r, ri2 = ri * ri;
+        const float qq = qi * pj.w;
+        float fc, dfc, uc;
+        if (KIND == 1) {
+            const float t = 1.0f / (1.0f + A * r);
+            const float P = (((A5 * t + A4) * t + A3) * t + A2) * t + A1;
+            const float dPt = (((5.0f * A5 * t + 4.0f * A4) * t + 3.0f * A3) * t + 2.0f * A2) * t + A1;
+            const float ex = __expf(-alsq * rsq);
+            const float E = P * t * ex;
+            const float dE = -dPt * A * t * t * ex - 2.0f * alsq * r * E;
+            const float h = spi * ex + E * ri;
+            const float dh = -2.0f * alsq * r * spi * ex + dE * ri - E * ri2;
+            fc = qq * (h - W) * ri2;
+            dfc = qq * (dh * ri2 - 2.0f * (h - W) * ri2 * ri);
+            uc = qq * (E * ri - g.ucc() + W * __logf(r * g.rcinv()));
+        } else {
+            fc = qq * (ri * ri2 - g.reacf());
+            dfc = -3.0f * qq * ri2 * ri2;
+            uc = qq * (ri + 0.5f * g.reacf() * rsq - g.ucc());
+        }
+        const float2 l = lj[ti * MD_MAXTYPE + tj];
+        const float ri6 = ri2 * ri2 * ri2, ri8 = ri6 * ri2, ri14 = ri6 * ri8;
+        const float ff = fc + l.x * ri14 - l.y * ri8;
+        const float gg = (dfc - 14.0f * l.x * ri14 * ri + 8.0f * l.y * ri8 * ri) * ri;
+        /* observable: - wpe F_i */
+        gx -= wpe * ff * dx;
+        gy -= wpe * ff * dy;
+        gz -= wpe * ff * dz;
+        float dwi = 0.0f;
+        if (ap.with_w) {
+            const float4 wj = w4[j];
+            const float ux = wi.x - wj.x, uy = wi.y - wj.y, uz = wi.z - wj.z;
+            const float dd = dx * ux + dy * uy + dz * uz;
+            gx += ff * ux + gg * dd * dx;
+            gy += ff * uy + gg * dd * dy;
+            gz += ff * uz + gg * dd * dz;
+            dwi = dx * wi.x + dy * wi.y + dz * wi.z;
+        }
+        /* RDF pairs (a, b) in either orientation */
+        if (((ra && tj == ap.rdf_b) || (rb && tj == ap.rdf_a)) && rsq < ap.rmaxsq) {
+            int b0 = (int)ceilf((r - reach) / ap.dr - 0.5f), b1 = (int)floorf((r + reach) / ap.dr - 0.5f);
+            b0 = max(b0, 0);
+            b1 = min(b1, ap.nbins - 1);
+            float coef = 0.0f;
+            for (int b = b0; b <= b1; b++) {
+                const float y = ((float)b + 0.5f) * ap.dr - r;
+                coef += sb[b] * y * __expf(-y * y * ap.inv_2s2);
+            }
+            coef *= ap.rdf_fac * ri;
+            gx += coef * dx;
+            gy += coef * dy;
+            gz += coef * dz;
+        }
+        /* parameter slots: dynamics (d.w_i) and the explicit PE derivative
+         * (half of the pair's energy belongs to this row) */
+        const float rc6i = g.rc6i();
+        const float v1 = ri14 * dwi + 0.5f * wpe * (ri6 * ri6 - rc6i * rc6i) * (1.0f / 12.0f);
+        const float v2 = -ri8 * dwi - 0.5f * wpe * (ri6 - rc6i) * (1.0f / 6.0f);
+#pragma unroll
+        for (int q = 0; q < NT; q++) {
+            sl.p1[q] += q == tj ? v1 : 0.0f;
+            sl.p2[q] += q == tj ? v2 : 0.0f;
+        }
+        sl.ps += 2.0f * fc * dwi + wpe * uc;
+    }
+    /* combine the lanes of the row (fixed order) */
+#pragma unroll
+    for (int off = ADJ_TPA / 2; off > 0; off >>= 1) {
+        gx += __shfl_down_sync(0xffffffffu, gx, off, ADJ_TPA);
+        gy += __shfl_down_sync(0xffffffffu, gy, off, ADJ_TPA);
+        gz += __shfl_down_sync(0xffffffffu, gz, off, ADJ_TPA);
+#pragma unroll
+        for (int q = 0; q < NT; q++) {
+            sl.p1[q] += __shfl_down_sync(0xffffffffu, sl.p1[q], off, ADJ_TPA);
+            sl.p2[q] += __shfl_down_sync(0xffffffffu, sl.p2[q], off, ADJ_TPA);
+        }
+        sl.ps += __shfl_down_sync(0xffffffffu, sl.ps, off, ADJ_TPA);
+    }
+    if (lane == 0) {
+        if (active) {
+            const size_t P = (size_t)ap.pitch;
+            G[i] = gx;
+            G[P + i] = gy;
+            G[2 * P + i] = gz;
+        }
+#pragma unroll
+        for (int q = 0; q < NT; q++) {
+            s_val[a][q] = active ? sl.p1[q] : 0.0f;
+            s_val[a][NT + q] = active ? sl.p2[q] : 0.0f;
+        }
+        s_val[a][2 * NT] = active ? sl.ps : 0.0f;
+        s_type[a] = active ? ti : -1;
+    }
+    __syncthreads();
+    /* block slots: (row type, neighbour type, lj1 | lj2) and the charge
+     * scale, each summed over the block's rows in order */
+    if (threadIdx.x < NB) {
+        const int k = threadIdx.x;
+        double acc = 0.0;
+        if (k == NB - 1) {
+            for (int r2 = 0; r2 < MD_LA; r2++) acc += (double)s_val[r2][2 * NT];
+        } else {
+            const int tt = k / (2 * NT), rem = k % (2 * NT);   /* row type, slot */
+            for (int r2 = 0; r2 < MD_LA; r2++)
+                if (s_type[r2] == tt) acc += (double)s_val[r2][rem];
+        }
+        part[(size_t)blockIdx.x * NB + k] = acc;
+    }
+}
+
+/* Per replica and block slot: the replica's blocks summed in order, added
+ * to its gradient accumulators. */
+__global__ void k_adj_param(int nrep, int nb_slots, const md_rep *__restrict__ reps,
+                            const double *__restrict__ part, double *acc)
+{
+    int t = blockIdx.x * blockDim.x + threadIdx.x;
+    if (t >= nrep * nb_slots) return;
+    const int r = t / nb_slots, k = t % nb_slots;
+    const md_rep &R = reps[r];
+    double s = 0.0;
+    for (int b = 0; b < R.nblk; b++) s += part[(size_t)(R.blk0 + b) * nb_slots + k];
+    acc[t] += s;
+}
+
+template <int KIND, int NT>
+void launch_back_nt(md_ctx *c, const adj_par &ap, const float *ebn, const float4 *w4, double *G,
+                    double *part)
+{
+    const int k = md_grid_index(MD_LA);
+    k_adj_back<KIND, NT><<<c->grid_cnt[k], MD_LA * ADJ_TPA, 0, c->stream>>>(
+        ap, c->grid_tab + c->grid_off[k], c->reps_dev, c->ljr_dev, ebn, c->pos4, c->type, c->nl,
+        c->nl_n, w4, G, part);
+}
+
+int adj_nt(int ntype) { return ntype <= 1 ? 1 : (ntype <= 2 ? 2 : (ntype <= 4 ? 4 : 8)); }
+
+void launch_back(md_ctx *c, const adj_par &ap, const float *ebn, const float4 *w4, double *G,
+                 double *part)
+{
+    const int nt = adj_nt(c->ntype);
+#define MD_ADJ_NT(K, N) \
+    if (c->lkspace == K && nt == N) { launch_back_nt<K == 0 ? 0 : 1, N>(c, ap, ebn, w4, G, part); return; }
+    MD_ADJ_NT(0, 1) MD_ADJ_NT(0, 2) MD_ADJ_NT(0, 4) MD_ADJ_NT(0, 8)
+    MD_ADJ_NT(1, 1) MD_ADJ_NT(1, 2) MD_ADJ_NT(1, 4) MD_ADJ_NT(1, 8)
+    MD_ADJ_NT(2, 1) MD_ADJ_NT(2, 2) MD_ADJ_NT(2, 4) MD_ADJ_NT(2, 8)
+#undef MD_ADJ_NT
+}
+
+/* Device buffers of one adjoint run. */
+struct adj_buffers {
+    double *ck_x = nullptr, *ck_v = nullptr;   /* checkpoints, original order (3n each) */
+    double *seg = nullptr;                     /* positions of one segment's frames */
+    double *xK = nullptr, *vK = nullptr;       /* the final state */
+    double *P = nullptr, *U = nullptr, *G = nullptr, *pe_sum = nullptr, *part = nullptr,
+           *acc = nullptr;
+    float4 *w4 = nullptr;
+    float *ebn = nullptr;
+    unsigned long long *hist = nullptr;
+    ~adj_buffers()
+    {
+        void *p[] = {ck_x, ck_v, seg, xK, vK, P, U, G, pe_sum, part, acc, w4, ebn, hist};
+        for (void *q : p)
+            if (q) cudaFree(q);
+    }
+};
+
+template <class T>
+cudaError_t adj_alloc(T **p, size_t count)
+{
+    return cudaMalloc((void **)p, sizeof(T) * std::max<size_t>(count, 1));
+}
+
+}  // namespace
+
+extern "C" md_status md_adjoint_run(md_ctx *c, const md_adjoint_cfg *cfg, const double *target,
+                                    double *loss, double *gbar, double *dlj1, double *dlj2,
+                                    double *dlns)
+{
+    if (!c || !cfg || !loss) return MD_ERR_ARG;
+    if (!c->batch || c->integrator != MD_VV || c->enstype != 0) {
+        c->last_error = "md_adjoint_run: needs a batch context with velocity Verlet NVE";
+        return MD_ERR_UNSUPPORTED;
+    }
+    const int K = cfg->nsteps, C = cfg->checkpoint > 0 ? cfg->checkpoint : 50;
+    const int nb = cfg->nbins, nrep = c->nrep, n = c->n;
+    if (K < 1 || nb < 1 || nb > ADJ_MAXBINS || cfg->rdf_dr <= 0 || cfg->rdf_sigma <= 0 ||
+        cfg->rdf_a < 0 || cfg->rdf_b < 0 || cfg->rdf_a >= c->ntype || cfg->rdf_b >= c->ntype ||
+        (cfg->gradient && (!dlj1 || !dlj2 || !dlns))) {
+        c->last_error = "md_adjoint_run: invalid configuration";
+        return MD_ERR_ARG;
+    }
+    const double rmax = nb * cfg->rdf_dr + 5.0 * cfg->rdf_sigma;
+    for (const md_rep &R : c->reps)
+        if (rmax * rmax > (double)R.rcutsq) {
+            c->last_error = "md_adjoint_run: RDF range beyond a replica's cutoff";
+            return MD_ERR_ARG;
+        }
+    const int nseg = (K + C - 1) / C;
+    const int nt = adj_nt(c->ntype), NB = 2 * nt * nt + 1;
+    const int kla = md_grid_index(MD_LA), nblk = c->grid_cnt[kla];
+    adj_buffers B;
+    MD_CUDA_TRY(c, adj_alloc(&B.ck_x, 3 * (size_t)n * (nseg + 1)));
+    MD_CUDA_TRY(c, adj_alloc(&B.ck_v, 3 * (size_t)n * (nseg + 1)));
+    MD_CUDA_TRY(c, adj_alloc(&B.seg, 3 * (size_t)n * (C + 1)));
+    MD_CUDA_TRY(c, adj_alloc(&B.xK, 3 * (size_t)n));
+    MD_CUDA_TRY(c, adj_alloc(&B.vK, 3 * (size_t)n));
+    MD_CUDA_TRY(c, adj_alloc(&B.P, 3 * (size_t)n));
+    MD_CUDA_TRY(c, adj_alloc(&B.U, 3 * (size_t)n));
+    MD_CUDA_TRY(c, adj_alloc(&B.G, 3 * (size_t)c->pitch));
+    MD_CUDA_TRY(c, adj_alloc(&B.pe_sum, nrep));
+    MD_CUDA_TRY(c, adj_alloc(&B.part, (size_t)nblk * NB));
+    MD_CUDA_TRY(c, adj_alloc(&B.acc, (size_t)nrep * NB));
+    MD_CUDA_TRY(c, adj_alloc(&B.w4, c->pitch));
+    MD_CUDA_TRY(c, adj_alloc(&B.ebn, (size_t)nrep * nb));
+    MD_CUDA_TRY(c, adj_alloc(&B.hist, (size_t)nrep * nb));
+    cudaStream_t s = c->stream;
+    MD_CUDA_TRY(c, cudaMemsetAsync(B.hist, 0, sizeof(unsigned long long) * nrep * nb, s));
+    MD_CUDA_TRY(c, cudaMemsetAsync(B.pe_sum, 0, sizeof(double) * nrep, s));
+
+    adj_par ap;
+    ap.cap = c->cap;
+    ap.pitch = c->pitch;
+    ap.nbins = nb;
+    ap.rdf_a = cfg->rdf_a;
+    ap.rdf_b = cfg->rdf_b;
+    ap.with_w = 0;
+    ap.dr = (float)cfg->rdf_dr;
+    ap.sigma = (float)cfg->rdf_sigma;
+    ap.inv_2s2 = (float)(0.5 / (cfg->rdf_sigma * cfg->rdf_sigma));
+    ap.kn = (float)(1.0 / (sqrt(2.0 * M_PI) * cfg->rdf_sigma));
+    ap.rmaxsq = (float)(rmax * rmax);
+    ap.rdf_fac = cfg->rdf_a == cfg->rdf_b ? 2.0f : 1.0f;
+    ap.wpe_k = (float)(cfg->w_pe / (K + 1));
+    const int rgrid = (nrep + 255) / 256;
+    const int agrid = (n + 255) / 256;
+
+    md_kparams kp = md_make_kparams(c);
+    auto obs = [&]() {
+        k_adj_rdf<<<nblk, MD_LA * ADJ_TPA, 0, s>>>(ap, c->grid_tab + c->grid_off[kla], c->reps_dev,
+                                                  c->pos4, c->type, c->nl, c->nl_n, B.hist);
+        k_adj_pe<<<rgrid, 256, 0, s>>>(nrep, c->repst, B.pe_sum);
+    };
+    auto save = [&](double *x, double *v) {
+        launch_gather_out(c, kp, 0, c->io_dev);
+        cudaMemcpyAsync(x, c->io_dev, sizeof(double) * 3 * n, cudaMemcpyDeviceToDevice, s);
+        if (v) {
+            launch_gather_out(c, kp, 1, c->io_dev);
+            cudaMemcpyAsync(v, c->io_dev, sizeof(double) * 3 * n, cudaMemcpyDeviceToDevice, s);
+        }
+    };
+    /* one VV step, the list forced at checkpoint frames */
+    auto step = [&](int s_idx) {
+        launch_vv_first(c, kp, 0, 0);
+        launch_rebuild(c, kp, (s_idx + 1) % C == 0, (s_idx + 1) % C == 0);
+        launch_forces(c, kp, true, MD_TERM_ALL);
+        launch_vv_second(c, kp, 1);
+    };
+
+    /* ---- forward ---- */
+    launch_rebuild(c, kp, true, true);
+    launch_forces(c, kp, true, MD_TERM_ALL);
+    launch_thermo_from_state(c, kp, 1);
+    obs();
+    save(B.ck_x, B.ck_v);
+    for (int st = 0; st < K; st++) {
+        step(st);
+        obs();
+        if ((st + 1) % C == 0) save(B.ck_x + 3 * (size_t)n * ((st + 1) / C), B.ck_v + 3 * (size_t)n * ((st + 1) / C));
+    }
+    save(B.xK, B.vK);
+    std::vector<unsigned long long> hh((size_t)nrep * nb);
+    std::vector<double> pes(nrep);
+    MD_CUDA_TRY(c, cudaMemcpyAsync(hh.data(), B.hist, sizeof(unsigned long long) * hh.size(),
+                                   cudaMemcpyDeviceToHost, s));
+    MD_CUDA_TRY(c, cudaMemcpyAsync(pes.data(), B.pe_sum, sizeof(double) * nrep, cudaMemcpyDeviceToHost, s));
+    MD_CUDA_TRY(c, cudaStreamSynchronize(s));
+    MD_CUDA_TRY(c, cudaGetLastError());
+    std::vector<float> ebn((size_t)nrep * nb);
+    for (int r = 0; r < nrep; r++) {
+        const md_rep &R = c->reps[r];
+        int na = 0, nbt = 0;
+        for (int i = 0; i < R.natom; i++) {
+            na += c->itype[R.atom0 + i] == cfg->rdf_a;
+            nbt += c->itype[R.atom0 + i] == cfg->rdf_b;
+        }
+        const double V = (double)R.box[0] * R.box[1] * R.box[2];
+        double L = cfg->w_pe * pes[r] / (K + 1) / R.natom;
+        for (int b = 0; b < nb; b++) {
+            const double rb = (b + 0.5) * cfg->rdf_dr;
+            const double norm = (na > 0 && nbt > 0) ? V / ((double)na * nbt * 4.0 * M_PI * rb * rb) : 0.0;
+            const double g = norm * (double)hh[(size_t)r * nb + b] / ADJ_HFIX / (K + 1);
+            const double t = target ? target[(size_t)r * nb + b] : 0.0;
+            L += cfg->w_rdf * (g - t) * (g - t);
+            if (gbar) gbar[(size_t)r * nb + b] = g;
+            const double e = cfg->w_rdf * 2.0 * (g - t) / (K + 1);
+            ebn[(size_t)r * nb + b] = (float)(e * norm / (sqrt(2.0 * M_PI) * cfg->rdf_sigma) /
+                                              (cfg->rdf_sigma * cfg->rdf_sigma));
+        }
+        loss[r] = L;
+    }
+    if (!cfg->gradient) return MD_OK;
+
+    /* ---- backward ---- */
+    MD_CUDA_TRY(c, cudaMemcpyAsync(B.ebn, ebn.data(), sizeof(float) * ebn.size(), cudaMemcpyHostToDevice, s));
+    MD_CUDA_TRY(c, cudaMemsetAsync(B.P, 0, sizeof(double) * 3 * n, s));
+    MD_CUDA_TRY(c, cudaMemsetAsync(B.U, 0, sizeof(double) * 3 * n, s));
+    MD_CUDA_TRY(c, cudaMemsetAsync(B.acc, 0, sizeof(double) * nrep * NB, s));
+    for (int sg = nseg - 1; sg >= 0; sg--) {
+        const int m0 = sg * C, m1 = std::min(K, m0 + C);
+        /* recompute the segment from its checkpoint, as the forward run did */
+        launch_scatter_in(c, kp, 0, B.ck_x + 3 * (size_t)n * sg);
+        launch_scatter_in(c, kp, 1, B.ck_v + 3 * (size_t)n * sg);
+        launch_rebuild(c, kp, true, true);
+        launch_forces(c, kp, true, MD_TERM_ALL);
+        MD_CUDA_TRY(c, cudaMemcpyAsync(B.seg, B.ck_x + 3 * (size_t)n * sg, sizeof(double) * 3 * n,
+                                       cudaMemcpyDeviceToDevice, s));
+        for (int st = m0; st < m1; st++) {
+            step(st);
+            launch_gather_out(c, kp, 0, c->io_dev);
+            MD_CUDA_TRY(c, cudaMemcpyAsync(B.seg + 3 * (size_t)n * (st + 1 - m0), c->io_dev,
+                                           sizeof(double) * 3 * n, cudaMemcpyDeviceToDevice, s));
+        }
+        /* sweep the segment's frames backwards (its last frame belongs to
+         * the later segment, except at the end of the trajectory) */
+        for (int m = (m1 == K ? m1 : m1 - 1); m >= m0; m--) {
+            launch_scatter_in(c, kp, 0, B.seg + 3 * (size_t)n * (m - m0));
+            launch_check(c, kp);
+            launch_rebuild(c, kp, false, false);
+            ap.with_w = m < K ? 1 : 0;
+            if (m < K)
+                k_adj_w<<<agrid, 256, 0, s>>>(n, (double)c->dt, 1, m >= 1 ? 2.0 : 1.0, c->perm, c->kick,
+                                               B.U, B.P, B.w4);
+            launch_back(c, ap, B.ebn, B.w4, B.G, B.part);
+            k_adj_param<<<(nrep * NB + 255) / 256, 256, 0, s>>>(nrep, NB, c->reps_dev, B.part, B.acc);
+            k_adj_acc<<<agrid, 256, 0, s>>>(n, c->pitch, c->perm, B.G, B.P);
+        }
+    }
+    std::vector<double> acc((size_t)nrep * NB);
+    MD_CUDA_TRY(c, cudaMemcpyAsync(acc.data(), B.acc, sizeof(double) * acc.size(), cudaMemcpyDeviceToHost, s));
+    /* leave the context at the end of the trajectory */
+    launch_scatter_in(c, kp, 0, B.xK);
+    launch_scatter_in(c, kp, 1, B.vK);
+    launch_rebuild(c, kp, true, true);
+    launch_forces(c, kp, true, MD_TERM_ALL);
+    launch_thermo_from_state(c, kp, 1);
+    MD_CUDA_TRY(c, cudaStreamSynchronize(s));
+    MD_CUDA_TRY(c, cudaGetLastError());
+    for (int r = 0; r < nrep; r++) {
+        const double *a = acc.data() + (size_t)r * NB;
+        for (int k = 0; k < MD_MAXTYPE * MD_MAXTYPE; k++) {
+            dlj1[(size_t)r * MD_MAXTYPE * MD_MAXTYPE + k] = 0.0;
+            dlj2[(size_t)r * MD_MAXTYPE * MD_MAXTYPE + k] = 0.0;
+        }
+        for (int ti = 0; ti < nt; ti++)
+            for (int tj = 0; tj < nt; tj++) {
+                dlj1[(size_t)r * MD_MAXTYPE * MD_MAXTYPE + ti * MD_MAXTYPE + tj] = a[ti * 2 * nt + tj];
+                dlj2[(size_t)r * MD_MAXTYPE * MD_MAXTYPE + ti * MD_MAXTYPE + tj] = a[ti * 2 * nt + nt + tj];
+            }
+        dlns[r] = a[NB - 1];
+    }
+    return MD_OK;
+}

@@ -18,25 +18,6 @@
 
 namespace {
 
-__device__ __forceinline__ geom_reg rep_geom(const md_rep &R)
-{
-    geom_reg g;
-    for (int d = 0; d < 3; d++) {
-        g.L_[d] = R.box[d];
-        g.Li_[d] = R.boxi[d];
-    }
-    g.rcsq_ = R.rcutsq;
-    g.reacf_ = R.reacf;
-    g.palfa_ = R.palfa;
-    g.spiialfa_ = R.spiialfa;
-    g.alfasq_ = R.alfasq;
-    g.wolf_ = R.wolf;
-    g.ucc_ = R.ucc;
-    g.rc6i_ = R.rc6i;
-    g.rcinv_ = R.rcinv;
-    return g;
-}
-
 /* Pair forces of a batch: block b holds 128/TPA atoms of replica tab[b].x
  * starting at tab[b].y. */
 template <int KIND, int TPA, int B, bool ENERGY>

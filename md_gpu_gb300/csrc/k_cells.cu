@@ -561,7 +561,7 @@ __global__ void __launch_bounds__(CW_WARPS * 32) k_build_cells(
 void launch_check(md_ctx *c, const md_kparams &kp)
 {
     int nb = (kp.n + 255) / 256;
-    if (c->nrep > 1) {
+    if (c->batch) {
         k_check_b<<<nb, 256, 0, c->stream>>>(kp.n, c->reps_dev, c->arep, c->pos4, c->pos_old, c->st,
                                              c->rep_upd);
         return;
@@ -574,7 +574,7 @@ void launch_rebuild(md_ctx *c, const md_kparams &kp, bool unconditional, bool al
     int always = unconditional ? 1 : 0;
     int nb = (kp.n + 255) / 256;
     cudaStream_t s = c->stream;
-    const bool batch = c->nrep > 1;
+    const bool batch = c->batch;
     const int rb = (c->nrep + 255) / 256;
     const int *arep = batch ? c->arep : nullptr;
     const int *crep = batch ? c->crep : nullptr;

@@ -151,7 +151,7 @@ void pair_dispatch(md_ctx *c, const md_kparams &kp, const pair_consts &pc)
 
 void launch_forces(md_ctx *c, const md_kparams &kp, bool energy, int terms)
 {
-    if (c->nrep > 1) {
+    if (c->batch) {
         launch_forces_b(c, kp, energy, terms);
         return;
     }

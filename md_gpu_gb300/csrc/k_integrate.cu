@@ -207,7 +207,7 @@ __global__ void k_scatter_in(md_kparams kp, int what, md_devstate *st, md_repsta
 
 void launch_leapfrog(md_ctx *c, const md_kparams &kp, int energy, unsigned long long cond, int has_cond)
 {
-    if (c->nrep > 1) {
+    if (c->batch) {
         launch_leapfrog_b(c, kp, energy, cond, has_cond);
         return;
     }
@@ -219,7 +219,7 @@ void launch_leapfrog(md_ctx *c, const md_kparams &kp, int energy, unsigned long 
 
 void launch_vv_first(md_ctx *c, const md_kparams &kp, unsigned long long cond, int has_cond)
 {
-    if (c->nrep > 1) {
+    if (c->batch) {
         launch_vv_first_b(c, kp, cond, has_cond);
         return;
     }
@@ -231,7 +231,7 @@ void launch_vv_first(md_ctx *c, const md_kparams &kp, unsigned long long cond, i
 
 void launch_vv_second(md_ctx *c, const md_kparams &kp, int energy)
 {
-    if (c->nrep > 1) {
+    if (c->batch) {
         launch_vv_second_b(c, kp, energy, 1);
         return;
     }
@@ -243,7 +243,7 @@ void launch_vv_second(md_ctx *c, const md_kparams &kp, int energy)
 
 void launch_thermo_from_state(md_ctx *c, const md_kparams &kp, int energy)
 {
-    if (c->nrep > 1) {
+    if (c->batch) {
         launch_vv_second_b(c, kp, energy, 0);
         return;
     }
@@ -256,7 +256,7 @@ void launch_thermo_from_state(md_ctx *c, const md_kparams &kp, int energy)
 void launch_gather_out(md_ctx *c, const md_kparams &kp, int what, void *dst)
 {
     int nb = (kp.n + 255) / 256;
-    k_gather_out<<<nb, 256, 0, c->stream>>>(kp, what, c->st, c->nrep > 1 ? c->repst : nullptr,
+    k_gather_out<<<nb, 256, 0, c->stream>>>(kp, what, c->st, c->batch ? c->repst : nullptr,
                                             c->arep, c->perm, c->x, c->v, c->f, c->vir, c->epot,
                                             (double *)dst);
 }
@@ -265,7 +265,7 @@ void launch_scatter_in(md_ctx *c, const md_kparams &kp, int what, const void *sr
 {
     int nb = (kp.n + 255) / 256;
     int nbs = std::max(nb, (c->nrep + 255) / 256);
-    k_scatter_in<<<nbs, 256, 0, c->stream>>>(kp, what, c->st, c->nrep > 1 ? c->repst : nullptr,
+    k_scatter_in<<<nbs, 256, 0, c->stream>>>(kp, what, c->st, c->batch ? c->repst : nullptr,
                                              c->nrep, c->iperm, (const double *)src, c->x, c->v,
                                              c->pos4);
 }

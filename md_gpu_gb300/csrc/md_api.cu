@@ -533,7 +533,7 @@ md_status setup_device(md_ctx *c, void *stream, host_stage &h, md_ctx **out)
     cudaGetDevice(&c->device);
     const size_t P = c->pitch;
     const int n = c->n;
-    const bool batch = c->nrep > 1;
+    const bool batch = c->batch;
     /* block partials of the integrators (256 threads; one grid per replica
      * in a batch) and of the fused step (128 threads, up to 32 per atom) */
     size_t npart = 3 * (P / 4 + 256) + 8;
@@ -665,7 +665,7 @@ int md_cell_shift(const int stencil[3], const float binlen[3], const float box[3
 
 int md_ndf(const md_ctx *c)
 {
-    if (c->nrep > 1) {
+    if (c->batch) {
         long long s = 0;
         for (const md_rep &r : c->reps) s += r.ndf;
         return (int)s;
@@ -897,7 +897,7 @@ md_status md_create(const md_system_desc *d, void *stream, md_ctx **out)
 md_status md_create_batch(const md_system_desc *descs, int nrep, void *stream, md_ctx **out)
 {
     if (!descs || !out || nrep < 1) return fail(nullptr, MD_ERR_ARG, "md_create_batch: null argument");
-    if (nrep == 1) return md_create(descs, stream, out);
+
     const md_system_desc &d0 = descs[0];
     long long ntot = 0;
     int ntype = 1, nmax = 0;
@@ -932,6 +932,7 @@ md_status md_create_batch(const md_system_desc *descs, int nrep, void *stream, m
     md_ctx *c = new (std::nothrow) md_ctx();
     if (!c) return fail(nullptr, MD_ERR_ARG, "out of host memory");
     const int n = (int)ntot;
+    c->batch = 1;
     c->nrep = nrep;
     c->n = n;
     c->ntype = ntype;
@@ -1079,7 +1080,7 @@ md_status md_create_batch(const md_system_desc *descs, int nrep, void *stream, m
 md_status md_get_replica_thermo(md_ctx *c, md_thermo *out, int nrep)
 {
     if (!c || !out || nrep < 1) return MD_ERR_ARG;
-    if (c->nrep == 1) return md_get_thermo(c, out);
+    if (!c->batch) return md_get_thermo(c, out);
     MD_CUDA_TRY(c, cudaStreamSynchronize(c->stream));
     md_devstate h;
     MD_CUDA_TRY(c, cudaMemcpy(&h, c->st, sizeof(h), cudaMemcpyDeviceToHost));
@@ -1375,7 +1376,7 @@ md_status md_run_host(md_ctx *c, double *pos3, double *vel3, int nsteps, int ene
 md_status md_write_cfg(md_ctx *c, const char *path)
 {
     if (!c || !path) return MD_ERR_ARG;
-    if (c->nrep > 1) return fail(c, MD_ERR_UNSUPPORTED, "md_write_cfg: a batch holds several boxes");
+    if (c->batch) return fail(c, MD_ERR_UNSUPPORTED, "md_write_cfg: a batch holds several boxes");
     std::vector<double> p(3 * (size_t)c->n), v(3 * (size_t)c->n);
     md_status s = md_get_positions(c, p.data());
     if (s == MD_OK) s = md_get_velocities(c, v.data());
@@ -1421,7 +1422,7 @@ md_status md_get_info(md_ctx *c, md_info *out)
     /* single system: key, scan, scatter, order, permute, copyback, remap,
      * list, clear; batch: key, scan, scatter, order, permute, copyback,
      * list, clear */
-    out->kernels_per_rebuild = c->nrep > 1 ? 8 : 9;
+    out->kernels_per_rebuild = c->batch ? 8 : 9;
     out->kernels_per_graph = c->integrator == MD_LEAPFROG ? 1 : 0;
     return MD_OK;
 }
@@ -1489,7 +1490,7 @@ md_status md_autotune(md_ctx *c, int *pair_tpa, int *list_tpa)
     c->fuse_step = bf;
     best = 1e30f;
     for (int t : lt) {
-        if (c->nrep > 1 && t != 0) continue;   /* batches build one warp per cell */
+        if (c->batch && t != 0) continue;   /* batches build one warp per cell */
         c->list_tpa = t;
         float ms = 0.0f, m2 = 0.0f;
         md_status s = md_time_rebuild(c, 2, &ms);
@@ -1519,7 +1520,7 @@ md_status md_set_tuning(md_ctx *c, int pair_tpa, int list_tpa)
     if (!c) return MD_ERR_ARG;
     auto ok = [](int t) { return t == 1 || t == 2 || t == 4 || t == 8 || t == 16 || t == 32; };
     if (!ok(pair_tpa) || !(list_tpa == 0 || ok(list_tpa))) return MD_ERR_ARG;
-    if (c->nrep > 1 && list_tpa != 0)
+    if (c->batch && list_tpa != 0)
         return fail(c, MD_ERR_ARG, "md_set_tuning: a batch builds its lists one warp per cell");
     c->pair_tpa = pair_tpa;
     c->list_tpa = list_tpa;

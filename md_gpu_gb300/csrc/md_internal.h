@@ -192,7 +192,8 @@ struct md_ctx {
     int pair_tpa = 8;    /* threads per atom in the pair kernel */
     int list_tpa = 0;    /* list build: 0 = one warp per cell, else threads per atom */
 
-    /* batches of replicas (nrep > 1; md_create_batch) */
+    /* batches of replicas (md_create_batch; any number, 1 included) */
+    int batch = 0;
     int nrep = 1;
     std::vector<md_rep> reps;
     std::vector<int> rep_natom;
@@ -270,7 +271,7 @@ bool md_can_fuse(const md_ctx *c);
 void launch_pair_leapfrog(md_ctx *c, const md_kparams &kp, unsigned long long cond, int has_cond);
 
 /* ---- launchers of batches (k_batch.cu); the launchers above forward to
- * these when c->nrep > 1 (the list kernels of a batch live in k_cells.cu) ---- */
+ * these for batch contexts (the list kernels of a batch live in k_cells.cu) ---- */
 void launch_forces_b(md_ctx *c, const md_kparams &kp, bool energy, int terms);
 void launch_leapfrog_b(md_ctx *c, const md_kparams &kp, int energy, unsigned long long cond,
                        int has_cond);

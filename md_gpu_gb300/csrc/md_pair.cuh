@@ -96,6 +96,26 @@ struct geom_reg {
     __device__ __forceinline__ float rcinv() const { return rcinv_; }
 };
 
+/* The register geometry of one replica of a batch. */
+__device__ __forceinline__ geom_reg rep_geom(const md_rep &R)
+{
+    geom_reg g;
+    for (int d = 0; d < 3; d++) {
+        g.L_[d] = R.box[d];
+        g.Li_[d] = R.boxi[d];
+    }
+    g.rcsq_ = R.rcutsq;
+    g.reacf_ = R.reacf;
+    g.palfa_ = R.palfa;
+    g.spiialfa_ = R.spiialfa;
+    g.alfasq_ = R.alfasq;
+    g.wolf_ = R.wolf;
+    g.ucc_ = R.ucc;
+    g.rc6i_ = R.rc6i;
+    g.rcinv_ = R.rcinv;
+    return g;
+}
+
 /* One pair: F_i += ff d, w_i += ff r^2 (pair_forces.cu:165-200 / :74-120). */
 template <int KIND, bool ENERGY, class G>
 __device__ __forceinline__ void pair_term(const G &g, float4 pi, float qi, float4 pj, float2 l,

@@ -55,6 +55,12 @@ class Thermo(C.Structure):
         return {k: getattr(self, k) for k, _ in self._fields_}
 
 
+class AdjointCfg(C.Structure):
+    _fields_ = [("nsteps", C.c_int), ("checkpoint", C.c_int), ("gradient", C.c_int),
+                ("w_pe", C.c_double), ("w_rdf", C.c_double), ("rdf_a", C.c_int), ("rdf_b", C.c_int),
+                ("nbins", C.c_int), ("rdf_dr", C.c_double), ("rdf_sigma", C.c_double)]
+
+
 class Info(C.Structure):
     _fields_ = [("natom", C.c_int), ("pitch", C.c_int), ("capacity", C.c_int),
                 ("ncell", C.c_int * 3), ("stencil", C.c_int * 3), ("binlen", C.c_float * 3),
@@ -148,6 +154,7 @@ def library(path: Optional[str] = None):
     L.md_ref_kinetic_energy_noalloc.argtypes = [vp, C.c_int, vp, vp]
     L.md_create_batch.argtypes = [C.POINTER(SystemDesc), C.c_int, vp, C.POINTER(vp)]
     L.md_get_replica_thermo.argtypes = [vp, C.POINTER(Thermo), C.c_int]
+    L.md_adjoint_run.argtypes = [vp, C.POINTER(AdjointCfg), vp, vp, vp, vp, vp, vp]
     _lib = L
     return L
 
@@ -240,6 +247,34 @@ class MDSystem:
         buf = (Thermo * n)()
         _check(library().md_get_replica_thermo(self._ctx, buf, n), self._ctx)
         return [buf[i].as_dict() for i in range(n)]
+
+    def adjoint(self, nsteps, checkpoint=50, w_pe=1.0, w_rdf=1.0, rdf_types=(0, 1), nbins=200,
+                dr=0.05, sigma=0.05, target=None, gradient=True):
+        """Loss of the next `nsteps` velocity-Verlet steps of a batch and its
+        adjoint gradient (md_adjoint_run).  Returns a dict with per-replica
+        'loss' (nrep,), 'gbar' (nrep, nbins) and, with gradient, 'dlj1',
+        'dlj2' (nrep, 8, 8; entry [a, b] as used by atoms of type a) and
+        'dlns' (nrep,).  The system advances by nsteps steps."""
+        nrep = len(getattr(self, "replica_sizes", [self.natom]))
+        cfg = AdjointCfg(nsteps=int(nsteps), checkpoint=int(checkpoint), gradient=1 if gradient else 0,
+                         w_pe=float(w_pe), w_rdf=float(w_rdf), rdf_a=int(rdf_types[0]),
+                         rdf_b=int(rdf_types[1]), nbins=int(nbins), rdf_dr=float(dr),
+                         rdf_sigma=float(sigma))
+        loss = np.zeros(nrep)
+        gbar = np.zeros((nrep, nbins))
+        d1 = np.zeros((nrep, 8, 8))
+        d2 = np.zeros((nrep, 8, 8))
+        ds = np.zeros(nrep)
+        tg = None
+        if target is not None:
+            tg = np.ascontiguousarray(np.broadcast_to(np.asarray(target, np.float64), (nrep, nbins)))
+        _check(library().md_adjoint_run(self._ctx, C.byref(cfg), tg.ctypes.data if tg is not None else None,
+                                        loss.ctypes.data, gbar.ctypes.data, d1.ctypes.data,
+                                        d2.ctypes.data, ds.ctypes.data), self._ctx)
+        out = {"loss": loss, "gbar": gbar}
+        if gradient:
+            out.update(dlj1=d1, dlj2=d2, dlns=ds)
+        return out
 
     def close(self):
         if self._ctx:

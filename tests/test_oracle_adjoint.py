@@ -57,3 +57,31 @@ def test_adjoint_loss_is_forward_loss():
     assert l0 == l1
     assert np.array_equal(g, g1)
     assert abs(l0 - (pe / len(prob.itype) + (g * g).sum())) <= 1e-9 * abs(l0)
+
+
+def test_lorentz_berthelot_chain_rule():
+    """Table-entry gradients mapped to per-type eps and sigma agree with
+    central differences in eps / sigma space."""
+    from md_gpu_gb300 import params
+    prob = _problem(nsteps=8)
+    eps = np.array([0.13, 0.10]) * 4.184
+    sig = np.array([2.35, 4.40])
+    l1, l2 = params.lb_tables(eps, sig)
+    prob.lj1, prob.lj2 = l1, l2
+    _, g, _ = oracle.adj_loss(prob)
+    tg = 1.05 * g
+    _, d1, d2, _, _ = oracle.adj_grad(prob, tg)
+    de, ds = params.lb_chain(d1, d2, eps, sig)
+    h = 1e-6
+    for k in range(2):
+        for arr, ad in ((eps, de), (sig, ds)):
+            p, m = arr.copy(), arr.copy()
+            p[k] *= 1 + h
+            m[k] *= 1 - h
+            if arr is eps:
+                lp, lm = params.lb_tables(p, sig), params.lb_tables(m, sig)
+            else:
+                lp, lm = params.lb_tables(eps, p), params.lb_tables(eps, m)
+            fd = (oracle.adj_loss(prob, tg, lj1=lp[0], lj2=lp[1])[0] -
+                  oracle.adj_loss(prob, tg, lj1=lm[0], lj2=lm[1])[0]) / (2 * h * arr[k])
+            assert abs(fd - ad[k]) <= 1e-4 * abs(fd), (k, fd, ad[k])
