@@ -134,7 +134,7 @@ typedef struct {
     int gradient;       /* 0: forward pass only (loss, gbar) */
     double w_pe, w_rdf; /* loss weights */
     int rdf_a, rdf_b;   /* atom types of the RDF pair (0-based) */
-    int nbins;          /* <= 512 */
+    int nbins;          /* <= 256 */
     double rdf_dr, rdf_sigma;   /* A */
 } md_adjoint_cfg;
 md_status md_adjoint_run(md_ctx *ctx, const md_adjoint_cfg *cfg, const double *target, double *loss,

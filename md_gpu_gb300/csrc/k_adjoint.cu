@@ -39,7 +39,9 @@
 
 namespace {
 
-constexpr int ADJ_TPA = 4;            /* lanes per atom in the adjoint pair kernels */
+constexpr int ADJ_TPA = 8;            /* lanes per atom in the adjoint pair kernels */
+constexpr int ADJ_NA = MD_ADJ_ATOMS;  /* atoms per block (replica-aligned grid) */
+constexpr int ADJ_THREADS = ADJ_NA * ADJ_TPA;
 constexpr int ADJ_MAXBINS = 512;
 constexpr double ADJ_HFIX = 1048576.0; /* 2^20: fixed point of the RDF kernel values */
 
@@ -56,53 +58,93 @@ struct adj_slots {
     float p1[NT], p2[NT], ps;
 };
 
-/* RDF histogram of one frame: rows of type a, neighbours of type b inside
- * rmax; kernel values in fixed point (2^-20) summed with integer atomics in
- * shared memory, then into the replica's histogram. */
-__global__ void __launch_bounds__(MD_LA * ADJ_TPA) k_adj_rdf(adj_par ap, const int2 *__restrict__ tab,
-                                                           const md_rep *__restrict__ reps,
-                                                           const float4 *__restrict__ pos4,
-                                                           const int *__restrict__ type,
-                                                           const unsigned *__restrict__ nl,
-                                                           const int *__restrict__ nl_n,
-                                                           unsigned long long *hist)
+/* exp(-y_b^2 / (2 sigma^2)) on the equally spaced bins y_b = y0 + (b - b0) dr by
+ * the exact recurrence G(y + dr) = G(y) R(y), R(y + dr) = R(y) C with
+ * R(y) = exp(-(2 y dr + dr^2) k), C = exp(-2 dr^2 k), k = 1/(2 sigma^2):
+ * two exponentials per pair instead of one per bin. */
+struct gauss_walk {
+    float g, rr, c;
+    __device__ __forceinline__ gauss_walk(float y0, float dr, float k, float cstep)
+    {
+        g = __expf(-y0 * y0 * k);
+        rr = __expf(-(2.0f * y0 * dr + dr * dr) * k);
+        c = cstep;
+    }
+    __device__ __forceinline__ void next()
+    {
+        g *= rr;
+        rr *= c;
+    }
+};
+
+/* Bins whose centre lies within 5 sigma of r. */
+__device__ __forceinline__ void rdf_bins(const adj_par &ap, float r, int &b0, int &b1)
 {
-    __shared__ unsigned long long sh[ADJ_MAXBINS];
-    for (int k = threadIdx.x; k < ap.nbins; k += blockDim.x) sh[k] = 0ull;
+    const float reach = 5.0f * ap.sigma;
+    b0 = max((int)ceilf((r - reach) / ap.dr - 0.5f), 0);
+    b1 = min((int)floorf((r + reach) / ap.dr - 0.5f), ap.nbins - 1);
+}
+
+/* RDF histogram of one frame: every unordered (a, b) pair inside rmax is
+ * counted once, by the row of its lower (sorted) index, so rows of both
+ * types share the work (an (a, a) pair counts twice, as the ordered sum over
+ * i in a, j in b does).  Kernel values in fixed point (2^-20) are summed with
+ * integer atomics into per-warp histograms in shared memory, then added into
+ * the replica's histogram. */
+constexpr int ADJ_WARPS = ADJ_THREADS / 32;
+constexpr int ADJ_RDF_BINS = 256;   /* per-warp histograms hold up to 256 bins */
+
+__global__ void __launch_bounds__(ADJ_THREADS) k_adj_rdf(adj_par ap, const int2 *__restrict__ tab,
+                                                       const md_rep *__restrict__ reps,
+                                                       const float4 *__restrict__ pos4,
+                                                       const int *__restrict__ type,
+                                                       const unsigned *__restrict__ nl,
+                                                       const int *__restrict__ nl_n,
+                                                       unsigned long long *hist)
+{
+    __shared__ unsigned s_h[ADJ_WARPS][ADJ_RDF_BINS];
+    for (int k = threadIdx.x; k < ADJ_WARPS * ADJ_RDF_BINS; k += blockDim.x) (&s_h[0][0])[k] = 0u;
     __syncthreads();
     const int2 bt = tab[blockIdx.x];
     const md_rep &R = reps[bt.x];
     const geom_reg g = rep_geom(R);
-    const int a = threadIdx.x / ADJ_TPA, lane = threadIdx.x % ADJ_TPA;
+    const int a = threadIdx.x / ADJ_TPA, lane = threadIdx.x % ADJ_TPA, w = threadIdx.x >> 5;
     const int i = bt.y + a;
-    if (i < R.atom0 + R.natom && type[i] == ap.rdf_a) {
+    const float cstep = __expf(-2.0f * ap.dr * ap.dr * ap.inv_2s2);
+    const int ti = i < R.atom0 + R.natom ? type[i] : -1;
+    const int want = ti == ap.rdf_a ? ap.rdf_b : (ti == ap.rdf_b ? ap.rdf_a : -1);
+    const float wt = ap.rdf_fac * ap.kn * (float)ADJ_HFIX;
+    if (want >= 0) {
         const float4 pi = pos4[i];
         const int cnt = nl_n[i];
-        const float reach = 5.0f * ap.sigma;
         for (int k = lane; k < cnt; k += ADJ_TPA) {
             const unsigned e = nl[(size_t)i * ap.cap + k];
-            if ((int)(e >> MD_TYPE_SHIFT) != ap.rdf_b) continue;
-            const float4 pj = pos4[e & MD_INDEX_MASK];
+            const int j = (int)(e & MD_INDEX_MASK);
+            if ((int)(e >> MD_TYPE_SHIFT) != want || j <= i) continue;
+            const float4 pj = pos4[j];
             float dx = pi.x - pj.x, dy = pi.y - pj.y, dz = pi.z - pj.z;
             dx -= g.L(0) * rint_small(dx * g.Li(0));
             dy -= g.L(1) * rint_small(dy * g.Li(1));
             dz -= g.L(2) * rint_small(dz * g.Li(2));
             const float rsq = dx * dx + dy * dy + dz * dz;
-            if (rsq >= ap.rmaxsq || rsq == 0.0f) continue;
+            if (rsq >= ap.rmaxsq) continue;
             const float r = sqrtf(rsq);
-            int b0 = (int)ceilf((r - reach) / ap.dr - 0.5f), b1 = (int)floorf((r + reach) / ap.dr - 0.5f);
-            b0 = max(b0, 0);
-            b1 = min(b1, ap.nbins - 1);
+            int b0, b1;
+            rdf_bins(ap, r, b0, b1);
+            gauss_walk gw(((float)b0 + 0.5f) * ap.dr - r, ap.dr, ap.inv_2s2, cstep);
             for (int b = b0; b <= b1; b++) {
-                const float y = ((float)b + 0.5f) * ap.dr - r;
-                const float kv = ap.kn * __expf(-y * y * ap.inv_2s2);
-                atomicAdd(&sh[b], (unsigned long long)__float2uint_rn(kv * (float)ADJ_HFIX));
+                /* <= 1.7e7 per pair and bin; a warp's bin stays far below 2^32 per frame */
+                atomicAdd(&s_h[w][b], __float2uint_rn(wt * gw.g));
+                gw.next();
             }
         }
     }
     __syncthreads();
-    for (int k = threadIdx.x; k < ap.nbins; k += blockDim.x)
-        if (sh[k]) atomicAdd(&hist[(size_t)bt.x * ap.nbins + k], sh[k]);
+    for (int k = threadIdx.x; k < ap.nbins; k += blockDim.x) {
+        unsigned long long t = 0ull;
+        for (int q = 0; q < ADJ_WARPS; q++) t += s_h[q][k];
+        if (t) atomicAdd(&hist[(size_t)bt.x * ap.nbins + k], t);
+    }
 }
 
 /* Per-replica sum of the frame's potential energies (from the last
@@ -149,7 +191,7 @@ __global__ void k_adj_acc(int n, int pitch, const int *__restrict__ perm, const 
  * row's parameter slots; the block reduces its rows into (type, slot) sums
  * in a fixed order.  ebn[b] = e_b norm_b kn / sigma^2 of the replica. */
 template <int KIND, int NT>
-__global__ void __launch_bounds__(MD_LA * ADJ_TPA) k_adj_back(
+__global__ void __launch_bounds__(ADJ_THREADS) k_adj_back(
     adj_par ap, const int2 *__restrict__ tab, const md_rep *__restrict__ reps,
     const float2 *__restrict__ ljr, const float *__restrict__ ebn, const float4 *__restrict__ pos4,
     const int *__restrict__ type, const unsigned *__restrict__ nl, const int *__restrict__ nl_n,
@@ -159,8 +201,8 @@ __global__ void __launch_bounds__(MD_LA * ADJ_TPA) k_adj_back(
     constexpr int NB = 2 * NT * NT + 1;      /* slots of a block: (type, slot) */
     __shared__ float2 lj[MD_MAXTYPE * MD_MAXTYPE];
     __shared__ float sb[ADJ_MAXBINS];
-    __shared__ float s_val[MD_LA][NS];
-    __shared__ int s_type[MD_LA];
+    __shared__ float s_val[ADJ_NA][NS];
+    __shared__ int s_type[ADJ_NA];
     const int2 bt = tab[blockIdx.x];
     const md_rep &R = reps[bt.x];
     if (threadIdx.x < MD_MAXTYPE * MD_MAXTYPE)
@@ -181,17 +223,28 @@ __global__ void __launch_bounds__(MD_LA * ADJ_TPA) k_adj_back(
     const float qi = QFAC * pi.w;
     const float4 wi = ap.with_w ? w4[ii] : make_float4(0.f, 0.f, 0.f, 0.f);
     const bool ra = ti == ap.rdf_a, rb = ti == ap.rdf_b;
-    const float reach = 5.0f * ap.sigma;
+    const float cstep = __expf(-2.0f * ap.dr * ap.dr * ap.inv_2s2);
     float gx = 0.f, gy = 0.f, gz = 0.f;
     adj_slots<NT> sl;
 #pragma unroll
     for (int k = 0; k < NT; k++) { sl.p1[k] = 0.f; sl.p2[k] = 0.f; }
     sl.ps = 0.f;
     const int cnt = active ? nl_n[ii] : 0;
+    const unsigned *row = nl + (size_t)ii * ap.cap;
+    /* the next entry's position and w are loaded while this one is computed */
+    unsigned en = lane < cnt ? row[lane] : 0u;
+    float4 pn = pos4[lane < cnt ? (int)(en & MD_INDEX_MASK) : ii];
+    float4 wn = ap.with_w && lane < cnt ? w4[en & MD_INDEX_MASK] : make_float4(0.f, 0.f, 0.f, 0.f);
     for (int k = lane; k < cnt; k += ADJ_TPA) {
-        const unsigned e = nl[(size_t)ii * ap.cap + k];
-        const int j = (int)(e & MD_INDEX_MASK), tj = (int)(e >> MD_TYPE_SHIFT);
-        const float4 pj = pos4[j];
+        const unsigned e = en;
+        const float4 pj = pn;
+        const float4 wj = wn;
+        if (k + ADJ_TPA < cnt) {
+            en = row[k + ADJ_TPA];
+            pn = pos4[en & MD_INDEX_MASK];
+            if (ap.with_w) wn = w4[en & MD_INDEX_MASK];
+        }
+        const int tj = (int)(e >> MD_TYPE_SHIFT);
         float dx = pi.x - pj.x, dy = pi.y - pj.y, dz = pi.z - pj.z;
         dx -= g.L(0) * rint_small(dx * g.Li(0));
         dy -= g.L(1) * rint_small(dy * g.Li(1));
@@ -228,7 +281,6 @@ __global__ void __launch_bounds__(MD_LA * ADJ_TPA) k_adj_back(
         gz -= wpe * ff * dz;
         float dwi = 0.0f;
         if (ap.with_w) {
-            const float4 wj = w4[j];
             const float ux = wi.x - wj.x, uy = wi.y - wj.y, uz = wi.z - wj.z;
             const float dd = dx * ux + dy * uy + dz * uz;
             gx += ff * ux + gg * dd * dx;
@@ -238,13 +290,14 @@ __global__ void __launch_bounds__(MD_LA * ADJ_TPA) k_adj_back(
         }
         /* RDF pairs (a, b) in either orientation */
         if (((ra && tj == ap.rdf_b) || (rb && tj == ap.rdf_a)) && rsq < ap.rmaxsq) {
-            int b0 = (int)ceilf((r - reach) / ap.dr - 0.5f), b1 = (int)floorf((r + reach) / ap.dr - 0.5f);
-            b0 = max(b0, 0);
-            b1 = min(b1, ap.nbins - 1);
+            int b0, b1;
+            rdf_bins(ap, r, b0, b1);
+            const float y0 = ((float)b0 + 0.5f) * ap.dr - r;
+            gauss_walk gw(y0, ap.dr, ap.inv_2s2, cstep);
             float coef = 0.0f;
             for (int b = b0; b <= b1; b++) {
-                const float y = ((float)b + 0.5f) * ap.dr - r;
-                coef += sb[b] * y * __expf(-y * y * ap.inv_2s2);
+                coef += sb[b] * (y0 + (float)(b - b0) * ap.dr) * gw.g;
+                gw.next();
             }
             coef *= ap.rdf_fac * ri;
             gx += coef * dx;
@@ -298,36 +351,38 @@ __global__ void __launch_bounds__(MD_LA * ADJ_TPA) k_adj_back(
         const int k = threadIdx.x;
         double acc = 0.0;
         if (k == NB - 1) {
-            for (int r2 = 0; r2 < MD_LA; r2++) acc += (double)s_val[r2][2 * NT];
+            for (int r2 = 0; r2 < ADJ_NA; r2++) acc += (double)s_val[r2][2 * NT];
         } else {
             const int tt = k / (2 * NT), rem = k % (2 * NT);   /* row type, slot */
-            for (int r2 = 0; r2 < MD_LA; r2++)
+            for (int r2 = 0; r2 < ADJ_NA; r2++)
                 if (s_type[r2] == tt) acc += (double)s_val[r2][rem];
         }
         part[(size_t)blockIdx.x * NB + k] = acc;
     }
 }
 
-/* Per replica and block slot: the replica's blocks summed in order, added
- * to its gradient accumulators. */
+/* Per replica and block slot (one warp each): the replica's blocks summed
+ * lane-strided, then by a fixed shuffle tree, added to its gradient
+ * accumulators. */
 __global__ void k_adj_param(int nrep, int nb_slots, const md_rep *__restrict__ reps,
                             const double *__restrict__ part, double *acc)
 {
-    int t = blockIdx.x * blockDim.x + threadIdx.x;
+    const int t = (blockIdx.x * blockDim.x + threadIdx.x) >> 5, lane = threadIdx.x & 31;
     if (t >= nrep * nb_slots) return;
     const int r = t / nb_slots, k = t % nb_slots;
     const md_rep &R = reps[r];
     double s = 0.0;
-    for (int b = 0; b < R.nblk; b++) s += part[(size_t)(R.blk0 + b) * nb_slots + k];
-    acc[t] += s;
+    for (int b = lane; b < R.anblk; b += 32) s += part[(size_t)(R.ablk0 + b) * nb_slots + k];
+    for (int o = 16; o > 0; o >>= 1) s += __shfl_down_sync(0xffffffffu, s, o);
+    if (lane == 0) acc[t] += s;
 }
 
 template <int KIND, int NT>
 void launch_back_nt(md_ctx *c, const adj_par &ap, const float *ebn, const float4 *w4, double *G,
                     double *part)
 {
-    const int k = md_grid_index(MD_LA);
-    k_adj_back<KIND, NT><<<c->grid_cnt[k], MD_LA * ADJ_TPA, 0, c->stream>>>(
+    const int k = md_grid_index(ADJ_NA);
+    k_adj_back<KIND, NT><<<c->grid_cnt[k], ADJ_THREADS, 0, c->stream>>>(
         ap, c->grid_tab + c->grid_off[k], c->reps_dev, c->ljr_dev, ebn, c->pos4, c->type, c->nl,
         c->nl_n, w4, G, part);
 }
@@ -383,7 +438,7 @@ extern "C" md_status md_adjoint_run(md_ctx *c, const md_adjoint_cfg *cfg, const 
     }
     const int K = cfg->nsteps, C = cfg->checkpoint > 0 ? cfg->checkpoint : 50;
     const int nb = cfg->nbins, nrep = c->nrep, n = c->n;
-    if (K < 1 || nb < 1 || nb > ADJ_MAXBINS || cfg->rdf_dr <= 0 || cfg->rdf_sigma <= 0 ||
+    if (K < 1 || nb < 1 || nb > ADJ_RDF_BINS || cfg->rdf_dr <= 0 || cfg->rdf_sigma <= 0 ||
         cfg->rdf_a < 0 || cfg->rdf_b < 0 || cfg->rdf_a >= c->ntype || cfg->rdf_b >= c->ntype ||
         (cfg->gradient && (!dlj1 || !dlj2 || !dlns))) {
         c->last_error = "md_adjoint_run: invalid configuration";
@@ -397,7 +452,7 @@ extern "C" md_status md_adjoint_run(md_ctx *c, const md_adjoint_cfg *cfg, const 
         }
     const int nseg = (K + C - 1) / C;
     const int nt = adj_nt(c->ntype), NB = 2 * nt * nt + 1;
-    const int kla = md_grid_index(MD_LA), nblk = c->grid_cnt[kla];
+    const int kla = md_grid_index(ADJ_NA), nblk = c->grid_cnt[kla];
     adj_buffers B;
     MD_CUDA_TRY(c, adj_alloc(&B.ck_x, 3 * (size_t)n * (nseg + 1)));
     MD_CUDA_TRY(c, adj_alloc(&B.ck_v, 3 * (size_t)n * (nseg + 1)));
@@ -436,7 +491,7 @@ extern "C" md_status md_adjoint_run(md_ctx *c, const md_adjoint_cfg *cfg, const 
 
     md_kparams kp = md_make_kparams(c);
     auto obs = [&]() {
-        k_adj_rdf<<<nblk, MD_LA * ADJ_TPA, 0, s>>>(ap, c->grid_tab + c->grid_off[kla], c->reps_dev,
+        k_adj_rdf<<<nblk, ADJ_THREADS, 0, s>>>(ap, c->grid_tab + c->grid_off[kla], c->reps_dev,
                                                   c->pos4, c->type, c->nl, c->nl_n, B.hist);
         k_adj_pe<<<rgrid, 256, 0, s>>>(nrep, c->repst, B.pe_sum);
     };
@@ -531,7 +586,7 @@ extern "C" md_status md_adjoint_run(md_ctx *c, const md_adjoint_cfg *cfg, const 
                 k_adj_w<<<agrid, 256, 0, s>>>(n, (double)c->dt, 1, m >= 1 ? 2.0 : 1.0, c->perm, c->kick,
                                                B.U, B.P, B.w4);
             launch_back(c, ap, B.ebn, B.w4, B.G, B.part);
-            k_adj_param<<<(nrep * NB + 255) / 256, 256, 0, s>>>(nrep, NB, c->reps_dev, B.part, B.acc);
+            k_adj_param<<<(nrep * NB * 32 + 255) / 256, 256, 0, s>>>(nrep, NB, c->reps_dev, B.part, B.acc);
             k_adj_acc<<<agrid, 256, 0, s>>>(n, c->pitch, c->perm, B.G, B.P);
         }
     }

@@ -8,8 +8,8 @@
  * replica-aligned grid (md_rep, grid_tab): a block covers atoms of one
  * replica only, so the replica's geometry and force-field constants are
  * uniform across the block (kept in registers, its LJ table in shared
- * memory), and the block partials of the FP64 reductions split cleanly by
- * replica.  The arithmetic per atom is the single-system arithmetic
+ * memory), and each block adds its energy sums into its replica's
+ * fixed-point accumulators.  The arithmetic per atom is the single-system arithmetic
  * (pair_sum, the leapfrog / velocity-Verlet updates of k_integrate.cu), so a
  * replica advances bit-for-bit as it would alone with the same tuning.
  */
@@ -52,27 +52,22 @@ __global__ void __launch_bounds__(128) k_pair_b(int cap, int pitch, const int2 *
     }
 }
 
-/* Per-replica FP64 totals from the block partials (each replica's blocks
- * are one contiguous range of the MD_LA-atom grid), one thread per replica
- * summing its blocks in order, then each replica's thermostat bookkeeping
- * and the batch's step record (sums over replicas, fixed order).  Runs in
- * the last block to finish. */
+/* Runs in the last block to finish: one thread per replica turns its
+ * accumulators into KE, PE and virial (and clears them for the next step),
+ * then does the replica's thermostat bookkeeping; the batch's step record
+ * sums the replicas in a fixed order. */
 __device__ void finalize_b(const md_kparams &kp, const thermo_par &tp, int mode, int nrep,
                            const md_rep *__restrict__ reps, md_repstate *repst,
-                           const double *partials, int npart, md_devstate *st, md_thermo *rec,
-                           int rec_cap, double *sh)
+                           unsigned long long *racc, md_devstate *st, md_thermo *rec, int rec_cap,
+                           double *sh)
 {
     double tke = 0.0, tpe = 0.0, tw = 0.0, tex = 0.0;
     for (int r = threadIdx.x; r < nrep; r += blockDim.x) {
         const md_rep &R = reps[r];
-        double a = 0.0, b = 0.0, c = 0.0;
-        for (int k = 0; k < R.nblk; k++) {
-            a += __ldcg(partials + R.blk0 + k);
-            if (tp.energy) {
-                b += __ldcg(partials + npart + R.blk0 + k);
-                c += __ldcg(partials + 2 * npart + R.blk0 + k);
-            }
-        }
+        const double a = fix_take(racc + 3 * r, MD_KFIX);
+        double b = fix_take(racc + 3 * r + 1, MD_EFIX);
+        double c = fix_take(racc + 3 * r + 2, MD_EFIX);
+        if (!tp.energy) b = c = 0.0;
         thermo_par t = tp;
         t.t0 = R.t0;
         t.ndf = R.ndf;
@@ -108,6 +103,7 @@ __global__ void __launch_bounds__(3 * MD_LA) k_leapfrog_b(md_kparams kp, thermo_
                                                          const int2 *__restrict__ tab,
                                                          const md_rep *__restrict__ reps,
                                                          md_repstate *repst, int *rep_upd,
+                                                         unsigned long long *racc,
                                                          double *x, double *v,
                                                          const double *__restrict__ mass,
                                                          const double *__restrict__ kick,
@@ -117,6 +113,7 @@ __global__ void __launch_bounds__(3 * MD_LA) k_leapfrog_b(md_kparams kp, thermo_
                                                          const float *__restrict__ vir)
 {
     __shared__ double sh[3 * MD_LA / 32];
+    __shared__ long long shl[3 * (3 * MD_LA / 32)];
     __shared__ float s_x[3][MD_LA];
     const int2 bt = tab[blockIdx.x];
     const md_rep &R = reps[bt.x];
@@ -145,9 +142,9 @@ __global__ void __launch_bounds__(3 * MD_LA) k_leapfrog_b(md_kparams kp, thermo_
             rep_upd[bt.x] = 1;
         }
     }
-    write_partials(ke2, pe, w, tp.energy, io.partials, sh);
+    block_fix_add(ke2, pe, w, tp.energy, racc + 3 * bt.x, shl);
     if (md_last_block(io.counter)) {
-        finalize_b(kp, tp, 0, nrep, reps, repst, io.partials, gridDim.x, io.st, io.rec, io.rec_cap, sh);
+        finalize_b(kp, tp, 0, nrep, reps, repst, racc, io.st, io.rec, io.rec_cap, sh);
         if (threadIdx.x == 0) {
             set_condition(io);
             *io.counter = 0;
@@ -206,7 +203,8 @@ __global__ void __launch_bounds__(3 * MD_LA) k_vv_second_b(md_kparams kp, thermo
                                                           int do_kick, step_io io, int nrep,
                                                           const int2 *__restrict__ tab,
                                                           const md_rep *__restrict__ reps,
-                                                          md_repstate *repst, double *v,
+                                                          md_repstate *repst,
+                                                          unsigned long long *racc, double *v,
                                                           const double *__restrict__ mass,
                                                           const double *__restrict__ kick,
                                                           const long long *__restrict__ f,
@@ -214,6 +212,7 @@ __global__ void __launch_bounds__(3 * MD_LA) k_vv_second_b(md_kparams kp, thermo
                                                           const float *__restrict__ vir)
 {
     __shared__ double sh[3 * MD_LA / 32];
+    __shared__ long long shl[3 * (3 * MD_LA / 32)];
     const int2 bt = tab[blockIdx.x];
     const md_rep &R = reps[bt.x];
     const int d = threadIdx.x / MD_LA, a = threadIdx.x - d * MD_LA;
@@ -231,10 +230,9 @@ __global__ void __launch_bounds__(3 * MD_LA) k_vv_second_b(md_kparams kp, thermo
         ke2 = mass[s] * (vv * vv);
         if (d == 0 && tp.energy) { pe = epot[s]; w = vir[s]; }
     }
-    write_partials(ke2, pe, w, tp.energy, io.partials, sh);
+    block_fix_add(ke2, pe, w, tp.energy, racc + 3 * bt.x, shl);
     if (md_last_block(io.counter)) {
-        finalize_b(kp, tp, do_kick ? 1 : 2, nrep, reps, repst, io.partials, gridDim.x, io.st,
-                   io.rec, io.rec_cap, sh);
+        finalize_b(kp, tp, do_kick ? 1 : 2, nrep, reps, repst, racc, io.st, io.rec, io.rec_cap, sh);
         if (threadIdx.x == 0) *io.counter = 0;
     }
 }
@@ -291,7 +289,8 @@ void launch_leapfrog_b(md_ctx *c, const md_kparams &kp, int energy, unsigned lon
 {
     k_leapfrog_b<<<grid_int_blocks(c), 3 * MD_LA, 0, c->stream>>>(
         kp, make_tp(c, energy), make_io(c, cond, has_cond), c->nrep, grid_int(c), c->reps_dev,
-        c->repst, c->rep_upd, c->x, c->v, c->mass, c->kick, c->pos4, c->f, c->epot, c->vir);
+        c->repst, c->rep_upd, c->racc, c->x, c->v, c->mass, c->kick, c->pos4, c->f, c->epot,
+        c->vir);
 }
 
 void launch_vv_first_b(md_ctx *c, const md_kparams &kp, unsigned long long cond, int has_cond)
@@ -306,5 +305,5 @@ void launch_vv_second_b(md_ctx *c, const md_kparams &kp, int energy, int kick)
 {
     k_vv_second_b<<<grid_int_blocks(c), 3 * MD_LA, 0, c->stream>>>(
         kp, make_tp(c, energy), kick, make_io(c, 0, 0), c->nrep, grid_int(c), c->reps_dev,
-        c->repst, c->v, c->mass, c->kick, c->f, c->epot, c->vir);
+        c->repst, c->racc, c->v, c->mass, c->kick, c->f, c->epot, c->vir);
 }

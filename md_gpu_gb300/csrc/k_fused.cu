@@ -4,7 +4,7 @@
  * thread the leapfrog update of that atom (nve_leapfrog.cu:31-60,
  * nvt_leapfrog_ber.cu:29-80), the next step's list check
  * (neighborlist.cu:157-176) and the FP64 kinetic-energy partial; the last
- * block to finish reduces the partials and sets the rebuild condition.
+ * block to finish turns the step's sums into T and sets the rebuild condition.
  *
  * Positions are double buffered: the step reads pos4 and writes the updated
  * copy to pos4_next, so no thread sees a neighbour that has already moved.
@@ -25,7 +25,7 @@ __global__ void __launch_bounds__(128) k_pair_leapfrog(
 {
     constexpr int NA = 128 / TPA;   /* atoms per block */
     __shared__ float2 lj[MD_MAXTYPE * MD_MAXTYPE];
-    __shared__ double sh[8];
+    __shared__ long long sh[12];   /* 3 integers per warp */
     __shared__ long long s_f[NA][3];
     __shared__ float s_x[NA][3];
     if (threadIdx.x < MD_MAXTYPE * MD_MAXTYPE) lj[threadIdx.x] = ljtab[threadIdx.x];
@@ -76,9 +76,9 @@ __global__ void __launch_bounds__(128) k_pair_leapfrog(
             check_moved(p, io.pos_old[ia], kp, io.st);
         }
     }
-    write_partials(ke2, 0.0, 0.0, 0, io.partials, sh);
+    block_fix_add(ke2, 0.0, 0.0, 0, io.st->acc, sh);
     if (md_last_block(io.counter)) {
-        finalize(kp, tp, 0, gridDim.x, io.partials, io.st, io.rec, io.rec_cap, sh);
+        finalize(kp, tp, 0, io.st, io.rec, io.rec_cap);
         if (threadIdx.x == 0) {
             set_condition(io);
             *io.counter = 0;

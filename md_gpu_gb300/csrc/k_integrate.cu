@@ -6,9 +6,10 @@
  * with lambda = sqrt(1 + dt/tau (T0/T_prev - 1)) for Berendsen NVT
  * (integrator.cu:146-147, tau = 100 fs there) and 1 for NVE.  Positions and
  * velocities are FP64 here; the FP32 copy pos4 is refreshed in the same pass.
- * The kinetic energy is reduced in FP64, per block then by the last block to
- * finish in a fixed order (replacing the reference's single-block FP32 tree,
- * nvt_leapfrog_ber.cu:83-110, whose width is the block count).
+ * The kinetic energy of every (atom, axis) is FP64 and is summed exactly in
+ * fixed point (2^-24 kJ/mol; integer shuffles, one atomic add per block),
+ * replacing the reference's single-block FP32 tree (nvt_leapfrog_ber.cu:
+ * 83-110, whose width is the block count).
  *
  * The same pass performs the next step's neighbour-list check (any atom moved
  * >= skin/2 since the last build, neighborlist.cu:157-176) and, inside a
@@ -34,7 +35,7 @@ namespace {
  * The new FP32 positions meet in shared memory, where one thread per atom
  * writes pos4 and performs the list check.
  *
- * Leapfrog update + list check + KE partials; the last block finalises.
+ * Leapfrog update + list check + KE sums; the last block finalises.
  * kick[s] = dt/m * 2^-32 turns the fixed-point force into the velocity
  * change directly (the same product as F dt/m, rounded once). */
 __global__ void __launch_bounds__(3 * MD_LA) k_leapfrog(md_kparams kp, thermo_par tp, step_io io,
@@ -46,7 +47,7 @@ __global__ void __launch_bounds__(3 * MD_LA) k_leapfrog(md_kparams kp, thermo_pa
                                                        const float *__restrict__ epot,
                                                        const float *__restrict__ vir)
 {
-    __shared__ double sh[3 * MD_LA / 32];
+    __shared__ long long sh[3 * (3 * MD_LA / 32)];
     __shared__ float s_x[3][MD_LA];
     const int d = threadIdx.x / MD_LA, a = threadIdx.x - d * MD_LA;
     const int s = blockIdx.x * MD_LA + a;
@@ -69,9 +70,9 @@ __global__ void __launch_bounds__(3 * MD_LA) k_leapfrog(md_kparams kp, thermo_pa
         pos4[s] = p;
         check_moved(p, io.pos_old[s], kp, io.st);
     }
-    write_partials(ke2, pe, w, tp.energy, io.partials, sh);
+    block_fix_add(ke2, pe, w, tp.energy, io.st->acc, sh);
     if (md_last_block(io.counter)) {
-        finalize(kp, tp, 0, gridDim.x, io.partials, io.st, io.rec, io.rec_cap, sh);
+        finalize(kp, tp, 0, io.st, io.rec, io.rec_cap);
         if (threadIdx.x == 0) {
             set_condition(io);
             *io.counter = 0;
@@ -119,7 +120,7 @@ __global__ void __launch_bounds__(3 * MD_LA) k_vv_first(md_kparams kp, thermo_pa
     }
 }
 
-/* Velocity Verlet second half kick and KE (PE, virial) partials; the last
+/* Velocity Verlet second half kick and KE (PE, virial) sums; the last
  * block finalises.  do_kick = 0: observe the state only (pending NH scale
  * applied), mode 2. */
 __global__ void __launch_bounds__(3 * MD_LA) k_vv_second(md_kparams kp, thermo_par tp, int do_kick,
@@ -130,7 +131,7 @@ __global__ void __launch_bounds__(3 * MD_LA) k_vv_second(md_kparams kp, thermo_p
                                                         const float *__restrict__ epot,
                                                         const float *__restrict__ vir)
 {
-    __shared__ double sh[3 * MD_LA / 32];
+    __shared__ long long sh[3 * (3 * MD_LA / 32)];
     const int d = threadIdx.x / MD_LA, a = threadIdx.x - d * MD_LA;
     const int s = blockIdx.x * MD_LA + a;
     const size_t o = (size_t)d * kp.pitch + s;
@@ -146,9 +147,9 @@ __global__ void __launch_bounds__(3 * MD_LA) k_vv_second(md_kparams kp, thermo_p
         ke2 = mass[s] * (vv * vv);
         if (d == 0 && tp.energy) { pe = epot[s]; w = vir[s]; }
     }
-    write_partials(ke2, pe, w, tp.energy, io.partials, sh);
+    block_fix_add(ke2, pe, w, tp.energy, io.st->acc, sh);
     if (md_last_block(io.counter)) {
-        finalize(kp, tp, do_kick ? 1 : 2, gridDim.x, io.partials, io.st, io.rec, io.rec_cap, sh);
+        finalize(kp, tp, do_kick ? 1 : 2, io.st, io.rec, io.rec_cap);
         if (threadIdx.x == 0) *io.counter = 0;
     }
 }

@@ -249,9 +249,9 @@ void free_device(md_ctx *c)
                     c->vir, c->epot, c->nl, c->nl_n, c->excl_orig, c->excl_s, c->cell_rank, c->cell_lin,
                     c->cell_count, c->cell_start, c->cell_fill, c->key, c->src, c->tmp_d, c->tmp4,
                     c->tmp_i, c->bl_o, c->bl_on, c->al_o, c->al_on, c->bl_s, c->bl_sn, c->al_s,
-                    c->al_sn, c->partials, c->st, c->rec, c->lj_dev, c->bonded_par,
+                    c->al_sn, c->st, c->rec, c->lj_dev, c->bonded_par,
                     c->type_mask_dev, c->io_dev, c->reps_dev, c->repst, c->arep, c->crep,
-                    c->ljr_dev, c->grid_tab, c->rep_upd};
+                    c->ljr_dev, c->grid_tab, c->rep_upd, c->racc};
     for (void *p : ptrs)
         if (p) cudaFree(p);
 }
@@ -534,10 +534,6 @@ md_status setup_device(md_ctx *c, void *stream, host_stage &h, md_ctx **out)
     const size_t P = c->pitch;
     const int n = c->n;
     const bool batch = c->batch;
-    /* block partials of the integrators (256 threads; one grid per replica
-     * in a batch) and of the fused step (128 threads, up to 32 per atom) */
-    size_t npart = 3 * (P / 4 + 256) + 8;
-    if (batch) npart = std::max(npart, 3 * (size_t)c->grid_cnt[md_grid_index(MD_LA)] + 8);
     cudaError_t e = cudaSuccess;
 #define MD_ALLOC(ptr, cnt) if (e == cudaSuccess) e = dalloc(&(ptr), (cnt))
     MD_ALLOC(c->x, 3 * P); MD_ALLOC(c->v, 3 * P); MD_ALLOC(c->mass, P); MD_ALLOC(c->kick, P);
@@ -552,8 +548,6 @@ md_status setup_device(md_ctx *c, void *stream, host_stage &h, md_ctx **out)
     MD_ALLOC(c->tmp_d, 8 * P); MD_ALLOC(c->tmp4, P); MD_ALLOC(c->tmp_i, 3 * P);
     MD_ALLOC(c->bl_o, 4 * P); MD_ALLOC(c->bl_on, P); MD_ALLOC(c->al_o, 4 * P); MD_ALLOC(c->al_on, P);
     MD_ALLOC(c->bl_s, 4 * P); MD_ALLOC(c->bl_sn, P); MD_ALLOC(c->al_s, 4 * P); MD_ALLOC(c->al_sn, P);
-    c->npart = (int)(P / 256);
-    MD_ALLOC(c->partials, npart);
     MD_ALLOC(c->st, 1);
     c->rec_cap = 4096;
     MD_ALLOC(c->rec, c->rec_cap);
@@ -564,7 +558,7 @@ md_status setup_device(md_ctx *c, void *stream, host_stage &h, md_ctx **out)
     if (batch) {
         MD_ALLOC(c->reps_dev, c->nrep); MD_ALLOC(c->repst, c->nrep);
         MD_ALLOC(c->arep, P); MD_ALLOC(c->crep, c->ncells);
-        MD_ALLOC(c->rep_upd, c->nrep);
+        MD_ALLOC(c->rep_upd, c->nrep); MD_ALLOC(c->racc, 3 * (size_t)c->nrep);
         MD_ALLOC(c->ljr_dev, (size_t)MD_MAXTYPE * MD_MAXTYPE * c->nrep);
         MD_ALLOC(c->grid_tab, h.grid.size());
     }
@@ -628,6 +622,7 @@ md_status setup_device(md_ctx *c, void *stream, host_stage &h, md_ctx **out)
         up(c->ljr_dev, h.ljr.data(), sizeof(float2) * h.ljr.size());
         up(c->grid_tab, h.grid.data(), sizeof(int2) * h.grid.size());
         if (e == cudaSuccess) e = cudaMemset(c->rep_upd, 0, sizeof(int) * c->nrep);
+        if (e == cudaSuccess) e = cudaMemset(c->racc, 0, sizeof(unsigned long long) * 3 * c->nrep);
     }
     if (e == cudaSuccess) e = cudaMemset(c->f, 0, sizeof(long long) * 3 * P);
     if (e == cudaSuccess) e = cudaMemset(c->vir, 0, sizeof(float) * P);
@@ -1069,8 +1064,10 @@ md_status md_create_batch(const md_system_desc *descs, int nrep, void *stream, m
         for (int r = 0; r < nrep; r++) {
             md_rep &R = c->reps[r];
             if (A == MD_LA) R.blk0 = (int)h.grid.size() - c->grid_off[k];
+            if (A == MD_ADJ_ATOMS) R.ablk0 = (int)h.grid.size() - c->grid_off[k];
             for (int j = 0; j < R.natom; j += A) h.grid.push_back(make_int2(r, R.atom0 + j));
             if (A == MD_LA) R.nblk = (int)h.grid.size() - c->grid_off[k] - R.blk0;
+            if (A == MD_ADJ_ATOMS) R.anblk = (int)h.grid.size() - c->grid_off[k] - R.ablk0;
         }
         c->grid_cnt[k] = (int)h.grid.size() - c->grid_off[k];
     }
@@ -1464,11 +1461,16 @@ md_status md_autotune(md_ctx *c, int *pair_tpa, int *list_tpa)
     float best = 1e30f;
     int bp = c->pair_tpa, bl = c->list_tpa, bf = 0;
     c->fuse_step = 0;
+    /* best of three timings of 20 launches per candidate: robust to a slow
+     * first launch and to other work on the device */
     for (int t : pt) {
         c->pair_tpa = t;
-        float ms = 0.0f, m2 = 0.0f;
+        float ms = 0.0f, m2 = 1e30f;
         md_status s = md_time_pair(c, 5, &ms);
-        if (s == MD_OK) s = md_time_pair(c, 10, &m2);
+        for (int rep = 0; rep < 3 && s == MD_OK; rep++) {
+            s = md_time_pair(c, 20, &ms);
+            m2 = std::min(m2, ms);
+        }
         if (s != MD_OK) return s;
         if (m2 < best) { best = m2; bp = t; }
     }
@@ -1492,9 +1494,12 @@ md_status md_autotune(md_ctx *c, int *pair_tpa, int *list_tpa)
     for (int t : lt) {
         if (c->batch && t != 0) continue;   /* batches build one warp per cell */
         c->list_tpa = t;
-        float ms = 0.0f, m2 = 0.0f;
+        float ms = 0.0f, m2 = 1e30f;
         md_status s = md_time_rebuild(c, 2, &ms);
-        if (s == MD_OK) s = md_time_rebuild(c, 5, &m2);
+        for (int rep = 0; rep < 3 && s == MD_OK; rep++) {
+            s = md_time_rebuild(c, 5, &ms);
+            m2 = std::min(m2, ms);
+        }
         if (s != MD_OK) return s;
         if (m2 < best) { best = m2; bl = t; }
     }

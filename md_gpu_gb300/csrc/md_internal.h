@@ -58,6 +58,7 @@ struct md_devstate {
     double lam_next;     /* Berendsen scale of the next leapfrog step */
     double kick_scale;   /* velocity scale applied by the next VV first half (NH: s2*s1) */
     unsigned blocks_done; /* blocks finished in the current reduction kernel */
+    unsigned long long acc[3]; /* fixed-point KE (MD_KFIX), PE, sum ff r^2 (MD_EFIX) of the step */
 };
 
 /* Everything a kernel needs about the system, passed by value. */
@@ -95,6 +96,7 @@ struct md_rep {
     int cell0, ncells;   /* first cell rank (= offset of its cell_rank table), cell count */
     int atom0, natom;
     int blk0, nblk;      /* its blocks of the MD_LA-atom integrator grid */
+    int ablk0, anblk;    /* its blocks of the MD_ADJ_ATOMS-atom grid of the adjoint kernels */
     int ndf;
     double t0, q_nh, inv_ndfr, inv_q;   /* 1/(ndf R), 1/Q */
 };
@@ -115,6 +117,13 @@ struct md_repstate {
 #define MD_NGRID 7
 /* Integrator blocks: MD_LA atoms x 3 axes, one thread per (atom, axis). */
 #define MD_LA 128
+/* Atoms per block of the adjoint pair kernels. */
+#define MD_ADJ_ATOMS 32
+/* Fixed-point scales of the energy accumulators: kinetic energy 2^32 per
+ * kJ/mol (|KE| < 2.1e9 kJ/mol per system), potential energy and virial 2^24
+ * (|PE| < 5.4e11 kJ/mol). */
+#define MD_KFIX 4294967296.0
+#define MD_EFIX 16777216.0
 inline int md_grid_index(int atoms_per_block)
 {
     int k = 0;
@@ -171,8 +180,6 @@ struct md_ctx {
     int2 *bl_s = nullptr; int *bl_sn = nullptr;           /* column-major, 4*pitch */
     int4 *al_s = nullptr; int *al_sn = nullptr;
     int has_bonds = 0, has_angles = 0;
-    double *partials = nullptr;                           /* per-block reductions */
-    int npart = 0;
     md_devstate *st = nullptr;
     md_thermo *rec = nullptr;                             /* device ring of records */
     int rec_cap = 0;
@@ -203,6 +210,7 @@ struct md_ctx {
     int *rep_upd = nullptr;       /* per replica: an atom moved >= skin/2 since its last build */
     int *crep = nullptr;          /* cell rank -> replica */
     float2 *ljr_dev = nullptr;    /* nrep x 64 (lj1, lj2) */
+    unsigned long long *racc = nullptr; /* nrep x 3 fixed-point KE, PE, virial sums of a step */
     int2 *grid_tab = nullptr;     /* the MD_NGRID replica-aligned grids, concatenated */
     int grid_off[MD_NGRID] = {0}, grid_cnt[MD_NGRID] = {0};
 

@@ -22,7 +22,6 @@ struct thermo_par {
 /* Per-step bookkeeping buffers and the graph condition to set. */
 struct step_io {
     md_devstate *st;
-    double *partials;
     md_thermo *rec;
     int rec_cap;
     unsigned *counter;
@@ -74,21 +73,58 @@ __device__ __forceinline__ double nh_half_a(double dt, const thermo_par &tp, dou
     return s1;
 }
 
-/* Block partials of the reductions: ke2 is twice the kinetic energy (m v^2;
- * halved once per block, exactly), pe the potential energy, w sum ff r^2. */
-__device__ __forceinline__ void write_partials(double ke2, double pe, double w, int energy,
-                                               double *partials, double *sh)
+/* The reductions of a step: each thread's twice-kinetic energy ke2 (m v^2,
+ * FP64), potential energy and sum ff r^2 are converted once to fixed point
+ * (MD_KFIX = 2^32 per kJ/mol for KE, halved in the same conversion; MD_EFIX
+ * = 2^24 for the others) and summed
+ * with integer shuffles, shared memory and one atomic add per block and
+ * quantity.  Integer addition is exact and associative, so the totals do
+ * not depend on the order in which threads or blocks contribute, and the
+ * slow FP64 pipe only performs one conversion per thread.  sh holds 3
+ * integers per warp. */
+__device__ __forceinline__ void block_fix_add(double ke2, double pe, double w, int energy,
+                                              unsigned long long *acc, long long *sh)
 {
-    double a = 0.5 * block_sum(ke2, sh);
-    if (threadIdx.x == 0) partials[blockIdx.x] = a;
-    if (energy) {
-        double b = block_sum(pe, sh);
-        double c = block_sum(w, sh);
-        if (threadIdx.x == 0) {
-            partials[gridDim.x + blockIdx.x] = b;
-            partials[2 * gridDim.x + blockIdx.x] = c;
+    long long a = llrint(ke2 * (0.5 * MD_KFIX));
+    long long b = energy ? llrint(pe * MD_EFIX) : 0ll;
+    long long c = energy ? llrint(w * MD_EFIX) : 0ll;
+    for (int o = 16; o > 0; o >>= 1) {
+        a += __shfl_down_sync(0xffffffffu, a, o);
+        if (energy) {
+            b += __shfl_down_sync(0xffffffffu, b, o);
+            c += __shfl_down_sync(0xffffffffu, c, o);
         }
     }
+    const int wp = threadIdx.x >> 5, l = threadIdx.x & 31, nw = blockDim.x >> 5;
+    if (l == 0) {
+        sh[wp] = a;
+        sh[nw + wp] = b;
+        sh[2 * nw + wp] = c;
+    }
+    __syncthreads();
+    if (threadIdx.x == 0) {
+        long long ta = 0, tb = 0, tc = 0;
+        for (int k = 0; k < nw; k++) {
+            ta += sh[k];
+            tb += sh[nw + k];
+            tc += sh[2 * nw + k];
+        }
+        atomicAdd(acc, (unsigned long long)ta);
+        if (energy) {
+            atomicAdd(acc + 1, (unsigned long long)tb);
+            atomicAdd(acc + 2, (unsigned long long)tc);
+        }
+    }
+}
+
+/* Reads and clears fixed-point accumulators (in the last block, after every
+ * block's atomic adds). */
+__device__ __forceinline__ double fix_take(unsigned long long *p, double scale)
+{
+    volatile unsigned long long *v = p;
+    const long long x = (long long)*v;
+    *v = 0ull;
+    return (double)x / scale;
 }
 
 /* Thermostat bookkeeping of one system after a step, from its FP64 totals
@@ -168,21 +204,17 @@ __device__ void write_record(const thermo_par &tp, double inv_ndfr, double ke, d
     st->step = step + 1;
 }
 
-/* Fixed-order totals of the block partials, then (thread 0) temperature,
- * thermostat bookkeeping and the step record (mode as thermo_advance). */
-__device__ void finalize(const md_kparams &kp, const thermo_par &tp, int mode, int npart,
-                         const double *partials, md_devstate *st, md_thermo *rec, int rec_cap,
-                         double *sh)
+/* Thread 0 of the last block: the step's totals from the accumulators,
+ * temperature, thermostat bookkeeping and the step record (mode as
+ * thermo_advance). */
+__device__ void finalize(const md_kparams &kp, const thermo_par &tp, int mode, md_devstate *st,
+                         md_thermo *rec, int rec_cap)
 {
-    double a = 0.0, b = 0.0, c = 0.0;
-    for (int k = threadIdx.x; k < npart; k += blockDim.x) {
-        a += __ldcg(partials + k);
-        if (tp.energy) { b += __ldcg(partials + npart + k); c += __ldcg(partials + 2 * npart + k); }
-    }
-    double ke = block_sum(a, sh);
-    double pe = tp.energy ? block_sum(b, sh) : 0.0;
-    double w = tp.energy ? block_sum(c, sh) : 0.0;
     if (threadIdx.x != 0) return;
+    double ke = fix_take(&st->acc[0], MD_KFIX);
+    double pe = fix_take(&st->acc[1], MD_EFIX);
+    double w = fix_take(&st->acc[2], MD_EFIX);
+    if (!tp.energy) pe = w = 0.0;
     double xi, eta, lam;
     ke = thermo_advance(kp.dt, tp, mode, ke, pe, w, st, &xi, &eta, &lam);
     if (mode == 2) return;
@@ -242,7 +274,6 @@ inline step_io make_io(md_ctx *c, unsigned long long cond, int has_cond)
 {
     step_io io;
     io.st = c->st;
-    io.partials = c->partials;
     io.rec = c->rec;
     io.rec_cap = c->rec_cap;
     io.counter = &c->st->blocks_done;
