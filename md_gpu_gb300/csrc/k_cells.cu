@@ -376,8 +376,11 @@ __global__ void __launch_bounds__(256) k_build_list(
  * stencil.  The warp first gathers the stencil cells' atom ranges into
  * shared memory (in traversal order) with their prefix sums, then streams the
  * concatenated candidates 32 at a time (lane = candidate, located by binary
- * search over the prefix sums) and tests them against the cell's atoms one i
- * at a time; a ballot appends the hits to i's list.  Entries land in the
+ * search over the prefix sums).  A conservative test against the bounding
+ * box of the cell's atoms drops the candidates (about a third) that no atom
+ * of the cell can reach; the rest enter a per-warp queue in candidate order,
+ * and each full queue of 32 is tested exactly against the cell's atoms one i
+ * at a time, a ballot appending the hits to i's list.  Entries land in the
  * same order as in k_build_list (stencil cells in traversal order, ascending
  * j), so both builders produce identical lists. */
 constexpr int CW_WARPS = 4;
@@ -407,6 +410,9 @@ __global__ void __launch_bounds__(CW_WARPS * 32) k_build_cells(
     __shared__ int s_jb[CW_WARPS][CW_MAXST];
     __shared__ int s_pre[CW_WARPS][CW_MAXST + 1];
     __shared__ unsigned char s_sh[CW_WARPS][CW_MAXST];   /* image code per stencil cell */
+    __shared__ float4 s_fq[CW_WARPS][64];                 /* queue of near candidates: position, */
+    __shared__ unsigned s_fe[CW_WARPS][64];               /* list entry (j | type << 29) */
+    __shared__ unsigned char s_fc[CW_WARPS][64];          /* and image code */
     const int w = threadIdx.x >> 5, lane = threadIdx.x & 31;
     const int r = blockIdx.x * CW_WARPS + w;
     if (r >= ncells) return;
@@ -488,8 +494,72 @@ __global__ void __launch_bounds__(CW_WARPS * 32) k_build_cells(
         const unsigned excl_bits = __ballot_sync(0xffffffffu, any_excl);
         __syncwarp();
         int mycnt = 0;   /* list length of atom i0 + lane */
+        /* The exact test of 32 queued candidates against every atom of the
+         * group; a ballot appends the hits to each atom's row in candidate
+         * order. */
+        auto process = [&](int cnt) {
+            const bool vj = lane < cnt;
+            const float4 q = vj ? s_fq[w][lane] : make_float4(0.f, 0.f, 0.f, 0.f);
+            const unsigned entry = vj ? s_fe[w][lane] : 0u;
+            const int code = vj ? s_fc[w][lane] : 0;
+            const unsigned uj = entry & MD_INDEX_MASK;
+            const int tj = (int)(entry >> MD_TYPE_SHIFT);
+            /* exact images: u = L * rint(d / L) is -L, 0 or +L by stencil cell */
+            const float ux = (code & 3) == 1 ? -L0 : ((code & 3) == 2 ? L0 : 0.0f);
+            const float uy = ((code >> 2) & 3) == 1 ? -L1 : (((code >> 2) & 3) == 2 ? L1 : 0.0f);
+            const float uz = ((code >> 4) & 3) == 1 ? -L2 : (((code >> 4) & 3) == 2 ? L2 : 0.0f);
+            /* the group member this candidate is, if any (never its own neighbour) */
+            const int selfa = (vj && (int)uj >= i0 && (int)uj < i0 + ni) ? (int)uj - i0 : -1;
+            unsigned *rowp = nl + (size_t)i0 * kp.cap;
+            for (int a = 0; a < ni; a++, rowp += kp.cap) {
+                const float4 p = s_p[w][a];
+                float rsq;
+                if (G.shift) {
+                    /* fl(fl(px - qx) - u) is the reference's fl(d - fl(L rint(d/L))) */
+                    float dx = __fsub_rn(__fsub_rn(p.x, q.x), ux);
+                    float dy = __fsub_rn(__fsub_rn(p.y, q.y), uy);
+                    float dz = __fsub_rn(__fsub_rn(p.z, q.z), uz);
+                    rsq = __fadd_rn(__fadd_rn(__fmul_rn(dx, dx), __fmul_rn(dy, dy)), __fmul_rn(dz, dz));
+                } else {
+                    rsq = md_rsq_box(p, q, G.L, G.Li);
+                }
+                bool ok = vj && rsq < G.rskinsq && a != selfa;
+                if ((excl_bits >> a) & 1u) {
+                    uint4 ex = s_ex[w][a];
+                    ok = ok && uj != ex.x && uj != ex.y && uj != ex.z && uj != ex.w &&
+                         !((s_tm[w][a] >> tj) & 1u);
+                }
+                const unsigned bal = __ballot_sync(0xffffffffu, ok);
+                const int base = __shfl_sync(0xffffffffu, mycnt, a);
+                if (ok) {
+                    const int slot = base + __popc(bal & lt);
+                    if (slot < kp.cap) rowp[slot] = entry;
+                }
+                if (lane == a) mycnt += __popc(bal);
+            }
+        };
+        /* Bounding box of the group: candidates farther than rl from it
+         * cannot pass the exact test for any member and are dropped before
+         * it (a conservative FP32 test; the exact test decides the rest). */
+        float bx0 = 3.4e38f, by0 = 3.4e38f, bz0 = 3.4e38f, bx1 = -3.4e38f, by1 = -3.4e38f, bz1 = -3.4e38f;
+        if (lane < ni) {
+            const float4 p = s_p[w][lane];
+            bx0 = bx1 = p.x;
+            by0 = by1 = p.y;
+            bz0 = bz1 = p.z;
+        }
+        for (int o = 16; o > 0; o >>= 1) {
+            bx0 = fminf(bx0, __shfl_xor_sync(0xffffffffu, bx0, o));
+            by0 = fminf(by0, __shfl_xor_sync(0xffffffffu, by0, o));
+            bz0 = fminf(bz0, __shfl_xor_sync(0xffffffffu, bz0, o));
+            bx1 = fmaxf(bx1, __shfl_xor_sync(0xffffffffu, bx1, o));
+            by1 = fmaxf(by1, __shfl_xor_sync(0xffffffffu, by1, o));
+            bz1 = fmaxf(bz1, __shfl_xor_sync(0xffffffffu, bz1, o));
+        }
+        const float near_sq = G.rskinsq * 1.001f + 1e-4f;
+        int fill = 0;   /* queued candidates (in candidate order) */
         for (int g0 = 0; g0 < total; g0 += 32) {
-            int g = g0 + lane;
+            const int g = g0 + lane;
             bool vj = g < total;
             int j = 0, code = 0;
             if (vj) {
@@ -501,41 +571,49 @@ __global__ void __launch_bounds__(CW_WARPS * 32) k_build_cells(
                 j = s_jb[w][a] + (g - s_pre[w][a]);
                 code = s_sh[w][a];
             }
-            float4 q = vj ? pos4[j] : make_float4(0.f, 0.f, 0.f, 0.f);
-            int tj = vj ? type[j] : 0;
-            /* exact images: u = L * rint(d / L) is -L, 0 or +L by stencil cell */
-            const float ux = (code & 3) == 1 ? -L0 : ((code & 3) == 2 ? L0 : 0.0f);
-            const float uy = ((code >> 2) & 3) == 1 ? -L1 : (((code >> 2) & 3) == 2 ? L1 : 0.0f);
-            const float uz = ((code >> 4) & 3) == 1 ? -L2 : (((code >> 4) & 3) == 2 ? L2 : 0.0f);
-            unsigned entry = (unsigned)j | ((unsigned)tj << MD_TYPE_SHIFT);
-            unsigned uj = (unsigned)j;
-            for (int a = 0; a < ni; a++) {
-                float4 p = s_p[w][a];
-                float rsq;
-                if (G.shift) {
-                    /* fl(fl(px - qx) - u) is the reference's fl(d - fl(L rint(d/L))) */
-                    float dx = __fsub_rn(__fsub_rn(p.x, q.x), ux);
-                    float dy = __fsub_rn(__fsub_rn(p.y, q.y), uy);
-                    float dz = __fsub_rn(__fsub_rn(p.z, q.z), uz);
-                    rsq = __fadd_rn(__fadd_rn(__fmul_rn(dx, dx), __fmul_rn(dy, dy)), __fmul_rn(dz, dz));
-                } else {
-                    rsq = md_rsq_box(p, q, G.L, G.Li);
+            const float4 q = vj ? pos4[j] : make_float4(0.f, 0.f, 0.f, 0.f);
+            bool near = vj;
+            if (vj && G.shift) {
+                const float qx = q.x + ((code & 3) == 1 ? -L0 : ((code & 3) == 2 ? L0 : 0.0f));
+                const float qy = q.y + (((code >> 2) & 3) == 1 ? -L1 : (((code >> 2) & 3) == 2 ? L1 : 0.0f));
+                const float qz = q.z + (((code >> 4) & 3) == 1 ? -L2 : (((code >> 4) & 3) == 2 ? L2 : 0.0f));
+                const float ex = fmaxf(fmaxf(bx0 - qx, qx - bx1), 0.0f);
+                const float ey = fmaxf(fmaxf(by0 - qy, qy - by1), 0.0f);
+                const float ez = fmaxf(fmaxf(bz0 - qz, qz - bz1), 0.0f);
+                near = ex * ex + ey * ey + ez * ez < near_sq;
+            }
+            const unsigned nb = __ballot_sync(0xffffffffu, near);
+            if (near) {
+                const int pos = fill + __popc(nb & lt);
+                s_fq[w][pos] = q;
+                s_fe[w][pos] = (unsigned)j | ((unsigned)type[j] << MD_TYPE_SHIFT);
+                s_fc[w][pos] = (unsigned char)code;
+            }
+            fill += __popc(nb);
+            __syncwarp();
+            if (fill >= 32) {
+                process(32);
+                /* move the overflow to the front of the queue */
+                float4 tq;
+                unsigned te = 0;
+                unsigned char tc = 0;
+                const bool mv = lane < fill - 32;
+                if (mv) {
+                    tq = s_fq[w][32 + lane];
+                    te = s_fe[w][32 + lane];
+                    tc = s_fc[w][32 + lane];
                 }
-                bool ok = vj && rsq < G.rskinsq && j != i0 + a;
-                if ((excl_bits >> a) & 1u) {
-                    uint4 ex = s_ex[w][a];
-                    ok = ok && uj != ex.x && uj != ex.y && uj != ex.z && uj != ex.w &&
-                         !((s_tm[w][a] >> tj) & 1u);
+                __syncwarp();
+                if (mv) {
+                    s_fq[w][lane] = tq;
+                    s_fe[w][lane] = te;
+                    s_fc[w][lane] = tc;
                 }
-                unsigned bal = __ballot_sync(0xffffffffu, ok);
-                int base = __shfl_sync(0xffffffffu, mycnt, a);
-                if (ok) {
-                    int slot = base + __popc(bal & lt);
-                    if (slot < kp.cap) nl[(size_t)(i0 + a) * kp.cap + slot] = entry;
-                }
-                if (lane == a) mycnt += __popc(bal);
+                fill -= 32;
+                __syncwarp();
             }
         }
+        if (fill > 0) process(fill);
         /* pad every row to a multiple of 32 with the atom itself */
         for (int a = 0; a < ni; a++) {
             int c = __shfl_sync(0xffffffffu, mycnt, a);
