@@ -11,6 +11,8 @@
  * (cells of side >= rl/2), the atoms are re-sorted along a Hilbert curve of
  * cells at every build, and the rebuild decision never leaves the device.
  */
+#include <type_traits>
+
 #include "md_device.cuh"
 
 namespace {
@@ -510,33 +512,39 @@ __global__ void __launch_bounds__(CW_WARPS * 32) k_build_cells(
             const float uz = ((code >> 4) & 3) == 1 ? -L2 : (((code >> 4) & 3) == 2 ? L2 : 0.0f);
             /* the group member this candidate is, if any (never its own neighbour) */
             const int selfa = (vj && (int)uj >= i0 && (int)uj < i0 + ni) ? (int)uj - i0 : -1;
-            unsigned *rowp = nl + (size_t)i0 * kp.cap;
-            for (int a = 0; a < ni; a++, rowp += kp.cap) {
-                const float4 p = s_p[w][a];
-                float rsq;
-                if (G.shift) {
-                    /* fl(fl(px - qx) - u) is the reference's fl(d - fl(L rint(d/L))) */
-                    float dx = __fsub_rn(__fsub_rn(p.x, q.x), ux);
-                    float dy = __fsub_rn(__fsub_rn(p.y, q.y), uy);
-                    float dz = __fsub_rn(__fsub_rn(p.z, q.z), uz);
-                    rsq = __fadd_rn(__fadd_rn(__fmul_rn(dx, dx), __fmul_rn(dy, dy)), __fmul_rn(dz, dz));
-                } else {
-                    rsq = md_rsq_box(p, q, G.L, G.Li);
+            /* two copies of the loop: with and without the exclusion tests */
+            auto loop = [&](auto with_excl) {
+                unsigned *rowp = nl + (size_t)i0 * kp.cap;
+#pragma unroll 2
+                for (int a = 0; a < ni; a++, rowp += kp.cap) {
+                    const float4 p = s_p[w][a];
+                    float rsq;
+                    if (G.shift) {
+                        /* fl(fl(px - qx) - u) is the reference's fl(d - fl(L rint(d/L))) */
+                        float dx = __fsub_rn(__fsub_rn(p.x, q.x), ux);
+                        float dy = __fsub_rn(__fsub_rn(p.y, q.y), uy);
+                        float dz = __fsub_rn(__fsub_rn(p.z, q.z), uz);
+                        rsq = __fadd_rn(__fadd_rn(__fmul_rn(dx, dx), __fmul_rn(dy, dy)), __fmul_rn(dz, dz));
+                    } else {
+                        rsq = md_rsq_box(p, q, G.L, G.Li);
+                    }
+                    bool ok = vj && rsq < G.rskinsq && a != selfa;
+                    if (decltype(with_excl)::value && ((excl_bits >> a) & 1u)) {
+                        uint4 ex = s_ex[w][a];
+                        ok = ok && uj != ex.x && uj != ex.y && uj != ex.z && uj != ex.w &&
+                             !((s_tm[w][a] >> tj) & 1u);
+                    }
+                    const unsigned bal = __ballot_sync(0xffffffffu, ok);
+                    const int base = __shfl_sync(0xffffffffu, mycnt, a);
+                    if (ok) {
+                        const int slot = base + __popc(bal & lt);
+                        if (slot < kp.cap) rowp[slot] = entry;
+                    }
+                    if (lane == a) mycnt += __popc(bal);
                 }
-                bool ok = vj && rsq < G.rskinsq && a != selfa;
-                if ((excl_bits >> a) & 1u) {
-                    uint4 ex = s_ex[w][a];
-                    ok = ok && uj != ex.x && uj != ex.y && uj != ex.z && uj != ex.w &&
-                         !((s_tm[w][a] >> tj) & 1u);
-                }
-                const unsigned bal = __ballot_sync(0xffffffffu, ok);
-                const int base = __shfl_sync(0xffffffffu, mycnt, a);
-                if (ok) {
-                    const int slot = base + __popc(bal & lt);
-                    if (slot < kp.cap) rowp[slot] = entry;
-                }
-                if (lane == a) mycnt += __popc(bal);
-            }
+            };
+            if (excl_bits) loop(std::true_type());
+            else loop(std::false_type());
         };
         /* Bounding box of the group: candidates farther than rl from it
          * cannot pass the exact test for any member and are dropped before
