@@ -31,6 +31,7 @@ __global__ void __launch_bounds__(128) k_pair_b(int cap, int pitch, const int2 *
                                                 float *vir, float *epot)
 {
     __shared__ float2 lj[MD_MAXTYPE * MD_MAXTYPE];
+    pdl_trigger();   /* the integrator may be scheduled; it waits for this grid */
     const int2 bt = tab[blockIdx.x];
     const md_rep &R = reps[bt.x];
     if (threadIdx.x < MD_MAXTYPE * MD_MAXTYPE)
@@ -115,6 +116,7 @@ __global__ void __launch_bounds__(3 * MD_LA) k_leapfrog_b(md_kparams kp, thermo_
     __shared__ double sh[3 * MD_LA / 32];
     __shared__ long long shl[3 * (3 * MD_LA / 32)];
     __shared__ float s_x[3][MD_LA];
+    pdl_wait();   /* the forces of this step */
     const int2 bt = tab[blockIdx.x];
     const md_rep &R = reps[bt.x];
     const int d = threadIdx.x / MD_LA, a = threadIdx.x - d * MD_LA;
@@ -213,6 +215,7 @@ __global__ void __launch_bounds__(3 * MD_LA) k_vv_second_b(md_kparams kp, thermo
 {
     __shared__ double sh[3 * MD_LA / 32];
     __shared__ long long shl[3 * (3 * MD_LA / 32)];
+    pdl_wait();   /* the forces of this step */
     const int2 bt = tab[blockIdx.x];
     const md_rep &R = reps[bt.x];
     const int d = threadIdx.x / MD_LA, a = threadIdx.x - d * MD_LA;
@@ -287,10 +290,11 @@ void launch_forces_b(md_ctx *c, const md_kparams &kp, bool energy, int terms)
 void launch_leapfrog_b(md_ctx *c, const md_kparams &kp, int energy, unsigned long long cond,
                        int has_cond)
 {
-    k_leapfrog_b<<<grid_int_blocks(c), 3 * MD_LA, 0, c->stream>>>(
-        kp, make_tp(c, energy), make_io(c, cond, has_cond), c->nrep, grid_int(c), c->reps_dev,
-        c->repst, c->rep_upd, c->racc, c->x, c->v, c->mass, c->kick, c->pos4, c->f, c->epot,
-        c->vir);
+    md_launch_pdl(k_leapfrog_b, dim3(grid_int_blocks(c)), dim3(3 * MD_LA), c->stream, kp,
+                  make_tp(c, energy), make_io(c, cond, has_cond), c->nrep, grid_int(c),
+                  (const md_rep *)c->reps_dev, c->repst, c->rep_upd, c->racc, c->x, c->v,
+                  (const double *)c->mass, (const double *)c->kick, c->pos4,
+                  (const long long *)c->f, (const float *)c->epot, (const float *)c->vir);
 }
 
 void launch_vv_first_b(md_ctx *c, const md_kparams &kp, unsigned long long cond, int has_cond)
@@ -303,7 +307,9 @@ void launch_vv_first_b(md_ctx *c, const md_kparams &kp, unsigned long long cond,
 
 void launch_vv_second_b(md_ctx *c, const md_kparams &kp, int energy, int kick)
 {
-    k_vv_second_b<<<grid_int_blocks(c), 3 * MD_LA, 0, c->stream>>>(
-        kp, make_tp(c, energy), kick, make_io(c, 0, 0), c->nrep, grid_int(c), c->reps_dev,
-        c->repst, c->racc, c->v, c->mass, c->kick, c->f, c->epot, c->vir);
+    md_launch_pdl(k_vv_second_b, dim3(grid_int_blocks(c)), dim3(3 * MD_LA), c->stream, kp,
+                  make_tp(c, energy), kick, make_io(c, 0, 0), c->nrep, grid_int(c),
+                  (const md_rep *)c->reps_dev, c->repst, c->racc, c->v, (const double *)c->mass,
+                  (const double *)c->kick, (const long long *)c->f, (const float *)c->epot,
+                  (const float *)c->vir);
 }

@@ -31,6 +31,7 @@ __global__ void __launch_bounds__(128) k_pair(md_kparams kp, pair_consts pc,
                                               float *vir, float *epot)
 {
     __shared__ float2 lj[MD_MAXTYPE * MD_MAXTYPE];
+    pdl_trigger();   /* the integrator may be scheduled; it waits for this grid */
     if (threadIdx.x < MD_MAXTYPE * MD_MAXTYPE) lj[threadIdx.x] = ljtab[threadIdx.x];
     __syncthreads();
     int gt = blockIdx.x * blockDim.x + threadIdx.x;

@@ -49,6 +49,7 @@ __global__ void __launch_bounds__(3 * MD_LA) k_leapfrog(md_kparams kp, thermo_pa
 {
     __shared__ long long sh[3 * (3 * MD_LA / 32)];
     __shared__ float s_x[3][MD_LA];
+    pdl_wait();   /* the forces of this step */
     const int d = threadIdx.x / MD_LA, a = threadIdx.x - d * MD_LA;
     const int s = blockIdx.x * MD_LA + a;
     const size_t o = (size_t)d * kp.pitch + s;
@@ -132,6 +133,7 @@ __global__ void __launch_bounds__(3 * MD_LA) k_vv_second(md_kparams kp, thermo_p
                                                         const float *__restrict__ vir)
 {
     __shared__ long long sh[3 * (3 * MD_LA / 32)];
+    pdl_wait();   /* the forces of this step */
     const int d = threadIdx.x / MD_LA, a = threadIdx.x - d * MD_LA;
     const int s = blockIdx.x * MD_LA + a;
     const size_t o = (size_t)d * kp.pitch + s;
@@ -214,8 +216,10 @@ void launch_leapfrog(md_ctx *c, const md_kparams &kp, int energy, unsigned long 
     }
 
     int nb = (kp.n + MD_LA - 1) / MD_LA;
-    k_leapfrog<<<nb, 3 * MD_LA, 0, c->stream>>>(kp, make_tp(c, energy), make_io(c, cond, has_cond), c->x,
-                                          c->v, c->mass, c->kick, c->pos4, c->f, c->epot, c->vir);
+    md_launch_pdl(k_leapfrog, dim3(nb), dim3(3 * MD_LA), c->stream, kp, make_tp(c, energy),
+                  make_io(c, cond, has_cond), c->x, c->v, (const double *)c->mass,
+                  (const double *)c->kick, c->pos4, (const long long *)c->f,
+                  (const float *)c->epot, (const float *)c->vir);
 }
 
 void launch_vv_first(md_ctx *c, const md_kparams &kp, unsigned long long cond, int has_cond)
@@ -238,8 +242,9 @@ void launch_vv_second(md_ctx *c, const md_kparams &kp, int energy)
     }
 
     int nb = (kp.n + MD_LA - 1) / MD_LA;
-    k_vv_second<<<nb, 3 * MD_LA, 0, c->stream>>>(kp, make_tp(c, energy), 1, make_io(c, 0, 0), c->v,
-                                           c->mass, c->kick, c->f, c->epot, c->vir);
+    md_launch_pdl(k_vv_second, dim3(nb), dim3(3 * MD_LA), c->stream, kp, make_tp(c, energy), 1,
+                  make_io(c, 0, 0), c->v, (const double *)c->mass, (const double *)c->kick,
+                  (const long long *)c->f, (const float *)c->epot, (const float *)c->vir);
 }
 
 void launch_thermo_from_state(md_ctx *c, const md_kparams &kp, int energy)

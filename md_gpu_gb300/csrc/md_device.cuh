@@ -36,6 +36,15 @@ __device__ __forceinline__ int cell_of(float x, float box, float binlen, int nc)
     return c >= nc ? nc - 1 : c;
 }
 
+/* Programmatic dependent launch: a kernel launched with the
+ * programmatic-serialization attribute (md_launch_pdl) may be scheduled
+ * while its predecessor in the stream still runs.  pdl_wait() blocks until
+ * the predecessor has completed and its writes are visible; it returns at
+ * once for a kernel launched normally.  pdl_trigger() lets the dependent
+ * kernel be scheduled before this kernel's last blocks finish. */
+__device__ __forceinline__ void pdl_wait() { asm volatile("griddepcontrol.wait;" ::: "memory"); }
+__device__ __forceinline__ void pdl_trigger() { asm volatile("griddepcontrol.launch_dependents;" ::: "memory"); }
+
 /* True in every thread of the block that finishes last (threadfence
  * reduction).  The caller's prior global writes are visible to that block;
  * it must read other blocks' results with __ldcg / volatile and reset the

@@ -286,6 +286,26 @@ void launch_leapfrog_b(md_ctx *c, const md_kparams &kp, int energy, unsigned lon
 void launch_vv_first_b(md_ctx *c, const md_kparams &kp, unsigned long long cond, int has_cond);
 void launch_vv_second_b(md_ctx *c, const md_kparams &kp, int energy, int kick);
 
+/* Launches kernel k so that it may start before its predecessor in the
+ * stream ends (the kernel must call pdl_wait() before touching data that
+ * predecessor writes). */
+template <typename... KArgs, typename... Args>
+inline cudaError_t md_launch_pdl(void (*k)(KArgs...), dim3 grid, dim3 block, cudaStream_t s,
+                                 Args... args)
+{
+    cudaLaunchConfig_t cfg = {};
+    cfg.gridDim = grid;
+    cfg.blockDim = block;
+    cfg.dynamicSmemBytes = 0;
+    cfg.stream = s;
+    cudaLaunchAttribute at[1];
+    at[0].id = cudaLaunchAttributeProgrammaticStreamSerialization;
+    at[0].val.programmaticStreamSerializationAllowed = 1;
+    cfg.attrs = at;
+    cfg.numAttrs = 1;
+    return cudaLaunchKernelEx(&cfg, k, args...);
+}
+
 #define MD_CUDA_TRY(c, expr)                                                   \
     do {                                                                       \
         cudaError_t e_ = (expr);                                               \

@@ -11,7 +11,7 @@
 #ifndef MD_PAIR_CUH
 #define MD_PAIR_CUH
 
-#include "md_internal.h"
+#include "md_device.cuh"
 
 namespace {
 
