@@ -13,7 +13,10 @@ NaCl-like replicas of 256..8192 ions (own eps/sigma per type and charge scale
 within +-10%), velocity Verlet NVE at dt 2 fs, advanced together by
 md_create_batch (one launch per stage, one graph for the batch); and under
 "adjoint", gradients per second of a trajectory loss of 64 x 8000-ion NaCl
-over 2000 velocity-Verlet steps (md_adjoint_run, checkpoints every 50 steps).
+over 2000 velocity-Verlet steps (md_adjoint_run, checkpoints every 50 steps);
+and under "other_systems", the throughput of the 4000-atom argon (velocity
+Verlet NVE) and 98304-atom flexible water (Nose-Hoover velocity Verlet,
+bonds and angles) systems.
 
     python bench.py [--gpus N] [--steps K] [--warmup W] [--impl ours|reference]
 
@@ -148,6 +151,35 @@ def run_reference(args):
                              "sample": sample},
             "e2e": {"value": value, "unit": UNIT, "h2d_bytes_per_step": 0, "d2h_bytes_per_step": 0}}
     print(json.dumps(line), flush=True)
+
+
+def system_leg(name, sys_, integrator_name, dt_fs, args, flush):
+    """Atom-steps/s of one more single system through md_step (graphs of 32
+    steps, L2 flushed before each timed segment)."""
+    import torch
+
+    import md_gpu_gb300 as md
+    tmp = tempfile.mkdtemp(prefix="mdbench_")
+    from md_gpu_gb300 import synth
+    base = synth.write_case(sys_, tmp, name)
+    with md.MDSystem.from_files(base) as sim:
+        pt, lt = sim.autotune()
+        sim.step(args.md_steps)
+        b0 = sim.info()["builds"]
+        ms = []
+        for _ in range(args.other_segments):
+            flush.zero_()
+            torch.cuda.synchronize()
+            sim.step(args.md_steps)
+            ms.append(sim.last_step_ms())
+        info = sim.info()
+        n = sim.natom
+    steps = args.md_steps * len(ms)
+    sps = steps / (sum(ms) * 1e-3)
+    return {"value": n * sps, "unit": UNIT, "natom": n, "integrator": integrator_name,
+            "ms_per_md_step": sum(ms) / steps, "ns_per_day": sps * dt_fs * 0.0864,
+            "list_builds": info["builds"] - b0, "md_steps": steps, "pair_threads_per_atom": pt,
+            "list_builder": "warp per cell" if lt == 0 else f"{lt} threads per atom"}
 
 
 def batch_leg(args, flush):
@@ -343,6 +375,20 @@ def run_ours(args):
         if args.nrep > 0:
             extra_batch = batch_leg(args, flush)
         extra_adj = adjoint_leg(args) if args.adj_nrep > 0 else None
+        others = {}
+        if args.other_segments > 0:
+            from md_gpu_gb300 import synth
+            others["argon4000"] = dict(
+                workload=("plain LJ argon, 4000 atoms fcc 10^3 x 4, rho* 0.8442, sigma = 1 A, eps = 1 kJ/mol, "
+                          "m = 1 g/mol, rc 2.5, skin 0.3, T* 0.72, velocity Verlet NVE dt 0.5 fs"),
+                **system_leg("argon", synth.argon_fcc(10, seed=1, integrator="vv"), "velocity Verlet NVE",
+                             0.5, args, flush))
+            others["water98k"] = dict(
+                workload=("flexible 3-site water, 32768 molecules (98304 atoms) at 0.997 g/cm^3, harmonic "
+                          "O-H bonds and H-O-H angles, H-H excluded, Wolf alpha 0.2/A rc 10 A skin 1 A, "
+                          "Nose-Hoover velocity Verlet 300 K, dt 0.5 fs"),
+                **system_leg("water", synth.water_grid(32, seed=1), "Nose-Hoover velocity Verlet", 0.5,
+                             args, flush))
         cpu_v, cpu_dt, cores = cpu_reference_sample(base, 1, 0, args.ref_md_steps)
         extra = {"roofline": roof, "e2e": e2e, "force_rms_rel_err_vs_fp64": err,
                  "cpu_baseline": {"value": cpu_v, "unit": UNIT, "cores": cores, "kind": "port",
@@ -353,6 +399,8 @@ def run_ours(args):
             extra["batched_replicas"] = extra_batch
         if extra_adj is not None:
             extra["adjoint"] = extra_adj
+        if others:
+            extra["other_systems"] = others
     line = {"metric": METRIC, "value": value, "unit": UNIT, "n_gpus": world, "steps": args.steps,
             "warmup": args.warmup, "ms_per_step": total_ms / args.steps, "higher_is_better": True,
             "scaling": "weak", "vs_baseline": None, "dtype": "f32",
@@ -391,6 +439,8 @@ def main():
     ap.add_argument("--adj-nrep", type=int, default=64, help="replicas of the adjoint leg (0: skip it)")
     ap.add_argument("--adj-natom", type=int, default=8000)
     ap.add_argument("--adj-steps", type=int, default=2000)
+    ap.add_argument("--other-segments", type=int, default=3,
+                    help="timed segments of the argon and water systems (0: skip them)")
     ap.add_argument("--ref-md-steps", type=int, default=10)
     ap.add_argument("--ncell", type=int, default=20)
     ap.add_argument("--no-autotune", action="store_true")
