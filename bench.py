@@ -179,6 +179,7 @@ def system_leg(name, sys_, integrator_name, dt_fs, args, flush):
     return {"value": n * sps, "unit": UNIT, "natom": n, "integrator": integrator_name,
             "ms_per_md_step": sum(ms) / steps, "ns_per_day": sps * dt_fs * 0.0864,
             "list_builds": info["builds"] - b0, "md_steps": steps, "pair_threads_per_atom": pt,
+            "pair_entries_per_lane": info["pair_depth"],
             "list_builder": "warp per cell" if lt == 0 else f"{lt} threads per atom"}
 
 
@@ -411,6 +412,7 @@ def run_ours(args):
                        "ns_per_day": md_steps_per_s * DT_FS * 0.0864,
                        "list_builds_in_timed_region": builds,
                        "pair_threads_per_atom": info["pair_tpa"],
+                       "pair_entries_per_lane": info["pair_depth"],
                        "list_builder": "warp per cell" if info["list_tpa"] == 0
                        else f"{info['list_tpa']} threads per atom",
                        "autotuned": tuned is not None,

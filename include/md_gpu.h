@@ -206,6 +206,7 @@ typedef struct {
     int kernels_per_step;   /* kernel launches of one md_step step without a rebuild */
     int kernels_per_rebuild; /* kernels a list rebuild adds to a step */
     int kernels_per_graph;  /* kernels a step graph runs besides its steps (condition set-up) */
+    int pair_entries_per_lane; /* list entries each pair-kernel lane loads per batch */
 } md_info;
 md_status md_get_info(md_ctx *ctx, md_info *out);
 /* Sorted -> original index map of the current atom order. */
@@ -216,9 +217,15 @@ md_status md_get_cell_ranks(md_ctx *ctx, int *rank);
  * the list builder (0 = one warp per cell, the default; or 1..32 threads per
  * atom; batches take 0 only).  Every setting builds the identical list. */
 md_status md_set_tuning(md_ctx *ctx, int pair_tpa, int list_tpa);
-/* Autotuner: times the pair kernel for 2/4/8/16 threads per atom and the list
- * builders (warp per cell, 4/8/16 threads per atom) on the current state and
- * keeps the fastest of each; returns the choice.  For leapfrog systems
+/* List entries each pair-kernel lane loads per batch (memory-level
+ * parallelism against registers): 0 = the default for the lane count (8 for
+ * 1-4 lanes, 4 for 8, 2 for 16, 1 for 32); single systems also take half the
+ * default at 4, 8 and 16 lanes.  md_set_tuning resets it to 0. */
+md_status md_set_pair_depth(md_ctx *ctx, int depth);
+/* Autotuner: times the pair kernel for 2/4/8/16 threads per atom (single
+ * systems also at 4/8/16 threads with half the default entries per lane and
+ * batch) and the list builders (warp per cell, 4/8/16 threads per atom) on the
+ * current state and keeps the fastest of each; returns the choice.  For leapfrog systems
  * without bonded terms it also times the step with the pair kernel and the
  * integrator fused into one kernel against separate kernels, by running
  * steps: the system then advances by 192 steps. */

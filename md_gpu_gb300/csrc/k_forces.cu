@@ -129,19 +129,22 @@ void pair_dispatch(md_ctx *c, const md_kparams &kp, const pair_consts &pc)
     long long threads = (long long)kp.n * c->pair_tpa;
     int nb = (int)((threads + 127) / 128);
     const float2 *lj = (const float2 *)c->lj_dev;
-    switch (c->pair_tpa) {
-#define MD_PAIR_CASE(T)                                                                          \
-    case T:                                                                                      \
-        k_pair<KIND, T, (T >= 32 ? 1 : (T >= 16 ? 2 : (T >= 8 ? 4 : 8))), ENERGY>               \
-            <<<nb, 128, 0, c->stream>>>(                                                         \
+    const int key = c->pair_tpa * 100 + md_pair_depth(c);
+    switch (key) {
+#define MD_PAIR_CASE(T, BB)                                                                      \
+    case T * 100 + BB:                                                                           \
+        k_pair<KIND, T, BB, ENERGY><<<nb, 128, 0, c->stream>>>(                                  \
             kp, pc, c->pos4, c->type, c->nl, c->nl_n, lj, c->f, c->vir, c->epot);                \
         break;
-        MD_PAIR_CASE(1)
-        MD_PAIR_CASE(2)
-        MD_PAIR_CASE(4)
-        MD_PAIR_CASE(8)
-        MD_PAIR_CASE(16)
-        MD_PAIR_CASE(32)
+        MD_PAIR_CASE(1, 8)
+        MD_PAIR_CASE(2, 8)
+        MD_PAIR_CASE(4, 4)
+        MD_PAIR_CASE(4, 8)
+        MD_PAIR_CASE(8, 2)
+        MD_PAIR_CASE(8, 4)
+        MD_PAIR_CASE(16, 1)
+        MD_PAIR_CASE(16, 2)
+        MD_PAIR_CASE(32, 1)
 #undef MD_PAIR_CASE
     default:
         break;

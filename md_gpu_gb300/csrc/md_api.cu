@@ -1408,6 +1408,7 @@ md_status md_get_info(md_ctx *c, md_info *out)
         out->binlen[k] = c->binlen[k];
     }
     out->pair_threads_per_atom = c->pair_tpa;
+    out->pair_entries_per_lane = md_pair_depth(c);
     out->list_threads_per_atom = c->list_tpa;
     out->builds = h.builds;
     out->max_neighbors = *std::max_element(cnt.begin(), cnt.begin() + c->n);
@@ -1456,15 +1457,20 @@ md_status md_set_type_exclusions(md_ctx *c, const unsigned *mask)
 md_status md_autotune(md_ctx *c, int *pair_tpa, int *list_tpa)
 {
     if (!c) return MD_ERR_ARG;
-    const int pt[] = {2, 4, 8, 16};
     const int lt[] = {0, 4, 8, 16};
     float best = 1e30f;
     int bp = c->pair_tpa, bl = c->list_tpa, bf = 0;
     c->fuse_step = 0;
-    /* best of three timings of 20 launches per candidate: robust to a slow
-     * first launch and to other work on the device */
-    for (int t : pt) {
-        c->pair_tpa = t;
+    /* best of three timings of 20 launches per candidate (lanes per atom,
+     * entries per lane and batch): robust to a slow first launch and to other
+     * work on the device.  Batches and the fused kernel use the default depth
+     * (depth 0), so they time each lane count once. */
+    const int combos[][2] = {{2, 0}, {4, 0}, {4, 4}, {8, 0}, {8, 2}, {16, 0}, {16, 1}};
+    int bd = 0;
+    for (const auto &cb : combos) {
+        if (c->batch && cb[1] != 0) continue;
+        c->pair_tpa = cb[0];
+        c->pair_depth = cb[1];
         float ms = 0.0f, m2 = 1e30f;
         md_status s = md_time_pair(c, 5, &ms);
         for (int rep = 0; rep < 3 && s == MD_OK; rep++) {
@@ -1472,8 +1478,9 @@ md_status md_autotune(md_ctx *c, int *pair_tpa, int *list_tpa)
             m2 = std::min(m2, ms);
         }
         if (s != MD_OK) return s;
-        if (m2 < best) { best = m2; bp = t; }
+        if (m2 < best) { best = m2; bp = cb[0]; bd = c->pair_depth; }
     }
+    c->pair_depth = bd;
     c->pair_tpa = bp;
     /* leapfrog systems without bonded terms: separate or fused pair and
      * integrator kernels, timed as they run (the system advances 192 steps) */
@@ -1520,6 +1527,21 @@ md_status md_set_graphs(md_ctx *c, int use_graphs)
     return MD_OK;
 }
 
+md_status md_set_pair_depth(md_ctx *c, int depth)
+{
+    if (!c) return MD_ERR_ARG;
+    const int t = c->pair_tpa;
+    const bool ok = depth == 0 || (!c->batch && ((t == 4 && depth == 4) || (t == 8 && depth == 2) ||
+                                                 (t == 16 && depth == 1)));
+    if (!ok) return fail(c, MD_ERR_ARG, "md_set_pair_depth: depth not built for this lane count");
+    c->pair_depth = depth;
+    if (c->gexec) {
+        cudaGraphExecDestroy(c->gexec);
+        c->gexec = nullptr;
+    }
+    return MD_OK;
+}
+
 md_status md_set_tuning(md_ctx *c, int pair_tpa, int list_tpa)
 {
     if (!c) return MD_ERR_ARG;
@@ -1528,6 +1550,7 @@ md_status md_set_tuning(md_ctx *c, int pair_tpa, int list_tpa)
     if (c->batch && list_tpa != 0)
         return fail(c, MD_ERR_ARG, "md_set_tuning: a batch builds its lists one warp per cell");
     c->pair_tpa = pair_tpa;
+    c->pair_depth = 0;
     c->list_tpa = list_tpa;
     if (c->gexec) {
         cudaGraphExecDestroy(c->gexec);

@@ -197,6 +197,7 @@ struct md_ctx {
     long long host_step = 0;       /* steps run so far (mirrors st->step) */
     double *io_dev = nullptr;      /* 4*pitch doubles for host transfers */
     int pair_tpa = 8;    /* threads per atom in the pair kernel */
+    int pair_depth = 0;  /* list entries per lane and batch (0: the default for pair_tpa) */
     int list_tpa = 0;    /* list build: 0 = one warp per cell, else threads per atom */
 
     /* batches of replicas (md_create_batch; any number, 1 included) */
@@ -285,6 +286,16 @@ void launch_leapfrog_b(md_ctx *c, const md_kparams &kp, int energy, unsigned lon
                        int has_cond);
 void launch_vv_first_b(md_ctx *c, const md_kparams &kp, unsigned long long cond, int has_cond);
 void launch_vv_second_b(md_ctx *c, const md_kparams &kp, int energy, int kick);
+
+/* List entries each pair-kernel lane loads per batch for the context's
+ * lanes per atom: the autotuner's choice, else the default (TPA * depth
+ * divides the 32-entry row quantum). */
+inline int md_pair_depth(const md_ctx *c)
+{
+    const int t = c->pair_tpa;
+    if (c->pair_depth > 0 && MD_LIST_QUANTUM % (t * c->pair_depth) == 0) return c->pair_depth;
+    return t >= 32 ? 1 : (t >= 16 ? 2 : (t >= 8 ? 4 : 8));
+}
 
 /* Launches kernel k so that it may start before its predecessor in the
  * stream ends (the kernel must call pdl_wait() before touching data that

@@ -66,7 +66,8 @@ class Info(C.Structure):
                 ("ncell", C.c_int * 3), ("stencil", C.c_int * 3), ("binlen", C.c_float * 3),
                 ("pair_threads_per_atom", C.c_int), ("list_threads_per_atom", C.c_int),
                 ("builds", C.c_int), ("max_neighbors", C.c_int), ("kernels_per_step", C.c_int),
-                ("kernels_per_rebuild", C.c_int), ("kernels_per_graph", C.c_int)]
+                ("kernels_per_rebuild", C.c_int), ("kernels_per_graph", C.c_int),
+                ("pair_entries_per_lane", C.c_int)]
 
 
 def _make_desc(keep, *, box, itype, charge, pos, vel, type_mass, lj1, lj2, lkspace, rcutsq,
@@ -143,6 +144,7 @@ def library(path: Optional[str] = None):
     L.md_get_order.argtypes = [vp, vp]
     L.md_get_cell_ranks.argtypes = [vp, vp]
     L.md_set_tuning.argtypes = [vp, C.c_int, C.c_int]
+    L.md_set_pair_depth.argtypes = [vp, C.c_int]
     L.md_last_step_ms.argtypes = [vp, C.POINTER(C.c_float)]
     L.md_last_error.argtypes = [vp, C.c_char_p, C.c_int]
     L.md_time_pair.argtypes = [vp, C.c_int, C.POINTER(C.c_float)]
@@ -365,7 +367,8 @@ class MDSystem:
                 "builds": i.builds, "max_neighbors": i.max_neighbors,
                 "kernels_per_step": i.kernels_per_step,
                 "kernels_per_rebuild": i.kernels_per_rebuild,
-                "kernels_per_graph": i.kernels_per_graph}
+                "kernels_per_graph": i.kernels_per_graph,
+                "pair_depth": i.pair_entries_per_lane}
 
     def neighbor_list(self, nmax):
         """Reference layout (neighborlist.cu:284): (nnlist[pitch*nmax], nnlist_max[pitch])."""
@@ -414,8 +417,10 @@ class MDSystem:
         """Replay captured step graphs (default) or launch eagerly."""
         _check(library().md_set_graphs(self._ctx, 1 if use_graphs else 0), self._ctx)
 
-    def set_tuning(self, pair_tpa, list_tpa):
+    def set_tuning(self, pair_tpa, list_tpa, pair_depth=0):
         _check(library().md_set_tuning(self._ctx, pair_tpa, list_tpa), self._ctx)
+        if pair_depth:
+            _check(library().md_set_pair_depth(self._ctx, pair_depth), self._ctx)
 
     def write_cfg(self, path):
         _check(library().md_write_cfg(self._ctx, path.encode()), self._ctx)

@@ -286,17 +286,21 @@ def test_list_rebuilds_keep_parity():
     assert np.array_equal(gu.rows_canonical(nn, nm, n, 512), gu.rows_canonical(onn, onm, n, 512))
 
 
-@pytest.mark.parametrize("pair_tpa,list_tpa", [(1, 1), (2, 0), (8, 8), (16, 0), (32, 32)])
-def test_thread_split_variants(pair_tpa, list_tpa):
+@pytest.mark.parametrize("pair_tpa,list_tpa,depth", [(1, 1, 0), (2, 0, 0), (4, 4, 4), (8, 8, 0),
+                                                     (8, 0, 2), (16, 0, 0), (16, 16, 1), (32, 32, 0)])
+def test_thread_split_variants(pair_tpa, list_tpa, depth):
     case = oracle.load(_write(synth.nacl_rocksalt(ncell=5, seed=30, nmaxlist=512)))
     orc = gu.oracle_state(case)
     with gu.system_from_case(case) as sim:
-        sim.set_tuning(pair_tpa, list_tpa)
+        sim.set_tuning(pair_tpa, list_tpa, depth)
+        assert sim.info()["pair_depth"] == (depth or {1: 8, 2: 8, 4: 8, 8: 4, 16: 2, 32: 1}[pair_tpa])
         sim.update_neighbors(force=True)
-        sim.compute_forces(TERM_PAIR)
+        sim.compute_forces(TERM_PAIR, energy=True)
         F = sim.forces()
+        E = sim.energies()
         nn, nm = sim.neighbor_list(512)
     assert gu.rms_rel(F[:, :3], orc["f64"][:, :3]) <= FORCE_TOL
+    assert gu.rms_rel(E, orc["ep64"]) <= 2e-5
     n = case.natom
     assert np.array_equal(gu.rows_canonical(nn, nm, n, 512), gu.rows_canonical(orc["nn"], orc["nm"], n, 512))
 
