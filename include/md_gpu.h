@@ -207,6 +207,10 @@ typedef struct {
     int kernels_per_rebuild; /* kernels a list rebuild adds to a step */
     int kernels_per_graph;  /* kernels a step graph runs besides its steps (condition set-up) */
     int pair_entries_per_lane; /* list entries each pair-kernel lane loads per batch */
+    int positions_centered; /* 1: every position uploaded last lay in [-L/2, L/2] per axis,
+                               so the fast paths that rely on it are on (the integrators
+                               keep it so); 0: cells bin periodic images, every pair
+                               takes the minimum-image shift */
 } md_info;
 md_status md_get_info(md_ctx *ctx, md_info *out);
 /* Sorted -> original index map of the current atom order. */

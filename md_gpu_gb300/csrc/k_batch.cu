@@ -21,7 +21,8 @@ namespace {
 /* Pair forces of a batch: block b holds 128/TPA atoms of replica tab[b].x
  * starting at tab[b].y. */
 template <int KIND, int TPA, int B, bool ENERGY>
-__global__ void __launch_bounds__(128) k_pair_b(int cap, int pitch, const int2 *__restrict__ tab,
+__global__ void __launch_bounds__(128) k_pair_b(int cap, int pitch, int centered,
+                                                const int2 *__restrict__ tab,
                                                 const md_rep *__restrict__ reps,
                                                 const float2 *__restrict__ ljr,
                                                 const float4 *__restrict__ pos4,
@@ -36,7 +37,7 @@ __global__ void __launch_bounds__(128) k_pair_b(int cap, int pitch, const int2 *
     const md_rep &R = reps[bt.x];
     if (threadIdx.x < MD_MAXTYPE * MD_MAXTYPE)
         lj[threadIdx.x] = ljr[bt.x * MD_MAXTYPE * MD_MAXTYPE + threadIdx.x];
-    const geom_reg g = rep_geom(R);
+    const geom_reg g = rep_geom(R, centered != 0);
     const int end = R.atom0 + R.natom;
     __syncthreads();
     const int i = bt.y + (int)threadIdx.x / TPA, lane = (int)threadIdx.x % TPA;
@@ -250,7 +251,8 @@ void pair_dispatch_b(md_ctx *c, const md_kparams &kp)
 #define MD_PAIR_B_CASE(T)                                                                        \
     case T:                                                                                      \
         k_pair_b<KIND, T, (T >= 32 ? 1 : (T >= 16 ? 2 : (T >= 8 ? 4 : 8))), ENERGY>             \
-            <<<nb, 128, 0, c->stream>>>(kp.cap, kp.pitch, tab, c->reps_dev, c->ljr_dev, c->pos4, \
+            <<<nb, 128, 0, c->stream>>>(kp.cap, kp.pitch, kp.centered, tab, c->reps_dev,         \
+                                        c->ljr_dev, c->pos4,                                     \
                                         c->type, c->nl, c->nl_n, c->f, c->vir, c->epot);         \
         break;
         MD_PAIR_B_CASE(1)

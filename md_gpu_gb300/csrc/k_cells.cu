@@ -34,9 +34,9 @@ __global__ void k_cell_key(md_kparams kp, const md_devstate *st, int always,
     int i = blockIdx.x * blockDim.x + threadIdx.x;
     if (i >= kp.n) return;
     float4 p = pos4[i];
-    int cx = cell_of(p.x, kp.box[0], kp.binlen[0], kp.ncell[0]);
-    int cy = cell_of(p.y, kp.box[1], kp.binlen[1], kp.ncell[1]);
-    int cz = cell_of(p.z, kp.box[2], kp.binlen[2], kp.ncell[2]);
+    int cx = cell_of(cell_coord(p.x, kp.box[0], kp.boxi[0], kp.centered), kp.box[0], kp.binlen[0], kp.ncell[0]);
+    int cy = cell_of(cell_coord(p.y, kp.box[1], kp.boxi[1], kp.centered), kp.box[1], kp.binlen[1], kp.ncell[1]);
+    int cz = cell_of(cell_coord(p.z, kp.box[2], kp.boxi[2], kp.centered), kp.box[2], kp.binlen[2], kp.ncell[2]);
     int r = cell_rank[cx + kp.ncell[0] * (cy + kp.ncell[1] * cz)];
     key[i] = r;
     atomicAdd(&cell_count[r], 1);
@@ -61,7 +61,8 @@ __global__ void k_check_b(int n, const md_rep *__restrict__ reps, const int *__r
  * cell, so every replica's cells (and atoms) stay one contiguous range.
  * Only replicas with a rebuild request are re-binned; every other replica
  * keeps its order, cell ranges and list rows untouched by all build passes. */
-__global__ void k_cell_key_b(int n, const md_rep *__restrict__ reps, const int *__restrict__ arep,
+__global__ void k_cell_key_b(int n, int centered, const md_rep *__restrict__ reps,
+                             const int *__restrict__ arep,
                              const md_devstate *st, int always, const int *__restrict__ rep_upd,
                              const float4 *__restrict__ pos4, const int *__restrict__ cell_rank,
                              int *key, int *cell_count)
@@ -73,9 +74,9 @@ __global__ void k_cell_key_b(int n, const md_rep *__restrict__ reps, const int *
     if (!rep_upd[rep]) return;
     const md_rep &R = reps[rep];
     float4 p = pos4[i];
-    int cx = cell_of(p.x, R.box[0], R.binlen[0], R.ncell[0]);
-    int cy = cell_of(p.y, R.box[1], R.binlen[1], R.ncell[1]);
-    int cz = cell_of(p.z, R.box[2], R.binlen[2], R.ncell[2]);
+    int cx = cell_of(cell_coord(p.x, R.box[0], R.boxi[0], centered), R.box[0], R.binlen[0], R.ncell[0]);
+    int cy = cell_of(cell_coord(p.y, R.box[1], R.boxi[1], centered), R.box[1], R.binlen[1], R.ncell[1]);
+    int cz = cell_of(cell_coord(p.z, R.box[2], R.boxi[2], centered), R.box[2], R.binlen[2], R.ncell[2]);
     int r = cell_rank[R.cell0 + cx + R.ncell[0] * (cy + R.ncell[1] * cz)];
     key[i] = r;
     atomicAdd(&cell_count[r], 1);
@@ -322,9 +323,9 @@ __global__ void __launch_bounds__(256) k_build_list(
     uint4 ex = excl_s[ii];
     unsigned tmask = type_mask[ti];
     int c3[3];
-    c3[0] = cell_of(p.x, kp.box[0], kp.binlen[0], kp.ncell[0]);
-    c3[1] = cell_of(p.y, kp.box[1], kp.binlen[1], kp.ncell[1]);
-    c3[2] = cell_of(p.z, kp.box[2], kp.binlen[2], kp.ncell[2]);
+    for (int d = 0; d < 3; d++)
+        c3[d] = cell_of(cell_coord(d == 0 ? p.x : (d == 1 ? p.y : p.z), kp.box[d], kp.boxi[d], kp.centered),
+                        kp.box[d], kp.binlen[d], kp.ncell[d]);
     int lo[3], hi[3];
     for (int d = 0; d < 3; d++) {
         if (kp.stencil[d] < 0) { lo[d] = 0; hi[d] = kp.ncell[d] - 1; }
@@ -428,7 +429,7 @@ __global__ void __launch_bounds__(CW_WARPS * 32) k_build_cells(
         for (int d = 0; d < 3; d++) {
             G.L[d] = R.box[d]; G.Li[d] = R.boxi[d]; G.nc[d] = R.ncell[d]; G.sten[d] = R.stencil[d];
         }
-        G.rskinsq = R.rskinsq; G.shift = R.cell_shift; G.lin0 = R.cell0;
+        G.rskinsq = R.rskinsq; G.shift = R.cell_shift && kp.centered; G.lin0 = R.cell0;
     } else {
         for (int d = 0; d < 3; d++) {
             G.L[d] = kp.box[d]; G.Li[d] = kp.boxi[d]; G.nc[d] = kp.ncell[d]; G.sten[d] = kp.stencil[d];
@@ -666,7 +667,7 @@ void launch_rebuild(md_ctx *c, const md_kparams &kp, bool unconditional, bool al
     const int *crep = batch ? c->crep : nullptr;
     if (batch) {
         if (all_replicas) k_flag_all<<<rb, 256, 0, s>>>(c->rep_upd, c->nrep);
-        k_cell_key_b<<<nb, 256, 0, s>>>(kp.n, c->reps_dev, c->arep, c->st, always, c->rep_upd,
+        k_cell_key_b<<<nb, 256, 0, s>>>(kp.n, kp.centered, c->reps_dev, c->arep, c->st, always, c->rep_upd,
                                         c->pos4, c->cell_rank, c->key, c->cell_count);
         k_cell_scan_b<<<(c->nrep + 7) / 8, 256, 0, s>>>(c->st, always, c->nrep, c->reps_dev,
                                                         c->rep_upd, c->cell_count, c->cell_start,

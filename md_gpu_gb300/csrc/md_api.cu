@@ -686,7 +686,8 @@ md_kparams md_make_kparams(const md_ctx *c)
         kp.binlen[d] = c->binlen[d];
         kp.stencil[d] = c->stencil[d];
     }
-    kp.cell_shift = md_cell_shift(c->stencil, c->binlen, c->box);
+    /* the image shift by stencil cell holds when positions lie in the box */
+    kp.cell_shift = c->centered && md_cell_shift(c->stencil, c->binlen, c->box);
     kp.rcutsq = c->rcutsq;
     kp.reacf = c->reacf;
     kp.rskinsq = c->rskinsq;
@@ -697,7 +698,22 @@ md_kparams md_make_kparams(const md_ctx *c)
     kp.wolf = c->wc[3];
     kp.lkspace = c->lkspace;
     kp.dt = c->dt;
+    kp.centered = c->centered;
     return kp;
+}
+
+/* Whether every position of n atoms (3 per atom) lies in [-L/2, L/2] on
+ * each axis, as FP32.  Once it holds, the integrators' wrap keeps it (a
+ * step moves an atom far less than L/2), so the cells may take the image
+ * shift by stencil cell and the pair kernels may skip the minimum-image
+ * shifts of atoms at least rc from every face. */
+template <typename T>
+static bool centered_range(const T *pos3, int n, const float *box)
+{
+    for (int i = 0; i < n; i++)
+        for (int k = 0; k < 3; k++)
+            if (!(fabsf((float)pos3[3 * (size_t)i + k]) <= 0.5f * box[k])) return false;
+    return true;
 }
 
 extern "C" {
@@ -859,6 +875,7 @@ md_status md_create(const md_system_desc *d, void *stream, md_ctx **out)
     host_stage h;
     h.init(c->pitch);
     const size_t P = c->pitch;
+    c->centered = centered_range(d->pos, n, c->box) ? 1 : 0;
     for (int i = 0; i < n; i++) {
         for (int k = 0; k < 3; k++) {
             h.x[k * P + i] = d->pos[3 * i + k];
@@ -959,6 +976,7 @@ md_status md_create_batch(const md_system_desc *descs, int nrep, void *stream, m
     memset(c->ang2, 0, sizeof(c->ang2));
     memset(c->type_mass, 0, sizeof(c->type_mass));
     c->list_tpa = 0;   /* batches build their lists one warp per cell */
+    c->centered = 1;   /* cleared below by any replica with a position outside its box */
 
     host_stage h;
     const size_t P = c->pitch;
@@ -1030,6 +1048,7 @@ md_status md_create_batch(const md_system_desc *descs, int nrep, void *stream, m
             for (int b = 0; b < d->ntype; b++)
                 h.ljr[(size_t)r * MD_MAXTYPE * MD_MAXTYPE + a * MD_MAXTYPE + b] =
                     make_float2(d->lj1[a * d->ntype + b], d->lj2[a * d->ntype + b]);
+        if (!centered_range(d->pos, d->natom, d->box)) c->centered = 0;
         for (int i = 0; i < d->natom; i++) {
             int gi = atom0 + i;
             for (int k = 0; k < 3; k++) {
@@ -1194,6 +1213,23 @@ md_status md_get_energies(md_ctx *c, double *epot)
 
 static md_status scatter_from_host(md_ctx *c, int what, const double *src)
 {
+    if (what == 0) {
+        int cen = 1;
+        if (c->batch) {
+            size_t o = 0;
+            for (int r = 0; r < c->nrep && cen; r++) {
+                if (!centered_range(src + 3 * o, c->rep_natom[r], c->reps[r].box)) cen = 0;
+                o += (size_t)c->rep_natom[r];
+            }
+        } else {
+            cen = centered_range(src, c->n, c->box) ? 1 : 0;
+        }
+        if (cen != c->centered && c->gexec) {   /* the step graph holds the old flag */
+            cudaGraphExecDestroy(c->gexec);
+            c->gexec = nullptr;
+        }
+        c->centered = cen;
+    }
     md_kparams kp = md_make_kparams(c);
     MD_CUDA_TRY(c, cudaMemcpyAsync(c->io_dev, src, sizeof(double) * 3 * (size_t)c->n,
                                    cudaMemcpyHostToDevice, c->stream));
@@ -1409,6 +1445,7 @@ md_status md_get_info(md_ctx *c, md_info *out)
     }
     out->pair_threads_per_atom = c->pair_tpa;
     out->pair_entries_per_lane = md_pair_depth(c);
+    out->positions_centered = c->centered;
     out->list_threads_per_atom = c->list_tpa;
     out->builds = h.builds;
     out->max_neighbors = *std::max_element(cnt.begin(), cnt.begin() + c->n);

@@ -29,6 +29,15 @@ __device__ __forceinline__ float md_rsq_exact(float4 a, float4 b, const md_kpara
 
 /* (x + L/2) / bin truncated and clamped: the binning rule of the reference's
  * sketch (neighborlist_kernel_o.cu:20-25) with IEEE add and divide. */
+/* The coordinate an atom is binned by: its position when every position
+ * lies in [-L/2, L/2] (centered), else the periodic image of it in the box.
+ * The list predicate measures the positions themselves with the
+ * minimum-image shift either way; binning picks only the candidates. */
+__device__ __forceinline__ float cell_coord(float x, float L, float Li, int centered)
+{
+    return centered ? x : __fsub_rn(x, __fmul_rn(L, rintf(__fmul_rn(x, Li))));
+}
+
 __device__ __forceinline__ int cell_of(float x, float box, float binlen, int nc)
 {
     float s = __fdiv_rn(__fadd_rn(x, box / 2.0f), binlen);

@@ -73,9 +73,11 @@ struct md_kparams {
     int ncell[3];
     float binlen[3];
     int stencil[3];   /* cell range per axis: +-stencil, or -1 = all cells */
-    int cell_shift;   /* 1: a stencil cell's periodic image fixes the min-image shift */
+    int cell_shift;   /* 1: a stencil cell's periodic image fixes the min-image shift
+                         (positions centered, stencil narrow enough) */
     float wlim[3];    /* 0.4999 L: |x| below it needs no periodic wrap */
     double dt;
+    int centered;     /* 1: every position lies in [-L/2, L/2] on each axis */
 };
 
 /* One replica of a batch: its geometry, cutoffs, cell grid and thermostat
@@ -198,6 +200,7 @@ struct md_ctx {
     double *io_dev = nullptr;      /* 4*pitch doubles for host transfers */
     int pair_tpa = 8;    /* threads per atom in the pair kernel */
     int pair_depth = 0;  /* list entries per lane and batch (0: the default for pair_tpa) */
+    int centered = 0;    /* every position in [-L/2, L/2] (set at upload; the wraps keep it) */
     int list_tpa = 0;    /* list build: 0 = one warp per cell, else threads per atom */
 
     /* batches of replicas (md_create_batch; any number, 1 included) */

@@ -79,10 +79,12 @@ struct geom_kp {
     __device__ __forceinline__ float ucc() const { return pc.ucc; }
     __device__ __forceinline__ float rc6i() const { return pc.rc6i; }
     __device__ __forceinline__ float rcinv() const { return pc.rcinv; }
+    __device__ __forceinline__ bool centered() const { return kp.centered != 0; }
 };
 
 struct geom_reg {
     float L_[3], Li_[3], rcsq_, reacf_, palfa_, spiialfa_, alfasq_, wolf_, ucc_, rc6i_, rcinv_;
+    bool centered_;
     __device__ __forceinline__ float L(int d) const { return L_[d]; }
     __device__ __forceinline__ float Li(int d) const { return Li_[d]; }
     __device__ __forceinline__ float rcsq() const { return rcsq_; }
@@ -94,12 +96,15 @@ struct geom_reg {
     __device__ __forceinline__ float ucc() const { return ucc_; }
     __device__ __forceinline__ float rc6i() const { return rc6i_; }
     __device__ __forceinline__ float rcinv() const { return rcinv_; }
+    __device__ __forceinline__ bool centered() const { return centered_; }
 };
 
-/* The register geometry of one replica of a batch. */
-__device__ __forceinline__ geom_reg rep_geom(const md_rep &R)
+/* The register geometry of one replica of a batch; centered: every position
+ * of the batch lies inside its replica's box, centred on the origin. */
+__device__ __forceinline__ geom_reg rep_geom(const md_rep &R, bool centered = false)
 {
     geom_reg g;
+    g.centered_ = centered;
     for (int d = 0; d < 3; d++) {
         g.L_[d] = R.box[d];
         g.Li_[d] = R.boxi[d];
@@ -116,15 +121,19 @@ __device__ __forceinline__ geom_reg rep_geom(const md_rep &R)
     return g;
 }
 
-/* One pair: F_i += ff d, w_i += ff r^2 (pair_forces.cu:165-200 / :74-120). */
-template <int KIND, bool ENERGY, class G>
+/* One pair: F_i += ff d, w_i += ff r^2 (pair_forces.cu:165-200 / :74-120).
+ * WRAP = false skips the minimum-image shift, which is then zero for every
+ * pair inside rc (atom i at least rc from each face: see interior()). */
+template <int KIND, bool ENERGY, bool WRAP = true, class G>
 __device__ __forceinline__ void pair_term(const G &g, float4 pi, float qi, float4 pj, float2 l,
                                           bool valid, pair_acc &a)
 {
     float dx = pi.x - pj.x, dy = pi.y - pj.y, dz = pi.z - pj.z;
-    dx -= g.L(0) * rint_small(dx * g.Li(0));
-    dy -= g.L(1) * rint_small(dy * g.Li(1));
-    dz -= g.L(2) * rint_small(dz * g.Li(2));
+    if (WRAP) {
+        dx -= g.L(0) * rint_small(dx * g.Li(0));
+        dy -= g.L(1) * rint_small(dy * g.Li(1));
+        dz -= g.L(2) * rint_small(dz * g.Li(2));
+    }
     float rsq = dx * dx + dy * dy + dz * dz;
     float ri = rsqrt_approx(rsq);
     float ri2 = ri * ri;
@@ -162,37 +171,36 @@ struct pair_total {
     float fw, fe;
 };
 
-/* Pair forces of atom ii from its list: TPA lanes per atom, lane l takes the
- * entries l, l+TPA, ... in batches of B (TPA*B divides 32, the padding
- * quantum of the list rows, so no entry needs a bounds test).  The loads are
- * software pipelined: while batch t is computed, the positions of batch t+1
- * and the list entries of batch t+2 are in flight.  Each lane sums in FP32
- * and converts its sum to int64 once; lane sums are combined with integer
- * shuffles (exact), so the result depends only on TPA.  Every lane of the
- * warp must call this (the shuffles use the full mask). */
-template <int KIND, int TPA, int B, bool ENERGY, class G>
-__device__ __forceinline__ pair_total pair_sum(const G &g, int cap, int ii, bool active, int lane,
-                                               const float4 *__restrict__ pos4,
-                                               const int *__restrict__ type,
-                                               const unsigned *__restrict__ nl,
-                                               const int *__restrict__ nl_n, const float2 *lj)
+/* Whether atom i sits at least rc (plus 0.1% of the box) from every face of
+ * the box.  When every position lies in [-L/2, L/2] (G::centered()), for
+ * such an atom every j within rc in the minimum image is within rc without
+ * a shift: x_i - x_j needs no wrap, and equals the shifted difference bit
+ * for bit (the shift there is L * 0).  A pair the unshifted difference puts
+ * beyond L/2 on some axis is beyond rc (rc < L/2) and is dropped either way. */
+template <class G>
+__device__ __forceinline__ bool interior(const G &g, float4 pi)
 {
-    static_assert(MD_LIST_QUANTUM % (TPA * B) == 0, "batch must divide the list padding");
-    const float4 pi = pos4[ii];
-    const int cnt = active ? nl_n[ii] : 0;
-    const int nb = ((cnt + MD_LIST_QUANTUM - 1) / MD_LIST_QUANTUM) * (MD_LIST_QUANTUM / (TPA * B));
-    const float2 *ljrow = lj + type[ii] * MD_MAXTYPE;
-    const float qi = QFAC * pi.w;
-    pair_acc acc = {0.0f, 0.0f, 0.0f, 0.0f, 0.0f};
-    const unsigned *lp = nl + (size_t)ii * cap + lane;
+    const float rc = sqrtf(g.rcsq());
+    return fabsf(pi.x) + rc < 0.499f * g.L(0) && fabsf(pi.y) + rc < 0.499f * g.L(1) &&
+           fabsf(pi.z) + rc < 0.499f * g.L(2);
+}
+
+/* The entries of one lane in batches of B, software pipelined: while batch
+ * t is computed, the positions of batch t+1 and the list entries of batch
+ * t+2 are in flight.  ljrow may point into shared memory (a batch's
+ * per-replica table): plain loads there, not the read-only global path. */
+template <int KIND, int TPA, int B, bool ENERGY, bool WRAP, class G>
+__device__ __forceinline__ void pair_loop(const G &g, float4 pi, float qi, int nb,
+                                          const unsigned *__restrict__ lp,
+                                          const float4 *__restrict__ pos4, const float2 *ljrow,
+                                          pair_acc &acc)
+{
     unsigned e0[B], e1[B];
     float4 p0[B];
-    if (nb > 0) {
 #pragma unroll
-        for (int b = 0; b < B; b++) e0[b] = __ldg(lp + b * TPA);
+    for (int b = 0; b < B; b++) e0[b] = __ldg(lp + b * TPA);
 #pragma unroll
-        for (int b = 0; b < B; b++) p0[b] = __ldg(pos4 + (e0[b] & MD_INDEX_MASK));
-    }
+    for (int b = 0; b < B; b++) p0[b] = __ldg(pos4 + (e0[b] & MD_INDEX_MASK));
     if (nb > 1) {
 #pragma unroll
         for (int b = 0; b < B; b++) e1[b] = __ldg(lp + (B + b) * TPA);
@@ -211,13 +219,44 @@ __device__ __forceinline__ pair_total pair_sum(const G &g, int cap, int ii, bool
         }
 #pragma unroll
         for (int b = 0; b < B; b++)
-            pair_term<KIND, ENERGY>(g, pi, qi, p0[b], ljrow[e0[b] >> MD_TYPE_SHIFT], true, acc);
+            pair_term<KIND, ENERGY, WRAP>(g, pi, qi, p0[b], ljrow[e0[b] >> MD_TYPE_SHIFT], true, acc);
 #pragma unroll
         for (int b = 0; b < B; b++) {
             e0[b] = e1[b];
             p0[b] = p1[b];
             e1[b] = e2[b];
         }
+    }
+}
+
+/* Pair forces of atom ii from its list: TPA lanes per atom, lane l takes the
+ * entries l, l+TPA, ... in batches of B (TPA*B divides 32, the padding
+ * quantum of the list rows, so no entry needs a bounds test).  A warp whose
+ * atoms are all interior() skips the minimum-image shifts.  Each lane sums in
+ * FP32 and converts its sum to int64 once; lane sums are combined with
+ * integer shuffles (exact), so the result depends only on TPA.  Every lane of
+ * the warp must call this (the shuffles use the full mask). */
+template <int KIND, int TPA, int B, bool ENERGY, class G>
+__device__ __forceinline__ pair_total pair_sum(const G &g, int cap, int ii, bool active, int lane,
+                                               const float4 *__restrict__ pos4,
+                                               const int *__restrict__ type,
+                                               const unsigned *__restrict__ nl,
+                                               const int *__restrict__ nl_n, const float2 *lj)
+{
+    static_assert(MD_LIST_QUANTUM % (TPA * B) == 0, "batch must divide the list padding");
+    const float4 pi = pos4[ii];
+    const int cnt = active ? nl_n[ii] : 0;
+    const int nb = ((cnt + MD_LIST_QUANTUM - 1) / MD_LIST_QUANTUM) * (MD_LIST_QUANTUM / (TPA * B));
+    const float2 *ljrow = lj + type[ii] * MD_MAXTYPE;
+    const float qi = QFAC * pi.w;
+    pair_acc acc = {0.0f, 0.0f, 0.0f, 0.0f, 0.0f};
+    const unsigned *lp = nl + (size_t)ii * cap + lane;
+    const bool inner = g.centered() && __all_sync(0xffffffffu, !active || interior(g, pi));
+    if (nb > 0) {
+        if (inner)
+            pair_loop<KIND, TPA, B, ENERGY, false>(g, pi, qi, nb, lp, pos4, ljrow, acc);
+        else
+            pair_loop<KIND, TPA, B, ENERGY, true>(g, pi, qi, nb, lp, pos4, ljrow, acc);
     }
     pair_total r;
     r.fx = __float2ll_rn(acc.fx * 4294967296.0f);

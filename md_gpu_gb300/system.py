@@ -67,7 +67,7 @@ class Info(C.Structure):
                 ("pair_threads_per_atom", C.c_int), ("list_threads_per_atom", C.c_int),
                 ("builds", C.c_int), ("max_neighbors", C.c_int), ("kernels_per_step", C.c_int),
                 ("kernels_per_rebuild", C.c_int), ("kernels_per_graph", C.c_int),
-                ("pair_entries_per_lane", C.c_int)]
+                ("pair_entries_per_lane", C.c_int), ("positions_centered", C.c_int)]
 
 
 def _make_desc(keep, *, box, itype, charge, pos, vel, type_mass, lj1, lj2, lkspace, rcutsq,
@@ -368,7 +368,8 @@ class MDSystem:
                 "kernels_per_step": i.kernels_per_step,
                 "kernels_per_rebuild": i.kernels_per_rebuild,
                 "kernels_per_graph": i.kernels_per_graph,
-                "pair_depth": i.pair_entries_per_lane}
+                "pair_depth": i.pair_entries_per_lane,
+                "centered": bool(i.positions_centered)}
 
     def neighbor_list(self, nmax):
         """Reference layout (neighborlist.cu:284): (nnlist[pitch*nmax], nnlist_max[pitch])."""

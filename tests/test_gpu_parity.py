@@ -305,6 +305,41 @@ def test_thread_split_variants(pair_tpa, list_tpa, depth):
     assert np.array_equal(gu.rows_canonical(nn, nm, n, 512), gu.rows_canonical(orc["nn"], orc["nm"], n, 512))
 
 
+def test_positions_outside_the_box():
+    """Positions given in [0, L) instead of [-L/2, L/2] (the reference takes
+    either: its list is all pairs with the minimum-image shift).  Cells then
+    bin the periodic images and every pair takes the shift; the list stays
+    bit-exact and the forces within tolerance.  Centred input turns the fast
+    paths back on."""
+    case = oracle.load(_write(synth.nacl_rocksalt(ncell=10, seed=31, nmaxlist=512)))
+    L = case.box.astype(np.float64)
+    with gu.system_from_case(case) as sim:
+        assert sim.info()["centered"]
+        X = sim.positions()
+        sim.compute_forces(TERM_PAIR)
+        F0 = sim.forces()
+        moved = np.where(X < 0, X + L, X)
+        sim.set_positions(moved)
+        assert not sim.info()["centered"]
+        sim.compute_forces(TERM_PAIR)
+        F1 = sim.forces()
+        nn, nm = sim.neighbor_list(512)
+        sim.step(40)                       # the integrator wraps x >= L/2 back
+        sim.set_positions(X)
+        assert sim.info()["centered"]
+    pos4 = case.pos4().copy()
+    pos4[:, :3] = moved.astype(np.float32)
+    p = case.params
+    onn, onm, _ = oracle.nlist(pos4, case.box, case.boxi, oracle.rskinsq(p.skin, p.rcutsq),
+                               oracle.exclusions(case.natom, case.bonds), 512)
+    n = case.natom
+    assert np.array_equal(nm[:n], onm[:n])
+    assert np.array_equal(gu.rows_canonical(nn, nm, n, 512), gu.rows_canonical(onn, onm, n, 512))
+    orc = gu.oracle_state(case)
+    assert gu.rms_rel(F1[:, :3], orc["f64"][:, :3]) <= FORCE_TOL
+    assert gu.rms_rel(F1[:, :3], F0[:, :3]) <= FORCE_TOL
+
+
 def test_full_size_nacl_64k():
     """The 64000-ion system: bit-exact list, forces within tolerance, and
     size-independent properties (momentum, Newton's third law in sum)."""
