@@ -241,6 +241,10 @@ md_status md_set_type_exclusions(md_ctx *ctx, const unsigned *mask);
 /* md_step launches each step's kernels eagerly instead of replaying a
  * captured graph when use_graphs is 0 (for profilers and debugging). */
 md_status md_set_graphs(md_ctx *ctx, int use_graphs);
+/* Leapfrog systems without bonded terms: 1 runs each step (pair forces and
+ * the leapfrog update) as one kernel, 0 as two; MD_ERR_UNSUPPORTED for other
+ * systems when asked for 1.  md_autotune times both and keeps the faster. */
+md_status md_set_fused_step(md_ctx *ctx, int fused);
 /* Milliseconds of device time of the last md_step call (CUDA events). */
 md_status md_last_step_ms(md_ctx *ctx, float *ms);
 /* The pair-force kernel alone, nrep launches on the context's stream between

@@ -3,8 +3,11 @@
  * terms: pair forces (pair_forces.cu:133-205 / :34-131), then in the same
  * thread the leapfrog update of that atom (nve_leapfrog.cu:31-60,
  * nvt_leapfrog_ber.cu:29-80), the next step's list check
- * (neighborlist.cu:157-176) and the FP64 kinetic-energy partial; the last
- * block to finish turns the step's sums into T and sets the rebuild condition.
+ * (neighborlist.cu:157-176) and the kinetic-energy sums; the last block to
+ * finish turns the step's sums into T and sets the rebuild condition.  The
+ * update's inputs (x, v, 1/m, m, the positions at the last build) are copied
+ * into shared memory with cp.async at the start, so they arrive while the
+ * block computes its pair forces.
  *
  * Positions are double buffered: the step reads pos4 and writes the updated
  * copy to pos4_next, so no thread sees a neighbour that has already moved.
@@ -27,7 +30,25 @@ __global__ void __launch_bounds__(128) k_pair_leapfrog(
     __shared__ float2 lj[MD_MAXTYPE * MD_MAXTYPE];
     __shared__ long long sh[12];   /* 3 integers per warp */
     __shared__ long long s_f[NA][3];
+    __shared__ double s_x0[3][NA], s_v0[3][NA], s_kick[NA], s_mass[NA];
+    __shared__ float4 s_old[NA];
     __shared__ float s_x[NA][3];
+    const int i0 = blockIdx.x * NA;
+    const size_t P = (size_t)kp.pitch;
+    /* the update's inputs travel while the pair forces are computed */
+    for (int k = threadIdx.x; k < 3 * NA; k += blockDim.x) {
+        const int d = k / NA, a = k - d * NA, ia = i0 + a;
+        if (ia < kp.n) {
+            cp_async8(&s_x0[d][a], x + d * P + ia);
+            cp_async8(&s_v0[d][a], v + d * P + ia);
+        }
+    }
+    if (threadIdx.x < NA && i0 + (int)threadIdx.x < kp.n) {
+        const int ia = i0 + threadIdx.x;
+        cp_async8(&s_kick[threadIdx.x], kick + ia);
+        cp_async8(&s_mass[threadIdx.x], mass + ia);
+        cp_async16(&s_old[threadIdx.x], io.pos_old + ia);
+    }
     if (threadIdx.x < MD_MAXTYPE * MD_MAXTYPE) lj[threadIdx.x] = ljtab[threadIdx.x];
     __syncthreads();
     int gt = blockIdx.x * blockDim.x + threadIdx.x;
@@ -35,7 +56,6 @@ __global__ void __launch_bounds__(128) k_pair_leapfrog(
     bool active = i < kp.n;
     pair_total t = pair_sum<KIND, TPA, B, false>(geom_kp{kp, pc}, kp.cap, active ? i : 0, active, lane, pos4, type,
                                                  nl, nl_n, lj);
-    const size_t P = (size_t)kp.pitch;
     if (lane == 0) {
         int a = threadIdx.x / TPA;
         s_f[a][0] = t.fx;
@@ -48,41 +68,40 @@ __global__ void __launch_bounds__(128) k_pair_leapfrog(
             vir[i] = t.fw;
         }
     }
+    cp_async_wait();
     __syncthreads();
-    /* FP64 leapfrog of the block's atoms spread over all threads, one
-     * (atom, axis) per thread: full warps on the FP64 pipe */
-    const int i0 = blockIdx.x * NA;
+    /* FP64 leapfrog of the block's atoms, one (atom, axis) per thread, the
+     * same operations as k_leapfrog */
     const double lam = tp.berendsen ? io.st->lam_next : 1.0;
-    double ke2 = 0.0;
+    long long ke = 0;
     for (int k = threadIdx.x; k < 3 * NA; k += blockDim.x) {
-        int a = k / 3, d = k - 3 * a, ia = i0 + a;
+        const int d = k / NA, a = k - d * NA, ia = i0 + a;
         if (ia < kp.n) {
-            double vv = v[d * P + ia] + (double)s_f[a][d] * kick[ia];
+            const axis_par ax = axis_of(d, kp.wlim, kp.boxd, kp.box2i);
+            double vv = s_v0[d][a] + (double)s_f[a][d] * s_kick[a];
             if (tp.berendsen) vv *= lam;
             v[d * P + ia] = vv;
-            double xx = x[d * P + ia] + vv * kp.dt;
-            s_x[a][d] = wrap(xx, kp.wlim[d], kp.boxd[d], kp.box2i[d]);
+            double xx = s_x0[d][a] + vv * kp.dt;
+            s_x[a][d] = wrap(xx, ax.lim, ax.L, ax.two_over_l);
             x[d * P + ia] = xx;
-            ke2 += mass[ia] * vv * vv;
+            ke += ke_fix(s_mass[a], vv);
         }
     }
     __syncthreads();
+    bool moved = false;
     if (threadIdx.x < NA) {
         int ia = i0 + threadIdx.x;
         if (ia < kp.n) {
             float4 p = make_float4(s_x[threadIdx.x][0], s_x[threadIdx.x][1], s_x[threadIdx.x][2],
                                    pos4[ia].w);
             pos4_next[ia] = p;
-            check_moved(p, io.pos_old[ia], kp, io.st);
+            moved = md_rsq_exact(p, s_old[threadIdx.x], kp) >= kp.rmaxdif;
         }
     }
-    block_fix_add(ke2, 0.0, 0.0, 0, io.st->acc, sh);
-    if (md_last_block(io.counter)) {
+    if (block_close(ke, 0, 0, 1, moved, io.st, io.counter, sh)) {
         finalize(kp, tp, 0, io.st, io.rec, io.rec_cap);
-        if (threadIdx.x == 0) {
-            set_condition(io);
-            *io.counter = 0;
-        }
+        set_condition(io);
+        *io.counter = 0;
     }
 }
 
@@ -93,19 +112,22 @@ void fused_dispatch(md_ctx *c, const md_kparams &kp, const pair_consts &pc, cons
     long long threads = (long long)kp.n * c->pair_tpa;
     int nb = (int)((threads + 127) / 128);
     const float2 *lj = (const float2 *)c->lj_dev;
-    switch (c->pair_tpa) {
-#define MD_FUSED_CASE(T)                                                                         \
-    case T:                                                                                      \
-        k_pair_leapfrog<KIND, T, (T >= 32 ? 1 : (T >= 16 ? 2 : (T >= 8 ? 4 : 8)))>              \
-            <<<nb, 128, 0, c->stream>>>(kp, pc, tp, io, c->pos4, c->pos4_alt, c->type, c->nl,    \
-                                        c->nl_n, lj, c->f, c->vir, c->x, c->v, c->mass, c->kick); \
+    switch (c->pair_tpa * 100 + md_pair_depth(c)) {
+#define MD_FUSED_CASE(T, BB)                                                                     \
+    case T * 100 + BB:                                                                           \
+        k_pair_leapfrog<KIND, T, BB><<<nb, 128, 0, c->stream>>>(                                 \
+            kp, pc, tp, io, c->pos4, c->pos4_alt, c->type, c->nl, c->nl_n, lj, c->f, c->vir,     \
+            c->x, c->v, c->mass, c->kick);                                                       \
         break;
-        MD_FUSED_CASE(1)
-        MD_FUSED_CASE(2)
-        MD_FUSED_CASE(4)
-        MD_FUSED_CASE(8)
-        MD_FUSED_CASE(16)
-        MD_FUSED_CASE(32)
+        MD_FUSED_CASE(1, 8)
+        MD_FUSED_CASE(2, 8)
+        MD_FUSED_CASE(4, 4)
+        MD_FUSED_CASE(4, 8)
+        MD_FUSED_CASE(8, 2)
+        MD_FUSED_CASE(8, 4)
+        MD_FUSED_CASE(16, 1)
+        MD_FUSED_CASE(16, 2)
+        MD_FUSED_CASE(32, 1)
 #undef MD_FUSED_CASE
     default:
         break;

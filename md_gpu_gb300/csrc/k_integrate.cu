@@ -53,7 +53,7 @@ __global__ void __launch_bounds__(3 * MD_LA) k_leapfrog(md_kparams kp, thermo_pa
     const int d = threadIdx.x / MD_LA, a = threadIdx.x - d * MD_LA;
     const int s = blockIdx.x * MD_LA + a;
     const size_t o = (size_t)d * kp.pitch + s;
-    double ke2 = 0.0, pe = 0.0, w = 0.0;
+    long long ke = 0, pe = 0, w = 0;
     if (s < kp.n) {
         const axis_par ax = axis_of(d, kp.wlim, kp.boxd, kp.box2i);
         double vv = v[o] + (double)f[o] * kick[s];
@@ -62,22 +62,23 @@ __global__ void __launch_bounds__(3 * MD_LA) k_leapfrog(md_kparams kp, thermo_pa
         double xx = x[o] + vv * kp.dt;
         s_x[d][a] = wrap(xx, ax.lim, ax.L, ax.two_over_l);
         x[o] = xx;
-        ke2 = mass[s] * (vv * vv);
-        if (d == 0 && tp.energy) { pe = epot[s]; w = vir[s]; }
+        ke = ke_fix(mass[s], vv);
+        if (d == 0 && tp.energy) {
+            pe = llrint((double)epot[s] * MD_EFIX);
+            w = llrint((double)vir[s] * MD_EFIX);
+        }
     }
     __syncthreads();
+    bool moved = false;
     if (d == 0 && s < kp.n) {
         float4 p = make_float4(s_x[0][a], s_x[1][a], s_x[2][a], pos4[s].w);
         pos4[s] = p;
-        check_moved(p, io.pos_old[s], kp, io.st);
+        moved = md_rsq_exact(p, io.pos_old[s], kp) >= kp.rmaxdif;
     }
-    block_fix_add(ke2, pe, w, tp.energy, io.st->acc, sh);
-    if (md_last_block(io.counter)) {
+    if (block_close(ke, pe, w, tp.energy ? 3 : 1, moved, io.st, io.counter, sh)) {
         finalize(kp, tp, 0, io.st, io.rec, io.rec_cap);
-        if (threadIdx.x == 0) {
-            set_condition(io);
-            *io.counter = 0;
-        }
+        set_condition(io);
+        *io.counter = 0;
     }
 }
 
@@ -90,6 +91,7 @@ __global__ void __launch_bounds__(3 * MD_LA) k_vv_first(md_kparams kp, thermo_pa
                                                        const long long *__restrict__ f)
 {
     __shared__ float s_x[3][MD_LA];
+    __shared__ long long sh[3 * (3 * MD_LA / 32)];
     const int d = threadIdx.x / MD_LA, a = threadIdx.x - d * MD_LA;
     const int s = blockIdx.x * MD_LA + a;
     const size_t o = (size_t)d * kp.pitch + s;
@@ -108,16 +110,15 @@ __global__ void __launch_bounds__(3 * MD_LA) k_vv_first(md_kparams kp, thermo_pa
         x[o] = xx;
     }
     __syncthreads();
+    bool moved = false;
     if (d == 0 && s < kp.n) {
         float4 p = make_float4(s_x[0][a], s_x[1][a], s_x[2][a], pos4[s].w);
         pos4[s] = p;
-        check_moved(p, io.pos_old[s], kp, st);
+        moved = md_rsq_exact(p, io.pos_old[s], kp) >= kp.rmaxdif;
     }
-    if (md_last_block(io.counter)) {
-        if (threadIdx.x == 0) {
-            set_condition(io);
-            *io.counter = 0;
-        }
+    if (block_close(0, 0, 0, 0, moved, st, io.counter, sh)) {
+        set_condition(io);
+        *io.counter = 0;
     }
 }
 
@@ -137,7 +138,7 @@ __global__ void __launch_bounds__(3 * MD_LA) k_vv_second(md_kparams kp, thermo_p
     const int d = threadIdx.x / MD_LA, a = threadIdx.x - d * MD_LA;
     const int s = blockIdx.x * MD_LA + a;
     const size_t o = (size_t)d * kp.pitch + s;
-    double ke2 = 0.0, pe = 0.0, w = 0.0;
+    long long ke = 0, pe = 0, w = 0;
     if (s < kp.n) {
         double vv = v[o];
         if (do_kick) {
@@ -146,13 +147,15 @@ __global__ void __launch_bounds__(3 * MD_LA) k_vv_second(md_kparams kp, thermo_p
         } else {
             vv *= io.st->vscale;
         }
-        ke2 = mass[s] * (vv * vv);
-        if (d == 0 && tp.energy) { pe = epot[s]; w = vir[s]; }
+        ke = ke_fix(mass[s], vv);
+        if (d == 0 && tp.energy) {
+            pe = llrint((double)epot[s] * MD_EFIX);
+            w = llrint((double)vir[s] * MD_EFIX);
+        }
     }
-    block_fix_add(ke2, pe, w, tp.energy, io.st->acc, sh);
-    if (md_last_block(io.counter)) {
+    if (block_close(ke, pe, w, tp.energy ? 3 : 1, false, io.st, io.counter, sh)) {
         finalize(kp, tp, do_kick ? 1 : 2, io.st, io.rec, io.rec_cap);
-        if (threadIdx.x == 0) *io.counter = 0;
+        *io.counter = 0;
     }
 }
 

@@ -1564,10 +1564,30 @@ md_status md_set_graphs(md_ctx *c, int use_graphs)
     return MD_OK;
 }
 
+md_status md_set_fused_step(md_ctx *c, int fused)
+{
+    if (!c) return MD_ERR_ARG;
+    const int old = c->fuse_step;
+    c->fuse_step = 1;
+    if (fused && !md_can_fuse(c)) {
+        c->fuse_step = old;
+        return fail(c, MD_ERR_UNSUPPORTED,
+                    "md_set_fused_step: only leapfrog single systems without bonded terms fuse");
+    }
+    c->fuse_step = fused ? 1 : 0;
+    if (c->gexec && c->fuse_step != old) {
+        cudaGraphExecDestroy(c->gexec);
+        c->gexec = nullptr;
+    }
+    return MD_OK;
+}
+
 md_status md_set_pair_depth(md_ctx *c, int depth)
 {
     if (!c) return MD_ERR_ARG;
     const int t = c->pair_tpa;
+    const int def = t >= 32 ? 1 : (t >= 16 ? 2 : (t >= 8 ? 4 : 8));
+    if (depth == def) depth = 0;
     const bool ok = depth == 0 || (!c->batch && ((t == 4 && depth == 4) || (t == 8 && depth == 2) ||
                                                  (t == 16 && depth == 1)));
     if (!ok) return fail(c, MD_ERR_ARG, "md_set_pair_depth: depth not built for this lane count");

@@ -45,6 +45,27 @@ __device__ __forceinline__ int cell_of(float x, float box, float binlen, int nc)
     return c >= nc ? nc - 1 : c;
 }
 
+/* Asynchronous copies global -> shared (cp.async, sm_80 and later): the
+ * data lands while the thread goes on; cp_async_wait() waits for every
+ * copy the thread issued.  Both addresses must be aligned to the size, and
+ * src must point into global memory. */
+__device__ __forceinline__ void cp_async8(void *dst, const void *src)
+{
+    asm volatile("cp.async.ca.shared.global [%0], [%1], 8;\n" ::"r"((unsigned)__cvta_generic_to_shared(dst)),
+                 "l"(src)
+                 : "memory");
+}
+__device__ __forceinline__ void cp_async16(void *dst, const void *src)
+{
+    asm volatile("cp.async.cg.shared.global [%0], [%1], 16;\n" ::"r"((unsigned)__cvta_generic_to_shared(dst)),
+                 "l"(src)
+                 : "memory");
+}
+__device__ __forceinline__ void cp_async_wait()
+{
+    asm volatile("cp.async.commit_group;\ncp.async.wait_group 0;\n" ::: "memory");
+}
+
 /* Programmatic dependent launch: a kernel launched with the
  * programmatic-serialization attribute (md_launch_pdl) may be scheduled
  * while its predecessor in the stream still runs.  pdl_wait() blocks until

@@ -117,6 +117,62 @@ __device__ __forceinline__ void block_fix_add(double ke2, double pe, double w, i
     }
 }
 
+/* One (atom, axis) kinetic-energy term m v^2 / 2 in 2^-32 kJ/mol fixed
+ * point, rounded once (the same value block_fix_add takes from m v^2). */
+__device__ __forceinline__ long long ke_fix(double m, double vv)
+{
+    return llrint(m * (vv * vv) * (0.5 * MD_KFIX));
+}
+
+/* The end of an integrator block.  Each thread brings its fixed-point terms
+ * a (KE, 2^-32 kJ/mol units), b and c (PE, virial, 2^-24; nsum = 3 adds all
+ * three, 1 only a, 0 none) and whether its atom moved >= skin/2; the block
+ * sums them with integer shuffles, and thread 0 alone adds them to the
+ * device state, raises st->update, fences and counts the block.  Returns
+ * true in thread 0 of the last block to finish, which then finalises the
+ * step.  The other threads' stores (positions, velocities) are read only by
+ * later kernels, so they need no fence and their warps leave at once.
+ * sh holds 3 integers per warp. */
+__device__ __forceinline__ bool block_close(long long a, long long b, long long c, int nsum,
+                                            bool moved, md_devstate *st, unsigned *counter,
+                                            long long *sh)
+{
+    if (nsum > 0) {
+        for (int o = 16; o > 0; o >>= 1) {
+            a += __shfl_down_sync(0xffffffffu, a, o);
+            if (nsum > 1) {
+                b += __shfl_down_sync(0xffffffffu, b, o);
+                c += __shfl_down_sync(0xffffffffu, c, o);
+            }
+        }
+        const int wp = threadIdx.x >> 5, l = threadIdx.x & 31, nw = blockDim.x >> 5;
+        if (l == 0) {
+            sh[wp] = a;
+            sh[nw + wp] = b;
+            sh[2 * nw + wp] = c;
+        }
+    }
+    const int any = __syncthreads_or(moved ? 1 : 0);
+    if (threadIdx.x != 0) return false;
+    if (nsum > 0) {
+        const int nw = blockDim.x >> 5;
+        long long ta = 0, tb = 0, tc = 0;
+        for (int k = 0; k < nw; k++) {
+            ta += sh[k];
+            tb += sh[nw + k];
+            tc += sh[2 * nw + k];
+        }
+        atomicAdd(&st->acc[0], (unsigned long long)ta);
+        if (nsum > 1) {
+            atomicAdd(&st->acc[1], (unsigned long long)tb);
+            atomicAdd(&st->acc[2], (unsigned long long)tc);
+        }
+    }
+    if (any) st->update = 1;
+    __threadfence();
+    return atomicAdd(counter, 1u) == gridDim.x - 1;
+}
+
 /* Reads and clears fixed-point accumulators (in the last block, after every
  * block's atomic adds). */
 __device__ __forceinline__ double fix_take(unsigned long long *p, double scale)

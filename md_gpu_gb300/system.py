@@ -153,6 +153,7 @@ def library(path: Optional[str] = None):
     L.md_autotune.argtypes = [vp, C.POINTER(C.c_int), C.POINTER(C.c_int)]
     L.md_set_type_exclusions.argtypes = [vp, vp]
     L.md_set_graphs.argtypes = [vp, C.c_int]
+    L.md_set_fused_step.argtypes = [vp, C.c_int]
     L.md_ref_kinetic_energy_noalloc.argtypes = [vp, C.c_int, vp, vp]
     L.md_create_batch.argtypes = [C.POINTER(SystemDesc), C.c_int, vp, C.POINTER(vp)]
     L.md_get_replica_thermo.argtypes = [vp, C.POINTER(Thermo), C.c_int]
@@ -417,6 +418,10 @@ class MDSystem:
     def set_graphs(self, use_graphs=True):
         """Replay captured step graphs (default) or launch eagerly."""
         _check(library().md_set_graphs(self._ctx, 1 if use_graphs else 0), self._ctx)
+
+    def set_fused_step(self, fused=True):
+        """Leapfrog without bonded terms: pair forces and update in one kernel."""
+        _check(library().md_set_fused_step(self._ctx, 1 if fused else 0), self._ctx)
 
     def set_tuning(self, pair_tpa, list_tpa, pair_depth=0):
         _check(library().md_set_tuning(self._ctx, pair_tpa, list_tpa), self._ctx)

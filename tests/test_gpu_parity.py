@@ -375,6 +375,28 @@ def test_type_exclusions():
         assert np.array_equal(got, keep), i
 
 
+@pytest.mark.parametrize("pair_tpa,depth", [(8, 2), (4, 0), (16, 1)])
+def test_fused_step_matches_separate(pair_tpa, depth):
+    """One kernel per leapfrog step (pair forces and update fused) advances
+    bit for bit like the two-kernel step with the same lanes per atom: the
+    forces are exact integer sums of the same lane sums, the update performs
+    the same FP64 operations, and both sum the kinetic energy per (atom,
+    axis) term in fixed point.  40 steps include list rebuilds."""
+    case = oracle.load(_write(synth.nacl_rocksalt(ncell=6, seed=41, nmaxlist=512)))
+    out = []
+    for fused in (0, 1):
+        with gu.system_from_case(case) as sim:
+            sim.set_tuning(pair_tpa, 0, depth)
+            sim.set_fused_step(fused)
+            sim.step(40)
+            out.append((sim.positions(), sim.velocities(), sim.thermo(), sim.info()))
+    (x0, v0, t0, i0), (x1, v1, t1, i1) = out
+    assert i0["kernels_per_step"] == 2 and i1["kernels_per_step"] == 1
+    assert i0["builds"] == i1["builds"] >= 2
+    assert np.array_equal(x0, x1) and np.array_equal(v0, v1)
+    assert t0["ke"] == t1["ke"] and t0["lambda_"] == t1["lambda_"]
+
+
 def test_autotune_keeps_results():
     """After autotuning (which may advance the system), list and forces of the
     current positions still match the oracle."""
