@@ -413,6 +413,8 @@ def run_ours(args):
                        "list_builds_in_timed_region": builds,
                        "pair_threads_per_atom": info["pair_tpa"],
                        "pair_entries_per_lane": info["pair_depth"],
+                       "step_kernels": "pair+leapfrog fused" if info["fused_step"] else "pair, leapfrog",
+                       "rebuild_in_graph": "inline passes" if info["rebuild_inline"] else "conditional node",
                        "list_builder": "warp per cell" if info["list_tpa"] == 0
                        else f"{info['list_tpa']} threads per atom",
                        "autotuned": tuned is not None,

@@ -47,7 +47,8 @@ enum { MD_TERM_PAIR = 1, MD_TERM_BOND = 2, MD_TERM_ANGLE = 4, MD_TERM_ALL = 7 };
 typedef struct {
     int natom;
     int ntype;                  /* <= 8 (forces.cu:48-49) */
-    float box[3];               /* box edge, A; coordinates centred in [-L/2, L/2] */
+    float box[3];               /* box edge, A; coordinates centred in [-L/2, L/2] (others are
+                                   taken, on slower list and pair paths: md_info) */
     const int *itype;           /* natom, 0-based */
     const float *charge;        /* natom, e */
     const float *pos;           /* 3*natom */
@@ -203,14 +204,18 @@ typedef struct {
     int pair_threads_per_atom, list_threads_per_atom;
     int builds;
     int max_neighbors;
-    int kernels_per_step;   /* kernel launches of one md_step step without a rebuild */
-    int kernels_per_rebuild; /* kernels a list rebuild adds to a step */
+    int kernels_per_step;   /* kernel launches of one step of a step graph without a rebuild
+                               (inline rebuild passes included: they run every step) */
+    int kernels_per_rebuild; /* kernels a list rebuild adds to a step (0 with inline passes) */
     int kernels_per_graph;  /* kernels a step graph runs besides its steps (condition set-up) */
     int pair_entries_per_lane; /* list entries each pair-kernel lane loads per batch */
     int positions_centered; /* 1: every position uploaded last lay in [-L/2, L/2] per axis,
                                so the fast paths that rely on it are on (the integrators
                                keep it so); 0: cells bin periodic images, every pair
                                takes the minimum-image shift */
+    int fused_step;         /* 1: step graphs run pair forces and update as one kernel */
+    int rebuild_inline;     /* 1: step graphs hold the rebuild passes inline, 0: behind a
+                               conditional node */
 } md_info;
 md_status md_get_info(md_ctx *ctx, md_info *out);
 /* Sorted -> original index map of the current atom order. */
@@ -229,10 +234,12 @@ md_status md_set_pair_depth(md_ctx *ctx, int depth);
 /* Autotuner: times the pair kernel for 2/4/8/16 threads per atom (single
  * systems also at 4/8/16 threads with half the default entries per lane and
  * batch) and the list builders (warp per cell, 4/8/16 threads per atom) on the
- * current state and keeps the fastest of each; returns the choice.  For leapfrog systems
- * without bonded terms it also times the step with the pair kernel and the
- * integrator fused into one kernel against separate kernels, by running
- * steps: the system then advances by 192 steps. */
+ * current state and keeps the fastest of each; returns the choice.  It also
+ * times the step graphs by running steps: fused or separate pair and
+ * integrator kernels (leapfrog systems without bonded terms), and for single
+ * systems the rebuild inline or behind a conditional node
+ * (md_set_graph_rebuild).  The system advances 128 steps per combination
+ * tried (up to 4; batches have one and do not advance). */
 md_status md_autotune(md_ctx *ctx, int *pair_tpa, int *list_tpa);
 /* Per-type exclusions (no counterpart in the reference, which excludes only
  * 1-2 bonded pairs): bit b of mask[a] excludes every pair of types a and b
@@ -245,6 +252,12 @@ md_status md_set_graphs(md_ctx *ctx, int use_graphs);
  * the leapfrog update) as one kernel, 0 as two; MD_ERR_UNSUPPORTED for other
  * systems when asked for 1.  md_autotune times both and keeps the faster. */
 md_status md_set_fused_step(md_ctx *ctx, int fused);
+/* How a step graph holds the neighbour-list rebuild (single systems): 0 (the
+ * default) a conditional node per step whose body is the rebuild; 1 the
+ * rebuild passes inline in every step, launched as programmatic dependents
+ * that return at once when no rebuild is due.  Both rebuild at the same
+ * steps and give the same trajectory; md_autotune keeps the faster. */
+md_status md_set_graph_rebuild(md_ctx *ctx, int inline_passes);
 /* Milliseconds of device time of the last md_step call (CUDA events). */
 md_status md_last_step_ms(md_ctx *ctx, float *ms);
 /* The pair-force kernel alone, nrep launches on the context's stream between

@@ -30,6 +30,8 @@ __global__ void k_cell_key(md_kparams kp, const md_devstate *st, int always,
                            const float4 *__restrict__ pos4, const int *__restrict__ cell_rank,
                            int *key, int *cell_count)
 {
+    pdl_wait();      /* launched after the previous pass (programmatic launch) */
+    pdl_trigger();
     if (!always && !st->update) return;
     int i = blockIdx.x * blockDim.x + threadIdx.x;
     if (i >= kp.n) return;
@@ -141,6 +143,8 @@ __global__ void k_clear_update_b(md_devstate *st, int always, int *rep_upd, md_r
 __global__ void k_cell_scan(md_kparams kp, md_devstate *st, int always, int ncells,
                             int *cell_count, int *cell_start, int *cell_fill)
 {
+    pdl_wait();      /* launched after the previous pass (programmatic launch) */
+    pdl_trigger();
     if (!always && !st->update) return;
     __shared__ int part[1024];
     int t = threadIdx.x, nt = blockDim.x;
@@ -174,6 +178,8 @@ __global__ void k_cell_scatter(md_kparams kp, const md_devstate *st, int always,
                                int *cell_fill, int *src, const int *__restrict__ arep,
                                const int *__restrict__ rep_upd)
 {
+    pdl_wait();      /* launched after the previous pass (programmatic launch) */
+    pdl_trigger();
     if (!always && !st->update) return;
     int i = blockIdx.x * blockDim.x + threadIdx.x;
     if (i >= kp.n) return;
@@ -188,6 +194,8 @@ __global__ void k_cell_order(md_kparams kp, const md_devstate *st, int always, i
                              const int *__restrict__ cell_start, const int *__restrict__ perm,
                              int *src, const int *__restrict__ crep, const int *__restrict__ rep_upd)
 {
+    pdl_wait();      /* launched after the previous pass (programmatic launch) */
+    pdl_trigger();
     if (!always && !st->update) return;
     int c = blockIdx.x * blockDim.x + threadIdx.x;
     if (c >= ncells) return;
@@ -212,6 +220,8 @@ __global__ void k_permute(md_kparams kp, const md_devstate *st, int always,
                           const int *__restrict__ type, double *tmp_d, float4 *tmp4, int *tmp_i,
                           const int *__restrict__ arep, const int *__restrict__ rep_upd)
 {
+    pdl_wait();      /* launched after the previous pass (programmatic launch) */
+    pdl_trigger();
     if (!always && !st->update) return;
     int s = blockIdx.x * blockDim.x + threadIdx.x;
     if (s >= kp.n) return;
@@ -234,6 +244,8 @@ __global__ void k_copyback(md_kparams kp, const md_devstate *st, int always,
                            double *kick, float4 *pos4, int *perm, int *iperm, int *type,
                            const int *__restrict__ arep, const int *__restrict__ rep_upd)
 {
+    pdl_wait();      /* launched after the previous pass (programmatic launch) */
+    pdl_trigger();
     if (!always && !st->update) return;
     int s = blockIdx.x * blockDim.x + threadIdx.x;
     if (s >= kp.n) return;
@@ -260,6 +272,8 @@ __global__ void k_remap(md_kparams kp, const md_devstate *st, int always,
                         int *bl_sn, const int4 *__restrict__ al_o, const int *__restrict__ al_on,
                         int4 *al_s, int *al_sn, int has_bonds, int has_angles)
 {
+    pdl_wait();      /* launched after the previous pass (programmatic launch) */
+    pdl_trigger();
     if (!always && !st->update) return;
     int s = blockIdx.x * blockDim.x + threadIdx.x;
     if (s >= kp.n) return;
@@ -291,7 +305,11 @@ __global__ void k_remap(md_kparams kp, const md_devstate *st, int always,
 
 /* Ends a rebuild (or a step without one): the next step's check sets the
  * request again. */
-__global__ void k_clear_update(md_devstate *st) { st->update = 0; }
+__global__ void k_clear_update(md_devstate *st)
+{
+    pdl_wait();
+    st->update = 0;
+}
 
 /* First node of a captured step graph: the rebuild condition of its first
  * step comes from the check done by the step before the graph. */
@@ -311,6 +329,8 @@ __global__ void __launch_bounds__(256) k_build_list(
     const int *__restrict__ cell_rank, const int *__restrict__ cell_start,
     const unsigned *__restrict__ type_mask, unsigned *nl, int *nl_n, float4 *pos_old)
 {
+    pdl_wait();      /* launched after the previous pass (programmatic launch) */
+    pdl_trigger();
     if (!always && !st->update) return;
     int gt = blockIdx.x * blockDim.x + threadIdx.x;
     int i = gt / TPA, lane = gt % TPA;
@@ -406,6 +426,8 @@ __global__ void __launch_bounds__(CW_WARPS * 32) k_build_cells(
     int *nl_n, float4 *pos_old, const md_rep *__restrict__ reps, const int *__restrict__ crep,
     const int *__restrict__ rep_upd)
 {
+    pdl_wait();
+    pdl_trigger();
     if (!always && !st->update) return;
     __shared__ float4 s_p[CW_WARPS][CW_MAXI];
     __shared__ uint4 s_ex[CW_WARPS][CW_MAXI];
@@ -656,9 +678,21 @@ void launch_check(md_ctx *c, const md_kparams &kp)
     k_check<<<nb, 256, 0, c->stream>>>(kp, c->pos4, c->pos_old, c->st);
 }
 
-void launch_rebuild(md_ctx *c, const md_kparams &kp, bool unconditional, bool all_replicas)
+/* A pass of the rebuild: a plain launch, or (pdl) a programmatic dependent
+ * launch whose blocks may be scheduled while the previous pass finishes;
+ * every pass waits for its predecessor (pdl_wait) before it reads anything. */
+template <typename... KArgs, typename... Args>
+static void rb_launch(bool pdl, void (*k)(KArgs...), dim3 grid, dim3 block, cudaStream_t s,
+                      Args... args)
+{
+    if (pdl) md_launch_pdl(k, grid, block, s, args...);
+    else k<<<grid, block, 0, s>>>(args...);
+}
+
+void launch_rebuild(md_ctx *c, const md_kparams &kp, bool unconditional, bool all_replicas, bool pdl)
 {
     int always = unconditional ? 1 : 0;
+    if (c->batch) pdl = false;
     int nb = (kp.n + 255) / 256;
     cudaStream_t s = c->stream;
     const bool batch = c->batch;
@@ -673,25 +707,32 @@ void launch_rebuild(md_ctx *c, const md_kparams &kp, bool unconditional, bool al
                                                         c->rep_upd, c->cell_count, c->cell_start,
                                                         c->cell_fill);
     } else {
-        k_cell_key<<<nb, 256, 0, s>>>(kp, c->st, always, c->pos4, c->cell_rank, c->key, c->cell_count);
-        k_cell_scan<<<1, 1024, 0, s>>>(kp, c->st, always, c->ncells, c->cell_count, c->cell_start,
-                                       c->cell_fill);
+        rb_launch(pdl, k_cell_key, dim3(nb), dim3(256), s, kp, c->st, always, (const float4 *)c->pos4,
+                  (const int *)c->cell_rank, c->key, c->cell_count);
+        rb_launch(pdl, k_cell_scan, dim3(1), dim3(1024), s, kp, c->st, always, c->ncells, c->cell_count,
+                  c->cell_start, c->cell_fill);
     }
-    k_cell_scatter<<<nb, 256, 0, s>>>(kp, c->st, always, c->key, c->cell_start, c->cell_fill, c->src,
-                                      arep, c->rep_upd);
-    k_cell_order<<<(c->ncells + 255) / 256, 256, 0, s>>>(kp, c->st, always, c->ncells,
-                                                          c->cell_start, c->perm, c->src, crep,
-                                                          c->rep_upd);
-    k_permute<<<nb, 256, 0, s>>>(kp, c->st, always, c->src, c->x, c->v, c->mass, c->kick, c->pos4,
-                                 c->perm, c->type, c->tmp_d, c->tmp4, c->tmp_i, arep, c->rep_upd);
-    k_copyback<<<nb, 256, 0, s>>>(kp, c->st, always, c->tmp_d, c->tmp4, c->tmp_i, c->x, c->v,
-                                  c->mass, c->kick, c->pos4, c->perm, c->iperm, c->type, arep,
-                                  c->rep_upd);
+    rb_launch(pdl, k_cell_scatter, dim3(nb), dim3(256), s, kp, (const md_devstate *)c->st, always,
+              (const int *)c->key, (const int *)c->cell_start, c->cell_fill, c->src, arep,
+              (const int *)c->rep_upd);
+    rb_launch(pdl, k_cell_order, dim3((c->ncells + 255) / 256), dim3(256), s, kp,
+              (const md_devstate *)c->st, always, c->ncells, (const int *)c->cell_start,
+              (const int *)c->perm, c->src, crep, (const int *)c->rep_upd);
+    rb_launch(pdl, k_permute, dim3(nb), dim3(256), s, kp, (const md_devstate *)c->st, always,
+              (const int *)c->src, (const double *)c->x, (const double *)c->v,
+              (const double *)c->mass, (const double *)c->kick, (const float4 *)c->pos4,
+              (const int *)c->perm, (const int *)c->type, c->tmp_d, c->tmp4, c->tmp_i, arep,
+              (const int *)c->rep_upd);
+    rb_launch(pdl, k_copyback, dim3(nb), dim3(256), s, kp, (const md_devstate *)c->st, always,
+              (const double *)c->tmp_d, (const float4 *)c->tmp4, (const int *)c->tmp_i, c->x, c->v,
+              c->mass, c->kick, c->pos4, c->perm, c->iperm, c->type, arep, (const int *)c->rep_upd);
     /* a batch has no exclusions or bonded lists to re-express */
     if (!batch)
-        k_remap<<<nb, 256, 0, s>>>(kp, c->st, always, c->perm, c->iperm, c->excl_orig, c->excl_s,
-                                   c->bl_o, c->bl_on, c->bl_s, c->bl_sn, c->al_o, c->al_on, c->al_s,
-                                   c->al_sn, c->has_bonds, c->has_angles);
+        rb_launch(pdl, k_remap, dim3(nb), dim3(256), s, kp, (const md_devstate *)c->st, always,
+                  (const int *)c->perm, (const int *)c->iperm, (const uint4 *)c->excl_orig, c->excl_s,
+                  (const int2 *)c->bl_o, (const int *)c->bl_on, c->bl_s, c->bl_sn,
+                  (const int4 *)c->al_o, (const int *)c->al_on, c->al_s, c->al_sn, c->has_bonds,
+                  c->has_angles);
     if (batch) {
         /* at most 5 stencil cells per axis (cells of side >= rl/2): <= 125 */
         k_build_cells<true><<<(c->ncells + CW_WARPS - 1) / CW_WARPS, CW_WARPS * 32, 0, s>>>(
@@ -711,15 +752,19 @@ void launch_rebuild(md_ctx *c, const md_kparams &kp, bool unconditional, bool al
     int lb = (int)((threads + 255) / 256);
     switch (ltpa) {
     case 0:
-        k_build_cells<false><<<(c->ncells + CW_WARPS - 1) / CW_WARPS, CW_WARPS * 32, 0, s>>>(
-            kp, c->st, always, c->ncells, c->pos4, c->type, c->excl_s, c->cell_rank, c->cell_lin,
-            c->cell_start, c->type_mask_dev, c->nl, c->nl_n, c->pos_old, nullptr, nullptr, nullptr);
+        rb_launch(pdl, k_build_cells<false>, dim3((c->ncells + CW_WARPS - 1) / CW_WARPS),
+                  dim3(CW_WARPS * 32), s, kp, c->st, always, c->ncells, (const float4 *)c->pos4,
+                  (const int *)c->type, (const uint4 *)c->excl_s, (const int *)c->cell_rank,
+                  (const int *)c->cell_lin, (const int *)c->cell_start,
+                  (const unsigned *)c->type_mask_dev, c->nl, c->nl_n, c->pos_old,
+                  (const md_rep *)nullptr, (const int *)nullptr, (const int *)nullptr);
         break;
 #define MD_LIST_CASE(T)                                                                            \
     case T:                                                                                        \
-        k_build_list<T><<<lb, 256, 0, s>>>(kp, c->st, always, c->pos4, c->type, c->excl_s,         \
-                                           c->cell_rank, c->cell_start, c->type_mask_dev, c->nl,   \
-                                           c->nl_n, c->pos_old);                                   \
+        rb_launch(pdl, k_build_list<T>, dim3(lb), dim3(256), s, kp, c->st, always,                 \
+                  (const float4 *)c->pos4, (const int *)c->type, (const uint4 *)c->excl_s,         \
+                  (const int *)c->cell_rank, (const int *)c->cell_start,                           \
+                  (const unsigned *)c->type_mask_dev, c->nl, c->nl_n, c->pos_old);                 \
         break;
         MD_LIST_CASE(1)
         MD_LIST_CASE(2)
@@ -731,7 +776,7 @@ void launch_rebuild(md_ctx *c, const md_kparams &kp, bool unconditional, bool al
     default:
         break;
     }
-    k_clear_update<<<1, 1, 0, s>>>(c->st);
+    rb_launch(pdl, k_clear_update, dim3(1), dim3(1), s, c->st);
 }
 
 void launch_set_condition(md_ctx *c, unsigned long long handle)

@@ -33,6 +33,7 @@ __global__ void __launch_bounds__(128) k_pair_leapfrog(
     __shared__ double s_x0[3][NA], s_v0[3][NA], s_kick[NA], s_mass[NA];
     __shared__ float4 s_old[NA];
     __shared__ float s_x[NA][3];
+    pdl_trigger();   /* the list passes that follow may be scheduled */
     const int i0 = blockIdx.x * NA;
     const size_t P = (size_t)kp.pitch;
     /* the update's inputs travel while the pair forces are computed */

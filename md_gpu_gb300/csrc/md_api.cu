@@ -342,8 +342,10 @@ md_status capture_graph(md_ctx *c, int nsteps, int energy_first)
     md_kparams kp = md_make_kparams(c);
     cudaGraph_t g = nullptr;
     MD_CUDA_TRY(c, cudaGraphCreate(&g, 0));
-    std::vector<cudaGraphConditionalHandle> h(nsteps);
-    for (int k = 0; k < nsteps; k++) {
+    /* a batch keeps the conditional node (its passes gate on per-replica flags) */
+    const bool inl = c->rebuild_inline && !c->batch;
+    std::vector<cudaGraphConditionalHandle> h(nsteps, 0);
+    for (int k = 0; k < (inl ? 0 : nsteps); k++) {
         cudaError_t e = cudaGraphConditionalHandleCreate(&h[k], g, 0, cudaGraphCondAssignDefault);
         if (e != cudaSuccess) {
             cudaGraphDestroy(g);
@@ -358,28 +360,32 @@ md_status capture_graph(md_ctx *c, int nsteps, int energy_first)
     }
     md_status s = MD_OK;
     const float4 *start_pos4 = c->pos4;
-    if (c->integrator == MD_LEAPFROG) launch_set_condition(c, (unsigned long long)h[0]);
+    if (c->integrator == MD_LEAPFROG && !inl) launch_set_condition(c, (unsigned long long)h[0]);
     int fused = 0;
     for (int k = 0; k < nsteps && s == MD_OK; k++) {
         int energy = (energy_first && k == 0) ? 1 : 0;
         if (c->integrator == MD_LEAPFROG) {
-            s = capture_rebuild_node(c, kp, h[k]);
+            if (inl) launch_rebuild(c, kp, false, false, true);
+            else s = capture_rebuild_node(c, kp, h[k]);
             if (s != MD_OK) break;
             int next = k + 1 < nsteps;
-            unsigned long long hn = next ? (unsigned long long)h[k + 1] : 0ull;
+            /* with inline passes no kernel sets a condition */
+            unsigned long long hn = (next && !inl) ? (unsigned long long)h[k + 1] : 0ull;
             /* an even number of fused steps brings the position buffers back
              * to where the graph started */
             bool fuse = !energy && md_can_fuse(c) && (next || (fused & 1));
+            const int has = next && !inl;
             if (fuse) {
-                launch_pair_leapfrog(c, kp, hn, next);
+                launch_pair_leapfrog(c, kp, hn, has);
                 fused++;
             } else {
                 launch_forces(c, kp, energy != 0, MD_TERM_ALL);
-                launch_leapfrog(c, kp, energy, hn, next);
+                launch_leapfrog(c, kp, energy, hn, has);
             }
         } else {
-            launch_vv_first(c, kp, (unsigned long long)h[k], 1);
-            s = capture_rebuild_node(c, kp, h[k]);
+            launch_vv_first(c, kp, inl ? 0ull : (unsigned long long)h[k], inl ? 0 : 1);
+            if (inl) launch_rebuild(c, kp, false, false, true);
+            else s = capture_rebuild_node(c, kp, h[k]);
             if (s != MD_OK) break;
             launch_forces(c, kp, energy != 0, MD_TERM_ALL);
             launch_vv_second(c, kp, energy);
@@ -1446,6 +1452,8 @@ md_status md_get_info(md_ctx *c, md_info *out)
     out->pair_threads_per_atom = c->pair_tpa;
     out->pair_entries_per_lane = md_pair_depth(c);
     out->positions_centered = c->centered;
+    out->fused_step = md_can_fuse(c) ? 1 : 0;
+    out->rebuild_inline = (c->rebuild_inline && !c->batch) ? 1 : 0;
     out->list_threads_per_atom = c->list_tpa;
     out->builds = h.builds;
     out->max_neighbors = *std::max_element(cnt.begin(), cnt.begin() + c->n);
@@ -1459,6 +1467,11 @@ md_status md_get_info(md_ctx *c, md_info *out)
      * list, clear */
     out->kernels_per_rebuild = c->batch ? 8 : 9;
     out->kernels_per_graph = c->integrator == MD_LEAPFROG ? 1 : 0;
+    if (c->rebuild_inline && !c->batch) {   /* the passes run (and return) in every step */
+        out->kernels_per_step += out->kernels_per_rebuild;
+        out->kernels_per_rebuild = 0;
+        out->kernels_per_graph = 0;
+    }
     return MD_OK;
 }
 
@@ -1491,6 +1504,16 @@ md_status md_set_type_exclusions(md_ctx *c, const unsigned *mask)
     return refresh_state(c);
 }
 
+/* Builds so far (synchronises the stream). */
+static md_status read_builds(md_ctx *c, int *builds)
+{
+    MD_CUDA_TRY(c, cudaStreamSynchronize(c->stream));
+    md_devstate h;
+    MD_CUDA_TRY(c, cudaMemcpy(&h, c->st, sizeof(h), cudaMemcpyDeviceToHost));
+    *builds = h.builds;
+    return MD_OK;
+}
+
 md_status md_autotune(md_ctx *c, int *pair_tpa, int *list_tpa)
 {
     if (!c) return MD_ERR_ARG;
@@ -1519,21 +1542,41 @@ md_status md_autotune(md_ctx *c, int *pair_tpa, int *list_tpa)
     }
     c->pair_depth = bd;
     c->pair_tpa = bp;
-    /* leapfrog systems without bonded terms: separate or fused pair and
-     * integrator kernels, timed as they run (the system advances 192 steps) */
+    /* the step graph: separate or (leapfrog without bonded terms) fused pair
+     * and integrator kernels, the rebuild behind a conditional node or inline
+     * (single systems); each combination timed as it runs, 96 steps after 32
+     * of warm-up, less the list builds that fell in the window at the
+     * measured cost of one (the system advances 128 steps per combination) */
+    int bi = 0;
     c->fuse_step = 1;
-    if (md_can_fuse(c)) {
-        float tm[2] = {0.0f, 0.0f};
-        for (int fz = 0; fz < 2; fz++) {
-            c->fuse_step = fz;
-            md_status s = md_step(c, 32, 0);
-            if (s == MD_OK) s = md_step(c, 64, 0);
-            if (s == MD_OK) s = md_last_step_ms(c, &tm[fz]);
-            if (s != MD_OK) return s;
-        }
-        bf = tm[1] < tm[0] ? 1 : 0;
+    const int nf = md_can_fuse(c) ? 2 : 1, ni = c->batch ? 1 : 2;
+    if (nf * ni > 1) {   /* a batch has one choice: it keeps its state */
+        float t_rb = 0.0f;
+        md_status s = md_time_rebuild(c, 3, &t_rb);
+        if (s != MD_OK) return s;
+        float tbest = 1e30f;
+        for (int fz = 0; fz < nf; fz++)
+            for (int inl = 0; inl < ni; inl++) {
+                c->fuse_step = fz;
+                c->rebuild_inline = inl;
+                if (c->gexec) {
+                    cudaGraphExecDestroy(c->gexec);
+                    c->gexec = nullptr;
+                }
+                s = md_step(c, 32, 0);
+                int b0 = 0, b1 = 0;
+                float ms = 0.0f;
+                if (s == MD_OK) s = read_builds(c, &b0);
+                if (s == MD_OK) s = md_step(c, 96, 0);
+                if (s == MD_OK) s = md_last_step_ms(c, &ms);
+                if (s == MD_OK) s = read_builds(c, &b1);
+                if (s != MD_OK) return s;
+                const float t = ms - (float)(b1 - b0) * t_rb;
+                if (t < tbest) { tbest = t; bf = fz; bi = inl; }
+            }
     }
     c->fuse_step = bf;
+    c->rebuild_inline = bi;
     best = 1e30f;
     for (int t : lt) {
         if (c->batch && t != 0) continue;   /* batches build one warp per cell */
@@ -1561,6 +1604,18 @@ md_status md_set_graphs(md_ctx *c, int use_graphs)
 {
     if (!c) return MD_ERR_ARG;
     c->use_graphs = use_graphs ? 1 : 0;
+    return MD_OK;
+}
+
+md_status md_set_graph_rebuild(md_ctx *c, int inline_passes)
+{
+    if (!c) return MD_ERR_ARG;
+    const int v = inline_passes ? 1 : 0;
+    if (c->gexec && v != c->rebuild_inline) {
+        cudaGraphExecDestroy(c->gexec);
+        c->gexec = nullptr;
+    }
+    c->rebuild_inline = v;
     return MD_OK;
 }
 

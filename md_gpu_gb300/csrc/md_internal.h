@@ -196,6 +196,8 @@ struct md_ctx {
     const float4 *gpos4 = nullptr; /* position buffer current when the graph was captured */
     int use_graphs = 1;            /* 0: launch every step's kernels eagerly */
     int fuse_step = 0;             /* 1: fused pair+leapfrog kernel where applicable */
+    int rebuild_inline = 0;        /* step graphs: 1 = list passes inline (programmatic launches
+                                      that return at once without a request), 0 = a conditional node */
     long long host_step = 0;       /* steps run so far (mirrors st->step) */
     double *io_dev = nullptr;      /* 4*pitch doubles for host transfers */
     int pair_tpa = 8;    /* threads per atom in the pair kernel */
@@ -262,7 +264,8 @@ void launch_check(md_ctx *c, const md_kparams &kp);
  * body of a graph's conditional rebuild node, or a forced build).  In a
  * batch only the replicas whose atoms moved are rebuilt, unless
  * all_replicas is set (forced builds). */
-void launch_rebuild(md_ctx *c, const md_kparams &kp, bool unconditional, bool all_replicas);
+void launch_rebuild(md_ctx *c, const md_kparams &kp, bool unconditional, bool all_replicas,
+                    bool pdl = false);
 void launch_set_condition(md_ctx *c, unsigned long long handle);
 /* ---- launchers (k_forces.cu) ---- */
 void launch_forces(md_ctx *c, const md_kparams &kp, bool energy, int terms);

@@ -67,7 +67,8 @@ class Info(C.Structure):
                 ("pair_threads_per_atom", C.c_int), ("list_threads_per_atom", C.c_int),
                 ("builds", C.c_int), ("max_neighbors", C.c_int), ("kernels_per_step", C.c_int),
                 ("kernels_per_rebuild", C.c_int), ("kernels_per_graph", C.c_int),
-                ("pair_entries_per_lane", C.c_int), ("positions_centered", C.c_int)]
+                ("pair_entries_per_lane", C.c_int), ("positions_centered", C.c_int),
+                ("fused_step", C.c_int), ("rebuild_inline", C.c_int)]
 
 
 def _make_desc(keep, *, box, itype, charge, pos, vel, type_mass, lj1, lj2, lkspace, rcutsq,
@@ -154,6 +155,7 @@ def library(path: Optional[str] = None):
     L.md_set_type_exclusions.argtypes = [vp, vp]
     L.md_set_graphs.argtypes = [vp, C.c_int]
     L.md_set_fused_step.argtypes = [vp, C.c_int]
+    L.md_set_graph_rebuild.argtypes = [vp, C.c_int]
     L.md_ref_kinetic_energy_noalloc.argtypes = [vp, C.c_int, vp, vp]
     L.md_create_batch.argtypes = [C.POINTER(SystemDesc), C.c_int, vp, C.POINTER(vp)]
     L.md_get_replica_thermo.argtypes = [vp, C.POINTER(Thermo), C.c_int]
@@ -370,7 +372,8 @@ class MDSystem:
                 "kernels_per_rebuild": i.kernels_per_rebuild,
                 "kernels_per_graph": i.kernels_per_graph,
                 "pair_depth": i.pair_entries_per_lane,
-                "centered": bool(i.positions_centered)}
+                "centered": bool(i.positions_centered),
+                "fused_step": bool(i.fused_step), "rebuild_inline": bool(i.rebuild_inline)}
 
     def neighbor_list(self, nmax):
         """Reference layout (neighborlist.cu:284): (nnlist[pitch*nmax], nnlist_max[pitch])."""
@@ -418,6 +421,10 @@ class MDSystem:
     def set_graphs(self, use_graphs=True):
         """Replay captured step graphs (default) or launch eagerly."""
         _check(library().md_set_graphs(self._ctx, 1 if use_graphs else 0), self._ctx)
+
+    def set_graph_rebuild(self, inline=True):
+        """Step graphs: rebuild passes inline (True) or behind a conditional node."""
+        _check(library().md_set_graph_rebuild(self._ctx, 1 if inline else 0), self._ctx)
 
     def set_fused_step(self, fused=True):
         """Leapfrog without bonded terms: pair forces and update in one kernel."""

@@ -397,6 +397,34 @@ def test_fused_step_matches_separate(pair_tpa, depth):
     assert t0["ke"] == t1["ke"] and t0["lambda_"] == t1["lambda_"]
 
 
+@pytest.mark.parametrize("name", ["nacl_fused", "nacl", "argon_vv", "water_nh"])
+def test_graph_rebuild_inline_matches_conditional(name):
+    """Step graphs with the list-rebuild passes inline (programmatic launches
+    that return at once unless a rebuild is due) advance bit for bit like
+    graphs with a conditional rebuild node: the same steps rebuild."""
+    if name.startswith("nacl"):
+        sys_ = synth.nacl_rocksalt(ncell=6, seed=42, nmaxlist=512)
+    elif name == "argon_vv":
+        sys_ = synth.argon_fcc(ncell=7, seed=3)
+    else:
+        sys_ = synth.water_grid(nside=9, seed=4)
+    case = oracle.load(_write(sys_))
+    out = []
+    for inline in (0, 1):
+        with gu.system_from_case(case) as sim:
+            sim.set_tuning(8, 0)
+            if name.startswith("nacl"):
+                sim.set_fused_step(name == "nacl_fused")
+            sim.set_graph_rebuild(inline)
+            sim.step(96)
+            out.append((sim.positions(), sim.velocities(), sim.info(), sim.thermo()))
+    (x0, v0, i0, t0), (x1, v1, i1, t1) = out
+    assert i1["kernels_per_rebuild"] == 0 and i0["kernels_per_rebuild"] > 0
+    assert i0["builds"] == i1["builds"] >= 2
+    assert np.array_equal(x0, x1) and np.array_equal(v0, v1)
+    assert t0["ke"] == t1["ke"]
+
+
 def test_autotune_keeps_results():
     """After autotuning (which may advance the system), list and forces of the
     current positions still match the oracle."""
