@@ -138,37 +138,82 @@ __global__ void k_clear_update_b(md_devstate *st, int always, int *rep_upd, md_r
     }
 }
 
-/* Exclusive scan of the cell counts (one block), then zero the counters for
- * the next build.  cell_start has ncells + 1 entries. */
-__global__ void k_cell_scan(md_kparams kp, md_devstate *st, int always, int ncells,
-                            int *cell_count, int *cell_start, int *cell_fill)
+/* Exclusive scan of the cell counts (one block of 1024 threads), then zero
+ * the counters for the next build.  cell_start has ncells + 1 entries.  In
+ * rounds of 1024 x SCAN_K cells: the counts pass through shared memory, so
+ * that global loads and stores are coalesced (one SM issues them all) while
+ * each thread scans SCAN_K consecutive counts; warps scan their threads'
+ * sums with shuffles and warp 0 the warp totals.  Shared index i is stored
+ * at i + i / SCAN_K, so the per-thread reads hit distinct banks. */
+constexpr int SCAN_K = 8;
+constexpr int SCAN_N = 1024 * SCAN_K;
+__device__ __forceinline__ int scan_pad(int i) { return i + i / SCAN_K; }
+
+__global__ void __launch_bounds__(1024) k_cell_scan(md_kparams kp, md_devstate *st, int always,
+                                                    int ncells, int *cell_count, int *cell_start,
+                                                    int *cell_fill)
 {
     pdl_wait();      /* launched after the previous pass (programmatic launch) */
     pdl_trigger();
     if (!always && !st->update) return;
-    __shared__ int part[1024];
-    int t = threadIdx.x, nt = blockDim.x;
-    int chunk = (ncells + nt - 1) / nt;
-    int b = t * chunk, e = min(ncells, b + chunk);
-    int s = 0;
-    for (int c = b; c < e; c++) s += cell_count[c];
-    part[t] = s;
-    __syncthreads();
-    for (int off = 1; off < nt; off <<= 1) {
-        int v = t >= off ? part[t - off] : 0;
+    __shared__ int buf[SCAN_N + SCAN_N / SCAN_K];
+    __shared__ int wsum[32];
+    const int t = threadIdx.x, lane = t & 31, w = t >> 5;
+    int carry = 0;
+    for (int base = 0; base < ncells; base += SCAN_N) {
+#pragma unroll
+        for (int k = 0; k < SCAN_K; k++) {
+            const int i = k * 1024 + t, g = base + i;
+            buf[scan_pad(i)] = g < ncells ? cell_count[g] : 0;
+        }
         __syncthreads();
-        part[t] += v;
+        int v[SCAN_K], s = 0;
+#pragma unroll
+        for (int k = 0; k < SCAN_K; k++) {
+            v[k] = buf[scan_pad(t * SCAN_K + k)];
+            s += v[k];
+        }
+        int incl = s;
+#pragma unroll
+        for (int o = 1; o < 32; o <<= 1) {
+            const int y = __shfl_up_sync(0xffffffffu, incl, o);
+            if (lane >= o) incl += y;
+        }
+        if (lane == 31) wsum[w] = incl;
         __syncthreads();
+        if (w == 0) {
+            int x = wsum[lane];
+#pragma unroll
+            for (int o = 1; o < 32; o <<= 1) {
+                const int y = __shfl_up_sync(0xffffffffu, x, o);
+                if (lane >= o) x += y;
+            }
+            wsum[lane] = x;   /* inclusive over warps */
+        }
+        __syncthreads();
+        int run = carry + (w > 0 ? wsum[w - 1] : 0) + incl - s;
+#pragma unroll
+        for (int k = 0; k < SCAN_K; k++) {
+            buf[scan_pad(t * SCAN_K + k)] = run;
+            run += v[k];
+        }
+        carry += wsum[31];
+        __syncthreads();
+#pragma unroll
+        for (int k = 0; k < SCAN_K; k++) {
+            const int i = k * 1024 + t, g = base + i;
+            if (g < ncells) {
+                cell_start[g] = buf[scan_pad(i)];
+                cell_count[g] = 0;
+                cell_fill[g] = 0;
+            }
+        }
+        __syncthreads();   /* buf and wsum are rewritten by the next round */
     }
-    int run = part[t] - s;
-    for (int c = b; c < e; c++) {
-        cell_start[c] = run;
-        run += cell_count[c];
-        cell_count[c] = 0;
-        cell_fill[c] = 0;
+    if (t == 0) {
+        cell_start[ncells] = carry;
+        st->builds += 1;
     }
-    if (t == nt - 1) cell_start[ncells] = part[t];
-    if (t == 0) st->builds += 1;
 }
 
 /* In a batch (arep, rep_upd non-null) the passes below touch only the atoms
@@ -189,7 +234,11 @@ __global__ void k_cell_scatter(md_kparams kp, const md_devstate *st, int always,
 }
 
 /* Within each cell, order atoms by original index: the sorted order is then a
- * function of the positions alone. */
+ * function of the positions alone.  One warp per cell: each atom's place is
+ * the number of the cell's atoms with a smaller original index (indices are
+ * distinct), counted with shuffles; cells of more than 4 x 32 atoms (far
+ * denser than any liquid at these cell sizes) are sorted by one lane. */
+constexpr int ORD_MAX = 4;
 __global__ void k_cell_order(md_kparams kp, const md_devstate *st, int always, int ncells,
                              const int *__restrict__ cell_start, const int *__restrict__ perm,
                              int *src, const int *__restrict__ crep, const int *__restrict__ rep_upd)
@@ -197,11 +246,38 @@ __global__ void k_cell_order(md_kparams kp, const md_devstate *st, int always, i
     pdl_wait();      /* launched after the previous pass (programmatic launch) */
     pdl_trigger();
     if (!always && !st->update) return;
-    int c = blockIdx.x * blockDim.x + threadIdx.x;
+    const int c = (int)((blockIdx.x * blockDim.x + threadIdx.x) >> 5), lane = threadIdx.x & 31;
     if (c >= ncells) return;
     if (crep && !rep_upd[crep[c]]) return;
-    int b = cell_start[c], e = cell_start[c + 1];
-    for (int k = b + 1; k < e; k++) {
+    const int b = cell_start[c], n = cell_start[c + 1] - b;
+    if (n <= 1) return;
+    if (n <= 32 * ORD_MAX) {
+        int a[ORD_MAX], key[ORD_MAX], rank[ORD_MAX];
+#pragma unroll
+        for (int q = 0; q < ORD_MAX; q++) {
+            const int k = q * 32 + lane;
+            a[q] = k < n ? src[b + k] : 0;
+            key[q] = k < n ? perm[a[q]] : 0x7fffffff;
+            rank[q] = 0;
+        }
+#pragma unroll
+        for (int q2 = 0; q2 < ORD_MAX; q2++) {
+            if (q2 * 32 >= n) break;
+            const int m = min(32, n - q2 * 32);
+            for (int j = 0; j < m; j++) {
+                const int kj = __shfl_sync(0xffffffffu, key[q2], j);
+#pragma unroll
+                for (int q = 0; q < ORD_MAX; q++) rank[q] += kj < key[q] ? 1 : 0;
+            }
+        }
+        __syncwarp();   /* every read of src above precedes the writes below */
+#pragma unroll
+        for (int q = 0; q < ORD_MAX; q++)
+            if (q * 32 + lane < n) src[b + rank[q]] = a[q];
+        return;
+    }
+    if (lane != 0) return;
+    for (int k = b + 1; k < b + n; k++) {
         int a = src[k], ka = perm[a];
         int m = k - 1;
         while (m >= b && perm[src[m]] > ka) {
@@ -715,7 +791,7 @@ void launch_rebuild(md_ctx *c, const md_kparams &kp, bool unconditional, bool al
     rb_launch(pdl, k_cell_scatter, dim3(nb), dim3(256), s, kp, (const md_devstate *)c->st, always,
               (const int *)c->key, (const int *)c->cell_start, c->cell_fill, c->src, arep,
               (const int *)c->rep_upd);
-    rb_launch(pdl, k_cell_order, dim3((c->ncells + 255) / 256), dim3(256), s, kp,
+    rb_launch(pdl, k_cell_order, dim3((c->ncells + 7) / 8), dim3(256), s, kp,
               (const md_devstate *)c->st, always, c->ncells, (const int *)c->cell_start,
               (const int *)c->perm, c->src, crep, (const int *)c->rep_upd);
     rb_launch(pdl, k_permute, dim3(nb), dim3(256), s, kp, (const md_devstate *)c->st, always,
@@ -726,8 +802,9 @@ void launch_rebuild(md_ctx *c, const md_kparams &kp, bool unconditional, bool al
     rb_launch(pdl, k_copyback, dim3(nb), dim3(256), s, kp, (const md_devstate *)c->st, always,
               (const double *)c->tmp_d, (const float4 *)c->tmp4, (const int *)c->tmp_i, c->x, c->v,
               c->mass, c->kick, c->pos4, c->perm, c->iperm, c->type, arep, (const int *)c->rep_upd);
-    /* a batch has no exclusions or bonded lists to re-express */
-    if (!batch)
+    /* exclusions and bonded lists to re-express only with bonds or angles
+     * (a batch has neither) */
+    if (!batch && (c->has_bonds || c->has_angles))
         rb_launch(pdl, k_remap, dim3(nb), dim3(256), s, kp, (const md_devstate *)c->st, always,
                   (const int *)c->perm, (const int *)c->iperm, (const uint4 *)c->excl_orig, c->excl_s,
                   (const int2 *)c->bl_o, (const int *)c->bl_on, c->bl_s, c->bl_sn,

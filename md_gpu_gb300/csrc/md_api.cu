@@ -601,8 +601,9 @@ md_status setup_device(md_ctx *c, void *stream, host_stage &h, md_ctx **out)
     up(c->perm, hperm.data(), sizeof(int) * P);
     up(c->iperm, hperm.data(), sizeof(int) * P);
     up(c->excl_orig, h.excl.data(), sizeof(uint4) * P);
-    /* batches never remap exclusions (they have none): the sorted copy is set once */
-    if (batch) up(c->excl_s, h.excl.data(), sizeof(uint4) * P);
+    /* without bonds there are no exclusions to remap (batches never have
+     * bonds): the sorted copy, all empty, is set once */
+    if (batch || !c->has_bonds) up(c->excl_s, h.excl.data(), sizeof(uint4) * P);
     up(c->cell_rank, h.cell_rank.data(), sizeof(int) * c->ncells);
     up(c->cell_lin, h.cell_lin.data(), sizeof(int) * c->ncells);
     up(c->cell_count, zeros.data(), sizeof(int) * c->ncells);
@@ -1462,10 +1463,10 @@ md_status md_get_info(md_ctx *c, md_info *out)
     out->kernels_per_step = md_can_fuse(c) ? 1
                                            : 1 + ((c->has_bonds || c->has_angles) ? 1 : 0) +
                                                  (c->integrator == MD_LEAPFROG ? 1 : 2);
-    /* single system: key, scan, scatter, order, permute, copyback, remap,
-     * list, clear; batch: key, scan, scatter, order, permute, copyback,
-     * list, clear */
-    out->kernels_per_rebuild = c->batch ? 8 : 9;
+    /* single system: key, scan, scatter, order, permute, copyback, remap
+     * (with bonds or angles), list, clear; batch: key, scan, scatter, order,
+     * permute, copyback, list, clear */
+    out->kernels_per_rebuild = (c->batch || !(c->has_bonds || c->has_angles)) ? 8 : 9;
     out->kernels_per_graph = c->integrator == MD_LEAPFROG ? 1 : 0;
     if (c->rebuild_inline && !c->batch) {   /* the passes run (and return) in every step */
         out->kernels_per_step += out->kernels_per_rebuild;
