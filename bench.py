@@ -306,6 +306,12 @@ def run_ours(args):
     n = sim.natom
     flush = torch.empty(512 * 1024 * 1024, dtype=torch.uint8, device="cuda")
     tuned = sim.autotune() if not args.no_autotune else None
+    if tuned is None and args.tuning:
+        # fixed settings (profiling: timings under a profiler would mislead the tuner)
+        pt, depth, lt, fused, inline = (int(v) for v in args.tuning.split(","))
+        sim.set_tuning(pt, lt, depth)
+        sim.set_fused_step(fused)
+        sim.set_graph_rebuild(inline)
     if args.eager:
         sim.set_graphs(False)
 
@@ -448,6 +454,8 @@ def main():
     ap.add_argument("--ref-md-steps", type=int, default=10)
     ap.add_argument("--ncell", type=int, default=20)
     ap.add_argument("--no-autotune", action="store_true")
+    ap.add_argument("--tuning", default="",
+                    help="with --no-autotune: pair_tpa,pair_depth,list_tpa,fused,inline (e.g. 8,2,0,1,1)")
     ap.add_argument("--eager", action="store_true",
                     help="launch every step's kernels eagerly instead of replaying graphs (for profilers)")
     args = ap.parse_args()

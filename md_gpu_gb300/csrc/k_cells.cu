@@ -11,6 +11,7 @@
  * (cells of side >= rl/2), the atoms are re-sorted along a Hilbert curve of
  * cells at every build, and the rebuild decision never leaves the device.
  */
+#include <algorithm>
 #include <type_traits>
 
 #include "md_device.cuh"
@@ -131,6 +132,7 @@ __global__ void k_clear_update_b(md_devstate *st, int always, int *rep_upd, md_r
     if (r == 0) {
         if (always || st->update) st->builds += 1;
         st->update = 0;
+        st->cell_next = 0;
     }
     if (r < nrep && rep_upd[r]) {
         repst[r].builds += 1;
@@ -239,15 +241,12 @@ __global__ void k_cell_scatter(md_kparams kp, const md_devstate *st, int always,
  * distinct), counted with shuffles; cells of more than 4 x 32 atoms (far
  * denser than any liquid at these cell sizes) are sorted by one lane. */
 constexpr int ORD_MAX = 4;
-__global__ void k_cell_order(md_kparams kp, const md_devstate *st, int always, int ncells,
-                             const int *__restrict__ cell_start, const int *__restrict__ perm,
-                             int *src, const int *__restrict__ crep, const int *__restrict__ rep_upd)
+/* The rank sort of one cell's atoms (one warp). */
+__device__ __forceinline__ void order_cell(int c, const int *__restrict__ cell_start,
+                                           const int *__restrict__ perm, int *src,
+                                           const int *__restrict__ crep,
+                                           const int *__restrict__ rep_upd, int lane)
 {
-    pdl_wait();      /* launched after the previous pass (programmatic launch) */
-    pdl_trigger();
-    if (!always && !st->update) return;
-    const int c = (int)((blockIdx.x * blockDim.x + threadIdx.x) >> 5), lane = threadIdx.x & 31;
-    if (c >= ncells) return;
     if (crep && !rep_upd[crep[c]]) return;
     const int b = cell_start[c], n = cell_start[c + 1] - b;
     if (n <= 1) return;
@@ -285,6 +284,20 @@ __global__ void k_cell_order(md_kparams kp, const md_devstate *st, int always, i
             m--;
         }
         src[m + 1] = a;
+    }
+}
+
+__global__ void k_cell_order(md_kparams kp, const md_devstate *st, int always, int ncells,
+                             const int *__restrict__ cell_start, const int *__restrict__ perm,
+                             int *src, const int *__restrict__ crep, const int *__restrict__ rep_upd)
+{
+    pdl_wait();      /* launched after the previous pass (programmatic launch) */
+    pdl_trigger();
+    if (!always && !st->update) return;
+    const int lane = threadIdx.x & 31, nw = (int)((gridDim.x * blockDim.x) >> 5);
+    for (int c = (int)((blockIdx.x * blockDim.x + threadIdx.x) >> 5); c < ncells; c += nw) {
+        order_cell(c, cell_start, perm, src, crep, rep_upd, lane);
+        __syncwarp();
     }
 }
 
@@ -385,6 +398,7 @@ __global__ void k_clear_update(md_devstate *st)
 {
     pdl_wait();
     st->update = 0;
+    st->cell_next = 0;
 }
 
 /* First node of a captured step graph: the rebuild condition of its first
@@ -493,18 +507,16 @@ struct cell_geom {
     int nc[3], sten[3], shift, lin0;
 };
 
+/* The list rows of the atoms of cell r (sorted rank), built by one warp. */
 template <bool BATCH>
-__global__ void __launch_bounds__(CW_WARPS * 32) k_build_cells(
-    md_kparams kp, md_devstate *st, int always, int ncells, const float4 *__restrict__ pos4,
+__device__ __forceinline__ void build_cell(
+    int r, const md_kparams &kp, md_devstate *st, const float4 *__restrict__ pos4,
     const int *__restrict__ type, const uint4 *__restrict__ excl_s,
     const int *__restrict__ cell_rank, const int *__restrict__ cell_lin,
     const int *__restrict__ cell_start, const unsigned *__restrict__ type_mask, unsigned *nl,
     int *nl_n, float4 *pos_old, const md_rep *__restrict__ reps, const int *__restrict__ crep,
     const int *__restrict__ rep_upd)
 {
-    pdl_wait();
-    pdl_trigger();
-    if (!always && !st->update) return;
     __shared__ float4 s_p[CW_WARPS][CW_MAXI];
     __shared__ uint4 s_ex[CW_WARPS][CW_MAXI];
     __shared__ unsigned s_tm[CW_WARPS][CW_MAXI];
@@ -515,8 +527,6 @@ __global__ void __launch_bounds__(CW_WARPS * 32) k_build_cells(
     __shared__ unsigned s_fe[CW_WARPS][64];               /* list entry (j | type << 29) */
     __shared__ unsigned char s_fc[CW_WARPS][64];          /* and image code */
     const int w = threadIdx.x >> 5, lane = threadIdx.x & 31;
-    const int r = blockIdx.x * CW_WARPS + w;
-    if (r >= ncells) return;
     const int ib = cell_start[r], ie = cell_start[r + 1];
     if (ib == ie) return;
     cell_geom G;
@@ -741,6 +751,34 @@ __global__ void __launch_bounds__(CW_WARPS * 32) k_build_cells(
     }
 }
 
+/* The warp-per-cell list builder.  A persistent grid (the blocks that fit
+ * on the GPU at once): each warp takes the next cell from a counter in the
+ * device state until none is left, so cells of uneven work balance, and a
+ * launch without a rebuild due starts only that many blocks.  The counter
+ * is reset by the pass that ends the rebuild. */
+template <bool BATCH>
+__global__ void __launch_bounds__(CW_WARPS * 32) k_build_cells(
+    md_kparams kp, md_devstate *st, int always, int ncells, const float4 *__restrict__ pos4,
+    const int *__restrict__ type, const uint4 *__restrict__ excl_s,
+    const int *__restrict__ cell_rank, const int *__restrict__ cell_lin,
+    const int *__restrict__ cell_start, const unsigned *__restrict__ type_mask, unsigned *nl,
+    int *nl_n, float4 *pos_old, const md_rep *__restrict__ reps, const int *__restrict__ crep,
+    const int *__restrict__ rep_upd)
+{
+    pdl_wait();
+    pdl_trigger();
+    if (!always && !st->update) return;
+    const int lane = threadIdx.x & 31;
+    for (;;) {
+        int r = 0;
+        if (lane == 0) r = atomicAdd(&st->cell_next, 1);
+        r = __shfl_sync(0xffffffffu, r, 0);
+        if (r >= ncells) break;
+        build_cell<BATCH>(r, kp, st, pos4, type, excl_s, cell_rank, cell_lin, cell_start, type_mask, nl,
+                          nl_n, pos_old, reps, crep, rep_upd);
+    }
+}
+
 }  // namespace
 
 void launch_check(md_ctx *c, const md_kparams &kp)
@@ -765,10 +803,29 @@ static void rb_launch(bool pdl, void (*k)(KArgs...), dim3 grid, dim3 block, cuda
     else k<<<grid, block, 0, s>>>(args...);
 }
 
+/* Blocks of the persistent warp-per-cell builder: as many as are resident
+ * at once (found once per context, on its first, uncaptured, build), at
+ * most one warp per cell. */
+static int cw_blocks(md_ctx *c, bool batch)
+{
+    int &g = c->cw_grid[batch ? 1 : 0];
+    if (g == 0) {
+        int dev = 0, nsm = 0, occ = 0;
+        cudaGetDevice(&dev);
+        cudaDeviceGetAttribute(&nsm, cudaDevAttrMultiProcessorCount, dev);
+        c->nsm = std::max(1, nsm);
+        if (batch) cudaOccupancyMaxActiveBlocksPerMultiprocessor(&occ, k_build_cells<true>, CW_WARPS * 32, 0);
+        else cudaOccupancyMaxActiveBlocksPerMultiprocessor(&occ, k_build_cells<false>, CW_WARPS * 32, 0);
+        g = std::max(1, nsm) * std::max(1, occ);
+    }
+    return std::max(1, std::min(g, (c->ncells + CW_WARPS - 1) / CW_WARPS));
+}
+
 void launch_rebuild(md_ctx *c, const md_kparams &kp, bool unconditional, bool all_replicas, bool pdl)
 {
     int always = unconditional ? 1 : 0;
     if (c->batch) pdl = false;
+    const int cwb = cw_blocks(c, c->batch);   /* also finds the SM count */
     int nb = (kp.n + 255) / 256;
     cudaStream_t s = c->stream;
     const bool batch = c->batch;
@@ -791,7 +848,8 @@ void launch_rebuild(md_ctx *c, const md_kparams &kp, bool unconditional, bool al
     rb_launch(pdl, k_cell_scatter, dim3(nb), dim3(256), s, kp, (const md_devstate *)c->st, always,
               (const int *)c->key, (const int *)c->cell_start, c->cell_fill, c->src, arep,
               (const int *)c->rep_upd);
-    rb_launch(pdl, k_cell_order, dim3((c->ncells + 7) / 8), dim3(256), s, kp,
+    /* a warp per cell, at most two blocks of 8 warps per SM (a loop over cells) */
+    rb_launch(pdl, k_cell_order, dim3(std::min((c->ncells + 7) / 8, 2 * c->nsm)), dim3(256), s, kp,
               (const md_devstate *)c->st, always, c->ncells, (const int *)c->cell_start,
               (const int *)c->perm, c->src, crep, (const int *)c->rep_upd);
     rb_launch(pdl, k_permute, dim3(nb), dim3(256), s, kp, (const md_devstate *)c->st, always,
@@ -812,7 +870,7 @@ void launch_rebuild(md_ctx *c, const md_kparams &kp, bool unconditional, bool al
                   c->has_angles);
     if (batch) {
         /* at most 5 stencil cells per axis (cells of side >= rl/2): <= 125 */
-        k_build_cells<true><<<(c->ncells + CW_WARPS - 1) / CW_WARPS, CW_WARPS * 32, 0, s>>>(
+        k_build_cells<true><<<cwb, CW_WARPS * 32, 0, s>>>(
             kp, c->st, always, c->ncells, c->pos4, c->type, c->excl_s, c->cell_rank, c->cell_lin,
             c->cell_start, c->type_mask_dev, c->nl, c->nl_n, c->pos_old, c->reps_dev, c->crep,
             c->rep_upd);
@@ -829,7 +887,7 @@ void launch_rebuild(md_ctx *c, const md_kparams &kp, bool unconditional, bool al
     int lb = (int)((threads + 255) / 256);
     switch (ltpa) {
     case 0:
-        rb_launch(pdl, k_build_cells<false>, dim3((c->ncells + CW_WARPS - 1) / CW_WARPS),
+        rb_launch(pdl, k_build_cells<false>, dim3(cwb),
                   dim3(CW_WARPS * 32), s, kp, c->st, always, c->ncells, (const float4 *)c->pos4,
                   (const int *)c->type, (const uint4 *)c->excl_s, (const int *)c->cell_rank,
                   (const int *)c->cell_lin, (const int *)c->cell_start,

@@ -59,6 +59,7 @@ struct md_devstate {
     double kick_scale;   /* velocity scale applied by the next VV first half (NH: s2*s1) */
     unsigned blocks_done; /* blocks finished in the current reduction kernel */
     unsigned long long acc[3]; /* fixed-point KE (MD_KFIX), PE, sum ff r^2 (MD_EFIX) of the step */
+    int cell_next;       /* next cell a list-building warp takes (reset after each build) */
 };
 
 /* Everything a kernel needs about the system, passed by value. */
@@ -196,6 +197,8 @@ struct md_ctx {
     const float4 *gpos4 = nullptr; /* position buffer current when the graph was captured */
     int use_graphs = 1;            /* 0: launch every step's kernels eagerly */
     int fuse_step = 0;             /* 1: fused pair+leapfrog kernel where applicable */
+    int cw_grid[2] = {0, 0};       /* blocks of the persistent list builder (single, batch) */
+    int nsm = 1;                   /* SMs of the device (found with cw_grid) */
     int rebuild_inline = 0;        /* step graphs: 1 = list passes inline (programmatic launches
                                       that return at once without a request), 0 = a conditional node */
     long long host_step = 0;       /* steps run so far (mirrors st->step) */
