@@ -372,8 +372,7 @@ def run_ours(args):
         e2e_reps = max(1, min(args.steps, 5))
         t0 = time.perf_counter()
         for _ in range(e2e_reps):
-            hp2, hv2, _ = sim.run_host(hp, hv, args.md_steps)
-            hp[:], hv[:] = hp2, hv2
+            sim.run_host(hp, hv, args.md_steps, inplace=True, raw_records=True)
         e2e_dt = (time.perf_counter() - t0) / e2e_reps
         e2e = {"value": n * args.md_steps / e2e_dt, "unit": UNIT,
                "h2d_bytes_per_step": 2 * 3 * n * 8,

@@ -1387,11 +1387,16 @@ md_status md_get_thermo_history(md_ctx *c, md_thermo *out, int n, int *got)
     MD_CUDA_TRY(c, cudaMemcpy(&h, c->st, sizeof(h), cudaMemcpyDeviceToHost));
     long long avail = std::min<long long>(h.step, c->rec_cap);
     int k = (int)std::min<long long>(avail, n);
-    for (int t = 0; t < k; t++) {
-        long long s = h.step - k + t;
-        MD_CUDA_TRY(c, cudaMemcpy(out + t, c->rec + s % c->rec_cap, sizeof(md_thermo),
-                                  cudaMemcpyDeviceToHost));
+    /* the last k records of the ring: at most two contiguous ranges */
+    int t = 0;
+    while (t < k) {
+        const int r = (int)((h.step - k + t) % c->rec_cap);
+        const int len = std::min(k - t, c->rec_cap - r);
+        MD_CUDA_TRY(c, cudaMemcpyAsync(out + t, c->rec + r, sizeof(md_thermo) * (size_t)len,
+                                       cudaMemcpyDeviceToHost, c->stream));
+        t += len;
     }
+    MD_CUDA_TRY(c, cudaStreamSynchronize(c->stream));
     *got = k;
     return MD_OK;
 }
@@ -1401,16 +1406,38 @@ md_status md_run_host(md_ctx *c, double *pos3, double *vel3, int nsteps, int ene
 {
     if (!c || !pos3 || !vel3 || nsteps < 0) return MD_ERR_ARG;
     if (nsteps > c->rec_cap && records) return MD_ERR_ARG;
-    md_status s = md_set_positions(c, pos3);
-    if (s == MD_OK) s = md_set_velocities(c, vel3);
+    /* The launches of md_set_positions and md_set_velocities (upload, forced
+     * build, forces and thermodynamic state) with one synchronisation; on a
+     * list overflow those two calls run again and grow the list. */
+    md_status s = scatter_from_host(c, 0, pos3);
+    if (s != MD_OK) return s;
+    md_kparams kp = md_make_kparams(c);
+    launch_rebuild(c, kp, true, true);
+    launch_forces(c, kp, true, MD_TERM_ALL);
+    launch_thermo_from_state(c, kp, 1);
+    s = scatter_from_host(c, 1, vel3);
+    if (s != MD_OK) return s;
+    launch_thermo_from_state(c, kp, 0);
+    s = check_overflow_and_sync(c);
+    if (s == MD_ERR_LIST_OVERFLOW) {
+        s = md_set_positions(c, pos3);
+        if (s == MD_OK) s = md_set_velocities(c, vel3);
+    }
     if (s == MD_OK) s = md_step(c, nsteps, energy_every);
     if (s == MD_OK && records) {
         int got = 0;
         s = md_get_thermo_history(c, records, nsteps, &got);
     }
-    if (s == MD_OK) s = md_get_positions(c, pos3);
-    if (s == MD_OK) s = md_get_velocities(c, vel3);
-    return s;
+    if (s != MD_OK) return s;
+    /* positions, then velocities, through the staging buffer in stream order */
+    kp = md_make_kparams(c);
+    const size_t bytes = sizeof(double) * 3 * (size_t)c->n;
+    launch_gather_out(c, kp, 0, c->io_dev);
+    MD_CUDA_TRY(c, cudaMemcpyAsync(pos3, c->io_dev, bytes, cudaMemcpyDeviceToHost, c->stream));
+    launch_gather_out(c, kp, 1, c->io_dev);
+    MD_CUDA_TRY(c, cudaMemcpyAsync(vel3, c->io_dev, bytes, cudaMemcpyDeviceToHost, c->stream));
+    MD_CUDA_TRY(c, cudaStreamSynchronize(c->stream));
+    return MD_OK;
 }
 
 md_status md_write_cfg(md_ctx *c, const char *path)

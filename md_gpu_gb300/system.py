@@ -340,13 +340,27 @@ class MDSystem:
         _check(library().md_last_step_ms(self._ctx, C.byref(ms)), self._ctx)
         return ms.value
 
-    def run_host(self, pos, vel, nsteps, energy_every=0):
-        """End to end from host buffers; returns (pos, vel, records)."""
-        p = np.ascontiguousarray(pos, np.float64).copy()
-        v = np.ascontiguousarray(vel, np.float64).copy()
+    def run_host(self, pos, vel, nsteps, energy_every=0, inplace=False, raw_records=False):
+        """End to end from host buffers; returns (pos, vel, records).
+
+        inplace: pos and vel (float64, C-contiguous, (N, 3)) are read and
+        overwritten by the call itself (pinned buffers then go to the device
+        without a staging copy).  raw_records: the records as a NumPy
+        structured array over the returned buffer instead of dicts."""
+        if inplace:
+            for a in (pos, vel):
+                if not (isinstance(a, np.ndarray) and a.dtype == np.float64 and a.flags.c_contiguous
+                        and a.size == 3 * self.natom):
+                    raise ValueError("inplace run_host needs C-contiguous float64 arrays of N x 3")
+            p, v = pos, vel
+        else:
+            p = np.ascontiguousarray(pos, np.float64).copy()
+            v = np.ascontiguousarray(vel, np.float64).copy()
         rec = (Thermo * max(nsteps, 1))()
         _check(library().md_run_host(self._ctx, p.ctypes.data, v.ctypes.data, nsteps, energy_every,
                                      rec), self._ctx)
+        if raw_records:
+            return p, v, np.ctypeslib.as_array(rec)[:nsteps]
         return p, v, [rec[i].as_dict() for i in range(nsteps)]
 
     # ---- observation ----

@@ -261,6 +261,13 @@ def test_run_host_matches_step():
         assert np.array_equal(p, b.positions())
         assert np.array_equal(v, b.velocities())
         assert [r["temper"] for r in recs] == [h["temper"] for h in b.history(12)]
+    # in place from pinned-style buffers, records as a structured array
+    with gu.system_from_case(case) as c:
+        hp, hv = np.ascontiguousarray(p0), np.ascontiguousarray(v0)
+        out_p, out_v, raw = c.run_host(hp, hv, 12, inplace=True, raw_records=True)
+        assert out_p is hp and out_v is hv
+        assert np.array_equal(hp, p) and np.array_equal(hv, v)
+        assert list(raw["temper"]) == [r["temper"] for r in recs]
 
 
 def test_list_rebuilds_keep_parity():
