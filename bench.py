@@ -217,7 +217,7 @@ def batch_leg(args, flush):
         "value": sum(sizes) * steps / (sum(ms) * 1e-3), "unit": UNIT,
         "natom": int(sum(sizes)), "nrep": len(sizes), "min_natom": int(min(sizes)),
         "max_natom": int(max(sizes)), "md_steps": steps, "ms_per_md_step": sum(ms) / steps,
-        "pair_ms": pair_ms, "pair_threads_per_atom": pt,
+        "pair_ms": pair_ms, "pair_threads_per_atom": pt, "pair_entries_per_lane": info["pair_depth"],
         "batch_rebuild_events": info["builds"] - builds0,
         "replica_rebuilds_per_replica_step": rebuilt / (len(sizes) * steps),
         "temperature_K": {"min": min(t["temper"] for t in th), "mean": float(np.mean([t["temper"] for t in th])),

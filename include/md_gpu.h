@@ -228,12 +228,12 @@ md_status md_get_cell_ranks(md_ctx *ctx, int *rank);
 md_status md_set_tuning(md_ctx *ctx, int pair_tpa, int list_tpa);
 /* List entries each pair-kernel lane loads per batch (memory-level
  * parallelism against registers): 0 = the default for the lane count (8 for
- * 1-4 lanes, 4 for 8, 2 for 16, 1 for 32); single systems also take half the
- * default at 4, 8 and 16 lanes.  md_set_tuning resets it to 0. */
+ * 1-4 lanes, 4 for 8, 2 for 16, 1 for 32); also half the default at 4, 8
+ * and 16 lanes.  md_set_tuning resets it to 0. */
 md_status md_set_pair_depth(md_ctx *ctx, int depth);
-/* Autotuner: times the pair kernel for 2/4/8/16 threads per atom (single
- * systems also at 4/8/16 threads with half the default entries per lane and
- * batch) and the list builders (warp per cell, 4/8/16 threads per atom) on the
+/* Autotuner: times the pair kernel for 2/4/8/16 threads per atom (also at
+ * 4/8/16 threads with half the default entries per lane and batch) and the
+ * list builders (warp per cell, 4/8/16 threads per atom) on the
  * current state and keeps the fastest of each; returns the choice.  It also
  * times the step graphs by running steps: fused or separate pair and
  * integrator kernels (leapfrog systems without bonded terms), and for single

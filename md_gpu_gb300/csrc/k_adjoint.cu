@@ -128,7 +128,7 @@ __global__ void __launch_bounds__(ADJ_THREADS) k_adj_rdf(adj_par ap, const int2 
             dz -= g.L(2) * rint_small(dz * g.Li(2));
             const float rsq = dx * dx + dy * dy + dz * dz;
             if (rsq >= ap.rmaxsq) continue;
-            const float r = sqrtf(rsq);
+            const float r = rsq * rsqrt_approx(rsq);
             int b0, b1;
             rdf_bins(ap, r, b0, b1);
             gauss_walk gw(((float)b0 + 0.5f) * ap.dr - r, ap.dr, ap.inv_2s2, cstep);
@@ -251,14 +251,15 @@ __global__ void __launch_bounds__(ADJ_THREADS) k_adj_back(
         dz -= g.L(2) * rint_small(dz * g.Li(2));
         const float rsq = dx * dx + dy * dy + dz * dz;
         if (rsq > g.rcsq() || rsq == 0.0f) continue;
-        const float r = sqrtf(rsq), ri = 1.0f / r, ri2 = ri * ri;
+        /* the approximations the dynamics use (PTX rsqrt/rcp/ex2.approx) */
+        const float ri = rsqrt_approx(rsq), r = rsq * ri, ri2 = ri * ri;
         const float qq = qi * pj.w;
         float fc, dfc, uc;
         if (KIND == 1) {
-            const float t = 1.0f / (1.0f + A * r);
+            const float t = rcp_approx(1.0f + A * r);
             const float P = (((A5 * t + A4) * t + A3) * t + A2) * t + A1;
             const float dPt = (((5.0f * A5 * t + 4.0f * A4) * t + 3.0f * A3) * t + 2.0f * A2) * t + A1;
-            const float ex = __expf(-alsq * rsq);
+            const float ex = ex2_approx(R.alfasq * rsq);
             const float E = P * t * ex;
             const float dE = -dPt * A * t * t * ex - 2.0f * alsq * r * E;
             const float h = spi * ex + E * ri;

@@ -247,20 +247,22 @@ void pair_dispatch_b(md_ctx *c, const md_kparams &kp)
     const int k = md_grid_index(128 / c->pair_tpa);
     const int2 *tab = c->grid_tab + c->grid_off[k];
     const int nb = c->grid_cnt[k];
-    switch (c->pair_tpa) {
-#define MD_PAIR_B_CASE(T)                                                                        \
-    case T:                                                                                      \
-        k_pair_b<KIND, T, (T >= 32 ? 1 : (T >= 16 ? 2 : (T >= 8 ? 4 : 8))), ENERGY>             \
-            <<<nb, 128, 0, c->stream>>>(kp.cap, kp.pitch, kp.centered, tab, c->reps_dev,         \
-                                        c->ljr_dev, c->pos4,                                     \
-                                        c->type, c->nl, c->nl_n, c->f, c->vir, c->epot);         \
+    switch (c->pair_tpa * 100 + md_pair_depth(c)) {
+#define MD_PAIR_B_CASE(T, BB)                                                                    \
+    case T * 100 + BB:                                                                           \
+        k_pair_b<KIND, T, BB, ENERGY><<<nb, 128, 0, c->stream>>>(                                \
+            kp.cap, kp.pitch, kp.centered, tab, c->reps_dev, c->ljr_dev, c->pos4, c->type, c->nl, \
+            c->nl_n, c->f, c->vir, c->epot);                                                     \
         break;
-        MD_PAIR_B_CASE(1)
-        MD_PAIR_B_CASE(2)
-        MD_PAIR_B_CASE(4)
-        MD_PAIR_B_CASE(8)
-        MD_PAIR_B_CASE(16)
-        MD_PAIR_B_CASE(32)
+        MD_PAIR_B_CASE(1, 8)
+        MD_PAIR_B_CASE(2, 8)
+        MD_PAIR_B_CASE(4, 4)
+        MD_PAIR_B_CASE(4, 8)
+        MD_PAIR_B_CASE(8, 2)
+        MD_PAIR_B_CASE(8, 4)
+        MD_PAIR_B_CASE(16, 1)
+        MD_PAIR_B_CASE(16, 2)
+        MD_PAIR_B_CASE(32, 1)
 #undef MD_PAIR_B_CASE
     default:
         break;

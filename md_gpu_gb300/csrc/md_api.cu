@@ -1551,12 +1551,10 @@ md_status md_autotune(md_ctx *c, int *pair_tpa, int *list_tpa)
     c->fuse_step = 0;
     /* best of three timings of 20 launches per candidate (lanes per atom,
      * entries per lane and batch): robust to a slow first launch and to other
-     * work on the device.  Batches and the fused kernel use the default depth
-     * (depth 0), so they time each lane count once. */
+     * work on the device. */
     const int combos[][2] = {{2, 0}, {4, 0}, {4, 4}, {8, 0}, {8, 2}, {16, 0}, {16, 1}};
     int bd = 0;
     for (const auto &cb : combos) {
-        if (c->batch && cb[1] != 0) continue;
         c->pair_tpa = cb[0];
         c->pair_depth = cb[1];
         float ms = 0.0f, m2 = 1e30f;
@@ -1671,8 +1669,7 @@ md_status md_set_pair_depth(md_ctx *c, int depth)
     const int t = c->pair_tpa;
     const int def = t >= 32 ? 1 : (t >= 16 ? 2 : (t >= 8 ? 4 : 8));
     if (depth == def) depth = 0;
-    const bool ok = depth == 0 || (!c->batch && ((t == 4 && depth == 4) || (t == 8 && depth == 2) ||
-                                                 (t == 16 && depth == 1)));
+    const bool ok = depth == 0 || (t == 4 && depth == 4) || (t == 8 && depth == 2) || (t == 16 && depth == 1);
     if (!ok) return fail(c, MD_ERR_ARG, "md_set_pair_depth: depth not built for this lane count");
     c->pair_depth = depth;
     if (c->gexec) {
