@@ -42,14 +42,53 @@ namespace {
 constexpr int ADJ_TPA = 8;            /* lanes per atom in the adjoint pair kernels */
 constexpr int ADJ_NA = MD_ADJ_ATOMS;  /* atoms per block (replica-aligned grid) */
 constexpr int ADJ_THREADS = ADJ_NA * ADJ_TPA;
-constexpr int ADJ_MAXBINS = 512;
 constexpr double ADJ_HFIX = 1048576.0; /* 2^20: fixed point of the RDF kernel values */
 
 struct adj_par {
     int cap, pitch, nbins, rdf_a, rdf_b, with_w;
     float dr, sigma, inv_2s2, kn, rmaxsq, rdf_fac;
     float wpe_k;   /* w_pe / (K + 1): the PE weight of one frame, per atom over N */
+    int tab_n;     /* points of the RDF-gradient table per replica */
+    float tab_h, tab_hi;   /* its spacing (dr / 8) and inverse */
 };
+
+/* The RDF term of a pair's adjoint force at distance x:
+ *   C(x) = sum_b s_b (x_b - x) exp(-(x_b - x)^2 / (2 sigma^2)),
+ * over the bins whose centre x_b lies within 5 sigma of x (rdf_bins),
+ * s_b = ebn[b].  It is fixed for the whole backward pass, so it is
+ * tabulated once per replica, with its derivative
+ *   C'(x) = sum_b s_b exp(-y^2 / (2 sigma^2)) (y^2 / sigma^2 - 1), y = x_b - x,
+ * at spacing h = dr / 8, and read back by cubic Hermite interpolation
+ * (error ~ (h / sigma)^4 / 384 of the term). */
+__global__ void k_adj_rdf_table(adj_par ap, int nrep, const float *__restrict__ ebn, float2 *tab)
+{
+    const int k = blockIdx.x * blockDim.x + threadIdx.x;
+    if (k >= nrep * ap.tab_n) return;
+    const int r = k / ap.tab_n, q = k - r * ap.tab_n;
+    const double x = (double)q * ap.tab_h, dr = ap.dr, s = ap.sigma;
+    const double reach = 5.0 * s, kk = 0.5 / (s * s);
+    const int b0 = max((int)ceil((x - reach) / dr - 0.5), 0);
+    const int b1 = min((int)floor((x + reach) / dr - 0.5), ap.nbins - 1);
+    double c = 0.0, dc = 0.0;
+    for (int b = b0; b <= b1; b++) {
+        const double y = (b + 0.5) * dr - x, gq = exp(-y * y * kk), sb = ebn[(size_t)r * ap.nbins + b];
+        c += sb * y * gq;
+        dc += sb * gq * (2.0 * kk * y * y - 1.0);
+    }
+    tab[k] = make_float2((float)c, (float)dc);
+}
+
+/* C(r) from a replica's table (0 <= r < tab_h (tab_n - 1)). */
+__device__ __forceinline__ float rdf_coef(const adj_par &ap, const float2 *__restrict__ tab, float r)
+{
+    const float u = r * ap.tab_hi;
+    const int k = min((int)u, ap.tab_n - 2);
+    const float t = u - (float)k, t2 = t * t, t3 = t2 * t;
+    const float2 a = __ldg(tab + k), b = __ldg(tab + k + 1);
+    const float h00 = 2.0f * t3 - 3.0f * t2 + 1.0f, h10 = t3 - 2.0f * t2 + t;
+    const float h01 = 3.0f * t2 - 2.0f * t3, h11 = t3 - t2;
+    return h00 * a.x + h01 * b.x + ap.tab_h * (h10 * a.y + h11 * b.y);
+}
 
 /* A row's per-neighbour-type parameter slots: lj1 terms, lj2 terms, then
  * the charge scale. */
@@ -193,21 +232,19 @@ __global__ void k_adj_acc(int n, int pitch, const int *__restrict__ perm, const 
 template <int KIND, int NT>
 __global__ void __launch_bounds__(ADJ_THREADS) k_adj_back(
     adj_par ap, const int2 *__restrict__ tab, const md_rep *__restrict__ reps,
-    const float2 *__restrict__ ljr, const float *__restrict__ ebn, const float4 *__restrict__ pos4,
+    const float2 *__restrict__ ljr, const float2 *__restrict__ rtab, const float4 *__restrict__ pos4,
     const int *__restrict__ type, const unsigned *__restrict__ nl, const int *__restrict__ nl_n,
     const float4 *__restrict__ w4, double *G, double *part)
 {
     constexpr int NS = 2 * NT + 1;           /* slots of a row */
     constexpr int NB = 2 * NT * NT + 1;      /* slots of a block: (type, slot) */
     __shared__ float2 lj[MD_MAXTYPE * MD_MAXTYPE];
-    __shared__ float sb[ADJ_MAXBINS];
     __shared__ float s_val[ADJ_NA][NS];
     __shared__ int s_type[ADJ_NA];
     const int2 bt = tab[blockIdx.x];
     const md_rep &R = reps[bt.x];
     if (threadIdx.x < MD_MAXTYPE * MD_MAXTYPE)
         lj[threadIdx.x] = ljr[bt.x * MD_MAXTYPE * MD_MAXTYPE + threadIdx.x];
-    for (int k = threadIdx.x; k < ap.nbins; k += blockDim.x) sb[k] = ebn[(size_t)bt.x * ap.nbins + k];
     const geom_reg g = rep_geom(R);
     const float wpe = ap.wpe_k / (float)R.natom;
     const float W = R.wolf, A = R.palfa;
@@ -223,7 +260,7 @@ __global__ void __launch_bounds__(ADJ_THREADS) k_adj_back(
     const float qi = QFAC * pi.w;
     const float4 wi = ap.with_w ? w4[ii] : make_float4(0.f, 0.f, 0.f, 0.f);
     const bool ra = ti == ap.rdf_a, rb = ti == ap.rdf_b;
-    const float cstep = __expf(-2.0f * ap.dr * ap.dr * ap.inv_2s2);
+    const float2 *rt = rtab + (size_t)bt.x * ap.tab_n;
     float gx = 0.f, gy = 0.f, gz = 0.f;
     adj_slots<NT> sl;
 #pragma unroll
@@ -291,16 +328,7 @@ __global__ void __launch_bounds__(ADJ_THREADS) k_adj_back(
         }
         /* RDF pairs (a, b) in either orientation */
         if (((ra && tj == ap.rdf_b) || (rb && tj == ap.rdf_a)) && rsq < ap.rmaxsq) {
-            int b0, b1;
-            rdf_bins(ap, r, b0, b1);
-            const float y0 = ((float)b0 + 0.5f) * ap.dr - r;
-            gauss_walk gw(y0, ap.dr, ap.inv_2s2, cstep);
-            float coef = 0.0f;
-            for (int b = b0; b <= b1; b++) {
-                coef += sb[b] * (y0 + (float)(b - b0) * ap.dr) * gw.g;
-                gw.next();
-            }
-            coef *= ap.rdf_fac * ri;
+            const float coef = rdf_coef(ap, rt, r) * ap.rdf_fac * ri;
             gx += coef * dx;
             gy += coef * dy;
             gz += coef * dz;
@@ -379,23 +407,23 @@ __global__ void k_adj_param(int nrep, int nb_slots, const md_rep *__restrict__ r
 }
 
 template <int KIND, int NT>
-void launch_back_nt(md_ctx *c, const adj_par &ap, const float *ebn, const float4 *w4, double *G,
+void launch_back_nt(md_ctx *c, const adj_par &ap, const float2 *rtab, const float4 *w4, double *G,
                     double *part)
 {
     const int k = md_grid_index(ADJ_NA);
     k_adj_back<KIND, NT><<<c->grid_cnt[k], ADJ_THREADS, 0, c->stream>>>(
-        ap, c->grid_tab + c->grid_off[k], c->reps_dev, c->ljr_dev, ebn, c->pos4, c->type, c->nl,
+        ap, c->grid_tab + c->grid_off[k], c->reps_dev, c->ljr_dev, rtab, c->pos4, c->type, c->nl,
         c->nl_n, w4, G, part);
 }
 
 int adj_nt(int ntype) { return ntype <= 1 ? 1 : (ntype <= 2 ? 2 : (ntype <= 4 ? 4 : 8)); }
 
-void launch_back(md_ctx *c, const adj_par &ap, const float *ebn, const float4 *w4, double *G,
+void launch_back(md_ctx *c, const adj_par &ap, const float2 *rtab, const float4 *w4, double *G,
                  double *part)
 {
     const int nt = adj_nt(c->ntype);
 #define MD_ADJ_NT(K, N) \
-    if (c->lkspace == K && nt == N) { launch_back_nt<K == 0 ? 0 : 1, N>(c, ap, ebn, w4, G, part); return; }
+    if (c->lkspace == K && nt == N) { launch_back_nt<K == 0 ? 0 : 1, N>(c, ap, rtab, w4, G, part); return; }
     MD_ADJ_NT(0, 1) MD_ADJ_NT(0, 2) MD_ADJ_NT(0, 4) MD_ADJ_NT(0, 8)
     MD_ADJ_NT(1, 1) MD_ADJ_NT(1, 2) MD_ADJ_NT(1, 4) MD_ADJ_NT(1, 8)
     MD_ADJ_NT(2, 1) MD_ADJ_NT(2, 2) MD_ADJ_NT(2, 4) MD_ADJ_NT(2, 8)
@@ -411,10 +439,11 @@ struct adj_buffers {
            *acc = nullptr;
     float4 *w4 = nullptr;
     float *ebn = nullptr;
+    float2 *rtab = nullptr;
     unsigned long long *hist = nullptr;
     ~adj_buffers()
     {
-        void *p[] = {ck_x, ck_v, seg, xK, vK, P, U, G, pe_sum, part, acc, w4, ebn, hist};
+        void *p[] = {ck_x, ck_v, seg, xK, vK, P, U, G, pe_sum, part, acc, w4, ebn, rtab, hist};
         for (void *q : p)
             if (q) cudaFree(q);
     }
@@ -468,6 +497,9 @@ extern "C" md_status md_adjoint_run(md_ctx *c, const md_adjoint_cfg *cfg, const 
     MD_CUDA_TRY(c, adj_alloc(&B.acc, (size_t)nrep * NB));
     MD_CUDA_TRY(c, adj_alloc(&B.w4, c->pitch));
     MD_CUDA_TRY(c, adj_alloc(&B.ebn, (size_t)nrep * nb));
+    const float tab_h = (float)(cfg->rdf_dr / 8.0);
+    const int tab_n = (int)(rmax / (double)tab_h) + 3;   /* covers [0, rmax + h] */
+    MD_CUDA_TRY(c, adj_alloc(&B.rtab, (size_t)nrep * tab_n));
     MD_CUDA_TRY(c, adj_alloc(&B.hist, (size_t)nrep * nb));
     cudaStream_t s = c->stream;
     MD_CUDA_TRY(c, cudaMemsetAsync(B.hist, 0, sizeof(unsigned long long) * nrep * nb, s));
@@ -487,6 +519,9 @@ extern "C" md_status md_adjoint_run(md_ctx *c, const md_adjoint_cfg *cfg, const 
     ap.rmaxsq = (float)(rmax * rmax);
     ap.rdf_fac = cfg->rdf_a == cfg->rdf_b ? 2.0f : 1.0f;
     ap.wpe_k = (float)(cfg->w_pe / (K + 1));
+    ap.tab_h = tab_h;
+    ap.tab_hi = 1.0f / tab_h;
+    ap.tab_n = tab_n;
     const int rgrid = (nrep + 255) / 256;
     const int agrid = (n + 255) / 256;
 
@@ -558,6 +593,7 @@ extern "C" md_status md_adjoint_run(md_ctx *c, const md_adjoint_cfg *cfg, const 
 
     /* ---- backward ---- */
     MD_CUDA_TRY(c, cudaMemcpyAsync(B.ebn, ebn.data(), sizeof(float) * ebn.size(), cudaMemcpyHostToDevice, s));
+    k_adj_rdf_table<<<(nrep * ap.tab_n + 255) / 256, 256, 0, s>>>(ap, nrep, B.ebn, B.rtab);
     MD_CUDA_TRY(c, cudaMemsetAsync(B.P, 0, sizeof(double) * 3 * n, s));
     MD_CUDA_TRY(c, cudaMemsetAsync(B.U, 0, sizeof(double) * 3 * n, s));
     MD_CUDA_TRY(c, cudaMemsetAsync(B.acc, 0, sizeof(double) * nrep * NB, s));
@@ -586,7 +622,7 @@ extern "C" md_status md_adjoint_run(md_ctx *c, const md_adjoint_cfg *cfg, const 
             if (m < K)
                 k_adj_w<<<agrid, 256, 0, s>>>(n, (double)c->dt, 1, m >= 1 ? 2.0 : 1.0, c->perm, c->kick,
                                                B.U, B.P, B.w4);
-            launch_back(c, ap, B.ebn, B.w4, B.G, B.part);
+            launch_back(c, ap, B.rtab, B.w4, B.G, B.part);
             k_adj_param<<<(nrep * NB * 32 + 255) / 256, 256, 0, s>>>(nrep, NB, c->reps_dev, B.part, B.acc);
             k_adj_acc<<<agrid, 256, 0, s>>>(n, c->pitch, c->perm, B.G, B.P);
         }
