@@ -129,9 +129,25 @@ __device__ __forceinline__ void rdf_bins(const adj_par &ap, float r, int &b0, in
  * types share the work (an (a, a) pair counts twice, as the ordered sum over
  * i in a, j in b does).  Kernel values in fixed point (2^-20) are summed with
  * integer atomics into per-warp histograms in shared memory, then added into
- * the replica's histogram. */
+ * the replica's histogram.  The lanes of a warp first test their row
+ * entries and queue the distances of the pairs that count (a quarter or
+ * less of the entries) in shared memory; each full queue of 32 is deposited
+ * with every lane busy. */
 constexpr int ADJ_WARPS = ADJ_THREADS / 32;
 constexpr int ADJ_RDF_BINS = 256;   /* per-warp histograms hold up to 256 bins */
+
+__device__ __forceinline__ void rdf_deposit(const adj_par &ap, float r, float wt, float cstep,
+                                            unsigned *h)
+{
+    int b0, b1;
+    rdf_bins(ap, r, b0, b1);
+    gauss_walk gw(((float)b0 + 0.5f) * ap.dr - r, ap.dr, ap.inv_2s2, cstep);
+    for (int b = b0; b <= b1; b++) {
+        /* <= 1.7e7 per pair and bin; a warp's bin stays far below 2^32 per frame */
+        atomicAdd(&h[b], __float2uint_rn(wt * gw.g));
+        gw.next();
+    }
+}
 
 __global__ void __launch_bounds__(ADJ_THREADS) k_adj_rdf(adj_par ap, const int2 *__restrict__ tab,
                                                        const md_rep *__restrict__ reps,
@@ -142,42 +158,61 @@ __global__ void __launch_bounds__(ADJ_THREADS) k_adj_rdf(adj_par ap, const int2 
                                                        unsigned long long *hist)
 {
     __shared__ unsigned s_h[ADJ_WARPS][ADJ_RDF_BINS];
+    __shared__ float s_q[ADJ_WARPS][64];
     for (int k = threadIdx.x; k < ADJ_WARPS * ADJ_RDF_BINS; k += blockDim.x) (&s_h[0][0])[k] = 0u;
     __syncthreads();
     const int2 bt = tab[blockIdx.x];
     const md_rep &R = reps[bt.x];
     const geom_reg g = rep_geom(R);
     const int a = threadIdx.x / ADJ_TPA, lane = threadIdx.x % ADJ_TPA, w = threadIdx.x >> 5;
+    const int wl = threadIdx.x & 31;
+    const unsigned lt = (1u << wl) - 1u;
     const int i = bt.y + a;
     const float cstep = __expf(-2.0f * ap.dr * ap.dr * ap.inv_2s2);
     const int ti = i < R.atom0 + R.natom ? type[i] : -1;
     const int want = ti == ap.rdf_a ? ap.rdf_b : (ti == ap.rdf_b ? ap.rdf_a : -1);
     const float wt = ap.rdf_fac * ap.kn * (float)ADJ_HFIX;
-    if (want >= 0) {
-        const float4 pi = pos4[i];
-        const int cnt = nl_n[i];
-        for (int k = lane; k < cnt; k += ADJ_TPA) {
+    const float4 pi = want >= 0 ? pos4[i] : make_float4(0.f, 0.f, 0.f, 0.f);
+    const int cnt = want >= 0 ? nl_n[i] : 0;
+    int cmax = cnt;   /* the warp's longest row */
+    for (int o = 16; o > 0; o >>= 1) cmax = max(cmax, __shfl_xor_sync(0xffffffffu, cmax, o));
+    int fill = 0;
+    for (int k0 = 0; k0 < cmax; k0 += ADJ_TPA) {
+        const int k = k0 + lane;
+        bool ok = false;
+        float r = 0.0f;
+        if (k < cnt) {
             const unsigned e = nl[(size_t)i * ap.cap + k];
             const int j = (int)(e & MD_INDEX_MASK);
-            if ((int)(e >> MD_TYPE_SHIFT) != want || j <= i) continue;
-            const float4 pj = pos4[j];
-            float dx = pi.x - pj.x, dy = pi.y - pj.y, dz = pi.z - pj.z;
-            dx -= g.L(0) * rint_small(dx * g.Li(0));
-            dy -= g.L(1) * rint_small(dy * g.Li(1));
-            dz -= g.L(2) * rint_small(dz * g.Li(2));
-            const float rsq = dx * dx + dy * dy + dz * dz;
-            if (rsq >= ap.rmaxsq) continue;
-            const float r = rsq * rsqrt_approx(rsq);
-            int b0, b1;
-            rdf_bins(ap, r, b0, b1);
-            gauss_walk gw(((float)b0 + 0.5f) * ap.dr - r, ap.dr, ap.inv_2s2, cstep);
-            for (int b = b0; b <= b1; b++) {
-                /* <= 1.7e7 per pair and bin; a warp's bin stays far below 2^32 per frame */
-                atomicAdd(&s_h[w][b], __float2uint_rn(wt * gw.g));
-                gw.next();
+            if ((int)(e >> MD_TYPE_SHIFT) == want && j > i) {
+                const float4 pj = pos4[j];
+                float dx = pi.x - pj.x, dy = pi.y - pj.y, dz = pi.z - pj.z;
+                dx -= g.L(0) * rint_small(dx * g.Li(0));
+                dy -= g.L(1) * rint_small(dy * g.Li(1));
+                dz -= g.L(2) * rint_small(dz * g.Li(2));
+                const float rsq = dx * dx + dy * dy + dz * dz;
+                if (rsq < ap.rmaxsq) {
+                    ok = true;
+                    r = rsq * rsqrt_approx(rsq);
+                }
             }
         }
+        const unsigned bal = __ballot_sync(0xffffffffu, ok);
+        if (ok) s_q[w][fill + __popc(bal & lt)] = r;
+        fill += __popc(bal);
+        __syncwarp();
+        if (fill >= 32) {
+            rdf_deposit(ap, s_q[w][wl], wt, cstep, s_h[w]);
+            __syncwarp();
+            const bool mv = wl < fill - 32;
+            const float t = mv ? s_q[w][32 + wl] : 0.0f;
+            __syncwarp();
+            if (mv) s_q[w][wl] = t;
+            fill -= 32;
+            __syncwarp();
+        }
     }
+    if (wl < fill) rdf_deposit(ap, s_q[w][wl], wt, cstep, s_h[w]);
     __syncthreads();
     for (int k = threadIdx.x; k < ap.nbins; k += blockDim.x) {
         unsigned long long t = 0ull;
