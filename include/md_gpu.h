@@ -238,8 +238,9 @@ md_status md_set_pair_depth(md_ctx *ctx, int depth);
  * times the step graphs by running steps: fused or separate pair and
  * integrator kernels (leapfrog systems without bonded terms), and for single
  * systems the rebuild inline or behind a conditional node
- * (md_set_graph_rebuild).  The system advances 128 steps per combination
- * tried (up to 4; batches have one and do not advance). */
+ * (md_set_graph_rebuild), each for the three fastest pair settings.  The
+ * system advances 128 steps per combination tried (up to 12; batches have
+ * one and do not advance). */
 md_status md_autotune(md_ctx *ctx, int *pair_tpa, int *list_tpa);
 /* Per-type exclusions (no counterpart in the reference, which excludes only
  * 1-2 bonded pairs): bit b of mask[a] excludes every pair of types a and b

@@ -19,16 +19,18 @@
 
 namespace {
 
+constexpr int FUSED_THREADS = 128;   /* threads per block */
+
 template <int KIND, int TPA, int B>
-__global__ void __launch_bounds__(128) k_pair_leapfrog(
+__global__ void __launch_bounds__(FUSED_THREADS) k_pair_leapfrog(
     md_kparams kp, pair_consts pc, thermo_par tp, step_io io, const float4 *__restrict__ pos4,
     float4 *__restrict__ pos4_next, const int *__restrict__ type, const unsigned *__restrict__ nl,
     const int *__restrict__ nl_n, const float2 *__restrict__ ljtab, long long *f, float *vir,
     double *x, double *v, const double *__restrict__ mass, const double *__restrict__ kick)
 {
-    constexpr int NA = 128 / TPA;   /* atoms per block */
+    constexpr int NA = FUSED_THREADS / TPA;   /* atoms per block */
     __shared__ float2 lj[MD_MAXTYPE * MD_MAXTYPE];
-    __shared__ long long sh[12];   /* 3 integers per warp */
+    __shared__ long long sh[3 * FUSED_THREADS / 32];   /* 3 integers per warp */
     __shared__ long long s_f[NA][3];
     __shared__ double s_x0[3][NA], s_v0[3][NA], s_kick[NA], s_mass[NA];
     __shared__ float4 s_old[NA];
@@ -55,7 +57,9 @@ __global__ void __launch_bounds__(128) k_pair_leapfrog(
     int gt = blockIdx.x * blockDim.x + threadIdx.x;
     int i = gt / TPA, lane = gt % TPA;
     bool active = i < kp.n;
-    pair_total t = pair_sum<KIND, TPA, B, false>(geom_kp{kp, pc}, kp.cap, active ? i : 0, active, lane, pos4, type,
+    /* one entry at a time (pair_term): the packed form measured slower in
+     * this kernel (85 against 82 us per step on 64000 ions) */
+    pair_total t = pair_sum<KIND, TPA, B, false, false>(geom_kp{kp, pc}, kp.cap, active ? i : 0, active, lane, pos4, type,
                                                  nl, nl_n, lj);
     if (lane == 0) {
         int a = threadIdx.x / TPA;
@@ -111,12 +115,12 @@ void fused_dispatch(md_ctx *c, const md_kparams &kp, const pair_consts &pc, cons
                     const step_io &io)
 {
     long long threads = (long long)kp.n * c->pair_tpa;
-    int nb = (int)((threads + 127) / 128);
+    int nb = (int)((threads + FUSED_THREADS - 1) / FUSED_THREADS);
     const float2 *lj = (const float2 *)c->lj_dev;
     switch (c->pair_tpa * 100 + md_pair_depth(c)) {
 #define MD_FUSED_CASE(T, BB)                                                                     \
     case T * 100 + BB:                                                                           \
-        k_pair_leapfrog<KIND, T, BB><<<nb, 128, 0, c->stream>>>(                                 \
+        k_pair_leapfrog<KIND, T, BB><<<nb, FUSED_THREADS, 0, c->stream>>>(                                 \
             kp, pc, tp, io, c->pos4, c->pos4_alt, c->type, c->nl, c->nl_n, lj, c->f, c->vir,     \
             c->x, c->v, c->mass, c->kick);                                                       \
         break;

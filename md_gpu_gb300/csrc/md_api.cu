@@ -1553,10 +1553,10 @@ md_status md_autotune(md_ctx *c, int *pair_tpa, int *list_tpa)
      * entries per lane and batch): robust to a slow first launch and to other
      * work on the device. */
     const int combos[][2] = {{2, 0}, {4, 0}, {4, 4}, {8, 0}, {8, 2}, {16, 0}, {16, 1}};
-    int bd = 0;
-    for (const auto &cb : combos) {
-        c->pair_tpa = cb[0];
-        c->pair_depth = cb[1];
+    std::vector<std::pair<float, int>> ranked;   /* (ms, combo) */
+    for (int q = 0; q < (int)(sizeof(combos) / sizeof(combos[0])); q++) {
+        c->pair_tpa = combos[q][0];
+        c->pair_depth = combos[q][1];
         float ms = 0.0f, m2 = 1e30f;
         md_status s = md_time_pair(c, 5, &ms);
         for (int rep = 0; rep < 3 && s == MD_OK; rep++) {
@@ -1564,15 +1564,19 @@ md_status md_autotune(md_ctx *c, int *pair_tpa, int *list_tpa)
             m2 = std::min(m2, ms);
         }
         if (s != MD_OK) return s;
-        if (m2 < best) { best = m2; bp = cb[0]; bd = c->pair_depth; }
+        ranked.push_back({m2, q});
     }
-    c->pair_depth = bd;
-    c->pair_tpa = bp;
+    std::sort(ranked.begin(), ranked.end());
+    int bq = ranked[0].second;
+    c->pair_tpa = combos[bq][0];
+    c->pair_depth = combos[bq][1];
     /* the step graph: separate or (leapfrog without bonded terms) fused pair
      * and integrator kernels, the rebuild behind a conditional node or inline
-     * (single systems); each combination timed as it runs, 96 steps after 32
-     * of warm-up, less the list builds that fell in the window at the
-     * measured cost of one (the system advances 128 steps per combination) */
+     * (single systems), for the three fastest pair settings (the fused
+     * kernel's own ranking may differ); each combination timed as it runs,
+     * 96 steps after 32 of warm-up, less the list builds that fell in the
+     * window at the measured cost of one (the system advances 128 steps per
+     * combination) */
     int bi = 0;
     c->fuse_step = 1;
     const int nf = md_can_fuse(c) ? 2 : 1, ni = c->batch ? 1 : 2;
@@ -1581,8 +1585,12 @@ md_status md_autotune(md_ctx *c, int *pair_tpa, int *list_tpa)
         md_status s = md_time_rebuild(c, 3, &t_rb);
         if (s != MD_OK) return s;
         float tbest = 1e30f;
+        for (int cand = 0; cand < std::min(3, (int)ranked.size()); cand++)
         for (int fz = 0; fz < nf; fz++)
             for (int inl = 0; inl < ni; inl++) {
+                const int q = ranked[cand].second;
+                c->pair_tpa = combos[q][0];
+                c->pair_depth = combos[q][1];
                 c->fuse_step = fz;
                 c->rebuild_inline = inl;
                 if (c->gexec) {
@@ -1598,9 +1606,12 @@ md_status md_autotune(md_ctx *c, int *pair_tpa, int *list_tpa)
                 if (s == MD_OK) s = read_builds(c, &b1);
                 if (s != MD_OK) return s;
                 const float t = ms - (float)(b1 - b0) * t_rb;
-                if (t < tbest) { tbest = t; bf = fz; bi = inl; }
+                if (t < tbest) { tbest = t; bf = fz; bi = inl; bq = q; }
             }
     }
+    bp = combos[bq][0];
+    c->pair_tpa = bp;
+    c->pair_depth = combos[bq][1];
     c->fuse_step = bf;
     c->rebuild_inline = bi;
     best = 1e30f;

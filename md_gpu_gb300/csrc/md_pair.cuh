@@ -166,6 +166,124 @@ __device__ __forceinline__ void pair_term(const G &g, float4 pi, float qi, float
     }
 }
 
+/* Two FP32 lanes in one 64-bit register pair: the sm_100+ packed
+ * instructions add/sub/mul/fma.rn.f32x2 compute two entries' operations in
+ * one issue slot, each half rounded as the scalar instruction would. */
+typedef unsigned long long f32x2;
+template <bool PACKED>
+struct v2;
+template <>
+struct v2<true> {
+    f32x2 d;
+    __device__ __forceinline__ static v2 make(float a, float b)
+    {
+        v2 r;
+        asm("mov.b64 %0, {%1, %2};" : "=l"(r.d) : "f"(a), "f"(b));
+        return r;
+    }
+    __device__ __forceinline__ void get(float &a, float &b) const
+    {
+        asm("mov.b64 {%0, %1}, %2;" : "=f"(a), "=f"(b) : "l"(d));
+    }
+    __device__ __forceinline__ friend v2 operator+(v2 a, v2 b)
+    {
+        v2 r;
+        asm("add.rn.f32x2 %0, %1, %2;" : "=l"(r.d) : "l"(a.d), "l"(b.d));
+        return r;
+    }
+    __device__ __forceinline__ friend v2 operator-(v2 a, v2 b)
+    {
+        v2 r;
+        asm("sub.rn.f32x2 %0, %1, %2;" : "=l"(r.d) : "l"(a.d), "l"(b.d));
+        return r;
+    }
+    __device__ __forceinline__ friend v2 operator*(v2 a, v2 b)
+    {
+        v2 r;
+        asm("mul.rn.f32x2 %0, %1, %2;" : "=l"(r.d) : "l"(a.d), "l"(b.d));
+        return r;
+    }
+    __device__ __forceinline__ static v2 fma(v2 a, v2 b, v2 c)
+    {
+        v2 r;
+        asm("fma.rn.f32x2 %0, %1, %2, %3;" : "=l"(r.d) : "l"(a.d), "l"(b.d), "l"(c.d));
+        return r;
+    }
+};
+
+/* Lane sums of two entries at a time (even and odd entries of a batch). */
+template <bool PACKED>
+struct pair_acc2 {
+    v2<PACKED> fx, fy, fz, fw;
+};
+
+/* Two pairs (i, j0) and (i, j1) at once: the operations whose operands all
+ * vary per entry run on v2; those with a per-atom or per-system constant run
+ * as scalar IEEE operations with the constant (no register pair to hold it).
+ * The same formulas as pair_term, with every rounding step fixed. */
+template <int KIND, bool WRAP, bool PACKED, class G>
+__device__ __forceinline__ void pair_term2(const G &g, v2<PACKED> PX, v2<PACKED> PY, v2<PACKED> PZ,
+                                           float qi, float4 p0, float4 p1, float2 l0, float2 l1,
+                                           pair_acc2<PACKED> &a)
+{
+    typedef v2<PACKED> V;
+    V dx = PX - V::make(p0.x, p1.x), dy = PY - V::make(p0.y, p1.y), dz = PZ - V::make(p0.z, p1.z);
+    if (WRAP) {
+        float x0, x1, y0, y1, z0, z1;
+        dx.get(x0, x1);
+        dy.get(y0, y1);
+        dz.get(z0, z1);
+        x0 = __fmaf_rn(-g.L(0), rint_small(__fmul_rn(x0, g.Li(0))), x0);
+        x1 = __fmaf_rn(-g.L(0), rint_small(__fmul_rn(x1, g.Li(0))), x1);
+        y0 = __fmaf_rn(-g.L(1), rint_small(__fmul_rn(y0, g.Li(1))), y0);
+        y1 = __fmaf_rn(-g.L(1), rint_small(__fmul_rn(y1, g.Li(1))), y1);
+        z0 = __fmaf_rn(-g.L(2), rint_small(__fmul_rn(z0, g.Li(2))), z0);
+        z1 = __fmaf_rn(-g.L(2), rint_small(__fmul_rn(z1, g.Li(2))), z1);
+        dx = V::make(x0, x1);
+        dy = V::make(y0, y1);
+        dz = V::make(z0, z1);
+    }
+    const V rsq = V::fma(dz, dz, V::fma(dy, dy, dx * dx));
+    float s0, s1;
+    rsq.get(s0, s1);
+    const V ri = V::make(rsqrt_approx(s0), rsqrt_approx(s1));
+    const V ri2 = ri * ri;
+    const V qq = V::make(__fmul_rn(qi, p0.w), __fmul_rn(qi, p1.w));
+    V ff;
+    if (KIND == 1) {
+        float r0, r1;
+        (rsq * ri).get(r0, r1);
+        const float t0 = rcp_approx(__fmaf_rn(g.palfa(), r0, 1.0f));
+        const float t1 = rcp_approx(__fmaf_rn(g.palfa(), r1, 1.0f));
+        const float e0 = ex2_approx(__fmul_rn(g.alfasq(), s0)), e1 = ex2_approx(__fmul_rn(g.alfasq(), s1));
+        const float q0 = __fmul_rn(__fmaf_rn(__fmaf_rn(__fmaf_rn(__fmaf_rn(A5, t0, A4), t0, A3), t0, A2), t0, A1), t0);
+        const float q1 = __fmul_rn(__fmaf_rn(__fmaf_rn(__fmaf_rn(__fmaf_rn(A5, t1, A4), t1, A3), t1, A2), t1, A1), t1);
+        const V h = V::make(__fmaf_rn(g.spiialfa(), r0, q0), __fmaf_rn(g.spiialfa(), r1, q1));
+        float h0, h1;
+        (h * V::make(e0, e1) * ri).get(h0, h1);
+        ff = V::make(__fsub_rn(h0, g.wolf()), __fsub_rn(h1, g.wolf())) * qq;
+    } else {
+        float a0, a1;
+        ri.get(a0, a1);
+        ff = qq * V::make(__fmaf_rn(-g.reacf(), s0, a0), __fmaf_rn(-g.reacf(), s1, a1));
+    }
+    const V ri6 = ri2 * ri2 * ri2;
+    float m0, m1;
+    ri6.get(m0, m1);
+    const V lj = V::make(__fmaf_rn(l0.x, m0, -l0.y), __fmaf_rn(l1.x, m1, -l1.y)) * ri6 * ri2;
+    ff = V::fma(ff, ri2, lj);
+    /* list padding entries point at the atom itself: r = 0 is skipped */
+    float f0, f1;
+    ff.get(f0, f1);
+    f0 = (s0 <= g.rcsq() && s0 > 0.0f) ? f0 : 0.0f;
+    f1 = (s1 <= g.rcsq() && s1 > 0.0f) ? f1 : 0.0f;
+    ff = V::make(f0, f1);
+    a.fx = V::fma(ff, dx, a.fx);
+    a.fy = V::fma(ff, dy, a.fy);
+    a.fz = V::fma(ff, dz, a.fz);
+    a.fw = V::fma(ff, rsq, a.fw);
+}
+
 struct pair_total {
     long long fx, fy, fz;   /* int64 fixed point, valid in lane 0 of the atom's group */
     float fw, fe;
@@ -189,7 +307,7 @@ __device__ __forceinline__ bool interior(const G &g, float4 pi)
  * t is computed, the positions of batch t+1 and the list entries of batch
  * t+2 are in flight.  ljrow may point into shared memory (a batch's
  * per-replica table): plain loads there, not the read-only global path. */
-template <int KIND, int TPA, int B, bool ENERGY, bool WRAP, class G>
+template <int KIND, int TPA, int B, bool ENERGY, bool WRAP, bool PACK, class G>
 __device__ __forceinline__ void pair_loop(const G &g, float4 pi, float qi, int nb,
                                           const unsigned *__restrict__ lp,
                                           const float4 *__restrict__ pos4, const float2 *ljrow,
@@ -197,6 +315,10 @@ __device__ __forceinline__ void pair_loop(const G &g, float4 pi, float qi, int n
 {
     unsigned e0[B], e1[B];
     float4 p0[B];
+    typedef v2<true> V;   /* used when PACK */
+    const V PX = V::make(pi.x, pi.x), PY = V::make(pi.y, pi.y), PZ = V::make(pi.z, pi.z);
+    const V zero = V::make(0.0f, 0.0f);
+    pair_acc2<true> acc2 = {zero, zero, zero, zero};
 #pragma unroll
     for (int b = 0; b < B; b++) e0[b] = __ldg(lp + b * TPA);
 #pragma unroll
@@ -217,9 +339,16 @@ __device__ __forceinline__ void pair_loop(const G &g, float4 pi, float qi, int n
 #pragma unroll
             for (int b = 0; b < B; b++) e2[b] = __ldg(lp + ((t + 2) * B + b) * TPA);
         }
+        if (PACK && !ENERGY && B % 2 == 0) {
 #pragma unroll
-        for (int b = 0; b < B; b++)
-            pair_term<KIND, ENERGY, WRAP>(g, pi, qi, p0[b], ljrow[e0[b] >> MD_TYPE_SHIFT], true, acc);
+            for (int b = 0; b < B; b += 2)
+                pair_term2<KIND, WRAP, true>(g, PX, PY, PZ, qi, p0[b], p0[b + 1], ljrow[e0[b] >> MD_TYPE_SHIFT],
+                                             ljrow[e0[b + 1] >> MD_TYPE_SHIFT], acc2);
+        } else {
+#pragma unroll
+            for (int b = 0; b < B; b++)
+                pair_term<KIND, ENERGY, WRAP>(g, pi, qi, p0[b], ljrow[e0[b] >> MD_TYPE_SHIFT], true, acc);
+        }
 #pragma unroll
         for (int b = 0; b < B; b++) {
             e0[b] = e1[b];
@@ -227,16 +356,30 @@ __device__ __forceinline__ void pair_loop(const G &g, float4 pi, float qi, int n
             e1[b] = e2[b];
         }
     }
+    if (PACK && !ENERGY && B % 2 == 0) {
+        float a0, a1;
+        acc2.fx.get(a0, a1);
+        acc.fx = __fadd_rn(a0, a1);
+        acc2.fy.get(a0, a1);
+        acc.fy = __fadd_rn(a0, a1);
+        acc2.fz.get(a0, a1);
+        acc.fz = __fadd_rn(a0, a1);
+        acc2.fw.get(a0, a1);
+        acc.fw = __fadd_rn(a0, a1);
+    }
 }
 
 /* Pair forces of atom ii from its list: TPA lanes per atom, lane l takes the
  * entries l, l+TPA, ... in batches of B (TPA*B divides 32, the padding
  * quantum of the list rows, so no entry needs a bounds test).  A warp whose
- * atoms are all interior() skips the minimum-image shifts.  Each lane sums in
+ * atoms are all interior() skips the minimum-image shifts.  With PACK,
+ * without energies and with even B, entries go two at a time through
+ * pair_term2 as packed f32x2 instructions (each lane keeping even- and
+ * odd-entry sums); otherwise one at a time through pair_term.  Each lane sums in
  * FP32 and converts its sum to int64 once; lane sums are combined with
  * integer shuffles (exact), so the result depends only on TPA.  Every lane of
  * the warp must call this (the shuffles use the full mask). */
-template <int KIND, int TPA, int B, bool ENERGY, class G>
+template <int KIND, int TPA, int B, bool ENERGY, bool PACK = true, class G>
 __device__ __forceinline__ pair_total pair_sum(const G &g, int cap, int ii, bool active, int lane,
                                                const float4 *__restrict__ pos4,
                                                const int *__restrict__ type,
@@ -254,9 +397,9 @@ __device__ __forceinline__ pair_total pair_sum(const G &g, int cap, int ii, bool
     const bool inner = g.centered() && __all_sync(0xffffffffu, !active || interior(g, pi));
     if (nb > 0) {
         if (inner)
-            pair_loop<KIND, TPA, B, ENERGY, false>(g, pi, qi, nb, lp, pos4, ljrow, acc);
+            pair_loop<KIND, TPA, B, ENERGY, false, PACK>(g, pi, qi, nb, lp, pos4, ljrow, acc);
         else
-            pair_loop<KIND, TPA, B, ENERGY, true>(g, pi, qi, nb, lp, pos4, ljrow, acc);
+            pair_loop<KIND, TPA, B, ENERGY, true, PACK>(g, pi, qi, nb, lp, pos4, ljrow, acc);
     }
     pair_total r;
     r.fx = __float2ll_rn(acc.fx * 4294967296.0f);
