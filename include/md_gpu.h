@@ -183,6 +183,18 @@ md_status md_compute_forces(md_ctx *ctx, int terms, int energy);
  * energies on steps that are multiples of it (the reference's timprn).
  * Steps run as a captured CUDA graph; no host synchronisation inside. */
 md_status md_step(md_ctx *ctx, int nsteps, int energy_every);
+/* The integrate phase of one step alone, with the forces of the last
+ * md_compute_forces (for callers that drive the phases themselves, as the
+ * reference's loop does).  md_integrate = integrate() (integrator.cu:131-173:
+ * leapfrog, Berendsen when the ensemble is NVT); energy != 0 puts the
+ * energies of that force evaluation in the step's record.  md_integrate_pre /
+ * md_integrate_cor = integrate_pre() / integrate_cor() (integrator.h:53-54):
+ * the two halves of velocity Verlet around the force evaluation (standard VV,
+ * and Nose-Hoover for NVT); the first md_integrate_pre turns a leapfrog
+ * context into a velocity-Verlet one.  Each synchronises the stream. */
+md_status md_integrate(md_ctx *ctx, int energy);
+md_status md_integrate_pre(md_ctx *ctx);
+md_status md_integrate_cor(md_ctx *ctx, int energy);
 /* Record of the most recent step (synchronises the stream). */
 md_status md_get_thermo(md_ctx *ctx, md_thermo *out);
 /* The last min(n, nsteps run) records, oldest first; returns the count in *got. */

@@ -11,12 +11,14 @@ CSRC = os.path.join(HERE, "csrc")
 BUILD = os.path.join(HERE, "_build")
 LIB = os.path.join(BUILD, "libmdgpu_gb300.so")
 SOURCES = ["md_api.cu", "k_cells.cu", "k_forces.cu", "k_integrate.cu", "k_probe.cu", "k_noalloc.cu", "k_fused.cu",
-           "k_batch.cu", "k_adjoint.cu"]
+           "k_batch.cu", "k_adjoint.cu", "md_compat.cu"]
 HEADERS = ["md_internal.h", "md_device.cuh", "md_pair.cuh", "md_thermo.cuh",
-           os.path.join("..", "..", "include", "md_gpu.h")]
+           os.path.join("..", "..", "include", "md_gpu.h"), os.path.join("..", "..", "include", "md_gpu_compat.h")]
 NVCC = os.environ.get("NVCC", "/usr/local/cuda/bin/nvcc")
+# host code: no FMA contraction, so x86-64 (no FMA in its baseline) and
+# aarch64 (FMA in its baseline) compute the same host-side constants
 FLAGS = ["-std=c++17", "-O3", "-gencode", "arch=compute_103a,code=sm_103a", "-lineinfo",
-         "-Xcompiler", "-fPIC", "-Xcompiler", "-Wall"]
+         "-Xcompiler", "-fPIC", "-Xcompiler", "-Wall", "-Xcompiler", "-ffp-contract=off"]
 
 
 def _stale(obj, src):

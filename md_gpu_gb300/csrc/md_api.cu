@@ -1310,6 +1310,45 @@ md_status md_compute_forces(md_ctx *c, int terms, int energy)
     return check_overflow_and_sync(c);
 }
 
+md_status md_integrate(md_ctx *c, int energy)
+{
+    if (!c) return MD_ERR_ARG;
+    if (c->batch || c->integrator != MD_LEAPFROG)
+        return fail(c, MD_ERR_UNSUPPORTED, "md_integrate: leapfrog single systems (velocity Verlet: "
+                                           "md_integrate_pre / md_integrate_cor)");
+    md_kparams kp = md_make_kparams(c);
+    launch_leapfrog(c, kp, energy != 0, 0, 0);
+    c->host_step++;
+    return check_overflow_and_sync(c);
+}
+
+md_status md_integrate_pre(md_ctx *c)
+{
+    if (!c) return MD_ERR_ARG;
+    if (c->batch) return fail(c, MD_ERR_UNSUPPORTED, "md_integrate_pre: single systems");
+    if (c->integrator == MD_LEAPFROG) {   /* the caller runs velocity Verlet from now on */
+        c->integrator = c->enstype == 1 ? MD_NH : MD_VV;
+        if (c->gexec) {
+            cudaGraphExecDestroy(c->gexec);
+            c->gexec = nullptr;
+        }
+    }
+    md_kparams kp = md_make_kparams(c);
+    launch_vv_first(c, kp, 0, 0);
+    return check_overflow_and_sync(c);
+}
+
+md_status md_integrate_cor(md_ctx *c, int energy)
+{
+    if (!c) return MD_ERR_ARG;
+    if (c->batch || c->integrator == MD_LEAPFROG)
+        return fail(c, MD_ERR_UNSUPPORTED, "md_integrate_cor: after md_integrate_pre (single systems)");
+    md_kparams kp = md_make_kparams(c);
+    launch_vv_second(c, kp, energy != 0);
+    c->host_step++;
+    return check_overflow_and_sync(c);
+}
+
 md_status md_step(md_ctx *c, int nsteps, int energy_every)
 {
     if (!c || nsteps < 0 || energy_every < 0) return MD_ERR_ARG;
