@@ -34,3 +34,21 @@ def test_reference_loop_links(lib_path):
     with tempfile.TemporaryDirectory() as td:
         exe = cu.build_driver(lib_path, td)
         assert os.path.exists(exe)
+
+
+REF_SRC = "/root/reference/src"
+
+
+@pytest.mark.skipif(not os.path.isdir(REF_SRC), reason="reference sources not present")
+def test_reference_main_program_links(lib_path):
+    """The reference's own athom.cu, runGPU.cu, simulation.cu and prints.cu,
+    unmodified, link against the library (tests/compat/Makefile)."""
+    if not os.path.exists(cu.NVCC):
+        pytest.skip("nvcc not available")
+    here = os.path.join(cu.ROOT, "tests", "compat")
+    out = os.path.join(cu.ROOT, "oracle", "_ref", "athom_md")
+    if os.path.exists(out):
+        os.unlink(out)
+    r = subprocess.run(["make", "-s", "-C", here, "ref-main", f"NVCC={cu.NVCC}"], capture_output=True, text=True)
+    assert r.returncode == 0, r.stderr[-2000:]
+    assert os.path.exists(out)
