@@ -208,6 +208,20 @@ md_status md_run_host(md_ctx *ctx, double *pos3, double *vel3, int nsteps, int e
 /* Current configuration in the reference's .cfg grammar (simulation.cu:331-339),
  * with full float precision. */
 md_status md_write_cfg(md_ctx *ctx, const char *path);
+/* One frame in XYZ format (the reference's ConfigFinish writes one, with %f,
+ * simulation.cu:323-328): atom count, a comment line with the step and box,
+ * then "name x y z" per atom in original order with full double precision
+ * (names from the .fld when the context was read from files, else T1, T2,
+ * ...).  append != 0 adds the frame at the end of the file: a trajectory. */
+md_status md_write_xyz(md_ctx *ctx, const char *path, int append);
+/* Restart (no counterpart in the reference): md_write_restart stores the
+ * state of a single system exactly (FP64 positions and velocities as
+ * stored, the step count, the thermostat state and the last step's record);
+ * md_read_restart loads it
+ * into a context of the same system (same atom count), rebuilds the list
+ * and continues from there.  Binary, native byte order. */
+md_status md_write_restart(md_ctx *ctx, const char *path);
+md_status md_read_restart(md_ctx *ctx, const char *path);
 
 /* Introspection for tests and tools. */
 typedef struct {

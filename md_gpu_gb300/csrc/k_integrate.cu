@@ -162,7 +162,8 @@ __global__ void __launch_bounds__(3 * MD_LA) k_vv_second(md_kparams kp, thermo_p
 }
 
 /* Original-order output: what 0 positions (3), 1 velocities (3, pending NH
- * scale applied), 2 forces + sum ff r^2 (4), 3 per-atom energy (1). */
+ * scale applied), 2 forces + sum ff r^2 (4), 3 per-atom energy (1),
+ * 4 velocities as stored (3, pending scale not applied). */
 __global__ void k_gather_out(md_kparams kp, int what, const md_devstate *st,
                              const md_repstate *__restrict__ repst, const int *__restrict__ arep,
                              const int *__restrict__ perm, const double *__restrict__ x,
@@ -179,6 +180,8 @@ __global__ void k_gather_out(md_kparams kp, int what, const md_devstate *st,
     } else if (what == 1) {
         double sc = repst ? repst[arep[s]].vscale : st->vscale;
         for (int d = 0; d < 3; d++) out[3 * (size_t)o + d] = v[d * P + s] * sc;
+    } else if (what == 4) {
+        for (int d = 0; d < 3; d++) out[3 * (size_t)o + d] = v[d * P + s];
     } else if (what == 2) {
         for (int d = 0; d < 3; d++) out[4 * (size_t)o + d] = (double)f[d * P + s] * FX_INV;
         out[4 * (size_t)o + 3] = vir[s];

@@ -30,6 +30,7 @@ struct parsed_run {
     md_system_desc d;
     std::vector<int> itype, bonds, angles;
     std::vector<float> charge, pos, vel, mass, lj1, lj2, bnd1, bnd2, ang1, ang2;
+    std::vector<std::string> names;   /* per type, from the .fld */
     int timprn = 1;
     float rdel = 0.02f;
 };
@@ -105,6 +106,7 @@ md_status parse_fld(const char *path, parsed_run &r)
         if (fscanf(fin, "%d %d", &iaux, &cnt) != 2) goto out;
         if (fscanf(fin, "%63s %f %f", name, &m, &q) != 3) goto out;
         r.mass[t] = (float)((double)m * 10000.0);
+        r.names.push_back(name);
     }
     if (fscanf(fin, "%255s %d", lab, &nvdw) != 2) goto out;
     for (int t = 0; t < nvdw; t++) {
@@ -1166,7 +1168,10 @@ md_status md_create_from_files(const char *base, void *stream, md_ctx **out)
     d.ang1 = r.ang1.data();
     d.ang2 = r.ang2.data();
     s = md_create(&d, stream, out);
-    if (s == MD_OK) (*out)->timprn = r.timprn;
+    if (s == MD_OK) {
+        (*out)->timprn = r.timprn;
+        (*out)->type_names = r.names;
+    }
     return s;
 }
 
@@ -1497,6 +1502,129 @@ md_status md_write_cfg(md_ctx *c, const char *path)
         fprintf(fo, "%.17g %.17g %.17g\n", v[3 * i], v[3 * i + 1], v[3 * i + 2]);
     }
     fclose(fo);
+    return MD_OK;
+}
+
+md_status md_write_xyz(md_ctx *c, const char *path, int append)
+{
+    if (!c || !path) return MD_ERR_ARG;
+    std::vector<double> p(3 * (size_t)c->n);
+    md_status s = md_get_positions(c, p.data());
+    if (s != MD_OK) return s;
+    FILE *fo = fopen(path, append ? "a" : "w");
+    if (!fo) return fail(c, MD_ERR_IO, std::string("cannot write ") + path);
+    fprintf(fo, "%d\n", c->n);
+    if (c->batch)
+        fprintf(fo, "step %lld replicas %d\n", c->host_step, c->nrep);
+    else
+        fprintf(fo, "step %lld box %.9g %.9g %.9g\n", c->host_step, c->box[0], c->box[1], c->box[2]);
+    for (int i = 0; i < c->n; i++) {
+        const int t = c->itype[i];
+        if (t < (int)c->type_names.size())
+            fprintf(fo, "%s", c->type_names[t].c_str());
+        else
+            fprintf(fo, "T%d", t + 1);
+        fprintf(fo, " %.17g %.17g %.17g\n", p[3 * i], p[3 * i + 1], p[3 * i + 2]);
+    }
+    const int bad = ferror(fo);
+    fclose(fo);
+    return bad ? fail(c, MD_ERR_IO, std::string("writing ") + path) : MD_OK;
+}
+
+/* Restart file: magic, version, atoms, step, then FP64 positions and
+ * velocities as stored (original order) and the thermodynamic state. */
+static const char MD_RESTART_MAGIC[8] = {'M', 'D', 'G', 'B', '3', 'R', 'S', 'T'};
+struct md_restart_state {
+    long long step;
+    int builds, pad;
+    double temper, ke, pe, virial, xi, eta, xi_a, eta_a, vscale, lambda, lam_next, kick_scale;
+    md_thermo last;   /* the record of the last step (md_get_thermo) */
+};
+
+md_status md_write_restart(md_ctx *c, const char *path)
+{
+    if (!c || !path) return MD_ERR_ARG;
+    if (c->batch) return fail(c, MD_ERR_UNSUPPORTED, "md_write_restart: single systems");
+    const size_t n3 = 3 * (size_t)c->n;
+    std::vector<double> p(n3), v(n3);
+    md_status s = md_get_positions(c, p.data());
+    if (s != MD_OK) return s;
+    md_kparams kp = md_make_kparams(c);
+    launch_gather_out(c, kp, 4, c->io_dev);
+    MD_CUDA_TRY(c, cudaMemcpyAsync(v.data(), c->io_dev, sizeof(double) * n3, cudaMemcpyDeviceToHost, c->stream));
+    md_devstate h;
+    MD_CUDA_TRY(c, cudaMemcpyAsync(&h, c->st, sizeof(h), cudaMemcpyDeviceToHost, c->stream));
+    MD_CUDA_TRY(c, cudaStreamSynchronize(c->stream));
+    md_restart_state r;
+    memset(&r, 0, sizeof(r));
+    r.step = c->host_step;
+    r.builds = h.builds;
+    r.temper = h.temper;
+    r.ke = h.ke;
+    r.pe = h.pe;
+    r.virial = h.virial;
+    r.xi = h.xi;
+    r.eta = h.eta;
+    r.xi_a = h.xi_a;
+    r.eta_a = h.eta_a;
+    r.vscale = h.vscale;
+    r.lambda = h.lambda;
+    r.lam_next = h.lam_next;
+    r.kick_scale = h.kick_scale;
+    if (h.step > 0)
+        MD_CUDA_TRY(c, cudaMemcpy(&r.last, c->rec + (h.step - 1) % c->rec_cap, sizeof(md_thermo),
+                                  cudaMemcpyDeviceToHost));
+    FILE *fo = fopen(path, "wb");
+    if (!fo) return fail(c, MD_ERR_IO, std::string("cannot write ") + path);
+    const int head[2] = {1, c->n};
+    bool ok = fwrite(MD_RESTART_MAGIC, 1, 8, fo) == 8 && fwrite(head, sizeof(int), 2, fo) == 2 &&
+              fwrite(&r, sizeof(r), 1, fo) == 1 && fwrite(p.data(), sizeof(double), n3, fo) == n3 &&
+              fwrite(v.data(), sizeof(double), n3, fo) == n3;
+    ok = (fclose(fo) == 0) && ok;
+    return ok ? MD_OK : fail(c, MD_ERR_IO, std::string("writing ") + path);
+}
+
+md_status md_read_restart(md_ctx *c, const char *path)
+{
+    if (!c || !path) return MD_ERR_ARG;
+    if (c->batch) return fail(c, MD_ERR_UNSUPPORTED, "md_read_restart: single systems");
+    FILE *fi = fopen(path, "rb");
+    if (!fi) return fail(c, MD_ERR_IO, std::string("cannot read ") + path);
+    char magic[8];
+    int head[2] = {0, 0};
+    md_restart_state r;
+    const size_t n3 = 3 * (size_t)c->n;
+    std::vector<double> p(n3), v(n3);
+    bool ok = fread(magic, 1, 8, fi) == 8 && !memcmp(magic, MD_RESTART_MAGIC, 8) &&
+              fread(head, sizeof(int), 2, fi) == 2 && head[0] == 1 && head[1] == c->n &&
+              fread(&r, sizeof(r), 1, fi) == 1 && fread(p.data(), sizeof(double), n3, fi) == n3 &&
+              fread(v.data(), sizeof(double), n3, fi) == n3;
+    fclose(fi);
+    if (!ok) return fail(c, MD_ERR_PARSE, std::string(path) + ": not a restart file of this system");
+    md_status s = md_set_positions(c, p.data());
+    if (s == MD_OK) s = md_set_velocities(c, v.data());
+    if (s != MD_OK) return s;
+    md_devstate h;
+    MD_CUDA_TRY(c, cudaMemcpy(&h, c->st, sizeof(h), cudaMemcpyDeviceToHost));
+    h.step = r.step;
+    h.builds = r.builds;
+    h.temper = r.temper;
+    h.ke = r.ke;
+    h.pe = r.pe;
+    h.virial = r.virial;
+    h.xi = r.xi;
+    h.eta = r.eta;
+    h.xi_a = r.xi_a;
+    h.eta_a = r.eta_a;
+    h.vscale = r.vscale;
+    h.lambda = r.lambda;
+    h.lam_next = r.lam_next;
+    h.kick_scale = r.kick_scale;
+    MD_CUDA_TRY(c, cudaMemcpy(c->st, &h, sizeof(h), cudaMemcpyHostToDevice));
+    if (r.step > 0)
+        MD_CUDA_TRY(c, cudaMemcpy(c->rec + (r.step - 1) % c->rec_cap, &r.last, sizeof(md_thermo),
+                                  cudaMemcpyHostToDevice));
+    c->host_step = r.step;
     return MD_OK;
 }
 

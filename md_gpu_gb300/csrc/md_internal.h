@@ -202,6 +202,7 @@ struct md_ctx {
     int rebuild_inline = 0;        /* step graphs: 1 = list passes inline (programmatic launches
                                       that return at once without a request), 0 = a conditional node */
     long long host_step = 0;       /* steps run so far (mirrors st->step) */
+    std::vector<std::string> type_names;   /* element names per type (.fld), if known */
     double *io_dev = nullptr;      /* 4*pitch doubles for host transfers */
     int pair_tpa = 8;    /* threads per atom in the pair kernel */
     int pair_depth = 0;  /* list entries per lane and batch (0: the default for pair_tpa) */

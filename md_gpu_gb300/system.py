@@ -141,6 +141,9 @@ def library(path: Optional[str] = None):
     L.md_get_thermo_history.argtypes = [vp, C.POINTER(Thermo), C.c_int, C.POINTER(C.c_int)]
     L.md_run_host.argtypes = [vp, vp, vp, C.c_int, C.c_int, C.POINTER(Thermo)]
     L.md_write_cfg.argtypes = [vp, C.c_char_p]
+    L.md_write_xyz.argtypes = [vp, C.c_char_p, C.c_int]
+    L.md_write_restart.argtypes = [vp, C.c_char_p]
+    L.md_read_restart.argtypes = [vp, C.c_char_p]
     L.md_get_info.argtypes = [vp, C.POINTER(Info)]
     L.md_get_order.argtypes = [vp, vp]
     L.md_get_cell_ranks.argtypes = [vp, vp]
@@ -451,3 +454,16 @@ class MDSystem:
 
     def write_cfg(self, path):
         _check(library().md_write_cfg(self._ctx, path.encode()), self._ctx)
+
+    def write_xyz(self, path, append=False):
+        """One XYZ frame (full precision); append=True builds a trajectory."""
+        _check(library().md_write_xyz(self._ctx, path.encode(), 1 if append else 0), self._ctx)
+
+    def write_restart(self, path):
+        """The exact state of a single system (FP64 positions and velocities,
+        step count, thermostat state)."""
+        _check(library().md_write_restart(self._ctx, path.encode()), self._ctx)
+
+    def read_restart(self, path):
+        """Load a restart of the same system; the list is rebuilt."""
+        _check(library().md_read_restart(self._ctx, path.encode()), self._ctx)
