@@ -1331,14 +1331,17 @@ md_status md_integrate_pre(md_ctx *c)
 {
     if (!c) return MD_ERR_ARG;
     if (c->batch) return fail(c, MD_ERR_UNSUPPORTED, "md_integrate_pre: single systems");
+    md_kparams kp = md_make_kparams(c);
     if (c->integrator == MD_LEAPFROG) {   /* the caller runs velocity Verlet from now on */
         c->integrator = c->enstype == 1 ? MD_NH : MD_VV;
         if (c->gexec) {
             cudaGraphExecDestroy(c->gexec);
             c->gexec = nullptr;
         }
+        /* the thermostat's first half step from the current state, as a
+         * velocity-Verlet context has it from its creation */
+        launch_thermo_from_state(c, kp, 0);
     }
-    md_kparams kp = md_make_kparams(c);
     launch_vv_first(c, kp, 0, 0);
     return check_overflow_and_sync(c);
 }

@@ -11,7 +11,7 @@
 #include <cstring>
 #include <vector>
 
-#include "../../include/md_gpu.h"
+#include "md_internal.h"
 #include "../../include/md_gpu_compat.h"
 
 namespace {
@@ -277,7 +277,12 @@ void forces(gpu_struct *, gpu_nlist *, gpu_config *, gpu_ffield *, ffield *, con
 void energy(gpu_struct *, gpu_nlist *, gpu_config *, gpu_ffield *, ffield *, config *, params *)
 {
     need_context("energy");
-    check("energy", md_compute_forces(S.ctx, MD_TERM_ALL, 1));
+    /* forces with per-atom energies; the step's record takes them in the
+     * next integrate (no observation of the state in between: in the middle
+     * of a velocity-Verlet step it would move the thermostat) */
+    md_kparams kp = md_make_kparams(S.ctx);
+    launch_forces(S.ctx, kp, true, MD_TERM_ALL);
+    if (cudaStreamSynchronize(S.ctx->stream) != cudaSuccess) check("energy", MD_ERR_CUDA);
     S.energy_pending = 1;
 }
 

@@ -3,7 +3,10 @@
  * through the reference-compatible entry points of libmdgpu_gb300
  * (md_gpu_compat.h), on a system read from a flat binary file.
  *
- *   compat_driver <input.bin> <output.bin>
+ *   compat_driver <input.bin> <output.bin> [vv]
+ *
+ * With "vv" the loop takes its velocity-Verlet form (runGPU.cu:73-97 with
+ * vver = 1): integrate_pre, neighborlist, forces, energy, integrate_cor.
  *
  * input: int natom, ntype, lkspace, nmaxlist, enstype, nsteps, timprn;
  *        float box[3], rcutsq, reacf, alfa, skin, dt, temper_0;
@@ -29,7 +32,8 @@ static void rd(FILE *f, T *p, size_t n)
 
 int main(int argc, char **argv)
 {
-    if (argc != 3) return 2;
+    if (argc != 3 && argc != 4) return 2;
+    const bool vver = argc == 4;
     FILE *f = fopen(argv[1], "rb");
     if (!f) return 2;
     int hdr[7];
@@ -91,10 +95,14 @@ int main(int argc, char **argv)
     gpu_nlist *g_nlist = neighborlist_init(&conf, g_prop, &pars, g_conf, &fld);
     gpu_integr *g_integ = integrate_init(&integ, g_prop, &conf);
     for (int t = 0; t <= pars.timrun; t++) {
+        if (vver) integrate_pre(g_conf, g_integ, g_prop, &integ, &conf);
         neighborlist(g_prop, g_nlist, g_conf, &conf);
         forces(g_prop, g_nlist, g_conf, g_fld, &fld, &conf, &pars);
         if (t % pars.timprn == 0) energy(g_prop, g_nlist, g_conf, g_fld, &fld, &conf, &pars);
-        integrate(g_conf, g_integ, g_prop, &integ, &conf);
+        if (vver)
+            integrate_cor(g_conf, g_integ, g_prop, &integ, &conf);
+        else
+            integrate(g_conf, g_integ, g_prop, &integ, &conf);
         checkCUDAError("integrate");
         temper[t] = integ.temper;
     }

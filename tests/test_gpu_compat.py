@@ -2,8 +2,10 @@
 reference-compatible entry points (tests/compat/compat_driver.cpp) advances
 bit for bit like md_step on the same system: the same kernels run in the
 same order (list check and rebuild, forces, energies every timprn steps,
-leapfrog), with the charges the reference's kernels see (packed into pos.w
-and decoded in FP32).  config_finish leaves the charges unpacked in pos.w."""
+leapfrog; or in the velocity-Verlet form of the loop, integrate_pre before
+and integrate_cor after), with the charges the reference's kernels see
+(packed into pos.w and decoded in FP32).  config_finish leaves the charges
+unpacked in pos.w."""
 import os
 import subprocess
 import tempfile
@@ -20,8 +22,8 @@ pytestmark = pytest.mark.gpu
 NSTEPS, TIMPRN = 40, 10
 
 
-@pytest.mark.parametrize("enstype", [0, 1])
-def test_reference_loop_matches_md_step(enstype):
+@pytest.mark.parametrize("enstype,vv", [(0, False), (1, False), (0, True), (1, True)])
+def test_reference_loop_matches_md_step(enstype, vv):
     lib = mdbuild.build()
     a = synth.to_arrays(synth.nacl_rocksalt(ncell=5, seed=52, nmaxlist=512))
     a["integrator"] = 0
@@ -31,9 +33,11 @@ def test_reference_loop_matches_md_step(enstype):
         exe = cu.build_driver(lib, td)
         fin, fout = os.path.join(td, "in.bin"), os.path.join(td, "out.bin")
         cu.write_input(fin, a, NSTEPS, TIMPRN)
-        subprocess.run([exe, fin, fout], check=True, capture_output=True, timeout=300)
+        subprocess.run([exe, fin, fout] + (["vv"] if vv else []), check=True, capture_output=True, timeout=300)
         pos, vel, temper, qback = cu.read_output(fout, n, NSTEPS)
-    b = dict(a, charge=cu.packed_charges(a["itype"], a["charge"]), tau_t=100.0)
+    # velocity Verlet: NVE, or Nose-Hoover for NVT (what integrate_pre selects)
+    b = dict(a, charge=cu.packed_charges(a["itype"], a["charge"]), tau_t=100.0,
+             integrator=(2 if enstype else 1) if vv else 0)
     with MDSystem.from_arrays(**b) as sim:
         sim.step(NSTEPS, energy_every=TIMPRN)
         assert sim.info()["builds"] >= 2
