@@ -22,18 +22,22 @@ pytestmark = pytest.mark.gpu
 NSTEPS, TIMPRN = 40, 10
 
 
+@pytest.fixture(scope="module")
+def driver():
+    with tempfile.TemporaryDirectory() as td:
+        yield cu.build_driver(mdbuild.build(), td)
+
+
 @pytest.mark.parametrize("enstype,vv", [(0, False), (1, False), (0, True), (1, True)])
-def test_reference_loop_matches_md_step(enstype, vv):
-    lib = mdbuild.build()
+def test_reference_loop_matches_md_step(driver, enstype, vv):
     a = synth.to_arrays(synth.nacl_rocksalt(ncell=5, seed=52, nmaxlist=512))
     a["integrator"] = 0
     a["enstype"] = enstype
     n = len(a["itype"])
     with tempfile.TemporaryDirectory() as td:
-        exe = cu.build_driver(lib, td)
         fin, fout = os.path.join(td, "in.bin"), os.path.join(td, "out.bin")
         cu.write_input(fin, a, NSTEPS, TIMPRN)
-        subprocess.run([exe, fin, fout] + (["vv"] if vv else []), check=True, capture_output=True, timeout=300)
+        subprocess.run([driver, fin, fout] + (["vv"] if vv else []), check=True, capture_output=True, timeout=300)
         pos, vel, temper, qback = cu.read_output(fout, n, NSTEPS)
     # velocity Verlet: NVE, or Nose-Hoover for NVT (what integrate_pre selects)
     b = dict(a, charge=cu.packed_charges(a["itype"], a["charge"]), tau_t=100.0,
