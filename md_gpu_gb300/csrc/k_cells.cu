@@ -26,6 +26,19 @@ __global__ void k_check(md_kparams kp, const float4 *__restrict__ pos4,
     if (md_rsq_exact(pos4[i], pos_old[i], kp) >= kp.rmaxdif) st->update = 1;
 }
 
+/* Cell rank (Hilbert order) of atom i and its count in the cell. */
+__device__ __forceinline__ void key_one(const md_kparams &kp, int i, const float4 *__restrict__ pos4,
+                                        const int *__restrict__ cell_rank, int *key, int *cell_count)
+{
+    float4 p = pos4[i];
+    int cx = cell_of(cell_coord(p.x, kp.box[0], kp.boxi[0], kp.centered), kp.box[0], kp.binlen[0], kp.ncell[0]);
+    int cy = cell_of(cell_coord(p.y, kp.box[1], kp.boxi[1], kp.centered), kp.box[1], kp.binlen[1], kp.ncell[1]);
+    int cz = cell_of(cell_coord(p.z, kp.box[2], kp.boxi[2], kp.centered), kp.box[2], kp.binlen[2], kp.ncell[2]);
+    int r = cell_rank[cx + kp.ncell[0] * (cy + kp.ncell[1] * cz)];
+    key[i] = r;
+    atomicAdd(&cell_count[r], 1);
+}
+
 /* Cell rank (Hilbert order) of every atom and the per-cell counts. */
 __global__ void k_cell_key(md_kparams kp, const md_devstate *st, int always,
                            const float4 *__restrict__ pos4, const int *__restrict__ cell_rank,
@@ -36,13 +49,7 @@ __global__ void k_cell_key(md_kparams kp, const md_devstate *st, int always,
     if (!always && !st->update) return;
     int i = blockIdx.x * blockDim.x + threadIdx.x;
     if (i >= kp.n) return;
-    float4 p = pos4[i];
-    int cx = cell_of(cell_coord(p.x, kp.box[0], kp.boxi[0], kp.centered), kp.box[0], kp.binlen[0], kp.ncell[0]);
-    int cy = cell_of(cell_coord(p.y, kp.box[1], kp.boxi[1], kp.centered), kp.box[1], kp.binlen[1], kp.ncell[1]);
-    int cz = cell_of(cell_coord(p.z, kp.box[2], kp.boxi[2], kp.centered), kp.box[2], kp.binlen[2], kp.ncell[2]);
-    int r = cell_rank[cx + kp.ncell[0] * (cy + kp.ncell[1] * cz)];
-    key[i] = r;
-    atomicAdd(&cell_count[r], 1);
+    key_one(kp, i, pos4, cell_rank, key, cell_count);
 }
 
 /* The same for a batch: each atom is tested with its replica's box and skin. */
@@ -140,32 +147,30 @@ __global__ void k_clear_update_b(md_devstate *st, int always, int *rep_upd, md_r
     }
 }
 
-/* Exclusive scan of the cell counts (one block of 1024 threads), then zero
- * the counters for the next build.  cell_start has ncells + 1 entries.  In
- * rounds of 1024 x SCAN_K cells: the counts pass through shared memory, so
+/* Exclusive scan of the cell counts by one block of NT threads, then (ZERO)
+ * zero the counters for the next build; returns the total in thread 0.
+ * Without ZERO, cell_start may be cell_count itself (each round loads its
+ * counts before it writes their starts).  In
+ * rounds of NT x SCAN_K cells: the counts pass through shared memory, so
  * that global loads and stores are coalesced (one SM issues them all) while
  * each thread scans SCAN_K consecutive counts; warps scan their threads'
  * sums with shuffles and warp 0 the warp totals.  Shared index i is stored
  * at i + i / SCAN_K, so the per-thread reads hit distinct banks. */
 constexpr int SCAN_K = 8;
-constexpr int SCAN_N = 1024 * SCAN_K;
 __device__ __forceinline__ int scan_pad(int i) { return i + i / SCAN_K; }
 
-__global__ void __launch_bounds__(1024) k_cell_scan(md_kparams kp, md_devstate *st, int always,
-                                                    int ncells, int *cell_count, int *cell_start,
-                                                    int *cell_fill)
+template <int NT, bool ZERO = true>
+__device__ __forceinline__ int scan_cells(int ncells, int *cell_count, int *cell_start, int *cell_fill)
 {
-    pdl_wait();      /* launched after the previous pass (programmatic launch) */
-    pdl_trigger();
-    if (!always && !st->update) return;
-    __shared__ int buf[SCAN_N + SCAN_N / SCAN_K];
+    constexpr int N = NT * SCAN_K;
+    __shared__ int buf[N + N / SCAN_K];
     __shared__ int wsum[32];
     const int t = threadIdx.x, lane = t & 31, w = t >> 5;
     int carry = 0;
-    for (int base = 0; base < ncells; base += SCAN_N) {
+    for (int base = 0; base < ncells; base += N) {
 #pragma unroll
         for (int k = 0; k < SCAN_K; k++) {
-            const int i = k * 1024 + t, g = base + i;
+            const int i = k * NT + t, g = base + i;
             buf[scan_pad(i)] = g < ncells ? cell_count[g] : 0;
         }
         __syncthreads();
@@ -184,7 +189,7 @@ __global__ void __launch_bounds__(1024) k_cell_scan(md_kparams kp, md_devstate *
         if (lane == 31) wsum[w] = incl;
         __syncthreads();
         if (w == 0) {
-            int x = wsum[lane];
+            int x = lane < NT / 32 ? wsum[lane] : 0;
 #pragma unroll
             for (int o = 1; o < 32; o <<= 1) {
                 const int y = __shfl_up_sync(0xffffffffu, x, o);
@@ -199,21 +204,36 @@ __global__ void __launch_bounds__(1024) k_cell_scan(md_kparams kp, md_devstate *
             buf[scan_pad(t * SCAN_K + k)] = run;
             run += v[k];
         }
-        carry += wsum[31];
+        carry += wsum[NT / 32 - 1];
         __syncthreads();
 #pragma unroll
         for (int k = 0; k < SCAN_K; k++) {
-            const int i = k * 1024 + t, g = base + i;
+            const int i = k * NT + t, g = base + i;
             if (g < ncells) {
                 cell_start[g] = buf[scan_pad(i)];
-                cell_count[g] = 0;
-                cell_fill[g] = 0;
+                if (ZERO) {
+                    cell_count[g] = 0;
+                    cell_fill[g] = 0;
+                }
             }
         }
         __syncthreads();   /* buf and wsum are rewritten by the next round */
     }
-    if (t == 0) {
-        cell_start[ncells] = carry;
+    return carry;
+}
+
+/* The scan as its own pass (one block of 1024 threads); cell_start has
+ * ncells + 1 entries. */
+__global__ void __launch_bounds__(1024) k_cell_scan(md_kparams kp, md_devstate *st, int always,
+                                                    int ncells, int *cell_count, int *cell_start,
+                                                    int *cell_fill)
+{
+    pdl_wait();      /* launched after the previous pass (programmatic launch) */
+    pdl_trigger();
+    if (!always && !st->update) return;
+    const int total = scan_cells<1024>(ncells, cell_count, cell_start, cell_fill);
+    if (threadIdx.x == 0) {
+        cell_start[ncells] = total;
         st->builds += 1;
     }
 }
@@ -301,20 +321,14 @@ __global__ void k_cell_order(md_kparams kp, const md_devstate *st, int always, i
     }
 }
 
-__global__ void k_permute(md_kparams kp, const md_devstate *st, int always,
-                          const int *__restrict__ src, const double *__restrict__ x,
-                          const double *__restrict__ v, const double *__restrict__ mass,
-                          const double *__restrict__ kick,
-                          const float4 *__restrict__ pos4, const int *__restrict__ perm,
-                          const int *__restrict__ type, double *tmp_d, float4 *tmp4, int *tmp_i,
-                          const int *__restrict__ arep, const int *__restrict__ rep_upd)
+/* Sorted slot s takes the state of atom src[s] (into the staging arrays). */
+__device__ __forceinline__ void permute_one(const md_kparams &kp, int s, const int *__restrict__ src,
+                                            const double *__restrict__ x, const double *__restrict__ v,
+                                            const double *__restrict__ mass, const double *__restrict__ kick,
+                                            const float4 *__restrict__ pos4, const int *__restrict__ perm,
+                                            const int *__restrict__ type, double *tmp_d, float4 *tmp4,
+                                            int *tmp_i)
 {
-    pdl_wait();      /* launched after the previous pass (programmatic launch) */
-    pdl_trigger();
-    if (!always && !st->update) return;
-    int s = blockIdx.x * blockDim.x + threadIdx.x;
-    if (s >= kp.n) return;
-    if (arep && !rep_upd[arep[s]]) return;   /* atoms stay inside their replica's range */
     int o = src[s], P = kp.pitch;
     for (int d = 0; d < 3; d++) {
         tmp_d[d * P + s] = x[d * P + o];
@@ -327,18 +341,12 @@ __global__ void k_permute(md_kparams kp, const md_devstate *st, int always,
     tmp_i[P + s] = type[o];
 }
 
-__global__ void k_copyback(md_kparams kp, const md_devstate *st, int always,
-                           const double *__restrict__ tmp_d, const float4 *__restrict__ tmp4,
-                           const int *__restrict__ tmp_i, double *x, double *v, double *mass,
-                           double *kick, float4 *pos4, int *perm, int *iperm, int *type,
-                           const int *__restrict__ arep, const int *__restrict__ rep_upd)
+/* The staged state back into the per-atom arrays, and the inverse order. */
+__device__ __forceinline__ void copyback_one(const md_kparams &kp, int s, const double *__restrict__ tmp_d,
+                                             const float4 *__restrict__ tmp4, const int *__restrict__ tmp_i,
+                                             double *x, double *v, double *mass, double *kick, float4 *pos4,
+                                             int *perm, int *iperm, int *type)
 {
-    pdl_wait();      /* launched after the previous pass (programmatic launch) */
-    pdl_trigger();
-    if (!always && !st->update) return;
-    int s = blockIdx.x * blockDim.x + threadIdx.x;
-    if (s >= kp.n) return;
-    if (arep && !rep_upd[arep[s]]) return;
     int P = kp.pitch;
     for (int d = 0; d < 3; d++) {
         x[d * P + s] = tmp_d[d * P + s];
@@ -353,19 +361,14 @@ __global__ void k_copyback(md_kparams kp, const md_devstate *st, int always,
     type[s] = tmp_i[P + s];
 }
 
-/* Exclusions and bonded lists re-expressed in the new sorted indices. */
-__global__ void k_remap(md_kparams kp, const md_devstate *st, int always,
-                        const int *__restrict__ perm, const int *__restrict__ iperm,
-                        const uint4 *__restrict__ excl_orig, uint4 *excl_s,
-                        const int2 *__restrict__ bl_o, const int *__restrict__ bl_on, int2 *bl_s,
-                        int *bl_sn, const int4 *__restrict__ al_o, const int *__restrict__ al_on,
-                        int4 *al_s, int *al_sn, int has_bonds, int has_angles)
+/* Exclusions and bonded lists of sorted slot s in the new sorted indices. */
+__device__ __forceinline__ void remap_one(const md_kparams &kp, int s, const int *__restrict__ perm,
+                                          const int *__restrict__ iperm, const uint4 *__restrict__ excl_orig,
+                                          uint4 *excl_s, const int2 *__restrict__ bl_o,
+                                          const int *__restrict__ bl_on, int2 *bl_s, int *bl_sn,
+                                          const int4 *__restrict__ al_o, const int *__restrict__ al_on,
+                                          int4 *al_s, int *al_sn, int has_bonds, int has_angles)
 {
-    pdl_wait();      /* launched after the previous pass (programmatic launch) */
-    pdl_trigger();
-    if (!always && !st->update) return;
-    int s = blockIdx.x * blockDim.x + threadIdx.x;
-    if (s >= kp.n) return;
     int o = perm[s], P = kp.pitch;
     uint4 e = excl_orig[o];
     uint4 m;
@@ -390,6 +393,55 @@ __global__ void k_remap(md_kparams kp, const md_devstate *st, int always,
         }
         al_sn[s] = na;
     }
+}
+
+__global__ void k_permute(md_kparams kp, const md_devstate *st, int always,
+                          const int *__restrict__ src, const double *__restrict__ x,
+                          const double *__restrict__ v, const double *__restrict__ mass,
+                          const double *__restrict__ kick,
+                          const float4 *__restrict__ pos4, const int *__restrict__ perm,
+                          const int *__restrict__ type, double *tmp_d, float4 *tmp4, int *tmp_i,
+                          const int *__restrict__ arep, const int *__restrict__ rep_upd)
+{
+    pdl_wait();      /* launched after the previous pass (programmatic launch) */
+    pdl_trigger();
+    if (!always && !st->update) return;
+    int s = blockIdx.x * blockDim.x + threadIdx.x;
+    if (s >= kp.n) return;
+    if (arep && !rep_upd[arep[s]]) return;   /* atoms stay inside their replica's range */
+    permute_one(kp, s, src, x, v, mass, kick, pos4, perm, type, tmp_d, tmp4, tmp_i);
+}
+
+__global__ void k_copyback(md_kparams kp, const md_devstate *st, int always,
+                           const double *__restrict__ tmp_d, const float4 *__restrict__ tmp4,
+                           const int *__restrict__ tmp_i, double *x, double *v, double *mass,
+                           double *kick, float4 *pos4, int *perm, int *iperm, int *type,
+                           const int *__restrict__ arep, const int *__restrict__ rep_upd)
+{
+    pdl_wait();      /* launched after the previous pass (programmatic launch) */
+    pdl_trigger();
+    if (!always && !st->update) return;
+    int s = blockIdx.x * blockDim.x + threadIdx.x;
+    if (s >= kp.n) return;
+    if (arep && !rep_upd[arep[s]]) return;
+    copyback_one(kp, s, tmp_d, tmp4, tmp_i, x, v, mass, kick, pos4, perm, iperm, type);
+}
+
+/* Exclusions and bonded lists re-expressed in the new sorted indices. */
+__global__ void k_remap(md_kparams kp, const md_devstate *st, int always,
+                        const int *__restrict__ perm, const int *__restrict__ iperm,
+                        const uint4 *__restrict__ excl_orig, uint4 *excl_s,
+                        const int2 *__restrict__ bl_o, const int *__restrict__ bl_on, int2 *bl_s,
+                        int *bl_sn, const int4 *__restrict__ al_o, const int *__restrict__ al_on,
+                        int4 *al_s, int *al_sn, int has_bonds, int has_angles)
+{
+    pdl_wait();      /* launched after the previous pass (programmatic launch) */
+    pdl_trigger();
+    if (!always && !st->update) return;
+    int s = blockIdx.x * blockDim.x + threadIdx.x;
+    if (s >= kp.n) return;
+    remap_one(kp, s, perm, iperm, excl_orig, excl_s, bl_o, bl_on, bl_s, bl_sn, al_o, al_on, al_s, al_sn,
+              has_bonds, has_angles);
 }
 
 /* Ends a rebuild (or a step without one): the next step's check sets the
@@ -779,6 +831,144 @@ __global__ void __launch_bounds__(CW_WARPS * 32) k_build_cells(
     }
 }
 
+/* ---- The whole rebuild of a single system as one cooperative kernel ---- */
+
+/* Grid-wide barrier of the cooperative rebuild (every block is resident:
+ * the kernel is launched cooperatively).  The last block to arrive resets
+ * the count and advances the generation; the others wait for the
+ * generation to change for at most MD_BAR_NS of global time, after which
+ * they record the timeout in st->status and go on: the build is then
+ * invalid and the host reports it, but nothing waits forever.  (About 4 us
+ * per barrier at 1368 blocks on a GB300, fences included; a two-level
+ * version measured no faster.) */
+constexpr unsigned long long MD_BAR_NS = 50000000ull;   /* 50 ms */
+
+__device__ __forceinline__ unsigned long long global_ns()
+{
+    unsigned long long t;
+    asm volatile("mov.u64 %0, %%globaltimer;" : "=l"(t));
+    return t;
+}
+
+__device__ __forceinline__ void grid_barrier(md_devstate *st)
+{
+    __syncthreads();
+    if (threadIdx.x == 0) {
+        volatile unsigned *gen = &st->bar_gen;
+        const unsigned g = *gen;
+        __threadfence();
+        if (atomicAdd(&st->bar_count, 1u) == gridDim.x - 1) {
+            atomicExch(&st->bar_count, 0u);
+            __threadfence();
+            atomicAdd(&st->bar_gen, 1u);
+        } else {
+            const unsigned long long t0 = global_ns();
+            while (*gen == g) {
+                if (global_ns() - t0 > MD_BAR_NS) {
+                    atomicOr(&st->status, 1);
+                    break;
+                }
+                __nanosleep(20);
+            }
+        }
+        __threadfence();
+    }
+    __syncthreads();
+}
+
+/* The arrays the rebuild passes touch. */
+struct rb_ptrs {
+    const int *cell_rank, *cell_lin;
+    int *key, *cell_count, *cell_start, *cell_fill, *src;
+    double *x, *v, *mass, *kick, *tmp_d;
+    float4 *pos4, *tmp4, *pos_old;
+    int *perm, *iperm, *type, *tmp_i;
+    const uint4 *excl_orig;
+    uint4 *excl_s;
+    const int2 *bl_o;
+    const int *bl_on;
+    int2 *bl_s;
+    int *bl_sn;
+    const int4 *al_o;
+    const int *al_on;
+    int4 *al_s;
+    int *al_sn;
+    const unsigned *type_mask;
+    unsigned *nl;
+    int *nl_n;
+    int ncells, has_bonds, has_angles;
+};
+
+/* Binning, scan, scatter, in-cell order, permutation, remap, list build and
+ * the closing reset in one launch, the passes separated by grid barriers;
+ * a launch without a rebuild due returns at once.  128 threads per block,
+ * the warp-per-cell builder (stencils of up to CW_MAXST cells). */
+__global__ void __launch_bounds__(CW_WARPS * 32) k_rebuild_coop(md_kparams kp, md_devstate *st, int always,
+                                                                rb_ptrs p)
+{
+    if (!always && !st->update) return;   /* the same in every block: nothing writes it before the end */
+    const int tid = blockIdx.x * blockDim.x + threadIdx.x, nth = gridDim.x * blockDim.x;
+    const int n = kp.n;
+    for (int i = tid; i < n; i += nth) key_one(kp, i, p.pos4, p.cell_rank, p.key, p.cell_count);
+    grid_barrier(st);
+    /* one block scans (one barrier is dearer than its few rounds) */
+    if (blockIdx.x == 0) {
+        const int total = scan_cells<CW_WARPS * 32>(p.ncells, p.cell_count, p.cell_start, p.cell_fill);
+        if (threadIdx.x == 0) {
+            p.cell_start[p.ncells] = total;
+            st->builds += 1;
+        }
+    }
+    grid_barrier(st);
+    for (int i = tid; i < n; i += nth) {
+        const int r = p.key[i];
+        p.src[p.cell_start[r] + atomicAdd(&p.cell_fill[r], 1)] = i;
+    }
+    grid_barrier(st);
+    {
+        const int lane = threadIdx.x & 31, nw = nth >> 5;
+        for (int c = tid >> 5; c < p.ncells; c += nw) {
+            order_cell(c, p.cell_start, p.perm, p.src, nullptr, nullptr, lane);
+            __syncwarp();
+        }
+    }
+    grid_barrier(st);
+    for (int s = tid; s < n; s += nth)
+        permute_one(kp, s, p.src, p.x, p.v, p.mass, p.kick, p.pos4, p.perm, p.type, p.tmp_d, p.tmp4, p.tmp_i);
+    grid_barrier(st);
+    for (int s = tid; s < n; s += nth)
+        copyback_one(kp, s, p.tmp_d, p.tmp4, p.tmp_i, p.x, p.v, p.mass, p.kick, p.pos4, p.perm, p.iperm, p.type);
+    /* with bonds or angles the exclusions need the new order first; without,
+     * the list build reads the sorted positions and types from the staging
+     * arrays while the copy-back runs (it writes nothing the build reads) */
+    const bool remap = p.has_bonds || p.has_angles;   /* the same in every block */
+    if (remap) {
+        grid_barrier(st);
+        for (int s = tid; s < n; s += nth)
+            remap_one(kp, s, p.perm, p.iperm, p.excl_orig, p.excl_s, p.bl_o, p.bl_on, p.bl_s, p.bl_sn, p.al_o,
+                      p.al_on, p.al_s, p.al_sn, p.has_bonds, p.has_angles);
+        grid_barrier(st);
+    }
+    {
+        const float4 *bpos = remap ? p.pos4 : p.tmp4;
+        const int *btype = remap ? p.type : p.tmp_i + kp.pitch;
+        const int lane = threadIdx.x & 31;
+        for (;;) {
+            int r = 0;
+            if (lane == 0) r = atomicAdd(&st->cell_next, 1);
+            r = __shfl_sync(0xffffffffu, r, 0);
+            if (r >= p.ncells) break;
+            build_cell<false>(r, kp, st, bpos, btype, p.excl_s, p.cell_rank, p.cell_lin, p.cell_start,
+                              p.type_mask, p.nl, p.nl_n, p.pos_old, nullptr, nullptr, nullptr);
+        }
+    }
+    grid_barrier(st);
+    if (tid == 0) {
+        st->update = 0;
+        st->cell_next = 0;
+    }
+}
+
 }  // namespace
 
 void launch_check(md_ctx *c, const md_kparams &kp)
@@ -821,10 +1011,78 @@ static int cw_blocks(md_ctx *c, bool batch)
     return std::max(1, std::min(g, (c->ncells + CW_WARPS - 1) / CW_WARPS));
 }
 
+/* Whether a single system rebuilds with the one-kernel rebuild: the
+ * warp-per-cell builder with its stencil in shared memory, and enough
+ * resident blocks found for a cooperative launch. */
+bool md_rebuild_coop(md_ctx *c)
+{
+    if (c->batch || c->list_tpa != 0 || !c->rebuild_coop) return false;
+    int nst = 1;
+    for (int d = 0; d < 3; d++) nst *= c->stencil[d] < 0 ? c->ncell[d] : 2 * c->stencil[d] + 1;
+    if (nst > CW_MAXST) return false;
+    if (c->coop_grid == 0) {   /* found once, on the context's first, uncaptured, build */
+        int dev = 0, nsm = 0, occ = 0;
+        cudaGetDevice(&dev);
+        cudaDeviceGetAttribute(&nsm, cudaDevAttrMultiProcessorCount, dev);
+        cudaOccupancyMaxActiveBlocksPerMultiprocessor(&occ, k_rebuild_coop, CW_WARPS * 32, 0);
+        c->coop_grid = occ > 0 ? nsm * occ : -1;
+    }
+    return c->coop_grid > 0;
+}
+
 void launch_rebuild(md_ctx *c, const md_kparams &kp, bool unconditional, bool all_replicas, bool pdl)
 {
     int always = unconditional ? 1 : 0;
     if (c->batch) pdl = false;
+    if (md_rebuild_coop(c)) {
+        rb_ptrs p;
+        p.cell_rank = c->cell_rank;
+        p.cell_lin = c->cell_lin;
+        p.key = c->key;
+        p.cell_count = c->cell_count;
+        p.cell_start = c->cell_start;
+        p.cell_fill = c->cell_fill;
+        p.src = c->src;
+        p.x = c->x;
+        p.v = c->v;
+        p.mass = c->mass;
+        p.kick = c->kick;
+        p.tmp_d = c->tmp_d;
+        p.pos4 = c->pos4;
+        p.tmp4 = c->tmp4;
+        p.pos_old = c->pos_old;
+        p.perm = c->perm;
+        p.iperm = c->iperm;
+        p.type = c->type;
+        p.tmp_i = c->tmp_i;
+        p.excl_orig = c->excl_orig;
+        p.excl_s = c->excl_s;
+        p.bl_o = c->bl_o;
+        p.bl_on = c->bl_on;
+        p.bl_s = c->bl_s;
+        p.bl_sn = c->bl_sn;
+        p.al_o = c->al_o;
+        p.al_on = c->al_on;
+        p.al_s = c->al_s;
+        p.al_sn = c->al_sn;
+        p.type_mask = c->type_mask_dev;
+        p.nl = c->nl;
+        p.nl_n = c->nl_n;
+        p.ncells = c->ncells;
+        p.has_bonds = c->has_bonds;
+        p.has_angles = c->has_angles;
+        cudaLaunchConfig_t cfg = {};
+        cfg.gridDim = dim3(c->coop_grid);
+        cfg.blockDim = dim3(CW_WARPS * 32);
+        cfg.stream = c->stream;
+        cudaLaunchAttribute at[1];
+        at[0].id = cudaLaunchAttributeCooperative;
+        at[0].val.cooperative = 1;
+        cfg.attrs = at;
+        cfg.numAttrs = 1;
+        cudaLaunchKernelEx(&cfg, k_rebuild_coop, kp, c->st, always, p);
+        return;
+    }
     const int cwb = cw_blocks(c, c->batch);   /* also finds the SM count */
     int nb = (kp.n + 255) / 256;
     cudaStream_t s = c->stream;

@@ -263,6 +263,8 @@ md_status check_overflow_and_sync(md_ctx *c)
     MD_CUDA_TRY(c, cudaStreamSynchronize(c->stream));
     md_devstate h;
     MD_CUDA_TRY(c, cudaMemcpy(&h, c->st, sizeof(h), cudaMemcpyDeviceToHost));
+    if (h.status != 0)
+        return fail(c, MD_ERR_CUDA, "a grid barrier of the list rebuild timed out (device state invalid)");
     if (h.list_overflow > 0)
         return fail(c, MD_ERR_LIST_OVERFLOW,
                     "neighbour list overflow: " + std::to_string(h.list_overflow) + " > capacity " +
@@ -1660,10 +1662,10 @@ md_status md_get_info(md_ctx *c, md_info *out)
     out->kernels_per_step = md_can_fuse(c) ? 1
                                            : 1 + ((c->has_bonds || c->has_angles) ? 1 : 0) +
                                                  (c->integrator == MD_LEAPFROG ? 1 : 2);
-    /* single system: key, scan, scatter, order, permute, copyback, remap
-     * (with bonds or angles), list, clear; batch: key, scan, scatter, order,
-     * permute, copyback, list, clear */
-    out->kernels_per_rebuild = (c->batch || !(c->has_bonds || c->has_angles)) ? 8 : 9;
+    /* single system: one cooperative kernel, or key, scan, scatter, order,
+     * permute, copyback, remap (with bonds or angles), list, clear; batch:
+     * key, scan, scatter, order, permute, copyback, list, clear */
+    out->kernels_per_rebuild = md_rebuild_coop(c) ? 1 : (c->batch || !(c->has_bonds || c->has_angles)) ? 8 : 9;
     out->kernels_per_graph = c->integrator == MD_LEAPFROG ? 1 : 0;
     if (c->rebuild_inline && !c->batch) {   /* the passes run (and return) in every step */
         out->kernels_per_step += out->kernels_per_rebuild;

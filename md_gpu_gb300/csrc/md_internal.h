@@ -44,7 +44,7 @@
 struct md_devstate {
     int update;          /* neighbour-list rebuild requested this step */
     int list_overflow;   /* largest list length seen beyond capacity, or 0 */
-    int status;          /* sticky device-side error code */
+    int status;          /* sticky device-side error code (1: a grid barrier timed out) */
     int builds;          /* neighbour-list builds so far */
     long long step;
     double temper;       /* temperature after the last step, K */
@@ -60,6 +60,8 @@ struct md_devstate {
     unsigned blocks_done; /* blocks finished in the current reduction kernel */
     unsigned long long acc[3]; /* fixed-point KE (MD_KFIX), PE, sum ff r^2 (MD_EFIX) of the step */
     int cell_next;       /* next cell a list-building warp takes (reset after each build) */
+    unsigned bar_count;  /* grid barrier of the one-kernel rebuild: arrivals, */
+    unsigned bar_gen;    /* and generation */
 };
 
 /* Everything a kernel needs about the system, passed by value. */
@@ -198,6 +200,8 @@ struct md_ctx {
     int use_graphs = 1;            /* 0: launch every step's kernels eagerly */
     int fuse_step = 0;             /* 1: fused pair+leapfrog kernel where applicable */
     int cw_grid[2] = {0, 0};       /* blocks of the persistent list builder (single, batch) */
+    int rebuild_coop = 1;          /* single systems: the rebuild as one cooperative kernel */
+    int coop_grid = 0;             /* its blocks (0: not found yet, -1: unavailable) */
     int nsm = 1;                   /* SMs of the device (found with cw_grid) */
     int rebuild_inline = 0;        /* step graphs: 1 = list passes inline (programmatic launches
                                       that return at once without a request), 0 = a conditional node */
@@ -271,6 +275,7 @@ void launch_check(md_ctx *c, const md_kparams &kp);
 void launch_rebuild(md_ctx *c, const md_kparams &kp, bool unconditional, bool all_replicas,
                     bool pdl = false);
 void launch_set_condition(md_ctx *c, unsigned long long handle);
+bool md_rebuild_coop(md_ctx *c);
 /* ---- launchers (k_forces.cu) ---- */
 void launch_forces(md_ctx *c, const md_kparams &kp, bool energy, int terms);
 /* ---- launchers (k_integrate.cu) ---- */
