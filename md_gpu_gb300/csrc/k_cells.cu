@@ -540,12 +540,13 @@ __global__ void __launch_bounds__(256) k_build_list(
 /* List build, one warp per cell: every atom of a cell shares the cell's
  * stencil.  The warp first gathers the stencil cells' atom ranges into
  * shared memory (in traversal order) with their prefix sums, then streams the
- * concatenated candidates 32 at a time (lane = candidate, located by binary
- * search over the prefix sums).  A conservative test against the bounding
- * box of the cell's atoms drops the candidates (about a third) that no atom
- * of the cell can reach; the rest enter a per-warp queue in candidate order,
- * and each full queue of 32 is tested exactly against the cell's atoms one i
- * at a time, a ballot appending the hits to i's list.  Entries land in the
+ * concatenated candidates 32 at a time (lane = candidate, its stencil cell
+ * found by stepping forward through the prefix sums).  A conservative test
+ * against the bounding box of the cell's atoms drops the candidates (about a
+ * third) that no atom of the cell can reach; the rest enter a per-warp queue
+ * in candidate order, and each full queue of 32 is tested exactly against
+ * the cell's atoms, two at a time, a ballot per atom appending the hits to
+ * its list.  Entries land in the
  * same order as in k_build_list (stencil cells in traversal order, ascending
  * j), so both builders produce identical lists. */
 constexpr int CW_WARPS = 4;
@@ -570,6 +571,9 @@ __device__ __forceinline__ void build_cell(
     const int *__restrict__ rep_upd)
 {
     __shared__ float4 s_p[CW_WARPS][CW_MAXI];
+    /* the group's coordinates once more by axis, so that two atoms' x (y, z)
+     * are one aligned 8-byte load; slots past the group hold a far point */
+    __shared__ __align__(16) float s_h[CW_WARPS][3][CW_MAXI];
     __shared__ uint4 s_ex[CW_WARPS][CW_MAXI];
     __shared__ unsigned s_tm[CW_WARPS][CW_MAXI];
     __shared__ int s_jb[CW_WARPS][CW_MAXST];
@@ -644,6 +648,12 @@ __device__ __forceinline__ void build_cell(
     for (int i0 = ib; i0 < ie; i0 += CW_MAXI) {
         const int ni = min(CW_MAXI, ie - i0);
         bool any_excl = false;
+        {
+            const float4 p = lane < ni ? pos4[i0 + lane] : make_float4(1e30f, 1e30f, 1e30f, 0.0f);
+            s_h[w][0][lane] = p.x;
+            s_h[w][1][lane] = p.y;
+            s_h[w][2][lane] = p.z;
+        }
         if (lane < ni) {
             int i = i0 + lane;
             s_p[w][lane] = pos4[i];
@@ -704,8 +714,44 @@ __device__ __forceinline__ void build_cell(
                     if (lane == a) mycnt += __popc(bal);
                 }
             };
-            if (excl_bits) loop(std::true_type());
-            else loop(std::false_type());
+            if (excl_bits) {
+                loop(std::true_type());
+            } else if (G.shift) {
+                /* two group atoms per iteration: the differences and squares
+                 * in packed f32x2 instructions, the two sums in scalar adds
+                 * with explicit rounding (a packed multiply followed by a
+                 * packed add may be contracted into a packed FMA by the code
+                 * generator, which would change the rounding of r^2) */
+                typedef v2<true> V;
+                const V QX = V::make(q.x, q.x), QY = V::make(q.y, q.y), QZ = V::make(q.z, q.z);
+                const V UX = V::make(ux, ux), UY = V::make(uy, uy), UZ = V::make(uz, uz);
+                const float far = vj ? G.rskinsq : -1.0f;   /* no hit in an empty slot */
+                for (int a = 0; a < ni; a += 2) {
+                    const float2 hx = *reinterpret_cast<const float2 *>(&s_h[w][0][a]);
+                    const float2 hy = *reinterpret_cast<const float2 *>(&s_h[w][1][a]);
+                    const float2 hz = *reinterpret_cast<const float2 *>(&s_h[w][2][a]);
+                    const V dx = (V::make(hx.x, hx.y) - QX) - UX;
+                    const V dy = (V::make(hy.x, hy.y) - QY) - UY;
+                    const V dz = (V::make(hz.x, hz.y) - QZ) - UZ;
+                    float x0, x1, y0, y1, z0, z1;
+                    (dx * dx).get(x0, x1);
+                    (dy * dy).get(y0, y1);
+                    (dz * dz).get(z0, z1);
+                    const float r0 = __fadd_rn(__fadd_rn(x0, y0), z0);
+                    const float r1 = __fadd_rn(__fadd_rn(x1, y1), z1);
+#pragma unroll
+                    for (int h = 0; h < 2; h++) {
+                        const bool ok = (h ? r1 : r0) < far && a + h != selfa;
+                        const unsigned bal = __ballot_sync(0xffffffffu, ok);
+                        const int base = __shfl_sync(0xffffffffu, mycnt, a + h);
+                        const int slot = base + __popc(bal & lt);
+                        if (ok && slot < kp.cap) nl[(size_t)(i0 + a + h) * kp.cap + slot] = entry;
+                        mycnt += lane == a + h ? __popc(bal) : 0;
+                    }
+                }
+            } else {
+                loop(std::false_type());
+            }
         };
         /* Bounding box of the group: candidates farther than rl from it
          * cannot pass the exact test for any member and are dropped before
@@ -727,18 +773,17 @@ __device__ __forceinline__ void build_cell(
         }
         const float near_sq = G.rskinsq * 1.001f + 1e-4f;
         int fill = 0;   /* queued candidates (in candidate order) */
+        int kc = 0;     /* this lane's stencil cell: the largest k with s_pre[k] <= g */
         for (int g0 = 0; g0 < total; g0 += 32) {
             const int g = g0 + lane;
             bool vj = g < total;
             int j = 0, code = 0;
             if (vj) {
-                int a = 0, b = nst;   /* largest k with s_pre[k] <= g */
-                while (b - a > 1) {
-                    int m = (a + b) >> 1;
-                    if (s_pre[w][m] <= g) a = m; else b = m;
-                }
-                j = s_jb[w][a] + (g - s_pre[w][a]);
-                code = s_sh[w][a];
+                /* g grows by 32 per round and a cell holds ~10 candidates:
+                 * a few steps forward (s_pre[nst] = total > g stops it) */
+                while (s_pre[w][kc + 1] <= g) kc++;
+                j = s_jb[w][kc] + (g - s_pre[w][kc]);
+                code = s_sh[w][kc];
             }
             const float4 q = vj ? pos4[j] : make_float4(0.f, 0.f, 0.f, 0.f);
             bool near = vj;

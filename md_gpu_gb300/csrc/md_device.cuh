@@ -27,6 +27,51 @@ __device__ __forceinline__ float md_rsq_exact(float4 a, float4 b, const md_kpara
     return md_rsq_box(a, b, kp.box, kp.boxi);
 }
 
+/* Two FP32 lanes in one 64-bit register pair: the sm_100+ packed
+ * instructions add/sub/mul/fma.rn.f32x2 compute two entries' operations in
+ * one issue slot, each half rounded as the scalar instruction would. */
+typedef unsigned long long f32x2;
+template <bool PACKED>
+struct v2;
+template <>
+struct v2<true> {
+    f32x2 d;
+    __device__ __forceinline__ static v2 make(float a, float b)
+    {
+        v2 r;
+        asm("mov.b64 %0, {%1, %2};" : "=l"(r.d) : "f"(a), "f"(b));
+        return r;
+    }
+    __device__ __forceinline__ void get(float &a, float &b) const
+    {
+        asm("mov.b64 {%0, %1}, %2;" : "=f"(a), "=f"(b) : "l"(d));
+    }
+    __device__ __forceinline__ friend v2 operator+(v2 a, v2 b)
+    {
+        v2 r;
+        asm("add.rn.f32x2 %0, %1, %2;" : "=l"(r.d) : "l"(a.d), "l"(b.d));
+        return r;
+    }
+    __device__ __forceinline__ friend v2 operator-(v2 a, v2 b)
+    {
+        v2 r;
+        asm("sub.rn.f32x2 %0, %1, %2;" : "=l"(r.d) : "l"(a.d), "l"(b.d));
+        return r;
+    }
+    __device__ __forceinline__ friend v2 operator*(v2 a, v2 b)
+    {
+        v2 r;
+        asm("mul.rn.f32x2 %0, %1, %2;" : "=l"(r.d) : "l"(a.d), "l"(b.d));
+        return r;
+    }
+    __device__ __forceinline__ static v2 fma(v2 a, v2 b, v2 c)
+    {
+        v2 r;
+        asm("fma.rn.f32x2 %0, %1, %2, %3;" : "=l"(r.d) : "l"(a.d), "l"(b.d), "l"(c.d));
+        return r;
+    }
+};
+
 /* (x + L/2) / bin truncated and clamped: the binning rule of the reference's
  * sketch (neighborlist_kernel_o.cu:20-25) with IEEE add and divide. */
 /* The coordinate an atom is binned by: its position when every position

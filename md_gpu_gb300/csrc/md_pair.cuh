@@ -166,55 +166,38 @@ __device__ __forceinline__ void pair_term(const G &g, float4 pi, float qi, float
     }
 }
 
-/* Two FP32 lanes in one 64-bit register pair: the sm_100+ packed
- * instructions add/sub/mul/fma.rn.f32x2 compute two entries' operations in
- * one issue slot, each half rounded as the scalar instruction would. */
-typedef unsigned long long f32x2;
-template <bool PACKED>
-struct v2;
-template <>
-struct v2<true> {
-    f32x2 d;
-    __device__ __forceinline__ static v2 make(float a, float b)
-    {
-        v2 r;
-        asm("mov.b64 %0, {%1, %2};" : "=l"(r.d) : "f"(a), "f"(b));
-        return r;
-    }
-    __device__ __forceinline__ void get(float &a, float &b) const
-    {
-        asm("mov.b64 {%0, %1}, %2;" : "=f"(a), "=f"(b) : "l"(d));
-    }
-    __device__ __forceinline__ friend v2 operator+(v2 a, v2 b)
-    {
-        v2 r;
-        asm("add.rn.f32x2 %0, %1, %2;" : "=l"(r.d) : "l"(a.d), "l"(b.d));
-        return r;
-    }
-    __device__ __forceinline__ friend v2 operator-(v2 a, v2 b)
-    {
-        v2 r;
-        asm("sub.rn.f32x2 %0, %1, %2;" : "=l"(r.d) : "l"(a.d), "l"(b.d));
-        return r;
-    }
-    __device__ __forceinline__ friend v2 operator*(v2 a, v2 b)
-    {
-        v2 r;
-        asm("mul.rn.f32x2 %0, %1, %2;" : "=l"(r.d) : "l"(a.d), "l"(b.d));
-        return r;
-    }
-    __device__ __forceinline__ static v2 fma(v2 a, v2 b, v2 c)
-    {
-        v2 r;
-        asm("fma.rn.f32x2 %0, %1, %2, %3;" : "=l"(r.d) : "l"(a.d), "l"(b.d), "l"(c.d));
-        return r;
-    }
-};
-
 /* Lane sums of two entries at a time (even and odd entries of a batch). */
 template <bool PACKED>
 struct pair_acc2 {
     v2<PACKED> fx, fy, fz, fw;
+};
+
+/* The minimum-image constants as register pairs (the same value in both
+ * halves), so the shift of two entries is four packed instructions per axis:
+ * d - L rint(d / L) with rint done by adding and subtracting 1.5 * 2^23.
+ * The code generator may contract the packed multiply and the first add into
+ * one FMA, rounding d / L + 1.5 * 2^23 once; that changes the shift only
+ * where d / L lies within an ulp of a half-integer, i.e. |d| = L/2 to
+ * 1e-5 A, and such a pair is beyond rc (< L/2) with either shift. */
+template <bool PACKED>
+struct wrap2 {
+    v2<PACKED> li[3], nl[3], magic;
+    template <class G>
+    __device__ __forceinline__ static wrap2 make(const G &g)
+    {
+        wrap2 w;
+        for (int d = 0; d < 3; d++) {
+            w.li[d] = v2<PACKED>::make(g.Li(d), g.Li(d));
+            w.nl[d] = v2<PACKED>::make(-g.L(d), -g.L(d));
+        }
+        w.magic = v2<PACKED>::make(12582912.0f, 12582912.0f);
+        return w;
+    }
+    __device__ __forceinline__ v2<PACKED> shift(int d, v2<PACKED> x) const
+    {
+        const v2<PACKED> r = (x * li[d] + magic) - magic;
+        return v2<PACKED>::fma(nl[d], r, x);
+    }
 };
 
 /* Two pairs (i, j0) and (i, j1) at once: the operations whose operands all
@@ -222,26 +205,16 @@ struct pair_acc2 {
  * as scalar IEEE operations with the constant (no register pair to hold it).
  * The same formulas as pair_term, with every rounding step fixed. */
 template <int KIND, bool WRAP, bool PACKED, class G>
-__device__ __forceinline__ void pair_term2(const G &g, v2<PACKED> PX, v2<PACKED> PY, v2<PACKED> PZ,
-                                           float qi, float4 p0, float4 p1, float2 l0, float2 l1,
-                                           pair_acc2<PACKED> &a)
+__device__ __forceinline__ void pair_term2(const G &g, const wrap2<PACKED> &W, v2<PACKED> PX, v2<PACKED> PY,
+                                           v2<PACKED> PZ, float qi, float4 p0, float4 p1, float2 l0,
+                                           float2 l1, pair_acc2<PACKED> &a)
 {
     typedef v2<PACKED> V;
     V dx = PX - V::make(p0.x, p1.x), dy = PY - V::make(p0.y, p1.y), dz = PZ - V::make(p0.z, p1.z);
     if (WRAP) {
-        float x0, x1, y0, y1, z0, z1;
-        dx.get(x0, x1);
-        dy.get(y0, y1);
-        dz.get(z0, z1);
-        x0 = __fmaf_rn(-g.L(0), rint_small(__fmul_rn(x0, g.Li(0))), x0);
-        x1 = __fmaf_rn(-g.L(0), rint_small(__fmul_rn(x1, g.Li(0))), x1);
-        y0 = __fmaf_rn(-g.L(1), rint_small(__fmul_rn(y0, g.Li(1))), y0);
-        y1 = __fmaf_rn(-g.L(1), rint_small(__fmul_rn(y1, g.Li(1))), y1);
-        z0 = __fmaf_rn(-g.L(2), rint_small(__fmul_rn(z0, g.Li(2))), z0);
-        z1 = __fmaf_rn(-g.L(2), rint_small(__fmul_rn(z1, g.Li(2))), z1);
-        dx = V::make(x0, x1);
-        dy = V::make(y0, y1);
-        dz = V::make(z0, z1);
+        dx = W.shift(0, dx);
+        dy = W.shift(1, dy);
+        dz = W.shift(2, dz);
     }
     const V rsq = V::fma(dz, dz, V::fma(dy, dy, dx * dx));
     float s0, s1;
@@ -319,6 +292,8 @@ __device__ __forceinline__ void pair_loop(const G &g, float4 pi, float qi, int n
     const V PX = V::make(pi.x, pi.x), PY = V::make(pi.y, pi.y), PZ = V::make(pi.z, pi.z);
     const V zero = V::make(0.0f, 0.0f);
     pair_acc2<true> acc2 = {zero, zero, zero, zero};
+    wrap2<true> W;
+    if (PACK && WRAP) W = wrap2<true>::make(g);
 #pragma unroll
     for (int b = 0; b < B; b++) e0[b] = __ldg(lp + b * TPA);
 #pragma unroll
@@ -342,7 +317,7 @@ __device__ __forceinline__ void pair_loop(const G &g, float4 pi, float qi, int n
         if (PACK && !ENERGY && B % 2 == 0) {
 #pragma unroll
             for (int b = 0; b < B; b += 2)
-                pair_term2<KIND, WRAP, true>(g, PX, PY, PZ, qi, p0[b], p0[b + 1], ljrow[e0[b] >> MD_TYPE_SHIFT],
+                pair_term2<KIND, WRAP, true>(g, W, PX, PY, PZ, qi, p0[b], p0[b + 1], ljrow[e0[b] >> MD_TYPE_SHIFT],
                                              ljrow[e0[b + 1] >> MD_TYPE_SHIFT], acc2);
         } else {
 #pragma unroll

@@ -293,6 +293,55 @@ def test_list_rebuilds_keep_parity():
     assert np.array_equal(gu.rows_canonical(nn, nm, n, 512), gu.rows_canonical(onn, onm, n, 512))
 
 
+def _tie_lattice(seed, jitter=4e-6):
+    """Simple-cubic lattice of spacing rl/5 (8000 sites, box 4 rl): every site
+    has 30 lattice neighbours at exactly rl (vectors (5,0,0) and (3,4,0)
+    and their permutations), and the jitter of a few ulps puts the FP32 r^2
+    of each such pair within a few ulps of rl^2 on either side."""
+    s = synth.nacl_rocksalt(ncell=5, seed=seed, nmaxlist=640)
+    a, m = 13.0 / 5.0, 20
+    g = np.stack(np.meshgrid(*[np.arange(m)] * 3, indexing="ij"), -1).reshape(-1, 3)
+    L = a * m
+    rng = np.random.default_rng(seed)
+    s.box = np.full(3, L)
+    s.pos = g * a - 0.5 * L + 0.3 + rng.uniform(-jitter, jitter, g.shape)
+    s.itype = np.where(g.sum(1) % 2 == 0, 1, 2).astype(np.int64)
+    s.charge = np.where(s.itype == 1, 1.0, -1.0)
+    s.vel = np.zeros_like(s.pos)
+    return s
+
+
+@pytest.mark.parametrize("list_tpa", [0, 8])
+def test_list_threshold_ties(list_tpa):
+    """Pairs whose FP32 r^2 lies within a few ulps of (rc + skin)^2 (30 per
+    atom here): the list predicate rounds every operation exactly as the
+    reference writes it, so the list equals the oracle's bit for bit, for the
+    list built at creation and for a rebuild after new positions."""
+    case = oracle.load(_write(_tie_lattice(seed=3)))
+    assert case.params.skin == 1.0 and np.float32(case.params.rcutsq) == np.float32(144.0)
+    p = case.params
+    n = case.natom
+    with gu.system_from_case(case) as sim:
+        sim.set_tuning(8, list_tpa)
+        sim.update_neighbors(force=True)
+        nn, nm = sim.neighbor_list(640)
+        orc = gu.oracle_state(case)
+        assert np.array_equal(nm[:n], orc["nm"][:n])
+        assert np.array_equal(gu.rows_canonical(nn, nm, n, 640), gu.rows_canonical(orc["nn"], orc["nm"], n, 640))
+        # 484 lattice neighbours lie strictly inside rl; of the 30 ties about
+        # half are in, so the ties are really decided by rounding
+        assert (484 + 6) * n < int(orc["nm"][:n].sum()) < (484 + 24) * n
+        x2 = _tie_lattice(seed=4).pos
+        sim.set_positions(x2)
+        sim.update_neighbors(force=True)
+        nn, nm = sim.neighbor_list(640)
+    pos4 = case.pos4().copy()
+    pos4[:, :3] = x2.astype(np.float32)
+    onn, onm, _ = oracle.nlist(pos4, case.box, case.boxi, oracle.rskinsq(p.skin, p.rcutsq),
+                               oracle.exclusions(n, case.bonds), 640)
+    assert np.array_equal(gu.rows_canonical(nn, nm, n, 640), gu.rows_canonical(onn, onm, n, 640))
+
+
 @pytest.mark.parametrize("pair_tpa,list_tpa,depth", [(1, 1, 0), (2, 0, 0), (4, 4, 4), (8, 8, 0),
                                                      (8, 0, 2), (16, 0, 0), (16, 16, 1), (32, 32, 0)])
 def test_thread_split_variants(pair_tpa, list_tpa, depth):
