@@ -549,7 +549,7 @@ __global__ void __launch_bounds__(256) k_build_list(
  * its list.  Entries land in the
  * same order as in k_build_list (stencil cells in traversal order, ascending
  * j), so both builders produce identical lists. */
-constexpr int CW_WARPS = 4;
+constexpr int CW_WARPS = 8;   /* warps per block (fewer blocks: fewer grid-barrier arrivals) */
 constexpr int CW_MAXI = 32;
 constexpr int CW_MAXST = 128;
 

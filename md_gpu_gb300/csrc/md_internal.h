@@ -60,8 +60,11 @@ struct md_devstate {
     unsigned blocks_done; /* blocks finished in the current reduction kernel */
     unsigned long long acc[3]; /* fixed-point KE (MD_KFIX), PE, sum ff r^2 (MD_EFIX) of the step */
     int cell_next;       /* next cell a list-building warp takes (reset after each build) */
-    unsigned bar_count;  /* grid barrier of the one-kernel rebuild: arrivals, */
-    unsigned bar_gen;    /* and generation */
+    /* grid barrier of the one-kernel rebuild: arrivals and generation, each
+     * on its own 128-byte line, so that the waiting blocks' polls of the
+     * generation do not contend with the arrivals' atomics */
+    alignas(128) unsigned bar_count;
+    alignas(128) unsigned bar_gen;
 };
 
 /* Everything a kernel needs about the system, passed by value. */
