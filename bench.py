@@ -60,7 +60,9 @@ def rank_info():
 
 
 class Clocks:
-    """nvidia-smi sampled every 200 ms while the timed region runs."""
+    """nvidia-smi sampled every 50 ms while the timed region runs (entering
+    waits, at most 3 s, for the sampler's first line, so that its start-up
+    does not fall into the timed region)."""
 
     def __init__(self, index):
         self.index = index
@@ -76,10 +78,14 @@ class Clocks:
         try:
             self.fh = open(self.path, "w")
             self.proc = subprocess.Popen(["nvidia-smi", f"--id={self.index}", f"--query-gpu={q}",
-                                          "--format=csv,noheader,nounits", "-lms", "200"],
+                                          "--format=csv,noheader,nounits", "-lms", "50"],
                                          stdout=self.fh, stderr=subprocess.DEVNULL)
         except OSError:
             self.proc = None
+            return self
+        t0 = time.time()
+        while time.time() - t0 < 3.0 and self.proc.poll() is None and os.path.getsize(self.path) == 0:
+            time.sleep(0.02)
         return self
 
     def __exit__(self, *a):

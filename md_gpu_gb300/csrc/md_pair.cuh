@@ -121,19 +121,42 @@ __device__ __forceinline__ geom_reg rep_geom(const md_rep &R, bool centered = fa
     return g;
 }
 
+/* The x and y minimum-image constants of one entry as register pairs:
+ * (1/Lx, 1/Ly), (-Lx, -Ly) and 1.5 * 2^23 in both halves. */
+struct wrapxy {
+    v2<true> li, nl, magic;
+    template <class G>
+    __device__ __forceinline__ static wrapxy make(const G &g)
+    {
+        wrapxy w;
+        w.li = v2<true>::make(g.Li(0), g.Li(1));
+        w.nl = v2<true>::make(-g.L(0), -g.L(1));
+        w.magic = v2<true>::make(12582912.0f, 12582912.0f);
+        return w;
+    }
+};
+
 /* One pair: F_i += ff d, w_i += ff r^2 (pair_forces.cu:165-200 / :74-120).
- * WRAP = false skips the minimum-image shift, which is then zero for every
- * pair inside rc (atom i at least rc from each face: see interior()). */
+ * x and y of the difference and of its minimum-image shift go through
+ * packed f32x2 instructions (PXY = (x_i, y_i); x_j, y_j are the low half of
+ * the loaded float4), z through scalar ones; each half rounds as the scalar
+ * form (the shift's multiply and add may be contracted, which matters only
+ * for |d| = L/2, beyond rc).  WRAP = false skips the minimum-image shift,
+ * which is then zero for every pair inside rc (atom i at least rc from each
+ * face: see interior()). */
 template <int KIND, bool ENERGY, bool WRAP = true, class G>
-__device__ __forceinline__ void pair_term(const G &g, float4 pi, float qi, float4 pj, float2 l,
-                                          bool valid, pair_acc &a)
+__device__ __forceinline__ void pair_term(const G &g, const wrapxy &W, v2<true> PXY, float4 pi, float qi,
+                                          float4 pj, float2 l, bool valid, pair_acc &a)
 {
-    float dx = pi.x - pj.x, dy = pi.y - pj.y, dz = pi.z - pj.z;
+    typedef v2<true> V;
+    V dxy = PXY - V::make(pj.x, pj.y);
+    float dz = pi.z - pj.z;
     if (WRAP) {
-        dx -= g.L(0) * rint_small(dx * g.Li(0));
-        dy -= g.L(1) * rint_small(dy * g.Li(1));
+        dxy = V::fma(W.nl, (dxy * W.li + W.magic) - W.magic, dxy);
         dz -= g.L(2) * rint_small(dz * g.Li(2));
     }
+    float dx, dy;
+    dxy.get(dx, dy);
     float rsq = dx * dx + dy * dy + dz * dz;
     float ri = rsqrt_approx(rsq);
     float ri2 = ri * ri;
@@ -294,6 +317,9 @@ __device__ __forceinline__ void pair_loop(const G &g, float4 pi, float qi, int n
     pair_acc2<true> acc2 = {zero, zero, zero, zero};
     wrap2<true> W;
     if (PACK && WRAP) W = wrap2<true>::make(g);
+    const V PXY = V::make(pi.x, pi.y);
+    wrapxy WXY;
+    if (!(PACK && !ENERGY && B % 2 == 0) && WRAP) WXY = wrapxy::make(g);
 #pragma unroll
     for (int b = 0; b < B; b++) e0[b] = __ldg(lp + b * TPA);
 #pragma unroll
@@ -322,7 +348,8 @@ __device__ __forceinline__ void pair_loop(const G &g, float4 pi, float qi, int n
         } else {
 #pragma unroll
             for (int b = 0; b < B; b++)
-                pair_term<KIND, ENERGY, WRAP>(g, pi, qi, p0[b], ljrow[e0[b] >> MD_TYPE_SHIFT], true, acc);
+                pair_term<KIND, ENERGY, WRAP>(g, WXY, PXY, pi, qi, p0[b], ljrow[e0[b] >> MD_TYPE_SHIFT], true,
+                                              acc);
         }
 #pragma unroll
         for (int b = 0; b < B; b++) {
