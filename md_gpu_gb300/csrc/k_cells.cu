@@ -921,10 +921,36 @@ __device__ __forceinline__ void grid_barrier(md_devstate *st)
     __syncthreads();
 }
 
+/* The order in which the list-building warps take the cells: most atoms
+ * first (a counting sort of the cell ranks by atom count, counts above 63
+ * together), so that the last cells handed out are the cheapest and the
+ * warps finish close together.  Which warp builds a cell does not change
+ * the cell's rows, so the order within a count may vary.  One block. */
+__device__ __forceinline__ void work_order(int ncells, const int *cell_start, int *cell_work)
+{
+    __shared__ int s_at[64];
+    if (threadIdx.x < 64) s_at[threadIdx.x] = 0;
+    __syncthreads();
+    for (int c = threadIdx.x; c < ncells; c += blockDim.x)
+        atomicAdd(&s_at[min(cell_start[c + 1] - cell_start[c], 63)], 1);
+    __syncthreads();
+    if (threadIdx.x == 0) {
+        int run = 0;
+        for (int m = 63; m >= 0; m--) {
+            const int h = s_at[m];
+            s_at[m] = run;
+            run += h;
+        }
+    }
+    __syncthreads();
+    for (int c = threadIdx.x; c < ncells; c += blockDim.x)
+        cell_work[atomicAdd(&s_at[min(cell_start[c + 1] - cell_start[c], 63)], 1)] = c;
+}
+
 /* The arrays the rebuild passes touch. */
 struct rb_ptrs {
     const int *cell_rank, *cell_lin;
-    int *key, *cell_count, *cell_start, *cell_fill, *src;
+    int *key, *cell_count, *cell_start, *cell_fill, *cell_work, *src;
     double *x, *v, *mass, *kick, *tmp_d;
     float4 *pos4, *tmp4, *pos_old;
     int *perm, *iperm, *type, *tmp_i;
@@ -963,6 +989,7 @@ __global__ void __launch_bounds__(CW_WARPS * 32) k_rebuild_coop(md_kparams kp, m
             p.cell_start[p.ncells] = total;
             st->builds += 1;
         }
+        work_order(p.ncells, p.cell_start, p.cell_work);
     }
     grid_barrier(st);
     for (int i = tid; i < n; i += nth) {
@@ -1003,6 +1030,7 @@ __global__ void __launch_bounds__(CW_WARPS * 32) k_rebuild_coop(md_kparams kp, m
             if (lane == 0) r = atomicAdd(&st->cell_next, 1);
             r = __shfl_sync(0xffffffffu, r, 0);
             if (r >= p.ncells) break;
+            r = p.cell_work[r];
             build_cell<false>(r, kp, st, bpos, btype, p.excl_s, p.cell_rank, p.cell_lin, p.cell_start,
                               p.type_mask, p.nl, p.nl_n, p.pos_old, nullptr, nullptr, nullptr);
         }
@@ -1087,6 +1115,7 @@ void launch_rebuild(md_ctx *c, const md_kparams &kp, bool unconditional, bool al
         p.cell_count = c->cell_count;
         p.cell_start = c->cell_start;
         p.cell_fill = c->cell_fill;
+        p.cell_work = c->cell_work;
         p.src = c->src;
         p.x = c->x;
         p.v = c->v;

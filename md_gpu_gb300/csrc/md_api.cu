@@ -249,7 +249,7 @@ void free_device(md_ctx *c)
 {
     void *ptrs[] = {c->x, c->v, c->mass, c->kick, c->pos4, c->pos4_alt, c->pos_old, c->type, c->perm, c->iperm, c->f,
                     c->vir, c->epot, c->nl, c->nl_n, c->excl_orig, c->excl_s, c->cell_rank, c->cell_lin,
-                    c->cell_count, c->cell_start, c->cell_fill, c->key, c->src, c->tmp_d, c->tmp4,
+                    c->cell_count, c->cell_start, c->cell_fill, c->cell_work, c->key, c->src, c->tmp_d, c->tmp4,
                     c->tmp_i, c->bl_o, c->bl_on, c->al_o, c->al_on, c->bl_s, c->bl_sn, c->al_s,
                     c->al_sn, c->st, c->rec, c->lj_dev, c->bonded_par,
                     c->type_mask_dev, c->io_dev, c->reps_dev, c->repst, c->arep, c->crep,
@@ -553,7 +553,7 @@ md_status setup_device(md_ctx *c, void *stream, host_stage &h, md_ctx **out)
     MD_ALLOC(c->nl_n, P);
     MD_ALLOC(c->excl_orig, P); MD_ALLOC(c->excl_s, P);
     MD_ALLOC(c->cell_rank, c->ncells); MD_ALLOC(c->cell_lin, c->ncells); MD_ALLOC(c->cell_count, c->ncells);
-    MD_ALLOC(c->cell_start, c->ncells + 1); MD_ALLOC(c->cell_fill, c->ncells);
+    MD_ALLOC(c->cell_start, c->ncells + 1); MD_ALLOC(c->cell_fill, c->ncells); MD_ALLOC(c->cell_work, c->ncells);
     MD_ALLOC(c->key, P); MD_ALLOC(c->src, P);
     MD_ALLOC(c->tmp_d, 8 * P); MD_ALLOC(c->tmp4, P); MD_ALLOC(c->tmp_i, 3 * P);
     MD_ALLOC(c->bl_o, 4 * P); MD_ALLOC(c->bl_on, P); MD_ALLOC(c->al_o, 4 * P); MD_ALLOC(c->al_on, P);

@@ -178,6 +178,7 @@ struct md_ctx {
     uint4 *excl_orig = nullptr, *excl_s = nullptr;
     int *cell_rank = nullptr, *cell_count = nullptr, *cell_start = nullptr, *cell_fill = nullptr;
     int *cell_lin = nullptr;                              /* rank -> linear cell index */
+    int *cell_work = nullptr;                             /* cell ranks, most atoms first (list-build order) */
     int *key = nullptr, *src = nullptr;
     double *tmp_d = nullptr;                              /* 8*pitch scratch for permutation */
     float4 *tmp4 = nullptr;
