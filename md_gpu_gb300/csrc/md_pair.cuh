@@ -303,7 +303,7 @@ __device__ __forceinline__ bool interior(const G &g, float4 pi)
  * t is computed, the positions of batch t+1 and the list entries of batch
  * t+2 are in flight.  ljrow may point into shared memory (a batch's
  * per-replica table): plain loads there, not the read-only global path. */
-template <int KIND, int TPA, int B, bool ENERGY, bool WRAP, bool PACK, class G>
+template <int KIND, int TPA, int B, bool ENERGY, bool WRAP, bool PACK, int UNROLL, class G>
 __device__ __forceinline__ void pair_loop(const G &g, float4 pi, float qi, int nb,
                                           const unsigned *__restrict__ lp,
                                           const float4 *__restrict__ pos4, const float2 *ljrow,
@@ -328,9 +328,6 @@ __device__ __forceinline__ void pair_loop(const G &g, float4 pi, float qi, int n
 #pragma unroll
         for (int b = 0; b < B; b++) e1[b] = __ldg(lp + (B + b) * TPA);
     }
-    /* the packed loop runs fastest rolled (measured: 43 against 46 us per
-     * launch on 64000 ions), the scalar one unrolled twice */
-    constexpr int UNROLL = (PACK && !ENERGY && B % 2 == 0) ? 1 : 2;
 #pragma unroll UNROLL
     for (int t = 0; t < nb; t++) {
         float4 p1[B];
@@ -384,7 +381,7 @@ __device__ __forceinline__ void pair_loop(const G &g, float4 pi, float qi, int n
  * FP32 and converts its sum to int64 once; lane sums are combined with
  * integer shuffles (exact), so the result depends only on TPA.  Every lane of
  * the warp must call this (the shuffles use the full mask). */
-template <int KIND, int TPA, int B, bool ENERGY, bool PACK = true, class G>
+template <int KIND, int TPA, int B, bool ENERGY, bool PACK = true, int UNROLL = 0, class G>
 __device__ __forceinline__ pair_total pair_sum(const G &g, int cap, int ii, bool active, int lane,
                                                const float4 *__restrict__ pos4,
                                                const int *__restrict__ type,
@@ -400,11 +397,15 @@ __device__ __forceinline__ pair_total pair_sum(const G &g, int cap, int ii, bool
     pair_acc acc = {0.0f, 0.0f, 0.0f, 0.0f, 0.0f};
     const unsigned *lp = nl + (size_t)ii * cap + lane;
     const bool inner = g.centered() && __all_sync(0xffffffffu, !active || interior(g, pi));
+    /* unrolling of the batch loop (0: the packed loop rolled, which measured
+     * fastest for a single system, 43 against 46 us per launch on 64000
+     * ions; the scalar one twice) */
+    constexpr int UNR = UNROLL ? UNROLL : ((PACK && !ENERGY && B % 2 == 0) ? 1 : 2);
     if (nb > 0) {
         if (inner)
-            pair_loop<KIND, TPA, B, ENERGY, false, PACK>(g, pi, qi, nb, lp, pos4, ljrow, acc);
+            pair_loop<KIND, TPA, B, ENERGY, false, PACK, UNR>(g, pi, qi, nb, lp, pos4, ljrow, acc);
         else
-            pair_loop<KIND, TPA, B, ENERGY, true, PACK>(g, pi, qi, nb, lp, pos4, ljrow, acc);
+            pair_loop<KIND, TPA, B, ENERGY, true, PACK, UNR>(g, pi, qi, nb, lp, pos4, ljrow, acc);
     }
     pair_total r;
     r.fx = __float2ll_rn(acc.fx * 4294967296.0f);
