@@ -19,7 +19,7 @@
  * vector), f_0 = 1; J = dF/dx is symmetric, for a pair potential
  *   (J w)_i = sum_j [ff (w_i - w_j) + g (d.(w_i - w_j)) d],  g = (dff/dr)/r.
  * The pair terms differentiate the force law the dynamics use (A&S 7.1.26
- * erfc included), in FP32; the adjoint state P, u is FP64 in the original
+ * erfc included), in FP32, and so do the harmonic bonds and angles; the adjoint state P, u is FP64 in the original
  * atom order, and every sum is taken in a fixed order (block slots, then
  * replicas), so the gradient is deterministic.
  *
@@ -258,6 +258,104 @@ __global__ void k_adj_acc(int n, int pitch, const int *__restrict__ perm, const 
     if (s >= n) return;
     const size_t o = 3 * (size_t)perm[s];
     for (int d = 0; d < 3; d++) Pv[o + d] += G[(size_t)d * pitch + s];
+}
+
+/* The bonded part of one frame's adjoint force, added to G after the pair
+ * kernel: per sorted atom s, G_s += (J_b w)_s - wpe F_b,s for the harmonic
+ * bonds and angles of k_bonded (bonded_forces.cu:34-193 as the dynamics
+ * evaluate them, rsqrtf and acosf included).  (J_b w)_s is the derivative of
+ * F_b,s along w: the same expressions carried with their first-order
+ * variations (the minimum-image shift is constant; the clamp of cos(theta)
+ * has zero variation where it clamps).  One thread per atom. */
+__device__ __forceinline__ void adj_min_image(float &x, float &y, float &z, const float *L, const float *Li)
+{
+    x -= L[0] * rintf(x * Li[0]);
+    y -= L[1] * rintf(y * Li[1]);
+    z -= L[2] * rintf(z * Li[2]);
+}
+
+__global__ void k_adj_bonded(int n, int pitch, adj_par ap, const md_rep *__restrict__ reps,
+                             const int *__restrict__ arep, const float4 *__restrict__ pos4,
+                             const float4 *__restrict__ w4, const int2 *__restrict__ bl_s,
+                             const int *__restrict__ bl_sn, const int4 *__restrict__ al_s,
+                             const int *__restrict__ al_sn, const float *__restrict__ par, int has_bonds,
+                             int has_angles, double *G)
+{
+    const int s = blockIdx.x * blockDim.x + threadIdx.x;
+    if (s >= n) return;
+    const int nb = has_bonds ? bl_sn[s] : 0, na = has_angles ? al_sn[s] : 0;
+    if (nb == 0 && na == 0) return;
+    const md_rep &R = reps[arep[s]];
+    const float wpe = ap.wpe_k / (float)R.natom;
+    const float *bnd1 = par, *bnd2 = par + MD_MAXTYPE, *ang1 = par + 2 * MD_MAXTYPE,
+                *ang2 = par + 3 * MD_MAXTYPE;
+    const float4 zero = make_float4(0.f, 0.f, 0.f, 0.f);
+    auto wof = [&](int k) { return ap.with_w ? w4[k] : zero; };
+    const float4 p = pos4[s], ws = wof(s);
+    float fx = 0.f, fy = 0.f, fz = 0.f, tx = 0.f, ty = 0.f, tz = 0.f;
+    for (int k = 0; k < nb; k++) {
+        const int2 b = bl_s[(size_t)k * pitch + s];
+        const float4 q = pos4[b.x], wq = wof(b.x);
+        float dx = p.x - q.x, dy = p.y - q.y, dz = p.z - q.z;
+        adj_min_image(dx, dy, dz, R.box, R.boxi);
+        const float ux = ws.x - wq.x, uy = ws.y - wq.y, uz = ws.z - wq.z;
+        const float rsq = dx * dx + dy * dy + dz * dz;
+        const float ri = rsqrtf(rsq);
+        const float kk = bnd1[b.y], r0 = bnd2[b.y];
+        const float fa = kk * (r0 * ri - 1.0f);
+        const float ri_t = -ri * ri * ri * (dx * ux + dy * uy + dz * uz);
+        const float fa_t = kk * r0 * ri_t;
+        fx += fa * dx; fy += fa * dy; fz += fa * dz;
+        tx += fa_t * dx + fa * ux; ty += fa_t * dy + fa * uy; tz += fa_t * dz + fa * uz;
+    }
+    for (int k = 0; k < na; k++) {
+        const int4 a = al_s[(size_t)k * pitch + s];
+        const float4 qb = pos4[a.z], wb = wof(a.z);
+        float4 qa, cen, wa, wc;
+        if (a.x == 1) { qa = pos4[a.y]; wa = wof(a.y); cen = p; wc = ws; }   /* this atom is the centre */
+        else { qa = p; wa = ws; cen = pos4[a.y]; wc = wof(a.y); }           /* this atom is an end */
+        float ax = qa.x - cen.x, ay = qa.y - cen.y, az = qa.z - cen.z;
+        adj_min_image(ax, ay, az, R.box, R.boxi);
+        float bx = qb.x - cen.x, by = qb.y - cen.y, bz = qb.z - cen.z;
+        adj_min_image(bx, by, bz, R.box, R.boxi);
+        const float tax = wa.x - wc.x, tay = wa.y - wc.y, taz = wa.z - wc.z;
+        const float tbx = wb.x - wc.x, tby = wb.y - wc.y, tbz = wb.z - wc.z;
+        const float ai = rsqrtf(ax * ax + ay * ay + az * az);
+        const float bi = rsqrtf(bx * bx + by * by + bz * bz);
+        const float ai_t = -ai * ai * ai * (ax * tax + ay * tay + az * taz);
+        const float bi_t = -bi * bi * bi * (bx * tbx + by * tby + bz * tbz);
+        const float ab = ax * bx + ay * by + az * bz;
+        const float ab_t = tax * bx + tay * by + taz * bz + ax * tbx + ay * tby + az * tbz;
+        const float c0 = ab * ai * bi;
+        const float cang = fminf(fmaxf(c0, -0.9999999f), 0.9999999f);
+        const float c_t = cang == c0 ? ab_t * ai * bi + ab * ai_t * bi + ab * ai * bi_t : 0.0f;
+        const float th = acosf(cang);
+        const float s1 = rsqrtf(1.0f - cang * cang);
+        const float th_t = -c_t * s1;
+        const float s1_t = s1 * s1 * s1 * cang * c_t;
+        const float k1 = ang1[a.w], th0 = ang2[a.w];
+        const float ff = k1 * (th - th0) * s1 * ai * bi;
+        const float ff_t =
+            k1 * (th_t * s1 * ai * bi + (th - th0) * (s1_t * ai * bi + s1 * ai_t * bi + s1 * ai * bi_t));
+        const float aa = ab * ai * ai, aa_t = ab_t * ai * ai + 2.0f * ab * ai * ai_t;
+        float gx = bx - aa * ax, gy = by - aa * ay, gz = bz - aa * az;
+        float gx_t = tbx - aa_t * ax - aa * tax, gy_t = tby - aa_t * ay - aa * tay,
+              gz_t = tbz - aa_t * az - aa * taz;
+        if (a.x == 1) {
+            const float bb = ab * bi * bi, bb_t = ab_t * bi * bi + 2.0f * ab * bi * bi_t;
+            gx = bb * bx - ax - gx;
+            gy = bb * by - ay - gy;
+            gz = bb * bz - az - gz;
+            gx_t = bb_t * bx + bb * tbx - tax - gx_t;
+            gy_t = bb_t * by + bb * tby - tay - gy_t;
+            gz_t = bb_t * bz + bb * tbz - taz - gz_t;
+        }
+        fx += ff * gx; fy += ff * gy; fz += ff * gz;
+        tx += ff_t * gx + ff * gx_t; ty += ff_t * gy + ff * gy_t; tz += ff_t * gz + ff * gz_t;
+    }
+    G[s] += (double)tx - (double)(wpe * fx);
+    G[(size_t)pitch + s] += (double)ty - (double)(wpe * fy);
+    G[2 * (size_t)pitch + s] += (double)tz - (double)(wpe * fz);
 }
 
 /* The adjoint pair kernel of one frame: per atom i (ADJ_TPA lanes over its
@@ -658,6 +756,10 @@ extern "C" md_status md_adjoint_run(md_ctx *c, const md_adjoint_cfg *cfg, const 
                 k_adj_w<<<agrid, 256, 0, s>>>(n, (double)c->dt, 1, m >= 1 ? 2.0 : 1.0, c->perm, c->kick,
                                                B.U, B.P, B.w4);
             launch_back(c, ap, B.rtab, B.w4, B.G, B.part);
+            if (c->has_bonds || c->has_angles)
+                k_adj_bonded<<<agrid, 256, 0, s>>>(n, c->pitch, ap, c->reps_dev, c->arep, c->pos4, B.w4, c->bl_s,
+                                                    c->bl_sn, c->al_s, c->al_sn, c->bonded_par, c->has_bonds,
+                                                    c->has_angles, B.G);
             k_adj_param<<<(nrep * NB * 32 + 255) / 256, 256, 0, s>>>(nrep, NB, c->reps_dev, B.part, B.acc);
             k_adj_acc<<<agrid, 256, 0, s>>>(n, c->pitch, c->perm, B.G, B.P);
         }

@@ -291,6 +291,7 @@ void launch_forces_b(md_ctx *c, const md_kparams &kp, bool energy, int terms)
         cudaMemsetAsync(c->vir, 0, sizeof(float) * (size_t)c->pitch, c->stream);
         cudaMemsetAsync(c->epot, 0, sizeof(float) * (size_t)c->pitch, c->stream);
     }
+    launch_bonded(c, kp, energy, terms);
 }
 
 void launch_leapfrog_b(md_ctx *c, const md_kparams &kp, int energy, unsigned long long cond,

@@ -1256,8 +1256,9 @@ void launch_rebuild(md_ctx *c, const md_kparams &kp, bool unconditional, bool al
               (const double *)c->tmp_d, (const float4 *)c->tmp4, (const int *)c->tmp_i, c->x, c->v,
               c->mass, c->kick, c->pos4, c->perm, c->iperm, c->type, arep, (const int *)c->rep_upd);
     /* exclusions and bonded lists to re-express only with bonds or angles
-     * (a batch has neither) */
-    if (!batch && (c->has_bonds || c->has_angles))
+     * (in a batch every atom: a replica that kept its order maps to the
+     * same lists) */
+    if (c->has_bonds || c->has_angles)
         rb_launch(pdl, k_remap, dim3(nb), dim3(256), s, kp, (const md_devstate *)c->st, always,
                   (const int *)c->perm, (const int *)c->iperm, (const uint4 *)c->excl_orig, c->excl_s,
                   (const int2 *)c->bl_o, (const int *)c->bl_on, c->bl_s, c->bl_sn,

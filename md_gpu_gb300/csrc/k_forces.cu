@@ -49,20 +49,22 @@ __global__ void __launch_bounds__(128) k_pair(md_kparams kp, pair_consts pc,
     }
 }
 
-__device__ __forceinline__ void min_image(float &dx, float &dy, float &dz, const md_kparams &kp)
+__device__ __forceinline__ void min_image(float &dx, float &dy, float &dz, const float *box, const float *boxi)
 {
-    dx -= kp.box[0] * rintf(dx * kp.boxi[0]);
-    dy -= kp.box[1] * rintf(dy * kp.boxi[1]);
-    dz -= kp.box[2] * rintf(dz * kp.boxi[2]);
+    dx -= box[0] * rintf(dx * boxi[0]);
+    dy -= box[1] * rintf(dy * boxi[1]);
+    dz -= box[2] * rintf(dz * boxi[2]);
 }
 
 /* Harmonic bonds (U = k (r - r0)^2, bnd1 = 2k) and angles (U = k (th - th0)^2,
- * ang1 = 2k), one thread per sorted atom, added into the fixed-point forces. */
+ * ang1 = 2k), one thread per sorted atom, added into the fixed-point forces.
+ * In a batch (reps non-null) the minimum image uses the atom's replica box. */
 template <bool ENERGY>
 __global__ void k_bonded(md_kparams kp, const float4 *__restrict__ pos4,
                          const int2 *__restrict__ bl_s, const int *__restrict__ bl_sn,
                          const int4 *__restrict__ al_s, const int *__restrict__ al_sn,
                          const float *__restrict__ par, int has_bonds, int has_angles,
+                         const md_rep *__restrict__ reps, const int *__restrict__ arep,
                          long long *f, float *vir, float *epot)
 {
     int s = blockIdx.x * blockDim.x + threadIdx.x;
@@ -71,6 +73,7 @@ __global__ void k_bonded(md_kparams kp, const float4 *__restrict__ pos4,
     int nb = has_bonds ? bl_sn[s] : 0;
     int na = has_angles ? al_sn[s] : 0;
     if (nb == 0 && na == 0) return;
+    const float *box = reps ? reps[arep[s]].box : kp.box, *boxi = reps ? reps[arep[s]].boxi : kp.boxi;
     const float *bnd1 = par, *bnd2 = par + MD_MAXTYPE, *ang1 = par + 2 * MD_MAXTYPE,
                 *ang2 = par + 3 * MD_MAXTYPE;
     float4 p = pos4[s];
@@ -79,7 +82,7 @@ __global__ void k_bonded(md_kparams kp, const float4 *__restrict__ pos4,
         int2 b = bl_s[k * P + s];
         float4 q = pos4[b.x];
         float dx = p.x - q.x, dy = p.y - q.y, dz = p.z - q.z;
-        min_image(dx, dy, dz, kp);
+        min_image(dx, dy, dz, box, boxi);
         float rsq = dx * dx + dy * dy + dz * dz;
         float ri = rsqrtf(rsq);
         float kk = bnd1[b.y], r0 = bnd2[b.y];
@@ -95,9 +98,9 @@ __global__ void k_bonded(md_kparams kp, const float4 *__restrict__ pos4,
         if (a.x == 1) { qa = pos4[a.y]; cen = p; }   /* this atom is the centre */
         else { qa = p; cen = pos4[a.y]; }           /* this atom is an end */
         float ax = qa.x - cen.x, ay = qa.y - cen.y, az = qa.z - cen.z;
-        min_image(ax, ay, az, kp);
+        min_image(ax, ay, az, box, boxi);
         float bx = qb.x - cen.x, by = qb.y - cen.y, bz = qb.z - cen.z;
-        min_image(bx, by, bz, kp);
+        min_image(bx, by, bz, box, boxi);
         float ai = rsqrtf(ax * ax + ay * ay + az * az);
         float bi = rsqrtf(bx * bx + by * by + bz * bz);
         float ab = ax * bx + ay * by + az * bz;
@@ -173,17 +176,24 @@ void launch_forces(md_ctx *c, const md_kparams &kp, bool energy, int terms)
         cudaMemsetAsync(c->vir, 0, sizeof(float) * (size_t)c->pitch, c->stream);
         cudaMemsetAsync(c->epot, 0, sizeof(float) * (size_t)c->pitch, c->stream);
     }
+    launch_bonded(c, kp, energy, terms);
+}
+
+void launch_bonded(md_ctx *c, const md_kparams &kp, bool energy, int terms)
+{
     int hb = (terms & MD_TERM_BOND) ? c->has_bonds : 0;
     int ha = (terms & MD_TERM_ANGLE) ? c->has_angles : 0;
     if (hb || ha) {
         int nb = (kp.n + 255) / 256;
+        const md_rep *reps = c->batch ? c->reps_dev : nullptr;
+        const int *arep = c->batch ? c->arep : nullptr;
         if (energy)
             k_bonded<true><<<nb, 256, 0, c->stream>>>(kp, c->pos4, c->bl_s, c->bl_sn, c->al_s,
-                                                       c->al_sn, c->bonded_par, hb, ha,
+                                                       c->al_sn, c->bonded_par, hb, ha, reps, arep,
                                                        c->f, c->vir, c->epot);
         else
             k_bonded<false><<<nb, 256, 0, c->stream>>>(kp, c->pos4, c->bl_s, c->bl_sn, c->al_s,
-                                                        c->al_sn, c->bonded_par, hb, ha,
+                                                        c->al_sn, c->bonded_par, hb, ha, reps, arep,
                                                         c->f, c->vir, c->epot);
     }
 }

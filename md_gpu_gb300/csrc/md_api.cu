@@ -495,7 +495,7 @@ struct host_stage {
     std::vector<int> type;
     std::vector<uint4> excl;
     std::vector<int> cell_rank, cell_lin;
-    std::vector<int2> blo;      /* bonded lists (empty for batches) */
+    std::vector<int2> blo;      /* bonded lists (empty without bonds or angles) */
     std::vector<int> blon;
     std::vector<int4> alo;
     std::vector<int> alon;
@@ -605,9 +605,9 @@ md_status setup_device(md_ctx *c, void *stream, host_stage &h, md_ctx **out)
     up(c->perm, hperm.data(), sizeof(int) * P);
     up(c->iperm, hperm.data(), sizeof(int) * P);
     up(c->excl_orig, h.excl.data(), sizeof(uint4) * P);
-    /* without bonds there are no exclusions to remap (batches never have
-     * bonds): the sorted copy, all empty, is set once */
-    if (batch || !c->has_bonds) up(c->excl_s, h.excl.data(), sizeof(uint4) * P);
+    /* without bonds there are no exclusions to remap: the sorted copy, all
+     * empty, is set once */
+    if (!c->has_bonds) up(c->excl_s, h.excl.data(), sizeof(uint4) * P);
     up(c->cell_rank, h.cell_rank.data(), sizeof(int) * c->ncells);
     up(c->cell_lin, h.cell_lin.data(), sizeof(int) * c->ncells);
     up(c->cell_count, zeros.data(), sizeof(int) * c->ncells);
@@ -753,6 +753,59 @@ md_status md_last_error(const md_ctx *ctx, char *buf, int len)
     return MD_OK;
 }
 
+/* Exclusions with the reference's slot rule and the per-atom bonded lists
+ * of c->bonds / c->angles (n atoms, indices in the context's atom space);
+ * sets has_bonds / has_angles.  Errors leave c to the caller. */
+md_status bonded_lists(md_ctx *c, int n, std::vector<int2> &blo, std::vector<int> &blon,
+                       std::vector<int4> &alo, std::vector<int> &alon)
+{
+    /* exclusions with the reference's slot rule (neighborlist.cu:64-97) */
+    c->excl_host.assign(4 * (size_t)n, MD_EXCL_NONE);
+    for (size_t b = 0; b < c->bonds.size() / 3; b++) {
+        unsigned i = (unsigned)c->bonds[3 * b + 1], j = (unsigned)c->bonds[3 * b + 2];
+        if (i >= (unsigned)n || j >= (unsigned)n) {
+            return fail(c, MD_ERR_ARG, "bond atom out of range");
+        }
+        unsigned *ei = &c->excl_host[4 * i], *ej = &c->excl_host[4 * j];
+        auto empty = [](unsigned v) { return v == MD_EXCL_NONE; };
+        if (empty(ei[0])) ei[0] = j;
+        else if (empty(ei[1])) ei[1] = j;
+        else if (empty(ei[2])) ei[2] = j;
+        else if (empty(ei[3])) ei[3] = j;
+        if (empty(ej[0])) ej[0] = i;
+        else if (empty(ei[1])) ej[1] = i;
+        else if (empty(ei[2])) ej[2] = i;
+        else if (empty(ei[3])) ej[3] = i;
+    }
+    /* original-space bonded lists (forces.cu:118-173), at most four per atom */
+    blo.assign(4 * (size_t)n, make_int2(0, 0));
+    blon.assign(n, 0);
+    alo.assign(4 * (size_t)n, make_int4(0, 0, 0, 0));
+    alon.assign(n, 0);
+    for (size_t b = 0; b < c->bonds.size() / 3; b++) {
+        int t = c->bonds[3 * b], i = c->bonds[3 * b + 1], j = c->bonds[3 * b + 2];
+        if (blon[i] >= 4 || blon[j] >= 4) {
+            return fail(c, MD_ERR_BONDED, "more than four bonds on an atom");
+        }
+        blo[4 * i + blon[i]++] = make_int2(j, t);
+        blo[4 * j + blon[j]++] = make_int2(i, t);
+    }
+    for (size_t a = 0; a < c->angles.size() / 4; a++) {
+        int t = c->angles[4 * a], i = c->angles[4 * a + 1], j = c->angles[4 * a + 2],
+            k = c->angles[4 * a + 3];
+        if (i < 0 || j < 0 || k < 0 || i >= n || j >= n || k >= n || alon[i] >= 4 || alon[j] >= 4 ||
+            alon[k] >= 4) {
+            return fail(c, MD_ERR_BONDED, "more than four angles on an atom (or bad index)");
+        }
+        alo[4 * i + alon[i]++] = make_int4(0, j, k, t);
+        alo[4 * j + alon[j]++] = make_int4(1, i, k, t);
+        alo[4 * k + alon[k]++] = make_int4(0, j, i, t);
+    }
+    c->has_bonds = c->bonds.empty() ? 0 : 1;
+    c->has_angles = c->angles.empty() ? 0 : 1;
+    return MD_OK;
+}
+
 md_status md_create(const md_system_desc *d, void *stream, md_ctx **out)
 {
     if (!d || !out || d->natom <= 0 || d->ntype < 1 || d->ntype > MD_MAXTYPE || !d->itype ||
@@ -821,53 +874,16 @@ md_status md_create(const md_system_desc *d, void *stream, md_ctx **out)
     if (d->nbonds > 0) c->bonds.assign(d->bonds, d->bonds + 3 * (size_t)d->nbonds);
     if (d->nangle > 0) c->angles.assign(d->angles, d->angles + 4 * (size_t)d->nangle);
 
-    /* exclusions with the reference's slot rule (neighborlist.cu:64-97) */
-    c->excl_host.assign(4 * (size_t)n, MD_EXCL_NONE);
-    for (size_t b = 0; b < c->bonds.size() / 3; b++) {
-        unsigned i = (unsigned)c->bonds[3 * b + 1], j = (unsigned)c->bonds[3 * b + 2];
-        if (i >= (unsigned)n || j >= (unsigned)n) {
-            md_status s = fail(c, MD_ERR_ARG, "bond atom out of range");
+    std::vector<int2> blo;
+    std::vector<int> blon;
+    std::vector<int4> alo;
+    std::vector<int> alon;
+    {
+        md_status bs = bonded_lists(c, n, blo, blon, alo, alon);
+        if (bs != MD_OK) {
             delete c;
-            return s;
+            return bs;
         }
-        unsigned *ei = &c->excl_host[4 * i], *ej = &c->excl_host[4 * j];
-        auto empty = [](unsigned v) { return v == MD_EXCL_NONE; };
-        if (empty(ei[0])) ei[0] = j;
-        else if (empty(ei[1])) ei[1] = j;
-        else if (empty(ei[2])) ei[2] = j;
-        else if (empty(ei[3])) ei[3] = j;
-        if (empty(ej[0])) ej[0] = i;
-        else if (empty(ei[1])) ej[1] = i;
-        else if (empty(ei[2])) ej[2] = i;
-        else if (empty(ei[3])) ej[3] = i;
-    }
-    /* original-space bonded lists (forces.cu:118-173), at most four per atom */
-    std::vector<int2> blo(4 * (size_t)n);
-    std::vector<int> blon(n, 0);
-    std::vector<int4> alo(4 * (size_t)n);
-    std::vector<int> alon(n, 0);
-    for (size_t b = 0; b < c->bonds.size() / 3; b++) {
-        int t = c->bonds[3 * b], i = c->bonds[3 * b + 1], j = c->bonds[3 * b + 2];
-        if (blon[i] >= 4 || blon[j] >= 4) {
-            md_status s = fail(c, MD_ERR_BONDED, "more than four bonds on an atom");
-            delete c;
-            return s;
-        }
-        blo[4 * i + blon[i]++] = make_int2(j, t);
-        blo[4 * j + blon[j]++] = make_int2(i, t);
-    }
-    for (size_t a = 0; a < c->angles.size() / 4; a++) {
-        int t = c->angles[4 * a], i = c->angles[4 * a + 1], j = c->angles[4 * a + 2],
-            k = c->angles[4 * a + 3];
-        if (i < 0 || j < 0 || k < 0 || i >= n || j >= n || k >= n || alon[i] >= 4 || alon[j] >= 4 ||
-            alon[k] >= 4) {
-            md_status s = fail(c, MD_ERR_BONDED, "more than four angles on an atom (or bad index)");
-            delete c;
-            return s;
-        }
-        alo[4 * i + alon[i]++] = make_int4(0, j, k, t);
-        alo[4 * j + alon[j]++] = make_int4(1, i, k, t);
-        alo[4 * k + alon[k]++] = make_int4(0, j, i, t);
     }
     c->has_bonds = c->bonds.empty() ? 0 : 1;
     c->has_angles = c->angles.empty() ? 0 : 1;
@@ -930,8 +946,22 @@ md_status md_create_batch(const md_system_desc *descs, int nrep, void *stream, m
         if (d->natom <= 0 || d->ntype < 1 || d->ntype > MD_MAXTYPE || !d->itype || !d->charge ||
             !d->pos || !d->type_mass || !d->lj1 || !d->lj2)
             return fail(nullptr, MD_ERR_ARG, "md_create_batch: missing or invalid descriptor fields" + at);
-        if (d->nbonds > 0 || d->nangle > 0)
-            return fail(nullptr, MD_ERR_UNSUPPORTED, "md_create_batch: bonded terms in a batch" + at);
+        if ((d->nbonds > 0 && (!d->bonds || !d->bnd1 || !d->bnd2)) ||
+            (d->nangle > 0 && (!d->angles || !d->ang1 || !d->ang2)))
+            return fail(nullptr, MD_ERR_ARG, "md_create_batch: bonded terms without tables" + at);
+        /* one bonded parameter table for the batch: the bonded kernels read
+         * one set (every replica that has bonds or angles must carry it) */
+        for (int q = 0; q < r; q++) {
+            const md_system_desc *e = descs + q;
+            if ((d->nbonds > 0 && e->nbonds > 0 &&
+                 (memcmp(d->bnd1, e->bnd1, sizeof(float) * MD_MAXTYPE) ||
+                  memcmp(d->bnd2, e->bnd2, sizeof(float) * MD_MAXTYPE))) ||
+                (d->nangle > 0 && e->nangle > 0 &&
+                 (memcmp(d->ang1, e->ang1, sizeof(float) * MD_MAXTYPE) ||
+                  memcmp(d->ang2, e->ang2, sizeof(float) * MD_MAXTYPE))))
+                return fail(nullptr, MD_ERR_ARG,
+                            "md_create_batch: replicas with different bonded parameters" + at);
+        }
         if (d->lkspace < 0 || d->lkspace > 2 || d->rcutsq <= 0 || d->skin < 0 || d->dt <= 0 ||
             d->integrator < 0 || d->integrator > 2 || d->enstype < 0 || d->enstype > 1)
             return fail(nullptr, MD_ERR_ARG, "md_create_batch: invalid run parameters" + at);
@@ -988,6 +1018,57 @@ md_status md_create_batch(const md_system_desc *descs, int nrep, void *stream, m
     memset(c->type_mass, 0, sizeof(c->type_mass));
     c->list_tpa = 0;   /* batches build their lists one warp per cell */
     c->centered = 1;   /* cleared below by any replica with a position outside its box */
+    /* bonds and angles of every replica in batch atom indices */
+    {
+        long long a0 = 0;
+        for (int r = 0; r < nrep; r++) {
+            const md_system_desc *d = descs + r;
+            for (int k = 0; k < MD_MAXTYPE; k++) {
+                if (d->nbonds > 0) {
+                    c->bnd1[k] = d->bnd1[k];
+                    c->bnd2[k] = d->bnd2[k];
+                }
+                if (d->nangle > 0) {
+                    c->ang1[k] = d->ang1[k];
+                    c->ang2[k] = d->ang2[k];
+                }
+            }
+            for (int b = 0; b < d->nbonds; b++) {
+                const int *e = d->bonds + 3 * (size_t)b;
+                if (e[1] < 0 || e[2] < 0 || e[1] >= d->natom || e[2] >= d->natom) {
+                    md_status s = fail(c, MD_ERR_ARG, "md_create_batch: bond atom out of range");
+                    delete c;
+                    return s;
+                }
+                c->bonds.push_back(e[0]);
+                c->bonds.push_back((int)(a0 + e[1]));
+                c->bonds.push_back((int)(a0 + e[2]));
+            }
+            for (int b = 0; b < d->nangle; b++) {
+                const int *e = d->angles + 4 * (size_t)b;
+                if (e[1] < 0 || e[2] < 0 || e[3] < 0 || e[1] >= d->natom || e[2] >= d->natom ||
+                    e[3] >= d->natom) {
+                    md_status s = fail(c, MD_ERR_ARG, "md_create_batch: angle atom out of range");
+                    delete c;
+                    return s;
+                }
+                c->angles.push_back(e[0]);
+                for (int q = 1; q < 4; q++) c->angles.push_back((int)(a0 + e[q]));
+            }
+            a0 += d->natom;
+        }
+    }
+    std::vector<int2> blo;
+    std::vector<int> blon;
+    std::vector<int4> alo;
+    std::vector<int> alon;
+    {
+        md_status bs = bonded_lists(c, n, blo, blon, alo, alon);
+        if (bs != MD_OK) {
+            delete c;
+            return bs;
+        }
+    }
 
     host_stage h;
     const size_t P = c->pitch;
@@ -1082,6 +1163,19 @@ md_status md_create_batch(const md_system_desc *descs, int nrep, void *stream, m
         cell0 += g.ncells;
     }
     c->ncells = cell0;
+    for (int i = 0; i < n; i++)
+        h.excl[i] = make_uint4(c->excl_host[4 * i], c->excl_host[4 * i + 1], c->excl_host[4 * i + 2],
+                               c->excl_host[4 * i + 3]);
+    if (c->has_bonds || c->has_angles) {
+        h.blo = std::move(blo);
+        h.blon = std::move(blon);
+        h.alo = std::move(alo);
+        h.alon = std::move(alon);
+    }
+    for (int k = 0; k < MD_MAXTYPE; k++) {
+        h.bp[k] = c->bnd1[k]; h.bp[MD_MAXTYPE + k] = c->bnd2[k];
+        h.bp[2 * MD_MAXTYPE + k] = c->ang1[k]; h.bp[3 * MD_MAXTYPE + k] = c->ang2[k];
+    }
     for (int k = 0; k < 3; k++) {
         c->ncell[k] = c->reps[0].ncell[k];
         c->binlen[k] = c->reps[0].binlen[k];
@@ -1664,8 +1758,9 @@ md_status md_get_info(md_ctx *c, md_info *out)
                                                  (c->integrator == MD_LEAPFROG ? 1 : 2);
     /* single system: one cooperative kernel, or key, scan, scatter, order,
      * permute, copyback, remap (with bonds or angles), list, clear; batch:
-     * key, scan, scatter, order, permute, copyback, list, clear */
-    out->kernels_per_rebuild = md_rebuild_coop(c) ? 1 : (c->batch || !(c->has_bonds || c->has_angles)) ? 8 : 9;
+     * flag (forced builds only, not counted), key, scan, scatter, order,
+     * permute, copyback, remap (with bonds or angles), list, clear */
+    out->kernels_per_rebuild = md_rebuild_coop(c) ? 1 : !(c->has_bonds || c->has_angles) ? 8 : 9;
     out->kernels_per_graph = c->integrator == MD_LEAPFROG ? 1 : 0;
     if (c->rebuild_inline && !c->batch) {   /* the passes run (and return) in every step */
         out->kernels_per_step += out->kernels_per_rebuild;

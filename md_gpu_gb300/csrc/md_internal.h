@@ -282,6 +282,8 @@ void launch_set_condition(md_ctx *c, unsigned long long handle);
 bool md_rebuild_coop(md_ctx *c);
 /* ---- launchers (k_forces.cu) ---- */
 void launch_forces(md_ctx *c, const md_kparams &kp, bool energy, int terms);
+/* bonds and angles (when present and asked for in terms), added into the forces */
+void launch_bonded(md_ctx *c, const md_kparams &kp, bool energy, int terms);
 /* ---- launchers (k_integrate.cu) ---- */
 /* cond / has_cond: graph condition (cudaGraphConditionalHandle) the kernel's
  * last block sets to "rebuild the list before the next force evaluation". */

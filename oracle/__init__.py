@@ -389,7 +389,9 @@ class AdjCfg(C.Structure):
                 ("box", C.c_double * 3), ("rcutsq", C.c_double), ("alfa", C.c_double),
                 ("dt", C.c_double), ("w_pe", C.c_double), ("w_rdf", C.c_double),
                 ("rdf_a", C.c_int), ("rdf_b", C.c_int), ("nbins", C.c_int),
-                ("rdf_dr", C.c_double), ("rdf_sigma", C.c_double)]
+                ("rdf_dr", C.c_double), ("rdf_sigma", C.c_double),
+                ("nbonds", C.c_int), ("nangles", C.c_int), ("bonds", C.c_void_p), ("angles", C.c_void_p),
+                ("bnd1", C.c_void_p), ("bnd2", C.c_void_p), ("ang1", C.c_void_p), ("ang2", C.c_void_p)]
 
 
 @dataclasses.dataclass
@@ -416,6 +418,12 @@ class AdjProblem:
     nbins: int = 200
     rdf_dr: float = 0.05
     rdf_sigma: float = 0.05
+    bonds: Optional[np.ndarray] = None    # (nb, 3): type, i, j (0-based)
+    angles: Optional[np.ndarray] = None   # (na, 4): type, i, j (centre), k
+    bnd1: Optional[np.ndarray] = None     # per type, 2k
+    bnd2: Optional[np.ndarray] = None     # per type, r0
+    ang1: Optional[np.ndarray] = None     # per type, 2k
+    ang2: Optional[np.ndarray] = None     # per type, theta0 (rad)
 
     def cfg(self):
         c = AdjCfg()
@@ -426,6 +434,24 @@ class AdjProblem:
         c.w_pe, c.w_rdf = self.w_pe, self.w_rdf
         c.rdf_a, c.rdf_b, c.nbins = self.rdf_a, self.rdf_b, self.nbins
         c.rdf_dr, c.rdf_sigma = self.rdf_dr, self.rdf_sigma
+        # the arrays stay alive with the cfg (it holds their addresses)
+        c._keep = []
+
+        def arr(a, t):
+            a = np.ascontiguousarray(a, t)
+            c._keep.append(a)
+            return a.ctypes.data
+
+        zero8 = np.zeros(8)
+        if self.bonds is not None and len(self.bonds):
+            c.nbonds = len(self.bonds)
+            c.bonds = arr(np.asarray(self.bonds).reshape(-1), np.int32)
+        if self.angles is not None and len(self.angles):
+            c.nangles = len(self.angles)
+            c.angles = arr(np.asarray(self.angles).reshape(-1), np.int32)
+        for k in ("bnd1", "bnd2", "ang1", "ang2"):
+            v = getattr(self, k)
+            setattr(c, k, arr(zero8 if v is None else v, np.float64))
         return c
 
     def _arrays(self, lj1=None, lj2=None, q=None):

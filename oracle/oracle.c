@@ -1283,6 +1283,61 @@ static inline void adj_delta(const double *x, int i, int j, const double *L, dou
     }
 }
 
+/* Whether atoms i and j are bonded (excluded from the pair terms). */
+static int adj_excluded(const orc_adj_cfg *c, int i, int j)
+{
+    for (int b = 0; b < c->nbonds; b++) {
+        const int *e = c->bonds + 3 * b;
+        if ((e[1] == i && e[2] == j) || (e[1] == j && e[2] == i)) return 1;
+    }
+    return 0;
+}
+
+/* Bonded forces added to F and their energy (bonded_forces.cu:34-193 in
+ * FP64: the same force expressions, cos(theta) clamped to +-0.9999999). */
+static double adj_bonded(const orc_adj_cfg *c, const double *x, double *F)
+{
+    double U = 0.0;
+    for (int b = 0; b < c->nbonds; b++) {
+        const int *e = c->bonds + 3 * b;
+        const int i = e[1], j = e[2];
+        double d[3];
+        adj_delta(x, i, j, c->box, d);
+        const double r = sqrt(d[0] * d[0] + d[1] * d[1] + d[2] * d[2]);
+        const double kk = c->bnd1[e[0]], r0 = c->bnd2[e[0]];
+        const double fa = kk * (r0 / r - 1.0);
+        for (int k = 0; k < 3; k++) {
+            F[3 * i + k] += fa * d[k];
+            F[3 * j + k] -= fa * d[k];
+        }
+        U += 0.5 * kk * (r - r0) * (r - r0);
+    }
+    for (int a = 0; a < c->nangles; a++) {
+        const int *e = c->angles + 4 * a;
+        const int i = e[1], j = e[2], k2 = e[3];
+        double av[3], bv[3];
+        adj_delta(x, i, j, c->box, av);
+        adj_delta(x, k2, j, c->box, bv);
+        const double ai = 1.0 / sqrt(av[0] * av[0] + av[1] * av[1] + av[2] * av[2]);
+        const double bi = 1.0 / sqrt(bv[0] * bv[0] + bv[1] * bv[1] + bv[2] * bv[2]);
+        const double ab = av[0] * bv[0] + av[1] * bv[1] + av[2] * bv[2];
+        double cang = ab * ai * bi;
+        cang = cang < -0.9999999 ? -0.9999999 : (cang > 0.9999999 ? 0.9999999 : cang);
+        const double th = acos(cang), k1 = c->ang1[e[0]], th0 = c->ang2[e[0]];
+        const double ff = k1 * (th - th0) / sqrt(1.0 - cang * cang) * ai * bi;
+        const double aa = ab * ai * ai, bb = ab * bi * bi;
+        for (int q = 0; q < 3; q++) {
+            const double gi = bv[q] - aa * av[q];   /* end atom i */
+            const double gk = av[q] - bb * bv[q];   /* end atom k */
+            F[3 * i + q] += ff * gi;
+            F[3 * k2 + q] += ff * gk;
+            F[3 * j + q] -= ff * (gi + gk);         /* the centre */
+        }
+        U += 0.5 * k1 * (th - th0) * (th - th0);
+    }
+    return U;
+}
+
 /* Forces and potential energy at x (all pairs inside rc). */
 static double adj_forces(const orc_adj_cfg *c, const adjmodel *m, const int *itype, const double *q,
                          const double *lj1, const double *lj2, const double *x, double *F)
@@ -1294,7 +1349,7 @@ static double adj_forces(const orc_adj_cfg *c, const adjmodel *m, const int *ity
     for (int i = 0; i < n; i++) {
         double f0 = 0, f1 = 0, f2 = 0, U = 0.0;
         for (int j = 0; j < n; j++) {
-            if (j == i) continue;
+            if (j == i || (c->nbonds && adj_excluded(c, i, j))) continue;
             double d[3];
             adj_delta(x, i, j, c->box, d);
             double rsq = d[0] * d[0] + d[1] * d[1] + d[2] * d[2];
@@ -1311,7 +1366,7 @@ static double adj_forces(const orc_adj_cfg *c, const adjmodel *m, const int *ity
     double U = 0.0;   /* fixed order: the result does not depend on the thread count */
     for (int i = 0; i < n; i++) U += ui[i];
     free(ui);
-    return U;
+    return U + adj_bonded(c, x, F);
 }
 
 static double adj_rdf_norm(const orc_adj_cfg *c, const int *itype, int b)
@@ -1336,7 +1391,7 @@ static void adj_rdf_add(const orc_adj_cfg *c, const int *itype, const double *x,
     for (int i = 0; i < n; i++) {
         if (itype[i] != c->rdf_a) continue;
         for (int j = 0; j < n; j++) {
-            if (j == i || itype[j] != c->rdf_b) continue;
+            if (j == i || itype[j] != c->rdf_b || (c->nbonds && adj_excluded(c, i, j))) continue;
             double d[3];
             adj_delta(x, i, j, c->box, d);
             double r = sqrt(d[0] * d[0] + d[1] * d[1] + d[2] * d[2]);
@@ -1360,7 +1415,7 @@ static void adj_rdf_grad(const orc_adj_cfg *c, const int *itype, const double *x
     for (int i = 0; i < n; i++) {
         if (itype[i] != c->rdf_a) continue;
         for (int j = 0; j < n; j++) {
-            if (j == i || itype[j] != c->rdf_b) continue;
+            if (j == i || itype[j] != c->rdf_b || (c->nbonds && adj_excluded(c, i, j))) continue;
             double d[3];
             adj_delta(x, i, j, c->box, d);
             double r = sqrt(d[0] * d[0] + d[1] * d[1] + d[2] * d[2]);
@@ -1479,6 +1534,7 @@ double orc_adj_grad(const orc_adj_cfg *c, const int *itype, const double *q, con
         adj_rdf_grad(c, itype, x, norm, e, P);
         for (int i = 0; i < n; i++)
             for (int j = i + 1; j < n; j++) {
+                if (c->nbonds && adj_excluded(c, i, j)) continue;
                 double d[3];
                 adj_delta(x, i, j, c->box, d);
                 double rsq = d[0] * d[0] + d[1] * d[1] + d[2] * d[2];
@@ -1504,6 +1560,24 @@ double orc_adj_grad(const orc_adj_cfg *c, const int *itype, const double *q, con
                 dlj2[tij] += o.flj2 * dwi; dlj2[tji] -= o.flj2 * dwj;
                 *dlns += 2.0 * o.ffc * dd;
             }
+        /* bonded J w by central differences of the bonded forces along w
+         * (step 1e-6 A over the largest component of w) */
+        if (mfr < K && (c->nbonds || c->nangles)) {
+            double wmax = 0.0;
+            for (int i = 0; i < 3 * n; i++) wmax = fmax(wmax, fabs(w[i]));
+            if (wmax > 0.0) {
+                const double h = 1e-6 / wmax;
+                double *xp = (double *)malloc(sizeof(double) * 3 * n);
+                double *fp = (double *)calloc(3 * (size_t)n, sizeof(double));
+                double *fm = (double *)calloc(3 * (size_t)n, sizeof(double));
+                for (int i = 0; i < 3 * n; i++) xp[i] = x[i] + h * w[i];
+                adj_bonded(c, xp, fp);
+                for (int i = 0; i < 3 * n; i++) xp[i] = x[i] - h * w[i];
+                adj_bonded(c, xp, fm);
+                for (int i = 0; i < 3 * n; i++) P[i] += (fp[i] - fm[i]) / (2.0 * h);
+                free(xp); free(fp); free(fm);
+            }
+        }
     }
     if (gbar_out) memcpy(gbar_out, gbar, sizeof(double) * nb);
     free(norm); free(gbar); free(e); free(frames); free(P); free(U); free(w); free(F);

@@ -185,7 +185,7 @@ int orc_md_plain_run(const orc_params *p, const orc_ffield *f, int n, double *x,
 
 /* ---- adjoint of velocity-Verlet NVE (no reference counterpart) ----
  * One system, FP64, all pairs inside rc (O(N^2) per frame, small N only),
- * LJ + Wolf Coulomb with A&S 7.1.26 erfc.  Frames m = 0..K are the initial
+ * LJ + Wolf Coulomb with A&S 7.1.26 erfc, harmonic bonds and angles.  Frames m = 0..K are the initial
  * configuration and the K steps.  Loss
  *   L = w_pe <U>/N + w_rdf sum_b (gbar_b - t_b)^2,
  * <U> the frame average of the consistent potential energy, gbar the frame
@@ -202,6 +202,14 @@ typedef struct {
     double w_pe, w_rdf;
     int rdf_a, rdf_b, nbins;
     double rdf_dr, rdf_sigma;
+    /* harmonic bonds and angles (0-based atoms; may be 0 / NULL): the bonded
+     * pairs are excluded from the pair terms and from the RDF, as the
+     * neighbour list excludes them; bnd1 = 2k, ang1 = 2k per type
+     * (U = k (r - r0)^2, U = k (theta - theta0)^2, theta0 in rad) */
+    int nbonds, nangles;
+    const int *bonds;    /* type, i, j */
+    const int *angles;   /* type, i, j (centre), k */
+    const double *bnd1, *bnd2, *ang1, *ang2;
 } orc_adj_cfg;
 
 /* Forward run only: the loss; gbar (nbins) and the mean PE when non-NULL.

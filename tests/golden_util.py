@@ -133,3 +133,24 @@ def rms_rel(a, b):
     a = np.asarray(a, np.float64)
     b = np.asarray(b, np.float64)
     return float(np.sqrt(((a - b) ** 2).sum() / (b ** 2).sum()))
+
+
+def water_adjoint(nside, seed, rc, nsteps, **loss):
+    """A flexible-water system for the adjoint tests: from_batch keyword
+    arrays (velocity Verlet NVE) and the oracle's AdjProblem of the same
+    inputs (bonds, angles and their parameter tables included)."""
+    from md_gpu_gb300 import MD_VV
+    with tempfile.TemporaryDirectory() as td:
+        case = oracle.load(synth.write_case(synth.water_grid(nside=nside, seed=seed, rc=rc, integrator="vv"),
+                                            td, "w"))
+    a = case_arrays(case, integrator=MD_VV)
+    a["enstype"] = 0
+    nt = case.fld.ntype
+    f64 = lambda v: np.asarray(v, np.float64)
+    prob = oracle.AdjProblem(
+        box=f64(a["box"]), itype=a["itype"], q=f64(a["charge"]), mass=f64(a["type_mass"])[a["itype"]],
+        lj1=f64(a["lj1"]).reshape(nt, nt), lj2=f64(a["lj2"]).reshape(nt, nt), x0=f64(a["pos"]),
+        v0=f64(a["vel"]), rcutsq=a["rcutsq"], alfa=a["alfa"], dt=a["dt"], nsteps=nsteps,
+        bonds=a["bonds"], angles=a["angles"], bnd1=f64(a["bnd1"]), bnd2=f64(a["bnd2"]),
+        ang1=f64(a["ang1"]), ang2=f64(a["ang2"]), **loss)
+    return a, prob

@@ -90,8 +90,8 @@ def test_too_many_bonds(lib):
 
 
 def test_batch_rejects_bad_replicas(lib):
-    """md_create_batch validates every replica on the host: bonded terms are
-    not batched (7), replicas must share dt / integrator (1), and each
+    """md_create_batch validates every replica on the host: replicas must
+    share dt / integrator and their bonded parameter tables (1), and each
     replica's cutoff + skin must fit half its box (8)."""
     import numpy as np
     a = synth.to_arrays(synth.nacl_replica(600, seed=1))
@@ -105,9 +105,10 @@ def test_batch_rejects_bad_replicas(lib):
         MDSystem.from_batch([a, small])
     assert e.value.status == 8
     bonded = dict(b, bonds=np.array([[0, 0, 1]]), bnd1=[100.0], bnd2=[2.8])
+    other = dict(a, bonds=np.array([[0, 0, 1]]), bnd1=[120.0], bnd2=[2.8])
     with pytest.raises(MDError) as e:
-        MDSystem.from_batch([a, bonded])
-    assert e.value.status == 7
+        MDSystem.from_batch([other, bonded])
+    assert e.value.status == 1
 
 
 def test_replica_batch_generator():

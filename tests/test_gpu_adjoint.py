@@ -162,3 +162,35 @@ def test_autograd_wrapper(reference):
     assert np.allclose(loss.detach().numpy(), direct["loss"], rtol=0, atol=0)
     assert np.allclose(lj1.grad.numpy(), direct["dlj1"][:, :2, :2].sum(0), rtol=1e-12)
     assert np.isclose(lns.grad.item(), direct["dlns"].sum(), rtol=1e-12)
+
+
+def test_gpu_adjoint_with_bonds_and_angles():
+    """Flexible water replicas (harmonic bonds and angles, the bonded pairs
+    excluded): loss (1e-4 relative), RDF and gradients (1e-3) against the
+    oracle's FP64 adjoint (whose bonded part is checked against central
+    differences on the CPU), and the charge-scale gradient against FP64
+    central differences."""
+    import golden_util as gu
+    cases = [gu.water_adjoint(nside=6, seed=s, rc=8.0, nsteps=NSTEPS, nbins=NBINS, rdf_dr=DR,
+                              rdf_sigma=SIGMA) for s in (7, 8)]
+    refs = []
+    for _, prob in cases:
+        _, g, _ = oracle.adj_loss(prob)
+        target = 1.05 * g
+        refs.append((target,) + oracle.adj_grad(prob, target))
+    with MDSystem.from_batch([a for a, _ in cases]) as b:
+        out = b.adjoint(NSTEPS, checkpoint=8, nbins=NBINS, dr=DR, sigma=SIGMA,
+                        target=np.stack([r[0] for r in refs]), gradient=True)
+    for k, (target, loss, d1, d2, dlns, gbar) in enumerate(refs):
+        # the loss is a small difference of large pair and bonded energies:
+        # 1e-4 of it (~1e-5 kJ/mol per atom) covers the FP32 dynamics
+        assert abs(out["loss"][k] - loss) <= 1e-4 * abs(loss), (out["loss"][k], loss)
+        assert _close(out["gbar"][k], gbar, 1e-4)
+        assert _close(out["dlj1"][k, :2, :2], d1, 1e-3), (out["dlj1"][k, :2, :2], d1)
+        assert _close(out["dlj2"][k, :2, :2], d2, 1e-3), (out["dlj2"][k, :2, :2], d2)
+        assert abs(out["dlns"][k] - dlns) <= 1e-3 * abs(dlns), (out["dlns"][k], dlns)
+    prob, target = cases[1][1], refs[1][0]
+    h = 1e-5
+    L = lambda **kw: oracle.adj_loss(prob, target, **kw)[0]
+    fd = (L(q=prob.q * np.exp(h)) - L(q=prob.q * np.exp(-h))) / (2 * h)
+    assert abs(out["dlns"][1] - fd) <= 1e-3 * abs(fd)

@@ -85,3 +85,26 @@ def test_lorentz_berthelot_chain_rule():
             fd = (oracle.adj_loss(prob, tg, lj1=lp[0], lj2=lp[1])[0] -
                   oracle.adj_loss(prob, tg, lj1=lm[0], lj2=lm[1])[0]) / (2 * h * arr[k])
             assert abs(fd - ad[k]) <= 1e-4 * abs(fd), (k, fd, ad[k])
+
+
+def test_adjoint_with_bonds_and_angles_matches_finite_differences():
+    """Flexible water (bonds, angles, the bonded pairs excluded from the pair
+    terms and the RDF): the adjoint, whose bonded J w is a central difference
+    of the bonded forces along w, against central differences of the loss."""
+    import golden_util as gu
+    _, prob = gu.water_adjoint(nside=4, seed=5, rc=5.0, nsteps=12, nbins=80, rdf_dr=0.05, rdf_sigma=0.05)
+    _, g, _ = oracle.adj_loss(prob)
+    target = 1.05 * g
+    loss, d1, d2, dlns, _ = oracle.adj_grad(prob, target)
+    h = 1e-5
+    L = lambda **kw: oracle.adj_loss(prob, target, **kw)[0]
+    fd = (L(q=prob.q * np.exp(h)) - L(q=prob.q * np.exp(-h))) / (2 * h)
+    assert abs(fd - dlns) <= 1e-4 * abs(fd), (fd, dlns)
+    for kw, dd in (("lj1", d1), ("lj2", d2)):
+        base = getattr(prob, kw)
+        p, m = base.copy(), base.copy()
+        dv = h * base[0, 0]
+        p[0, 0] += dv
+        m[0, 0] -= dv
+        fd = (L(**{kw: p}) - L(**{kw: m})) / (2 * dv)
+        assert abs(fd - dd[0, 0]) <= 1e-4 * abs(fd), (kw, fd, dd[0, 0])
