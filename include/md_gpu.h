@@ -100,8 +100,10 @@ md_status md_last_error(const md_ctx *ctx, char *buf, int len);
  * the whole batch.  No counterpart in the reference, which runs one system
  * per process.  descs[r] describes replica r exactly as md_create would take
  * it; replicas must share lkspace, integrator, enstype, dt and tau_t, and
- * have no bonds or angles (MD_ERR_UNSUPPORTED).  Box, cutoff, skin, alpha,
- * LJ table, masses, charges and temperature are per replica.  Host arrays of
+ * the replicas that have bonds (angles) must share the bonded parameter
+ * tables bnd1/bnd2 (ang1/ang2) (MD_ERR_ARG otherwise).  Box, cutoff, skin,
+ * alpha, LJ table, masses, charges, temperature, bonds and angles are per
+ * replica.  Host arrays of
  * the context (positions, velocities, forces, energies, neighbour lists,
  * order) hold the replicas' atoms concatenated in replica order; the
  * neighbour list of a replica holds only its own atoms.  md_get_thermo
