@@ -117,6 +117,123 @@ class Clocks:
                 "sm_max_mhz": max(mx) if mx else None, "reasons": reasons, "samples": len(rows)}
 
 
+# ---- checks in FP64 (numpy / scipy), independent of the library's kernels ----
+AS_A = [float(np.float32(a)) for a in (0.254829592, -0.284496736, 1.421413741, -1.453152027, 1.061405429)]
+AS_P = float(np.float32(0.3275911))
+QFAC = 1389.35427611722
+
+
+def pairs_within(pos, box, rc):
+    """Unordered pairs (i < j) within rc under periodic boundaries (k-d tree)."""
+    from scipy.spatial import cKDTree
+    L = np.asarray(box, np.float64)
+    w = np.mod(np.asarray(pos, np.float64) + 0.5 * L, L)
+    w = np.where(w >= L, w - L, w)
+    return cKDTree(w, boxsize=L).query_pairs(rc, output_type="ndarray")
+
+
+def fp64_pair_forces(pos, box, itype, q, lj1, lj2, rcutsq, alfa, pairs):
+    """Pair forces of the FP64 plain form: LJ + Wolf with the A&S 7.1.26 erfc
+    (the force law of pair_forces.cu:133-205 in FP64), over unordered pairs."""
+    x = np.asarray(pos, np.float64)
+    L = np.asarray(box, np.float64)
+    i, j = pairs[:, 0], pairs[:, 1]
+    d = x[i] - x[j]
+    d -= L * np.rint(d / L)
+    rsq = (d * d).sum(1)
+    keep = rsq <= rcutsq
+    i, j, d, rsq = i[keep], j[keep], d[keep], rsq[keep]
+    r = np.sqrt(rsq)
+    ri2 = 1.0 / rsq
+
+    def erfc_as(t_, e_):
+        poly = ((((AS_A[4] * t_ + AS_A[3]) * t_ + AS_A[2]) * t_ + AS_A[1]) * t_ + AS_A[0]) * t_
+        return poly * e_
+
+    a = float(alfa)
+    spi = 2.0 / np.sqrt(np.pi) * a
+    rc = np.sqrt(rcutsq)
+    ec = np.exp(-a * a * rcutsq)
+    W = erfc_as(1.0 / (1.0 + AS_P * a * rc), ec) / rc + spi * ec
+    e = np.exp(-a * a * rsq)
+    E = erfc_as(1.0 / (1.0 + AS_P * a * r), e)
+    qq = QFAC * np.asarray(q, np.float64)[i] * np.asarray(q, np.float64)[j]
+    ti, tj = np.asarray(itype)[i], np.asarray(itype)[j]
+    l1 = np.asarray(lj1, np.float64).reshape(len(lj1) if np.ndim(lj1) == 2 else int(np.sqrt(np.size(lj1))), -1)
+    l2 = np.asarray(lj2, np.float64).reshape(l1.shape)
+    ri6 = ri2 * ri2 * ri2
+    ff = qq * (spi * e + E / r - W) * ri2 + l1[ti, tj] * ri6 * ri6 * ri2 - l2[ti, tj] * ri6 * ri2
+    n = x.shape[0]
+    F = np.zeros((n, 3))
+    for k in range(3):
+        fk = ff * d[:, k]
+        F[:, k] = np.bincount(i, fk, n) - np.bincount(j, fk, n)
+    return F, int(len(ff))
+
+
+def fp64_lj_vv(pos, vel, mass4, box, lj1, lj2, rcutsq, dt, nsteps):
+    """Velocity Verlet NVE of one-type LJ in FP64 (force truncated at rc, the
+    energy shifted to zero there), all pairs: (KE + PE) after every step."""
+    x = np.array(pos, np.float64)
+    v = np.array(vel, np.float64)
+    L = np.asarray(box, np.float64)
+    n = x.shape[0]
+    iu, ju = np.triu_indices(n, 1)
+    rc6i = 1.0 / rcutsq ** 3
+
+    def force(x):
+        d = x[iu] - x[ju]
+        d -= L * np.rint(d / L)
+        rsq = (d * d).sum(1)
+        m = rsq <= rcutsq
+        ri2 = 1.0 / rsq[m]
+        ri6 = ri2 * ri2 * ri2
+        ff = lj1 * ri6 * ri6 * ri2 - lj2 * ri6 * ri2
+        F = np.zeros((n, 3))
+        for k in range(3):
+            fk = ff * d[m, k]
+            F[:, k] = np.bincount(iu[m], fk, n) - np.bincount(ju[m], fk, n)
+        U = (lj1 / 12.0 * (ri6 * ri6 - rc6i * rc6i) - lj2 / 6.0 * (ri6 - rc6i)).sum()
+        return F, U
+
+    c = 0.5 * dt / mass4[:, None]
+    F, U = force(x)
+    out = []
+    for _ in range(nsteps):
+        v += c * F
+        x += dt * v
+        x -= L * np.trunc(2.0 * x / L)
+        F, U = force(x)
+        v += c * F
+        out.append(0.5 * (mass4[:, None] * v * v).sum() + U)
+    return np.array(out)
+
+
+def drift_leg():
+    """Total-energy drift of velocity Verlet NVE, 500-atom LJ argon (T* 0.72,
+    dt 0.5 fs, 2000 steps), from the library (energies every step) and from
+    the FP64 plain form of the same run; kT per atom per ns, linear fit."""
+    import md_gpu_gb300 as md
+    from md_gpu_gb300 import synth
+    nsteps, dt, kt = 2000, 0.5, 0.72
+    sys_ = synth.argon_fcc(ncell=5, seed=6, integrator="vv")
+    a = synth.to_arrays(sys_)
+    with md.MDSystem.from_arrays(**a) as sim:
+        sim.step(nsteps, energy_every=1)
+        e_gpu = np.array([h["ke"] + h["pe"] for h in sim.history(nsteps)])
+    m4 = np.asarray(a["type_mass"], np.float64)[a["itype"]]
+    e_64 = fp64_lj_vv(np.asarray(a["pos"], np.float64), np.asarray(a["vel"], np.float64), m4, a["box"],
+                      float(a["lj1"][0, 0]), float(a["lj2"][0, 0]), a["rcutsq"], dt, nsteps)
+    n = len(a["itype"])
+    t_ns = np.arange(1, nsteps + 1) * dt * 1e-6
+    slope = lambda e: float(np.polyfit(t_ns, e / n, 1)[0] / kt)
+    d_gpu, d_64 = slope(e_gpu), slope(e_64)
+    return {"value": d_gpu, "fp64_plain_form": d_64, "difference": d_gpu - d_64, "unit": "kT/atom/ns",
+            "workload": "LJ argon 500 atoms (fcc 5^3 x 4), T* 0.72, velocity Verlet NVE dt 0.5 fs, 2000 steps",
+            "note": "the force is truncated at rc (the reference's LJ), so the model itself drifts; the "
+                    "difference from the FP64 plain form of the same run is the precision's share"}
+
+
 def make_case(seed, ncell, tmp):
     from md_gpu_gb300 import synth
     return synth.write_case(synth.nacl_rocksalt(ncell=ncell, seed=seed), tmp, "nacl")
@@ -343,14 +460,13 @@ def run_ours(args):
 
     extra = {}
     if rank == 0:
-        import oracle
         # roofline of the dominant kernel (pair forces), timed alone on the same state
+        from md_gpu_gb300 import synth
         pair_ms = sim.time_pair(50)
-        pos = sim.positions().astype(np.float32)
-        case = oracle.load(base)
-        pos4 = np.ascontiguousarray(np.concatenate([pos, np.zeros((n, 1), np.float32)], 1))
-        p = case.params
-        pc = oracle.count_pairs(pos4, case.box, p.rcutsq)
+        arrs = synth.to_arrays(synth.nacl_rocksalt(ncell=args.ncell, seed=replica_seed(1, rank)))
+        pos = sim.positions().astype(np.float32).astype(np.float64)
+        rc = float(np.sqrt(arrs["rcutsq"]))
+        pc = len(pairs_within(pos, arrs["box"], rc))
         achieved = FLOPS_PER_PAIR * pc / (pair_ms * 1e-3) / 1e12
         peak = md.fp32_peak_tflops()
         roof = {"bound": "fp32", "achieved": achieved, "peak": peak, "unit": "TFLOP/s",
@@ -360,16 +476,14 @@ def run_ours(args):
                 "peak_source": "measured FP32 FMA probe (md_probe_fp32_peak); no FP32 entry in "
                                "MEASURED_PEAKS.json"}
         # accuracy of the first frame against the FP64 plain form
-        case = oracle.load(base)
         with md.MDSystem.from_files(base) as fresh:
             fresh.compute_forces(md.TERM_PAIR)
             F = fresh.forces()
-            fpos4 = case.pos4()
-            excl = oracle.exclusions(n, case.bonds)
-            nn, nm, _ = oracle.nlist(fpos4, case.box, case.boxi, oracle.rskinsq(p.skin, p.rcutsq), excl, 512)
-            f64, _ = oracle.pair_f64(1, fpos4, case.itype, case.q, case.box, nn, nm, case.fld.ntype,
-                                     case.lj1, case.lj2, p.rcutsq, 0.0, p.alfa)
-            err = float(np.sqrt(((F[:, :3] - f64[:, :3]) ** 2).sum() / (f64[:, :3] ** 2).sum()))
+            x0 = fresh.positions().astype(np.float32).astype(np.float64)
+        f64, _ = fp64_pair_forces(x0, arrs["box"], arrs["itype"], arrs["charge"], arrs["lj1"], arrs["lj2"],
+                                  float(np.float32(arrs["rcutsq"])), arrs["alfa"],
+                                  pairs_within(x0, arrs["box"], rc * 1.001))
+        err = float(np.sqrt(((F[:, :3] - f64) ** 2).sum() / (f64 ** 2).sum()))
         # end to end through the C ABI from pinned host buffers
         hp = torch.empty((n, 3), dtype=torch.float64, pin_memory=True).numpy()
         hv = torch.empty((n, 3), dtype=torch.float64, pin_memory=True).numpy()
@@ -402,7 +516,7 @@ def run_ours(args):
                 **system_leg("water", synth.water_grid(32, seed=1), "Nose-Hoover velocity Verlet", 0.5,
                              args, flush))
         cpu_v, cpu_dt, cores = cpu_reference_sample(base, 1, 0, args.ref_md_steps)
-        extra = {"roofline": roof, "e2e": e2e, "force_rms_rel_err_vs_fp64": err,
+        extra = {"roofline": roof, "e2e": e2e, "force_rms_rel_err_vs_fp64": err, "nve_drift": drift_leg(),
                  "cpu_baseline": {"value": cpu_v, "unit": UNIT, "cores": cores, "kind": "port",
                                   "sample": f"{args.ref_md_steps} MD steps of the same system (one O(N^2) "
                                             "list build, then rebuilds on the skin/2 criterion), oracle "
