@@ -50,7 +50,8 @@ WORKLOAD = ("nacl64k: 64000-ion molten NaCl, rocksalt 20^3x8 at 1.5 g/cm^3, LJ (
 DT_FS = 2.0
 FLOPS_PER_PAIR = 60.0     # LJ + Wolf per unique pair inside rc (algorithmic count)
 # ncu dram__bytes_read.sum + dram__bytes_write.sum of one pair-kernel launch on
-# this workload, cold caches (profiles/pair_wolf_nacl64k.md: 75.28 + 1.54 MB).
+# this workload, cold caches (75.28 + 1.54 MB), from an ncu capture of k_pair
+# with the tuning bench.py picks; not measured by bench.py itself.
 PAIR_TRAFFIC_BYTES = 76.82e6
 
 

@@ -274,6 +274,19 @@ md_status md_autotune(md_ctx *ctx, int *pair_tpa, int *list_tpa);
  * 1-2 bonded pairs): bit b of mask[a] excludes every pair of types a and b
  * from the neighbour list (made symmetric); ntype entries.  Rebuilds the list. */
 md_status md_set_type_exclusions(md_ctx *ctx, const unsigned *mask);
+/* Test hook of the one-kernel list rebuild of a single system (no
+ * counterpart in the reference, whose list build has no grid barriers):
+ * its phases are separated by grid barriers whose waits give up after
+ * timeout_ms (0: the default, 50 ms) and set a sticky error; with
+ * drop_block >= 0 that block of the rebuild leaves before the first barrier,
+ * so the other blocks' waits run out.  After a timed-out wait every block
+ * of the rebuild returns at once, every later kernel of the context returns
+ * without work, and the next synchronising call (md_step,
+ * md_update_neighbors, ...) returns MD_ERR_CUDA with the message "a grid
+ * barrier of the list rebuild timed out"; the context must then be
+ * destroyed (its atom order may be half permuted), while the CUDA context
+ * stays usable.  timeout_ms = 0 and drop_block = -1 restore the defaults. */
+md_status md_debug_rebuild_barrier(md_ctx *ctx, double timeout_ms, int drop_block);
 /* md_step launches each step's kernels eagerly instead of replaying a
  * captured graph when use_graphs is 0 (for profilers and debugging). */
 md_status md_set_graphs(md_ctx *ctx, int use_graphs);
@@ -300,9 +313,9 @@ md_status md_time_rebuild(md_ctx *ctx, int nrep, float *ms_per_build);
  * measured FP32-pipe peak the pair kernel is compared against. */
 md_status md_probe_fp32_peak(double *tflops);
 
-/* Kinetic energy and temperature of a velocity array in the reference's
- * float4 layout (vx, vy, vz, m*1e4; the gpu_config vel buffer, config.h:114),
- * without allocating any device memory.  No counterpart in the reference: it
+/* Kinetic energy and temperature of a float4 velocity array, one record per
+ * atom holding (vx, vy, vz, mass * 1e4), without allocating any device
+ * memory.  No counterpart in the reference: it
  * serves callers that cannot let a library call cudaMalloc, such as hosts that
  * manage all device memory through their own allocator and budget, or step
  * loops that must not risk the device synchronisation cudaMalloc/cudaFree can
@@ -310,8 +323,11 @@ md_status md_probe_fp32_peak(double *tflops);
  * KE (kJ/mol, FP64 fixed-order sum), out[1] = T = 2 KE / ((3N-3) R).  Scratch
  * is a fixed 32 KB __device__ array shared by all calls: at most 1,048,576
  * atoms (larger calls return MD_ERR_ARG), and calls that overlap on the GPU
- * race.  The first call on a device resolves the array's address; make it
- * before any stream capture.  stream: cudaStream_t or NULL. */
+ * race.  A call made outside stream capture resolves the array's address on
+ * the current device (so a device reset between calls is harmless); a call
+ * made while its stream is being captured reuses the address the last
+ * uncaptured call on that device resolved, so make one call on each device
+ * before capturing.  stream: cudaStream_t or NULL. */
 md_status md_ref_kinetic_energy_noalloc(const void *vel4, int natom, double *out, void *stream);
 
 #ifdef __cplusplus

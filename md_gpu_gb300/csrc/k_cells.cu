@@ -944,9 +944,14 @@ __global__ void __launch_bounds__(CW_WARPS * 32) k_build_cells(
 /* Grid-wide barrier of the cooperative rebuild (every block is resident:
  * the kernel is launched cooperatively).  The last block to arrive resets
  * the count and advances the generation; the others wait for the
- * generation to change for at most MD_BAR_NS of global time, after which
- * they record the timeout in st->status and go on: the build is then
- * invalid and the host reports it, but nothing waits forever.  The waiting
+ * generation to change for at most bar_ns of global time (MD_BAR_NS unless
+ * a test shortens it), after which they record the timeout in st->status.
+ * Returns false in every thread of the block when the wait timed out or
+ * st->status is set (by any block, now or earlier): the caller then returns
+ * at once, so no phase runs on counts or prefix sums that a barrier did not
+ * complete.  A block passes only a barrier every block has reached, i.e.
+ * after every block finished the phase before it; blocks that passed find
+ * the missing ones absent at the next barrier and leave there.  The waiting
  * blocks poll the generation, which lies on another cache line than the
  * arrival counter, so the polls do not slow the arrivals' atomics (the two
  * on one line cost ~12 us per rebuild of 64000 ions with 1216 blocks of 4
@@ -961,13 +966,15 @@ __device__ __forceinline__ unsigned long long global_ns()
     return t;
 }
 
-__device__ __forceinline__ void grid_barrier(md_devstate *st)
+__device__ __forceinline__ bool grid_barrier(md_devstate *st, unsigned long long bar_ns)
 {
+    __shared__ int s_ok;
     __syncthreads();
     if (threadIdx.x == 0) {
         volatile unsigned *gen = &st->bar_gen;
         const unsigned g = *gen;
         __threadfence();
+        int ok = 1;
         if (atomicAdd(&st->bar_count, 1u) == gridDim.x - 1) {
             atomicExch(&st->bar_count, 0u);
             __threadfence();
@@ -975,16 +982,20 @@ __device__ __forceinline__ void grid_barrier(md_devstate *st)
         } else {
             const unsigned long long t0 = global_ns();
             while (*gen == g) {
-                if (global_ns() - t0 > MD_BAR_NS) {
+                if (global_ns() - t0 > bar_ns) {
                     atomicOr(&st->status, 1);
+                    ok = 0;
                     break;
                 }
                 __nanosleep(20);
             }
         }
         __threadfence();
+        if (*(volatile int *)&st->status != 0) ok = 0;
+        s_ok = ok;
     }
     __syncthreads();
+    return s_ok != 0;
 }
 
 /* The order in which the list-building warps take the cells: most atoms
@@ -1034,6 +1045,8 @@ struct rb_ptrs {
     unsigned *nl;
     int *nl_n;
     int ncells, has_bonds, has_angles;
+    unsigned long long bar_ns;   /* limit of each barrier wait */
+    int bar_drop;                /* test hook: this block leaves before the first barrier (-1: none) */
 };
 
 /* Binning, scan, scatter, in-cell order, permutation, remap, list build and
@@ -1043,11 +1056,17 @@ struct rb_ptrs {
 __global__ void __launch_bounds__(CW_WARPS * 32) k_rebuild_coop(md_kparams kp, md_devstate *st, int always,
                                                                 rb_ptrs p)
 {
-    if (!always && !st->update) return;   /* the same in every block: nothing writes it before the end */
+    /* the same in every block: nothing writes either before the end, and a
+     * status left by an earlier launch (a barrier that timed out, whose
+     * arrival count is then stale) stops every later one */
+    if (*(volatile int *)&st->status != 0) return;
+    if (!always && !st->update) return;
     const int tid = blockIdx.x * blockDim.x + threadIdx.x, nth = gridDim.x * blockDim.x;
     const int n = kp.n;
+    const unsigned long long bns = p.bar_ns;
     for (int i = tid; i < n; i += nth) key_one(kp, i, p.pos4, p.cell_rank, p.key, p.cell_count);
-    grid_barrier(st);
+    if ((int)blockIdx.x == p.bar_drop) return;
+    if (!grid_barrier(st, bns)) return;
     /* one block scans (one barrier is dearer than its few rounds) */
     if (blockIdx.x == 0) {
         const int total = scan_cells<CW_WARPS * 32>(p.ncells, p.cell_count, p.cell_start, p.cell_fill);
@@ -1057,12 +1076,12 @@ __global__ void __launch_bounds__(CW_WARPS * 32) k_rebuild_coop(md_kparams kp, m
         }
         work_order(p.ncells, p.cell_start, p.cell_work);
     }
-    grid_barrier(st);
+    if (!grid_barrier(st, bns)) return;
     for (int i = tid; i < n; i += nth) {
         const int r = p.key[i];
         p.src[p.cell_start[r] + atomicAdd(&p.cell_fill[r], 1)] = i;
     }
-    grid_barrier(st);
+    if (!grid_barrier(st, bns)) return;
     {
         const int lane = threadIdx.x & 31, nw = nth >> 5;
         for (int c = tid >> 5; c < p.ncells; c += nw) {
@@ -1070,10 +1089,10 @@ __global__ void __launch_bounds__(CW_WARPS * 32) k_rebuild_coop(md_kparams kp, m
             __syncwarp();
         }
     }
-    grid_barrier(st);
+    if (!grid_barrier(st, bns)) return;
     for (int s = tid; s < n; s += nth)
         permute_one(kp, s, p.src, p.x, p.v, p.mass, p.kick, p.pos4, p.perm, p.type, p.tmp_d, p.tmp4, p.tmp_i);
-    grid_barrier(st);
+    if (!grid_barrier(st, bns)) return;
     for (int s = tid; s < n; s += nth)
         copyback_one(kp, s, p.tmp_d, p.tmp4, p.tmp_i, p.x, p.v, p.mass, p.kick, p.pos4, p.perm, p.iperm, p.type);
     /* with bonds or angles the exclusions need the new order first; without,
@@ -1081,11 +1100,11 @@ __global__ void __launch_bounds__(CW_WARPS * 32) k_rebuild_coop(md_kparams kp, m
      * arrays while the copy-back runs (it writes nothing the build reads) */
     const bool remap = p.has_bonds || p.has_angles;   /* the same in every block */
     if (remap) {
-        grid_barrier(st);
+        if (!grid_barrier(st, bns)) return;
         for (int s = tid; s < n; s += nth)
             remap_one(kp, s, p.perm, p.iperm, p.excl_orig, p.excl_s, p.bl_o, p.bl_on, p.bl_s, p.bl_sn, p.al_o,
                       p.al_on, p.al_s, p.al_sn, p.has_bonds, p.has_angles);
-        grid_barrier(st);
+        if (!grid_barrier(st, bns)) return;
     }
     {
         const float4 *bpos = remap ? p.pos4 : p.tmp4;
@@ -1101,7 +1120,7 @@ __global__ void __launch_bounds__(CW_WARPS * 32) k_rebuild_coop(md_kparams kp, m
                               p.type_mask, p.nl, p.nl_n, p.pos_old, nullptr, nullptr, nullptr);
         }
     }
-    grid_barrier(st);
+    if (!grid_barrier(st, bns)) return;
     if (tid == 0) {
         st->update = 0;
         st->cell_next = 0;
@@ -1211,6 +1230,8 @@ void launch_rebuild(md_ctx *c, const md_kparams &kp, bool unconditional, bool al
         p.ncells = c->ncells;
         p.has_bonds = c->has_bonds;
         p.has_angles = c->has_angles;
+        p.bar_ns = c->dbg_bar_ns > 0 ? c->dbg_bar_ns : MD_BAR_NS;
+        p.bar_drop = c->dbg_bar_drop;
         cudaLaunchConfig_t cfg = {};
         cfg.gridDim = dim3(c->coop_grid);
         cfg.blockDim = dim3(CW_WARPS * 32);
@@ -1220,8 +1241,17 @@ void launch_rebuild(md_ctx *c, const md_kparams &kp, bool unconditional, bool al
         at[0].val.cooperative = 1;
         cfg.attrs = at;
         cfg.numAttrs = 1;
-        cudaLaunchKernelEx(&cfg, k_rebuild_coop, kp, c->st, always, p);
-        return;
+        const cudaError_t e = cudaLaunchKernelEx(&cfg, k_rebuild_coop, kp, c->st, always, p);
+        if (e == cudaSuccess) return;
+        /* a refused cooperative launch (fewer resident blocks than found
+         * when the context was set up) falls back to the chain of passes,
+         * for good when not capturing (during a capture the error stays
+         * sticky in the capture, which then fails and is reported) */
+        (void)cudaGetLastError();
+        cudaStreamCaptureStatus cs = cudaStreamCaptureStatusNone;
+        cudaStreamIsCapturing(c->stream, &cs);
+        if (cs != cudaStreamCaptureStatusNone) return;
+        c->coop_grid = -1;
     }
     const int cwb = cw_blocks(c, c->batch);   /* also finds the SM count */
     int nb = (kp.n + 255) / 256;

@@ -17,9 +17,14 @@
  *  - every call shares it: calls whose kernels overlap on the GPU (different
  *    streams, no ordering between them) race on the partial sums; order them
  *    on one stream or synchronise between them;
- *  - the first call on a device looks up the array's device address with
- *    cudaGetSymbolAddress (host code cannot use the symbol itself as a
- *    pointer); make that first call before any stream capture.
+ *  - host code cannot use the array's symbol as a pointer: every call made
+ *    outside stream capture looks up its device address on the current
+ *    device with cudaGetSymbolAddress (cheap, allocates nothing), so an
+ *    address cached before a cudaDeviceReset (which loads the module again)
+ *    is never used; a call made while its stream is being captured cannot
+ *    make that lookup safely and reuses the address the last uncaptured
+ *    call on the device resolved, so make one call on each device before
+ *    capturing.
  */
 #include <mutex>
 
@@ -103,10 +108,18 @@ extern "C" md_status md_ref_kinetic_energy_noalloc(const void *vel4, int natom, 
         md_set_global_error("md_ref_kinetic_energy_noalloc: no usable current device");
         return MD_ERR_CUDA;
     }
+    cudaStream_t s = (cudaStream_t)stream;
+    cudaStreamCaptureStatus cap = cudaStreamCaptureStatusNone;
+    e = cudaStreamIsCapturing(s, &cap);
+    if (e != cudaSuccess) {
+        md_set_global_error(std::string("md_ref_kinetic_energy_noalloc: cudaStreamIsCapturing: ") +
+                            cudaGetErrorString(e));
+        return MD_ERR_CUDA;
+    }
     double *partials = nullptr;
     {
         std::lock_guard<std::mutex> lock(g_mu);
-        if (!g_partials_addr[dev]) {
+        if (cap == cudaStreamCaptureStatusNone) {
             void *p = nullptr;
             e = cudaGetSymbolAddress(&p, g_ke_partials);
             if (e != cudaSuccess) {
@@ -118,7 +131,11 @@ extern "C" md_status md_ref_kinetic_energy_noalloc(const void *vel4, int natom, 
         }
         partials = g_partials_addr[dev];
     }
-    cudaStream_t s = (cudaStream_t)stream;
+    if (!partials) {
+        md_set_global_error("md_ref_kinetic_energy_noalloc: first call on this device made during stream "
+                            "capture; make one call before capturing");
+        return MD_ERR_ARG;
+    }
     int nb = (natom + MD_NOALLOC_BLOCK - 1) / MD_NOALLOC_BLOCK;
     k_ke_partials<<<nb, MD_NOALLOC_BLOCK, 0, s>>>((const float4 *)vel4, natom, partials);
     k_ke_finish<<<1, MD_NOALLOC_BLOCK, 0, s>>>(partials, nb, natom, out);

@@ -1904,6 +1904,18 @@ md_status md_autotune(md_ctx *c, int *pair_tpa, int *list_tpa)
     return MD_OK;
 }
 
+md_status md_debug_rebuild_barrier(md_ctx *c, double timeout_ms, int drop_block)
+{
+    if (!c || timeout_ms < 0.0 || drop_block < -1) return MD_ERR_ARG;
+    c->dbg_bar_ns = (unsigned long long)(timeout_ms * 1e6);
+    c->dbg_bar_drop = drop_block;
+    if (c->gexec) {   /* graphs hold the launch parameters they were captured with */
+        cudaGraphExecDestroy(c->gexec);
+        c->gexec = nullptr;
+    }
+    return MD_OK;
+}
+
 md_status md_set_graphs(md_ctx *c, int use_graphs)
 {
     if (!c) return MD_ERR_ARG;

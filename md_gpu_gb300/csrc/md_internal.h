@@ -205,6 +205,9 @@ struct md_ctx {
     int fuse_step = 0;             /* 1: fused pair+leapfrog kernel where applicable */
     int cw_grid[2] = {0, 0};       /* blocks of the persistent list builder (single, batch) */
     int rebuild_coop = 1;          /* single systems: the rebuild as one cooperative kernel */
+    unsigned long long dbg_bar_ns = 0; /* test hook: grid-barrier wait limit, ns (0: 50 ms) */
+    int dbg_bar_drop = -1;         /* test hook: block of the cooperative rebuild that leaves
+                                      before its first barrier (-1: none) */
     int coop_grid = 0;             /* its blocks (0: not found yet, -1: unavailable) */
     int nsm = 1;                   /* SMs of the device (found with cw_grid) */
     int rebuild_inline = 0;        /* step graphs: 1 = list passes inline (programmatic launches

@@ -157,6 +157,7 @@ def library(path: Optional[str] = None):
     L.md_autotune.argtypes = [vp, C.POINTER(C.c_int), C.POINTER(C.c_int)]
     L.md_set_type_exclusions.argtypes = [vp, vp]
     L.md_set_graphs.argtypes = [vp, C.c_int]
+    L.md_debug_rebuild_barrier.argtypes = [vp, C.c_double, C.c_int]
     L.md_set_fused_step.argtypes = [vp, C.c_int]
     L.md_set_graph_rebuild.argtypes = [vp, C.c_int]
     L.md_ref_kinetic_energy_noalloc.argtypes = [vp, C.c_int, vp, vp]

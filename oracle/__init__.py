@@ -18,6 +18,13 @@ import numpy as np
 HERE = os.path.dirname(os.path.abspath(__file__))
 LIB_PATH = os.path.join(HERE, "_build", "liboracle.so")
 REF_EMU = os.path.join(HERE, "_ref", "ref_emu")
+# Root of the reference project's source tree (the unmodified md_gpu
+# checkout): environment variable MD_GPU_REFERENCE, default /root/reference.
+# Only the recipes that compile the CPU-emulated reference and the scripts
+# that generate golden vectors read it; nothing does at run time on a
+# machine without the reference.
+REF_ROOT = os.environ.get("MD_GPU_REFERENCE", "/root/reference")
+REF_SRC = os.path.join(REF_ROOT, "src")
 
 _lib = None
 
@@ -30,7 +37,7 @@ def build(force: bool = False) -> str:
     return LIB_PATH
 
 
-def build_ref(ref_src: str = "/root/reference/src") -> Optional[str]:
+def build_ref(ref_src: str = REF_SRC) -> Optional[str]:
     """Compile the CPU-emulated reference kernels when the reference tree exists."""
     if not os.path.isdir(ref_src):
         return None

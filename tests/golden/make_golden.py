@@ -12,7 +12,7 @@ and stores per case an .npz with:
   (byte-exact FP32 results), plus small samples for diagnostics.
 
 Usage (needs the reference tree; run in the build container):
-    python tests/golden/make_golden.py [--ref /root/reference]
+    python tests/golden/make_golden.py [--ref <reference root>]   (default: $MD_GPU_REFERENCE)
 """
 from __future__ import annotations
 
@@ -78,7 +78,7 @@ def synth_case(spec, directory):
 
 def main():
     ap = argparse.ArgumentParser()
-    ap.add_argument("--ref", default="/root/reference")
+    ap.add_argument("--ref", default=oracle.REF_ROOT)
     args = ap.parse_args()
     exe = oracle.build_ref(os.path.join(args.ref, "src"))
     if exe is None:

@@ -14,7 +14,7 @@ import oracle
 from md_gpu_gb300 import synth
 
 GOLDEN_DIR = os.path.join(os.path.dirname(os.path.abspath(__file__)), "golden")
-REF_ROOT = "/root/reference"
+REF_ROOT = oracle.REF_ROOT
 
 
 def names():

@@ -10,6 +10,7 @@ import tempfile
 import pytest
 
 import compat_util as cu
+import oracle
 from md_gpu_gb300 import build as mdbuild
 
 
@@ -36,7 +37,7 @@ def test_reference_loop_links(lib_path):
         assert os.path.exists(exe)
 
 
-REF_SRC = "/root/reference/src"
+REF_SRC = oracle.REF_SRC
 
 
 @pytest.mark.skipif(not os.path.isdir(REF_SRC), reason="reference sources not present")

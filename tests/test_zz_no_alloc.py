@@ -43,6 +43,38 @@ def test_noalloc_kinetic_energy_matches_context_path():
         assert abs(temper - th["temper"]) <= REL_TOL * abs(th["temper"])
 
 
+def test_noalloc_allocates_nothing_and_runs_on_any_stream():
+    """After the first call (which loads the kernels), further calls leave the
+    device's free memory unchanged, also on a stream other than the default."""
+    torch = pytest.importorskip("torch")
+    mdbuild.build()
+    L = library()
+    rng = np.random.default_rng(5)
+    n = 50000
+    vel4 = np.empty((n, 4), np.float32)
+    vel4[:, :3] = rng.normal(0.0, 0.01, (n, 3))
+    vel4[:, 3] = 230000.0
+    d_vel = torch.from_numpy(vel4).cuda()
+    d_out = torch.zeros(2, dtype=torch.float64, device="cuda")
+    s = torch.cuda.Stream()
+    torch.cuda.synchronize()
+    assert L.md_ref_kinetic_energy_noalloc(C.c_void_p(d_vel.data_ptr()), n, C.c_void_p(d_out.data_ptr()),
+                                           None) == 0
+    torch.cuda.synchronize()
+    ref = d_out.cpu().numpy().copy()
+    free0, _ = torch.cuda.mem_get_info()
+    for k in range(6):
+        stream = C.c_void_p(s.cuda_stream) if k % 2 else None
+        assert L.md_ref_kinetic_energy_noalloc(C.c_void_p(d_vel.data_ptr()), n,
+                                               C.c_void_p(d_out.data_ptr()), stream) == 0
+        torch.cuda.synchronize()
+        assert np.array_equal(d_out.cpu().numpy(), ref)
+    free1, _ = torch.cuda.mem_get_info()
+    assert free1 == free0
+    ke64 = 0.5 * (vel4[:, 3].astype(np.float64) * (vel4[:, :3].astype(np.float64) ** 2).sum(1)).sum()
+    assert abs(ref[0] - ke64) <= 1e-12 * ke64
+
+
 def test_noalloc_rejects_sizes_beyond_its_scratch():
     library()
     L = library()
