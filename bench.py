@@ -172,67 +172,46 @@ def fp64_pair_forces(pos, box, itype, q, lj1, lj2, rcutsq, alfa, pairs):
     return F, int(len(ff))
 
 
-def fp64_lj_vv(pos, vel, mass4, box, lj1, lj2, rcutsq, dt, nsteps):
-    """Velocity Verlet NVE of one-type LJ in FP64 (force truncated at rc, the
-    energy shifted to zero there), all pairs: (KE + PE) after every step."""
-    x = np.array(pos, np.float64)
-    v = np.array(vel, np.float64)
-    L = np.asarray(box, np.float64)
-    n = x.shape[0]
-    iu, ju = np.triu_indices(n, 1)
-    rc6i = 1.0 / rcutsq ** 3
-
-    def force(x):
-        d = x[iu] - x[ju]
-        d -= L * np.rint(d / L)
-        rsq = (d * d).sum(1)
-        m = rsq <= rcutsq
-        ri2 = 1.0 / rsq[m]
-        ri6 = ri2 * ri2 * ri2
-        ff = lj1 * ri6 * ri6 * ri2 - lj2 * ri6 * ri2
-        F = np.zeros((n, 3))
-        for k in range(3):
-            fk = ff * d[m, k]
-            F[:, k] = np.bincount(iu[m], fk, n) - np.bincount(ju[m], fk, n)
-        U = (lj1 / 12.0 * (ri6 * ri6 - rc6i * rc6i) - lj2 / 6.0 * (ri6 - rc6i)).sum()
-        return F, U
-
-    c = 0.5 * dt / mass4[:, None]
-    F, U = force(x)
-    out = []
-    for _ in range(nsteps):
-        v += c * F
-        x += dt * v
-        x -= L * np.trunc(2.0 * x / L)
-        F, U = force(x)
-        v += c * F
-        out.append(0.5 * (mass4[:, None] * v * v).sum() + U)
-    return np.array(out)
-
-
-def drift_leg():
-    """Total-energy drift of velocity Verlet NVE, 500-atom LJ argon (T* 0.72,
-    dt 0.5 fs, 2000 steps), from the library (energies every step) and from
-    the FP64 plain form of the same run; kT per atom per ns, linear fit."""
-    import md_gpu_gb300 as md
-    from md_gpu_gb300 import synth
-    nsteps, dt, kt = 2000, 0.5, 0.72
-    sys_ = synth.argon_fcc(ncell=5, seed=6, integrator="vv")
-    a = synth.to_arrays(sys_)
-    with md.MDSystem.from_arrays(**a) as sim:
-        sim.step(nsteps, energy_every=1)
-        e_gpu = np.array([h["ke"] + h["pe"] for h in sim.history(nsteps)])
-    m4 = np.asarray(a["type_mass"], np.float64)[a["itype"]]
-    e_64 = fp64_lj_vv(np.asarray(a["pos"], np.float64), np.asarray(a["vel"], np.float64), m4, a["box"],
-                      float(a["lj1"][0, 0]), float(a["lj2"][0, 0]), a["rcutsq"], dt, nsteps)
-    n = len(a["itype"])
-    t_ns = np.arange(1, nsteps + 1) * dt * 1e-6
-    slope = lambda e: float(np.polyfit(t_ns, e / n, 1)[0] / kt)
-    d_gpu, d_64 = slope(e_gpu), slope(e_64)
-    return {"value": d_gpu, "fp64_plain_form": d_64, "difference": d_gpu - d_64, "unit": "kT/atom/ns",
-            "workload": "LJ argon 500 atoms (fcc 5^3 x 4), T* 0.72, velocity Verlet NVE dt 0.5 fs, 2000 steps",
-            "note": "the force is truncated at rc (the reference's LJ), so the model itself drifts; the "
-                    "difference from the FP64 plain form of the same run is the precision's share"}
+def drift_leg(args):
+    """Total-energy drift of velocity Verlet NVE on LJ argon, 4000 atoms (fcc
+    10^3 x 4, rho* 0.8442, T* 0.72, dt 0.5 fs): a batch of seeded replicas
+    run by the FP32 kernels over the long horizon and by the FP64 kernels
+    (md_set_precision 64, the plain FP64 form on the GPU) over a shorter one;
+    per replica the slope of a straight-line fit of E/N against time, in kT
+    per atom per ns; mean and standard error over replicas for each, and
+    their difference, gated at 1e-4 kT/atom/ns."""
+    from md_gpu_gb300 import nve, synth
+    R, every, dt, kt, gate = args.drift_reps, 100, 0.5, 0.72, 1e-4
+    reps = [synth.to_arrays(synth.argon_fcc(ncell=10, seed=100 + r, integrator="vv")) for r in range(R)]
+    natom = [len(a["itype"]) for a in reps]
+    out = {}
+    for prec, ps in ((32, args.drift_ps), (64, args.drift_fp64_ps)):
+        nsteps = int(round(ps * 1000 / dt / every)) * every
+        t0 = time.perf_counter()
+        st, E = nve.energy_series(reps, nsteps, every, precision=prec)
+        wall = time.perf_counter() - t0
+        d = nve.drift(st, E, natom, dt, kt)
+        m, se = nve.summary(d)
+        out[prec] = {"mean": m, "se": se, "horizon_ps": nsteps * dt / 1000, "replicas": R,
+                     "seconds": wall, "per_replica": [float(x) for x in d]}
+    diff = out[32]["mean"] - out[64]["mean"]
+    se_diff = float(np.hypot(out[32]["se"], out[64]["se"]))
+    resolved = se_diff <= gate
+    return {
+        "workload": (f"LJ argon, {R} replicas of 4000 atoms (fcc 10^3 x 4, rho* 0.8442, sigma = 1 A, "
+                     "eps = 1 kJ/mol, m = 1 g/mol), T* 0.72 from seeded Maxwell-Boltzmann velocities, "
+                     "rc 2.5 (force truncated, energy shifted), skin 0.3, velocity Verlet NVE dt 0.5 fs; "
+                     f"E = KE + PE every {every} steps"),
+        "unit": "kT/atom/ns",
+        "value": out[32]["mean"], "se": out[32]["se"], "horizon_ps": out[32]["horizon_ps"],
+        "fp64": {k: out[64][k] for k in ("mean", "se", "horizon_ps", "replicas", "seconds")},
+        "fp32_seconds": out[32]["seconds"],
+        "difference": diff, "difference_se": se_diff, "gate": gate,
+        "gate_passed": bool(resolved and abs(diff) <= gate),
+        "gate_resolved": bool(resolved),
+        "note": ("FP32 and FP64 kernels on the same seeded replicas; the model (the reference's LJ force "
+                 "truncated at rc) drifts by itself, so the gate is on the difference; "
+                 "gate_resolved is false when the difference's standard error exceeds the gate")}
 
 
 def make_case(seed, ncell, tmp):
@@ -517,7 +496,7 @@ def run_ours(args):
                 **system_leg("water", synth.water_grid(32, seed=1), "Nose-Hoover velocity Verlet", 0.5,
                              args, flush))
         cpu_v, cpu_dt, cores = cpu_reference_sample(base, 1, 0, args.ref_md_steps)
-        extra = {"roofline": roof, "e2e": e2e, "force_rms_rel_err_vs_fp64": err, "nve_drift": drift_leg(),
+        extra = {"roofline": roof, "e2e": e2e, "force_rms_rel_err_vs_fp64": err, "nve_drift": drift_leg(args) if args.drift_reps > 0 else None,
                  "cpu_baseline": {"value": cpu_v, "unit": UNIT, "cores": cores, "kind": "port",
                                   "sample": f"{args.ref_md_steps} MD steps of the same system (one O(N^2) "
                                             "list build, then rebuilds on the skin/2 criterion), oracle "
@@ -572,6 +551,9 @@ def main():
     ap.add_argument("--other-segments", type=int, default=3,
                     help="timed segments of the argon and water systems (0: skip them)")
     ap.add_argument("--ref-md-steps", type=int, default=10)
+    ap.add_argument("--drift-reps", type=int, default=16, help="argon replicas of the NVE drift leg (0: skip)")
+    ap.add_argument("--drift-ps", type=float, default=100.0, help="FP32 horizon of the drift leg, ps")
+    ap.add_argument("--drift-fp64-ps", type=float, default=10.0, help="FP64 horizon of the drift leg, ps")
     ap.add_argument("--ncell", type=int, default=20)
     ap.add_argument("--no-autotune", action="store_true")
     ap.add_argument("--tuning", default="",

@@ -202,6 +202,15 @@ md_status md_get_thermo(md_ctx *ctx, md_thermo *out);
 /* The last min(n, nsteps run) records, oldest first; returns the count in *got. */
 md_status md_get_thermo_history(md_ctx *ctx, md_thermo *out, int n, int *got);
 
+/* Per-replica records of a batch (no counterpart in the reference): for the
+ * last min(n, steps run, 4096) steps, oldest first, out[(t * nrep + r) * 3 +
+ * {0, 1, 2}] = replica r's kinetic energy, potential energy and conserved
+ * quantity (KE + PE, plus the Nose-Hoover terms) after step t, kJ/mol; PE
+ * and the conserved quantity are 0 on steps without energies (md_step's
+ * energy_every).  The matching batch records are md_get_thermo_history's.
+ * *got = the number of steps returned.  MD_ERR_ARG for a single system. */
+md_status md_get_replica_history(md_ctx *ctx, double *out, int n, int *got);
+
 /* One call end to end from host buffers: uploads pos/vel (3N doubles),
  * runs nsteps, downloads pos/vel and the per-step records (nsteps). */
 md_status md_run_host(md_ctx *ctx, double *pos3, double *vel3, int nsteps, int energy_every,
@@ -274,6 +283,17 @@ md_status md_autotune(md_ctx *ctx, int *pair_tpa, int *list_tpa);
  * 1-2 bonded pairs): bit b of mask[a] excludes every pair of types a and b
  * from the neighbour list (made symmetric); ntype entries.  Rebuilds the list. */
 md_status md_set_type_exclusions(md_ctx *ctx, const unsigned *mask);
+/* Arithmetic of the force kernels: 32 (the default) evaluates pair terms in
+ * FP32 on the FP32 copy of the positions, as the reference's kernels do
+ * (pair_forces.cu:34-205); 64 evaluates pair, bond and angle terms in FP64
+ * on the FP64 positions with IEEE sqrt, divide, exp and log (the plain FP64
+ * form of the same force law, A&S erfc included).  Forces, integrators and
+ * reductions are shared (int64 fixed-point forces, FP64 state).  No
+ * counterpart in the reference; the FP64 mode is the GPU reference point of
+ * the precision checks.  Recomputes the forces of the current state.  FP64
+ * contexts run no fused step and no adjoint (md_adjoint_run returns
+ * MD_ERR_UNSUPPORTED). */
+md_status md_set_precision(md_ctx *ctx, int bits);
 /* Test hook of the one-kernel list rebuild of a single system (no
  * counterpart in the reference, whose list build has no grid barriers):
  * its phases are separated by grid barriers whose waits give up after

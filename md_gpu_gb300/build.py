@@ -11,7 +11,7 @@ CSRC = os.path.join(HERE, "csrc")
 BUILD = os.path.join(HERE, "_build")
 LIB = os.path.join(BUILD, "libmdgpu_gb300.so")
 SOURCES = ["md_api.cu", "k_cells.cu", "k_forces.cu", "k_integrate.cu", "k_probe.cu", "k_noalloc.cu", "k_fused.cu",
-           "k_batch.cu", "k_adjoint.cu", "md_compat.cu"]
+           "k_batch.cu", "k_adjoint.cu", "md_compat.cu", "k_pair64.cu"]
 HEADERS = ["md_internal.h", "md_device.cuh", "md_pair.cuh", "md_thermo.cuh",
            os.path.join("..", "..", "include", "md_gpu.h"), os.path.join("..", "..", "include", "md_gpu_compat.h")]
 NVCC = os.environ.get("NVCC", "/usr/local/cuda/bin/nvcc")

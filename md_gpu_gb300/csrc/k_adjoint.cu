@@ -595,8 +595,8 @@ extern "C" md_status md_adjoint_run(md_ctx *c, const md_adjoint_cfg *cfg, const 
                                     double *dlns)
 {
     if (!c || !cfg || !loss) return MD_ERR_ARG;
-    if (!c->batch || c->integrator != MD_VV || c->enstype != 0) {
-        c->last_error = "md_adjoint_run: needs a batch context with velocity Verlet NVE";
+    if (!c->batch || c->integrator != MD_VV || c->enstype != 0 || c->fp64) {
+        c->last_error = "md_adjoint_run: needs a batch context with velocity Verlet NVE in FP32 mode";
         return MD_ERR_UNSUPPORTED;
     }
     const int K = cfg->nsteps, C = cfg->checkpoint > 0 ? cfg->checkpoint : 50;

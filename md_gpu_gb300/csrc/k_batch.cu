@@ -63,9 +63,12 @@ __global__ void __launch_bounds__(128) k_pair_b(int cap, int pitch, int centered
 __device__ void finalize_b(const md_kparams &kp, const thermo_par &tp, int mode, int nrep,
                            const md_rep *__restrict__ reps, md_repstate *repst,
                            unsigned long long *racc, md_devstate *st, md_thermo *rec, int rec_cap,
-                           double *sh)
+                           double *rep_hist, double *sh)
 {
     double tke = 0.0, tpe = 0.0, tw = 0.0, tex = 0.0;
+    /* the step this record belongs to (thread 0 advances it after the sums) */
+    const long long step = ((volatile md_devstate *)st)->step;
+    double *hist = (rep_hist && mode != 2) ? rep_hist + (size_t)(step % rec_cap) * 3 * nrep : nullptr;
     for (int r = threadIdx.x; r < nrep; r += blockDim.x) {
         const md_rep &R = reps[r];
         const double a = fix_take(racc + 3 * r, MD_KFIX);
@@ -83,7 +86,13 @@ __device__ void finalize_b(const md_kparams &kp, const thermo_par &tp, int mode,
         tke += ke;
         tpe += b;
         tw += c;
-        if (t.nh) tex += 0.5 * t.q_nh * xi * xi + t.ndf * RGAS * t.t0 * eta;
+        const double ex = t.nh ? 0.5 * t.q_nh * xi * xi + t.ndf * RGAS * t.t0 * eta : 0.0;
+        tex += ex;
+        if (hist) {
+            hist[3 * r] = ke;
+            hist[3 * r + 1] = tp.energy ? b : 0.0;
+            hist[3 * r + 2] = tp.energy ? ke + b + ex : 0.0;
+        }
     }
     const double KE = block_sum(tke, sh);
     const double PE = block_sum(tpe, sh);
@@ -149,7 +158,7 @@ __global__ void __launch_bounds__(3 * MD_LA) k_leapfrog_b(md_kparams kp, thermo_
     }
     block_fix_add(ke2, pe, w, tp.energy, racc + 3 * bt.x, shl);
     if (md_last_block(io.counter)) {
-        finalize_b(kp, tp, 0, nrep, reps, repst, racc, io.st, io.rec, io.rec_cap, sh);
+        finalize_b(kp, tp, 0, nrep, reps, repst, racc, io.st, io.rec, io.rec_cap, io.rep_hist, sh);
         if (threadIdx.x == 0) {
             set_condition(io);
             *io.counter = 0;
@@ -238,7 +247,7 @@ __global__ void __launch_bounds__(3 * MD_LA) k_vv_second_b(md_kparams kp, thermo
     }
     block_fix_add(ke2, pe, w, tp.energy, racc + 3 * bt.x, shl);
     if (md_last_block(io.counter)) {
-        finalize_b(kp, tp, do_kick ? 1 : 2, nrep, reps, repst, racc, io.st, io.rec, io.rec_cap, sh);
+        finalize_b(kp, tp, do_kick ? 1 : 2, nrep, reps, repst, racc, io.st, io.rec, io.rec_cap, io.rep_hist, sh);
         if (threadIdx.x == 0) *io.counter = 0;
     }
 }
@@ -278,7 +287,9 @@ inline int grid_int_blocks(const md_ctx *c) { return c->grid_cnt[md_grid_index(M
 
 void launch_forces_b(md_ctx *c, const md_kparams &kp, bool energy, int terms)
 {
-    if (terms & MD_TERM_PAIR) {
+    if ((terms & MD_TERM_PAIR) && c->fp64) {
+        launch_pair64(c, energy);
+    } else if (terms & MD_TERM_PAIR) {
         if (c->lkspace == 0) {
             if (energy) pair_dispatch_b<0, true>(c, kp);
             else pair_dispatch_b<0, false>(c, kp);

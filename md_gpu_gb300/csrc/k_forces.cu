@@ -165,7 +165,9 @@ void launch_forces(md_ctx *c, const md_kparams &kp, bool energy, int terms)
         return;
     }
     pair_consts pc = make_pair_consts(c);
-    if (terms & MD_TERM_PAIR) {
+    if ((terms & MD_TERM_PAIR) && c->fp64) {
+        launch_pair64(c, energy);
+    } else if (terms & MD_TERM_PAIR) {
         if (c->lkspace == 0) {
             if (energy) pair_dispatch<0, true>(c, kp, pc);
             else pair_dispatch<0, false>(c, kp, pc);
@@ -185,7 +187,9 @@ void launch_bonded(md_ctx *c, const md_kparams &kp, bool energy, int terms)
 {
     int hb = (terms & MD_TERM_BOND) ? c->has_bonds : 0;
     int ha = (terms & MD_TERM_ANGLE) ? c->has_angles : 0;
-    if (hb || ha) {
+    if ((hb || ha) && c->fp64) {
+        launch_bonded64(c, energy, hb, ha);
+    } else if (hb || ha) {
         int nb = (kp.n + 255) / 256;
         const md_rep *reps = c->batch ? c->reps_dev : nullptr;
         const int *arep = c->batch ? c->arep : nullptr;

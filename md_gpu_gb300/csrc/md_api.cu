@@ -253,7 +253,7 @@ void free_device(md_ctx *c)
                     c->tmp_i, c->bl_o, c->bl_on, c->al_o, c->al_on, c->bl_s, c->bl_sn, c->al_s,
                     c->al_sn, c->st, c->rec, c->lj_dev, c->bonded_par,
                     c->type_mask_dev, c->io_dev, c->reps_dev, c->repst, c->arep, c->crep,
-                    c->ljr_dev, c->grid_tab, c->rep_upd, c->racc};
+                    c->ljr_dev, c->grid_tab, c->rep_upd, c->racc, c->p64_dev, c->rep_hist};
     for (void *p : ptrs)
         if (p) cudaFree(p);
 }
@@ -571,6 +571,7 @@ md_status setup_device(md_ctx *c, void *stream, host_stage &h, md_ctx **out)
         MD_ALLOC(c->rep_upd, c->nrep); MD_ALLOC(c->racc, 3 * (size_t)c->nrep);
         MD_ALLOC(c->ljr_dev, (size_t)MD_MAXTYPE * MD_MAXTYPE * c->nrep);
         MD_ALLOC(c->grid_tab, h.grid.size());
+        MD_ALLOC(c->rep_hist, (size_t)c->rec_cap * 3 * c->nrep);
     }
 #undef MD_ALLOC
     if (e != cudaSuccess) {
@@ -1095,6 +1096,7 @@ md_status md_create_batch(const md_system_desc *descs, int nrep, void *stream, m
         }
         R.rcutsq = d->rcutsq;
         R.reacf = d->lkspace == 0 ? d->reacf : 0.0f;
+        c->rep_alfa.push_back(d->alfa);
         float wc[4] = {0.0f, 0.0f, 0.0f, 0.0f};
         if (d->lkspace > 0) wolf_consts(d->alfa, d->rcutsq, wc);
         R.palfa = wc[0];
@@ -1544,6 +1546,32 @@ md_status md_get_thermo_history(md_ctx *c, md_thermo *out, int n, int *got)
     return MD_OK;
 }
 
+md_status md_get_replica_history(md_ctx *c, double *out, int n, int *got)
+{
+    if (!c || !out || n < 0 || !got) return MD_ERR_ARG;
+    if (!c->batch) {
+        c->last_error = "md_get_replica_history: not a batch context";
+        return MD_ERR_ARG;
+    }
+    MD_CUDA_TRY(c, cudaStreamSynchronize(c->stream));
+    md_devstate h;
+    MD_CUDA_TRY(c, cudaMemcpy(&h, c->st, sizeof(h), cudaMemcpyDeviceToHost));
+    const long long avail = std::min<long long>(h.step, c->rec_cap);
+    const int k = (int)std::min<long long>(avail, n);
+    const size_t row = (size_t)3 * c->nrep;   /* doubles per step */
+    int t = 0;
+    while (t < k) {
+        const int r = (int)((h.step - k + t) % c->rec_cap);
+        const int len = std::min(k - t, c->rec_cap - r);
+        MD_CUDA_TRY(c, cudaMemcpyAsync(out + (size_t)t * row, c->rep_hist + (size_t)r * row,
+                                       sizeof(double) * row * (size_t)len, cudaMemcpyDeviceToHost, c->stream));
+        t += len;
+    }
+    MD_CUDA_TRY(c, cudaStreamSynchronize(c->stream));
+    *got = k;
+    return MD_OK;
+}
+
 md_status md_run_host(md_ctx *c, double *pos3, double *vel3, int nsteps, int energy_every,
                       md_thermo *records)
 {
@@ -1902,6 +1930,34 @@ md_status md_autotune(md_ctx *c, int *pair_tpa, int *list_tpa)
     if (pair_tpa) *pair_tpa = bp;
     if (list_tpa) *list_tpa = bl;
     return MD_OK;
+}
+
+md_status md_set_precision(md_ctx *c, int bits)
+{
+    if (!c || (bits != 32 && bits != 64)) return MD_ERR_ARG;
+    if (bits == 64 && !c->p64_dev) {
+        const int nm = c->batch ? c->nrep : 1;
+        std::vector<md_p64> h(nm);
+        for (int r = 0; r < nm; r++) {
+            if (c->batch) {
+                const md_rep &R = c->reps[r];
+                h[r] = md_make_p64(c->lkspace, R.rcutsq, R.reacf, c->rep_alfa[r], R.box);
+            } else {
+                h[r] = md_make_p64(c->lkspace, c->rcutsq, c->reacf, c->alfa, c->box);
+            }
+        }
+        MD_CUDA_TRY(c, dalloc(&c->p64_dev, (size_t)nm));
+        MD_CUDA_TRY(c, cudaMemcpy(c->p64_dev, h.data(), sizeof(md_p64) * nm, cudaMemcpyHostToDevice));
+    }
+    const int v = bits == 64 ? 1 : 0;
+    if (v == c->fp64) return MD_OK;
+    c->fp64 = v;
+    if (c->gexec) {   /* graphs hold the kernels they were captured with */
+        cudaGraphExecDestroy(c->gexec);
+        c->gexec = nullptr;
+    }
+    /* the forces (and record) of the current state in the new precision */
+    return refresh_state(c);
 }
 
 md_status md_debug_rebuild_barrier(md_ctx *c, double timeout_ms, int drop_block)

@@ -109,6 +109,16 @@ struct md_rep {
     double t0, q_nh, inv_ndfr, inv_q;   /* 1/(ndf R), 1/Q */
 };
 
+/* Constants of the FP64 force law of one system or replica (the FP64 mode,
+ * md_set_precision): cutoff, reaction-field or Wolf constants, the A&S erfc
+ * coefficients widened from the reference's floats, box. */
+struct md_p64 {
+    int kind;   /* lkspace: 0 reaction field, 1 Wolf, 2 LJ + no Coulomb shift */
+    double rcsq, rc, rcinv, rc6i, reacf, alpha, spi, pex, a[5], qfac, wolfw, ucc;
+    double L[3], Li[3];
+};
+md_p64 md_make_p64(int lkspace, float rcutsq, float reacf, float alfa, const float box[3]);
+
 /* Per-replica thermodynamic state of a batch (the fields md_devstate holds
  * for a single system). */
 struct md_repstate {
@@ -191,6 +201,7 @@ struct md_ctx {
     int has_bonds = 0, has_angles = 0;
     md_devstate *st = nullptr;
     md_thermo *rec = nullptr;                             /* device ring of records */
+    double *rep_hist = nullptr;   /* batches: ring of per-replica (KE, PE, conserved) per step */
     int rec_cap = 0;
     float *lj_dev = nullptr;                              /* lj1,lj2 interleaved (64 float2) */
     float *bonded_par = nullptr;                          /* bnd1,bnd2,ang1,ang2 (4x8) */
@@ -219,6 +230,9 @@ struct md_ctx {
     int pair_depth = 0;  /* list entries per lane and batch (0: the default for pair_tpa) */
     int centered = 0;    /* every position in [-L/2, L/2] (set at upload; the wraps keep it) */
     int list_tpa = 0;    /* list build: 0 = one warp per cell, else threads per atom */
+    int fp64 = 0;        /* 1: force kernels in FP64 on the FP64 positions (md_set_precision) */
+    md_p64 *p64_dev = nullptr;        /* FP64 model constants per replica (1 for a single system) */
+    std::vector<float> rep_alfa;      /* damping alpha per replica of a batch */
 
     /* batches of replicas (md_create_batch; any number, 1 included) */
     int batch = 0;
@@ -287,6 +301,9 @@ bool md_rebuild_coop(md_ctx *c);
 void launch_forces(md_ctx *c, const md_kparams &kp, bool energy, int terms);
 /* bonds and angles (when present and asked for in terms), added into the forces */
 void launch_bonded(md_ctx *c, const md_kparams &kp, bool energy, int terms);
+/* ---- launchers (k_pair64.cu): the FP64 mode ---- */
+void launch_pair64(md_ctx *c, bool energy);
+void launch_bonded64(md_ctx *c, bool energy, int has_bonds, int has_angles);
 /* ---- launchers (k_integrate.cu) ---- */
 /* cond / has_cond: graph condition (cudaGraphConditionalHandle) the kernel's
  * last block sets to "rebuild the list before the next force evaluation". */

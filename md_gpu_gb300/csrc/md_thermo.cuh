@@ -23,6 +23,7 @@ struct thermo_par {
 struct step_io {
     md_devstate *st;
     md_thermo *rec;
+    double *rep_hist;   /* batches: per step and replica (KE, PE, conserved), rec_cap steps */
     int rec_cap;
     unsigned *counter;
     const float4 *pos_old;
@@ -331,6 +332,7 @@ inline step_io make_io(md_ctx *c, unsigned long long cond, int has_cond)
     step_io io;
     io.st = c->st;
     io.rec = c->rec;
+    io.rep_hist = c->rep_hist;
     io.rec_cap = c->rec_cap;
     io.counter = &c->st->blocks_done;
     io.pos_old = c->pos_old;

@@ -158,6 +158,8 @@ def library(path: Optional[str] = None):
     L.md_set_type_exclusions.argtypes = [vp, vp]
     L.md_set_graphs.argtypes = [vp, C.c_int]
     L.md_debug_rebuild_barrier.argtypes = [vp, C.c_double, C.c_int]
+    L.md_set_precision.argtypes = [vp, C.c_int]
+    L.md_get_replica_history.argtypes = [vp, vp, C.c_int, C.POINTER(C.c_int)]
     L.md_set_fused_step.argtypes = [vp, C.c_int]
     L.md_set_graph_rebuild.argtypes = [vp, C.c_int]
     L.md_ref_kinetic_energy_noalloc.argtypes = [vp, C.c_int, vp, vp]
@@ -256,6 +258,19 @@ class MDSystem:
         buf = (Thermo * n)()
         _check(library().md_get_replica_thermo(self._ctx, buf, n), self._ctx)
         return [buf[i].as_dict() for i in range(n)]
+
+    def replica_history(self, n):
+        """Per-replica (KE, PE, conserved) of the last min(n, steps, 4096)
+        steps of a batch, oldest first: an array (steps, nrep, 3); PE and
+        the conserved quantity are 0 on steps without energies.  Returns
+        (array, steps) where steps are the step numbers of the rows."""
+        nrep = len(getattr(self, "replica_sizes", [self.natom]))
+        buf = np.zeros((max(n, 1), nrep, 3))
+        got = C.c_int()
+        _check(library().md_get_replica_history(self._ctx, buf.ctypes.data, int(n), C.byref(got)), self._ctx)
+        k = got.value
+        last = self.thermo()["step"]
+        return buf[:k], np.arange(last - k + 1, last + 1)
 
     def adjoint(self, nsteps, checkpoint=50, w_pe=1.0, w_rdf=1.0, rdf_types=(0, 1), nbins=200,
                 dr=0.05, sigma=0.05, target=None, gradient=True):
@@ -443,6 +458,11 @@ class MDSystem:
     def set_graph_rebuild(self, inline=True):
         """Step graphs: rebuild passes inline (True) or behind a conditional node."""
         _check(library().md_set_graph_rebuild(self._ctx, 1 if inline else 0), self._ctx)
+
+    def set_precision(self, bits):
+        """32: FP32 pair arithmetic (the default); 64: every force term in FP64
+        on the FP64 positions (the plain FP64 form, for reference runs)."""
+        _check(library().md_set_precision(self._ctx, int(bits)), self._ctx)
 
     def set_fused_step(self, fused=True):
         """Leapfrog without bonded terms: pair forces and update in one kernel."""
