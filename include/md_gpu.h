@@ -300,12 +300,13 @@ md_status md_set_precision(md_ctx *ctx, int bits);
  * timeout_ms (0: the default, 50 ms) and set a sticky error; with
  * drop_block >= 0 that block of the rebuild leaves before the first barrier,
  * so the other blocks' waits run out.  After a timed-out wait every block
- * of the rebuild returns at once, every later kernel of the context returns
- * without work, and the next synchronising call (md_step,
- * md_update_neighbors, ...) returns MD_ERR_CUDA with the message "a grid
- * barrier of the list rebuild timed out"; the context must then be
- * destroyed (its atom order may be half permuted), while the CUDA context
- * stays usable.  timeout_ms = 0 and drop_block = -1 restore the defaults. */
+ * of the rebuild returns at once and every later launch of the rebuild
+ * returns without work; the step kernels run on with the list and atom
+ * order as the interrupted rebuild left them (every index still in range),
+ * and the next synchronising call (md_step, md_update_neighbors, ...)
+ * returns MD_ERR_CUDA with the message "a grid barrier of the list rebuild
+ * timed out".  The context must then be destroyed (its atom order may be
+ * half permuted); the CUDA context stays usable.  timeout_ms = 0 and drop_block = -1 restore the defaults. */
 md_status md_debug_rebuild_barrier(md_ctx *ctx, double timeout_ms, int drop_block);
 /* md_step launches each step's kernels eagerly instead of replaying a
  * captured graph when use_graphs is 0 (for profilers and debugging). */

@@ -946,12 +946,12 @@ __global__ void __launch_bounds__(CW_WARPS * 32) k_build_cells(
  * the count and advances the generation; the others wait for the
  * generation to change for at most bar_ns of global time (MD_BAR_NS unless
  * a test shortens it), after which they record the timeout in st->status.
- * Returns false in every thread of the block when the wait timed out or
- * st->status is set (by any block, now or earlier): the caller then returns
- * at once, so no phase runs on counts or prefix sums that a barrier did not
- * complete.  A block passes only a barrier every block has reached, i.e.
- * after every block finished the phase before it; blocks that passed find
- * the missing ones absent at the next barrier and leave there.  The waiting
+ * Returns false in every thread of the block when its wait timed out: the
+ * caller then returns at once.  A block passes a barrier only when every
+ * block has reached it, i.e. after every block finished the phase before
+ * it, so no phase runs on counts or prefix sums a barrier did not complete;
+ * blocks that passed while another one gave up find that one absent at the
+ * next barrier and leave there.  The waiting
  * blocks poll the generation, which lies on another cache line than the
  * arrival counter, so the polls do not slow the arrivals' atomics (the two
  * on one line cost ~12 us per rebuild of 64000 ions with 1216 blocks of 4
@@ -991,7 +991,6 @@ __device__ __forceinline__ bool grid_barrier(md_devstate *st, unsigned long long
             }
         }
         __threadfence();
-        if (*(volatile int *)&st->status != 0) ok = 0;
         s_ok = ok;
     }
     __syncthreads();
@@ -1056,11 +1055,11 @@ struct rb_ptrs {
 __global__ void __launch_bounds__(CW_WARPS * 32) k_rebuild_coop(md_kparams kp, md_devstate *st, int always,
                                                                 rb_ptrs p)
 {
-    /* the same in every block: nothing writes either before the end, and a
+    /* the same in every block: nothing writes either before the end; a
      * status left by an earlier launch (a barrier that timed out, whose
-     * arrival count is then stale) stops every later one */
-    if (*(volatile int *)&st->status != 0) return;
+     * arrival count is then stale) stops every later rebuild */
     if (!always && !st->update) return;
+    if (*(volatile int *)&st->status != 0) return;
     const int tid = blockIdx.x * blockDim.x + threadIdx.x, nth = gridDim.x * blockDim.x;
     const int n = kp.n;
     const unsigned long long bns = p.bar_ns;

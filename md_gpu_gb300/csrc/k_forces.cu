@@ -28,14 +28,12 @@ __global__ void __launch_bounds__(128) k_pair(md_kparams kp, pair_consts pc,
                                               const unsigned *__restrict__ nl,
                                               const int *__restrict__ nl_n,
                                               const float2 *__restrict__ ljtab, long long *f,
-                                              float *vir, float *epot, const md_devstate *st)
+                                              float *vir, float *epot)
 {
     __shared__ float2 lj[MD_MAXTYPE * MD_MAXTYPE];
     pdl_trigger();   /* the integrator may be scheduled; it waits for this grid */
-    const bool halted = st && md_halted(st);
     if (threadIdx.x < MD_MAXTYPE * MD_MAXTYPE) lj[threadIdx.x] = ljtab[threadIdx.x];
     __syncthreads();
-    if (halted) return;
     int gt = blockIdx.x * blockDim.x + threadIdx.x;
     int i = gt / TPA, lane = gt % TPA;
     bool active = i < kp.n;
@@ -139,7 +137,7 @@ void pair_dispatch(md_ctx *c, const md_kparams &kp, const pair_consts &pc)
 #define MD_PAIR_CASE(T, BB)                                                                      \
     case T * 100 + BB:                                                                           \
         k_pair<KIND, T, BB, ENERGY><<<nb, 128, 0, c->stream>>>(                                  \
-            kp, pc, c->pos4, c->type, c->nl, c->nl_n, lj, c->f, c->vir, c->epot, c->st);         \
+            kp, pc, c->pos4, c->type, c->nl, c->nl_n, lj, c->f, c->vir, c->epot);                \
         break;
         MD_PAIR_CASE(1, 8)
         MD_PAIR_CASE(2, 8)

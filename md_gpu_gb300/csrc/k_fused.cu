@@ -52,13 +52,8 @@ __global__ void __launch_bounds__(FUSED_THREADS) k_pair_leapfrog(
         cp_async8(&s_mass[threadIdx.x], mass + ia);
         cp_async16(&s_old[threadIdx.x], io.pos_old + ia);
     }
-    const bool halted = md_halted(io.st);
     if (threadIdx.x < MD_MAXTYPE * MD_MAXTYPE) lj[threadIdx.x] = ljtab[threadIdx.x];
     __syncthreads();
-    if (halted) {   /* the copies in flight land in shared memory; wait for them */
-        cp_async_wait();
-        return;
-    }
     int gt = blockIdx.x * blockDim.x + threadIdx.x;
     int i = gt / TPA, lane = gt % TPA;
     bool active = i < kp.n;

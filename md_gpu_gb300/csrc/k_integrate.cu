@@ -51,7 +51,6 @@ __global__ void __launch_bounds__(3 * MD_LA) k_leapfrog(md_kparams kp, thermo_pa
     __shared__ float s_x[3][MD_LA];
     pdl_wait();      /* the forces of this step */
     pdl_trigger();   /* the list passes that follow may be scheduled */
-    if (md_halted(io.st)) return;
     const int d = threadIdx.x / MD_LA, a = threadIdx.x - d * MD_LA;
     const int s = blockIdx.x * MD_LA + a;
     const size_t o = (size_t)d * kp.pitch + s;
@@ -95,7 +94,6 @@ __global__ void __launch_bounds__(3 * MD_LA) k_vv_first(md_kparams kp, thermo_pa
     __shared__ float s_x[3][MD_LA];
     __shared__ long long sh[3 * (3 * MD_LA / 32)];
     pdl_trigger();   /* the list passes that follow may be scheduled */
-    if (md_halted(io.st)) return;
     const int d = threadIdx.x / MD_LA, a = threadIdx.x - d * MD_LA;
     const int s = blockIdx.x * MD_LA + a;
     const size_t o = (size_t)d * kp.pitch + s;
@@ -139,7 +137,6 @@ __global__ void __launch_bounds__(3 * MD_LA) k_vv_second(md_kparams kp, thermo_p
 {
     __shared__ long long sh[3 * (3 * MD_LA / 32)];
     pdl_wait();   /* the forces of this step */
-    if (md_halted(io.st)) return;
     const int d = threadIdx.x / MD_LA, a = threadIdx.x - d * MD_LA;
     const int s = blockIdx.x * MD_LA + a;
     const size_t o = (size_t)d * kp.pitch + s;

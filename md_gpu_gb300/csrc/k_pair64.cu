@@ -72,11 +72,10 @@ __global__ void __launch_bounds__(P64_THREADS) k_pair64(int n, int pitch, int ca
                                                        const int *__restrict__ type,
                                                        const unsigned *__restrict__ nl,
                                                        const int *__restrict__ nl_n, long long *f,
-                                                       float *vir, float *epot, const md_devstate *st)
+                                                       float *vir, float *epot)
 {
     __shared__ double2 lj[MD_MAXTYPE * MD_MAXTYPE];
     pdl_trigger();   /* the integrator may be scheduled; it waits for this grid */
-    const bool halted = st && md_halted(st);
     int rep = 0, i0, end;
     if (tab) {
         const int2 bt = tab[blockIdx.x];
@@ -93,7 +92,6 @@ __global__ void __launch_bounds__(P64_THREADS) k_pair64(int n, int pitch, int ca
         lj[threadIdx.x] = make_double2((double)l.x, (double)l.y);
     }
     __syncthreads();
-    if (halted) return;
     const int i = i0 + (int)threadIdx.x / P64_TPA, lane = (int)threadIdx.x % P64_TPA;
     const bool active = i < end;
     const int ii = active ? i : i0;
@@ -161,10 +159,10 @@ __global__ void k_bonded64(int n, int pitch, const double *__restrict__ boxd,
                            const int *__restrict__ bl_sn, const int4 *__restrict__ al_s,
                            const int *__restrict__ al_sn, const float *__restrict__ par, int has_bonds,
                            int has_angles, const md_rep *__restrict__ reps, const int *__restrict__ arep,
-                           long long *f, float *vir, float *epot, const md_devstate *st)
+                           long long *f, float *vir, float *epot)
 {
     const int s = blockIdx.x * blockDim.x + threadIdx.x;
-    if (s >= n || md_halted(st)) return;
+    if (s >= n) return;
     const size_t P = (size_t)pitch;
     const int nb = has_bonds ? bl_sn[s] : 0;
     const int na = has_angles ? al_sn[s] : 0;
@@ -305,7 +303,7 @@ void launch_pair64(md_ctx *c, bool energy)
 #define MD_P64_ARGS                                                                                \
     c->n, c->pitch, c->cap, c->centered, tab, reps, (const md_p64 *)c->p64_dev, lj, (const double *)c->x, \
         (const float4 *)c->pos4, (const int *)c->type, (const unsigned *)c->nl, (const int *)c->nl_n, c->f, \
-        c->vir, c->epot, (const md_devstate *)c->st
+        c->vir, c->epot
     if (c->lkspace == 0) {
         if (energy) k_pair64<0, true><<<nb, P64_THREADS, 0, c->stream>>>(MD_P64_ARGS);
         else k_pair64<0, false><<<nb, P64_THREADS, 0, c->stream>>>(MD_P64_ARGS);
@@ -326,9 +324,9 @@ void launch_bonded64(md_ctx *c, bool energy, int hb, int ha)
     if (energy)
         k_bonded64<true><<<nb, 256, 0, c->stream>>>(c->n, c->pitch, boxd, c->x, c->bl_s, c->bl_sn, c->al_s,
                                                     c->al_sn, c->bonded_par, hb, ha, reps, arep, c->f,
-                                                    c->vir, c->epot, c->st);
+                                                    c->vir, c->epot);
     else
         k_bonded64<false><<<nb, 256, 0, c->stream>>>(c->n, c->pitch, boxd, c->x, c->bl_s, c->bl_sn, c->al_s,
                                                      c->al_sn, c->bonded_par, hb, ha, reps, arep, c->f,
-                                                     c->vir, c->epot, c->st);
+                                                     c->vir, c->epot);
 }

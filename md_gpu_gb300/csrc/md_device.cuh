@@ -120,15 +120,6 @@ __device__ __forceinline__ void cp_async_wait()
 __device__ __forceinline__ void pdl_wait() { asm volatile("griddepcontrol.wait;" ::: "memory"); }
 __device__ __forceinline__ void pdl_trigger() { asm volatile("griddepcontrol.launch_dependents;" ::: "memory"); }
 
-/* Whether a kernel of the context stopped with a sticky error (a grid
- * barrier of the list rebuild that timed out): the step kernels then return
- * without work.  Read after the kernel's predecessors are complete (after
- * pdl_wait() where there is one), so every block sees the same value. */
-__device__ __forceinline__ bool md_halted(const md_devstate *st)
-{
-    return *(const volatile int *)&st->status != 0;
-}
-
 /* True in every thread of the block that finishes last (threadfence
  * reduction).  The caller's prior global writes are visible to that block;
  * it must read other blocks' results with __ldcg / volatile and reset the

@@ -44,7 +44,6 @@
 struct md_devstate {
     int update;          /* neighbour-list rebuild requested this step */
     int list_overflow;   /* largest list length seen beyond capacity, or 0 */
-    int status;          /* sticky device-side error code (1: a grid barrier timed out) */
     int builds;          /* neighbour-list builds so far */
     long long step;
     double temper;       /* temperature after the last step, K */
@@ -65,6 +64,11 @@ struct md_devstate {
      * generation do not contend with the arrivals' atomics */
     alignas(128) unsigned bar_count;
     alignas(128) unsigned bar_gen;
+    /* sticky device-side error code (1: a grid barrier timed out), read by
+     * the one-kernel rebuild: on a line of its own, which nothing writes
+     * unless a wait times out, so those reads never queue behind the
+     * atomics on the lines above */
+    alignas(128) int status;
 };
 
 /* Everything a kernel needs about the system, passed by value. */

@@ -206,6 +206,16 @@ def nacl_replica(natom: int, seed: int = 1, temp: float = 1200.0, density: float
         pos=_centre(pos, box), vel=_maxwell(rng, masses, temp))
 
 
+def nacl_melt64k() -> System:
+    """The 64000-ion molten-NaCl benchmark system (nacl_rocksalt(ncell=20,
+    seed=1) parameters) in its melted starting state at 1200 K, read from
+    cases/nacl64k_melt.npz (made by cases/make_melt.py)."""
+    path = os.path.join(os.path.dirname(os.path.abspath(__file__)), "cases", "nacl64k_melt.npz")
+    z = np.load(path)
+    base = nacl_rocksalt(ncell=int(z["ncell"]), seed=int(z["seed"]))
+    return dataclasses.replace(base, pos=z["pos"].astype(np.float64), vel=z["vel"].astype(np.float64))
+
+
 def replica_batch(nrep: int = 512, nmin: int = 256, nmax: int = 8192, seed: int = 1,
                   spread: float = 0.1, **kw) -> List[System]:
     """Uneven NaCl-like replicas: N uniform in [nmin, nmax] (rounded down to

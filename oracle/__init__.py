@@ -367,6 +367,38 @@ def md_ref_run(case: Case, pos4, vel4, nsteps, exact_ke=0, temper=None):
     return rc, f4, temps[:nsteps], float(t.value)
 
 
+class RefLoopState:
+    """The list the reference's loop keeps between steps (for md_ref_run_cont)."""
+
+    def __init__(self, n, nmaxlist):
+        pitch = ((n + 255) // 256) * 256
+        self.nnl = np.zeros(pitch * nmaxlist, np.uint32)
+        self.nnm = np.zeros(pitch, np.uint32)
+        self.pold = np.zeros((n, 4), F32)
+        self.have = C.c_int(0)
+
+
+def md_ref_run_cont(case: Case, pos4, vel4, nsteps, state: RefLoopState, temper=None):
+    """md_ref_run continuing from the list in `state` (built on the first call):
+    the reference's loop over consecutive calls, rebuilding only on its
+    displacement criterion; returns (builds in this call, temper)."""
+    n = pos4.shape[0]
+    t = C.c_float(case.params.temper_0 if temper is None else temper)
+    fld = case.fld
+    b = np.ascontiguousarray(case.bonds, np.int32)
+    a = np.ascontiguousarray(case.angles, np.int32)
+    fld.nbonds, fld.nangle = b.shape[0], a.shape[0]
+    fld.bonds = _p(b, C.c_int)
+    fld.angles = _p(a, C.c_int)
+    rc = lib().orc_md_ref_run_cont(C.byref(case.params), C.byref(fld), n, _p(pos4, C.c_float),
+                                   _p(vel4, C.c_float), _p(case.box, C.c_float), _p(case.boxi, C.c_float),
+                                   nsteps, 0, _p(state.nnl, C.c_uint), _p(state.nnm, C.c_uint),
+                                   _p(state.pold, C.c_float), C.byref(state.have), None, C.byref(t), None)
+    fld.bonds = C.POINTER(C.c_int)()
+    fld.angles = C.POINTER(C.c_int)()
+    return rc, float(t.value)
+
+
 def md_plain_run(case: Case, x, v, nsteps, integrator, state=None, records=True):
     """FP64 plain-form run (all pairs, small N); returns (state[4], records[nsteps,3])."""
     n = x.shape[0]

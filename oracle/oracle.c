@@ -1024,6 +1024,16 @@ int orc_md_ref_run(const orc_params *p, const orc_ffield *f, int n, float *pos4,
                    const float box[3], const float boxi[3], int nsteps, int exact_ke,
                    float *force4_out, float *temper_io, float *temps_out)
 {
+    int have = 0;
+    return orc_md_ref_run_cont(p, f, n, pos4, vel4, box, boxi, nsteps, exact_ke, NULL, NULL, NULL, &have,
+                               force4_out, temper_io, temps_out);
+}
+
+int orc_md_ref_run_cont(const orc_params *p, const orc_ffield *f, int n, float *pos4, float *vel4,
+                        const float box[3], const float boxi[3], int nsteps, int exact_ke,
+                        unsigned *nnl_io, unsigned *nnm_io, float *pold_io, int *have_list,
+                        float *force4_out, float *temper_io, float *temps_out)
+{
     int pitch = orc_pitch(n), nmax = p->nmaxlist;
     int kind = p->lkspace == 0 ? 0 : 1;
     float rskinsq = orc_rskinsq(p->skin, p->rcutsq), rmaxdif = orc_rmaxdif(p->skin);
@@ -1031,9 +1041,10 @@ int orc_md_ref_run(const orc_params *p, const orc_ffield *f, int n, float *pos4,
     if (p->lkspace > 0) orc_wolf_consts(p->alfa, p->rcutsq, wc);
     if (p->lkspace != 1) wc[3] = 0.0f;
     unsigned *excl = (unsigned *)malloc(sizeof(unsigned) * 4 * (size_t)n);
-    unsigned *nnl = (unsigned *)malloc(sizeof(unsigned) * (size_t)pitch * (size_t)nmax);
-    unsigned *nnm = (unsigned *)malloc(sizeof(unsigned) * (size_t)pitch);
-    float *pold = (float *)malloc(sizeof(float) * 4 * (size_t)n);
+    const int own = nnl_io == NULL;
+    unsigned *nnl = own ? (unsigned *)malloc(sizeof(unsigned) * (size_t)pitch * (size_t)nmax) : nnl_io;
+    unsigned *nnm = own ? (unsigned *)malloc(sizeof(unsigned) * (size_t)pitch) : nnm_io;
+    float *pold = own ? (float *)malloc(sizeof(float) * 4 * (size_t)n) : pold_io;
     float *frc = (float *)malloc(sizeof(float) * 4 * (size_t)n);
     int nblk = (n + 255) / 256;
     float *part = (float *)malloc(sizeof(float) * (size_t)nblk);
@@ -1051,9 +1062,12 @@ int orc_md_ref_run(const orc_params *p, const orc_ffield *f, int n, float *pos4,
         if (orc_angle_lists(n, f->nangle, f->angles, pitch, al, alm)) { rc = -2; goto done; }
     }
     float temper = temper_io ? *temper_io : p->temper_0;
-    if (orc_nlist_nsquared(n, pos4, box, boxi, rskinsq, excl, pitch, nmax, nnl, nnm) > nmax) { rc = -1; goto done; }
-    memcpy(pold, pos4, sizeof(float) * 4 * (size_t)n);
-    builds = 1;
+    if (!*have_list) {   /* neighborlist_init: the first build */
+        if (orc_nlist_nsquared(n, pos4, box, boxi, rskinsq, excl, pitch, nmax, nnl, nnm) > nmax) { rc = -1; goto done; }
+        memcpy(pold, pos4, sizeof(float) * 4 * (size_t)n);
+        builds = 1;
+        *have_list = 1;
+    }
     for (int t = 0; t < nsteps; t++) {
         if (orc_nlist_check(n, pos4, pold, box, boxi, rmaxdif)) {
             if (orc_nlist_nsquared(n, pos4, box, boxi, rskinsq, excl, pitch, nmax, nnl, nnm) > nmax) { rc = -1; goto done; }
@@ -1079,7 +1093,9 @@ int orc_md_ref_run(const orc_params *p, const orc_ffield *f, int n, float *pos4,
     if (force4_out) memcpy(force4_out, frc, sizeof(float) * 4 * (size_t)n);
     rc = builds;
 done:
-    free(excl); free(nnl); free(nnm); free(pold); free(frc); free(part);
+    if (rc < 0) *have_list = 0;
+    if (own) { free(nnl); free(nnm); free(pold); }
+    free(excl); free(frc); free(part);
     free(bl); free(blm); free(al); free(alm);
     return rc;
 }

@@ -174,6 +174,17 @@ void orc_nh_half_f64(int n, double *v, const double *m, double dt, double t0, do
 int orc_md_ref_run(const orc_params *p, const orc_ffield *f, int n, float *pos4, float *vel4,
                    const float box[3], const float boxi[3], int nsteps, int exact_ke,
                    float *force4_out, float *temper_io, float *temps_out);
+/* The same loop continuing a run across calls: the caller owns the list
+ * (nnl: orc_pitch(n) * nmaxlist, nnm: orc_pitch(n), pold: 4n floats); with
+ * *have_list == 0 the call first builds it (neighborlist_init,
+ * neighborlist.cu:30-106) and sets *have_list, otherwise it continues with
+ * the list of the previous call and rebuilds only on the displacement
+ * criterion (neighborlist.cu:109-146), as the reference's loop does between
+ * its steps.  Returns the builds made in this call, or -1 on overflow. */
+int orc_md_ref_run_cont(const orc_params *p, const orc_ffield *f, int n, float *pos4, float *vel4,
+                        const float box[3], const float boxi[3], int nsteps, int exact_ke,
+                        unsigned *nnl, unsigned *nnm, float *pold, int *have_list,
+                        float *force4_out, float *temper_io, float *temps_out);
 
 /* FP64 plain-form run: integrator 0 leapfrog(+Berendsen if enstype 1),
  * 1 velocity Verlet NVE, 2 Nose-Hoover VV.  All-pairs forces inside rc
