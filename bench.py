@@ -216,6 +216,49 @@ def drift_leg(args):
                  "gate_resolved is false when the difference's standard error exceeds the gate")}
 
 
+def reference_cuda_leg(args, value, e2e_value):
+    """The reference's own CUDA build (its sources compat-patched and compiled
+    for sm_103a, baseline/reference_cuda.py) on the same melted 64000-ion
+    case: its SimulationRun_CUDA loop timed for --ref-cuda-steps steps less a
+    0-step run, and one list build + force evaluation of its kernels compared
+    with the library's."""
+    from baseline import reference_cuda as rc
+
+    import md_gpu_gb300 as md
+    from md_gpu_gb300 import synth
+    if not rc.have_sources():
+        return {"unavailable": "patched reference sources absent (made from the reference tree by build())"}
+    binary = rc.build()
+    sys_ = synth.nacl_melt64k() if args.ncell == 20 else synth.nacl_rocksalt(ncell=args.ncell, seed=1)
+    tmp = tempfile.mkdtemp(prefix="mdref_")
+    base = synth.write_case(sys_, os.path.join(tmp, "f"), "ref")
+    maxcount = rc.check_case(base)
+    nmax_ref, f_ref, cols_ref = rc.forces(binary, base)
+    with md.MDSystem.from_files(base) as s:
+        nn, nm = s.neighbor_list(int(nmax_ref.max()) + 1)
+        s.compute_forces(md.TERM_PAIR)
+        F = s.forces()
+    n = len(nmax_ref)
+    cols = nn.reshape(-1, nm.shape[0])
+    same_list = bool(np.array_equal(nm[:n], nmax_ref) and all(
+        np.array_equal(cols[k, :n][nmax_ref > k], cols_ref[k][nmax_ref > k]) for k in range(int(nmax_ref.max()))))
+    f_ref64 = f_ref[:, :3].astype(np.float64)
+    diff = float(np.sqrt(((F[:, :3] - f_ref64) ** 2).sum() / (f_ref64 ** 2).sum()))
+    secs, best = rc.time_steps(binary, sys_, tmp, args.ref_cuda_steps)
+    rate = n * args.ref_cuda_steps / secs
+    return {"value": rate, "unit": UNIT, "md_steps": args.ref_cuda_steps, "seconds": secs,
+            "run_seconds": {str(k): v for k, v in best.items()},
+            "speedup": value / rate, "e2e_speedup": e2e_value / rate, "target_speedup": 5.0,
+            "list_bit_exact_vs_reference_gpu": same_list, "largest_neighbour_count": maxcount,
+            "force_rms_rel_diff_vs_reference_gpu": diff,
+            "note": ("the reference's sources (src/: the 8 translation units besides athom.cu) with the CUDA 13 "
+                     "compat patch (texture reference -> __constant__ pointer, tex1Dfetch -> index, string "
+                     "symbols -> symbols) and its parser's heap overflows repaired, nvcc -O3 sm_103a, its "
+                     "SimulationRun_CUDA loop (O(N^2) list, 1 thread per atom, host round trips every step) "
+                     "from the same melted state, driven by baseline/ref_driver.cu; wall time of "
+                     f"{args.ref_cuda_steps} steps less a 0-step run, best of 2")}
+
+
 def make_case(seed, ncell, tmp):
     """The benchmark system: at the full size (ncell 20) the melted state
     every arm starts from; other sizes a seeded jittered lattice."""
@@ -513,6 +556,7 @@ def run_ours(args):
                "h2d_bytes_per_step": 2 * 3 * n * 8,
                "d2h_bytes_per_step": 2 * 3 * n * 8 + args.md_steps * 72,
                "call": "md_run_host (upload pos/vel, list build, md_steps steps, download records + pos/vel)"}
+        ref_cuda = reference_cuda_leg(args, value, e2e["value"]) if args.ref_cuda_steps > 0 else None
         if args.nrep > 0:
             extra_batch = batch_leg(args, flush)
         extra_adj = adjoint_leg(args) if args.adj_nrep > 0 else None
@@ -537,6 +581,8 @@ def run_ours(args):
                                             "continuing run from the melted state (after one untimed slice; "
                                             f"{cpu_builds} O(N^2) builds on the skin/2 criterion), oracle "
                                             "FP32 restatement of the reference's loop, OpenMP"}}
+        if ref_cuda is not None:
+            extra["reference_cuda"] = ref_cuda
         if args.nrep > 0:
             extra["batched_replicas"] = extra_batch
         if extra_adj is not None:
@@ -590,6 +636,8 @@ def main():
                     help="timed segments of the argon and water systems (0: skip them)")
     ap.add_argument("--ref-md-steps", type=int, default=32,
                     help="MD steps per timed slice of the CPU reference loop (slices of one continuing run)")
+    ap.add_argument("--ref-cuda-steps", type=int, default=1000,
+                    help="steps of the reference's own CUDA loop timed beside the library (0: skip)")
     ap.add_argument("--drift-reps", type=int, default=16, help="argon replicas of the NVE drift leg (0: skip)")
     ap.add_argument("--drift-ps", type=float, default=100.0, help="FP32 horizon of the drift leg, ps")
     ap.add_argument("--drift-fp64-ps", type=float, default=10.0, help="FP64 horizon of the drift leg, ps")
