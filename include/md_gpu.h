@@ -183,7 +183,13 @@ md_status md_compute_forces(md_ctx *ctx, int terms, int energy);
 /* nsteps iterations of the reference's loop body (runGPU.cu:69-104):
  * list check and rebuild, forces, integrate.  energy_every > 0 computes
  * energies on steps that are multiples of it (the reference's timprn).
- * Steps run as a captured CUDA graph; no host synchronisation inside. */
+ * Steps run as a captured CUDA graph; no host synchronisation inside.  A
+ * list rebuild inside the run that finds a row longer than the list holds
+ * (the reference writes past its list then, neighborlist.cu:284) truncates
+ * rows, so the call saves the state on the device when it starts; after an
+ * overflow it restores that state, grows the list, rebuilds it and runs the
+ * same steps again (md_info.list_regrows counts such calls), and returns
+ * MD_ERR_LIST_OVERFLOW only when that fails three times. */
 md_status md_step(md_ctx *ctx, int nsteps, int energy_every);
 /* The integrate phase of one step alone, with the forces of the last
  * md_compute_forces (for callers that drive the phases themselves, as the
@@ -253,6 +259,7 @@ typedef struct {
     int fused_step;         /* 1: step graphs run pair forces and update as one kernel */
     int rebuild_inline;     /* 1: step graphs hold the rebuild passes inline, 0: behind a
                                conditional node */
+    int list_regrows;       /* md_step calls run again after their list overflowed (md_step) */
 } md_info;
 md_status md_get_info(md_ctx *ctx, md_info *out);
 /* Sorted -> original index map of the current atom order. */
@@ -308,6 +315,12 @@ md_status md_set_precision(md_ctx *ctx, int bits);
  * timed out".  The context must then be destroyed (its atom order may be
  * half permuted); the CUDA context stays usable.  timeout_ms = 0 and drop_block = -1 restore the defaults. */
 md_status md_debug_rebuild_barrier(md_ctx *ctx, double timeout_ms, int drop_block);
+/* Test hook (no counterpart in the reference): gives the list capacity
+ * entries per atom (a multiple of 32, >= 32; the list is reallocated) and
+ * makes the next step rebuild it, so that a too-small list overflows inside
+ * a run; retry 0 makes md_step report the overflow (MD_ERR_LIST_OVERFLOW)
+ * instead of growing the list and running the steps again. */
+md_status md_debug_list_capacity(md_ctx *ctx, int capacity, int retry);
 /* md_step launches each step's kernels eagerly instead of replaying a
  * captured graph when use_graphs is 0 (for profilers and debugging). */
 md_status md_set_graphs(md_ctx *ctx, int use_graphs);

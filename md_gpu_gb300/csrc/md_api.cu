@@ -253,7 +253,7 @@ void free_device(md_ctx *c)
                     c->tmp_i, c->bl_o, c->bl_on, c->al_o, c->al_on, c->bl_s, c->bl_sn, c->al_s,
                     c->al_sn, c->st, c->rec, c->lj_dev, c->bonded_par,
                     c->type_mask_dev, c->io_dev, c->reps_dev, c->repst, c->arep, c->crep,
-                    c->ljr_dev, c->grid_tab, c->rep_upd, c->racc, c->p64_dev, c->rep_hist};
+                    c->ljr_dev, c->grid_tab, c->rep_upd, c->racc, c->p64_dev, c->rep_hist, c->snap};
     for (void *p : ptrs)
         if (p) cudaFree(p);
 }
@@ -1455,9 +1455,8 @@ md_status md_integrate_cor(md_ctx *c, int energy)
     return check_overflow_and_sync(c);
 }
 
-md_status md_step(md_ctx *c, int nsteps, int energy_every)
+static md_status step_body(md_ctx *c, int nsteps, int energy_every)
 {
-    if (!c || nsteps < 0 || energy_every < 0) return MD_ERR_ARG;
     MD_CUDA_TRY(c, cudaEventRecord(c->ev0, c->stream));
     int left = nsteps;
     while (left > 0) {
@@ -1492,6 +1491,98 @@ md_status md_step(md_ctx *c, int nsteps, int energy_every)
     MD_CUDA_TRY(c, cudaEventRecord(c->ev1, c->stream));
     MD_CUDA_TRY(c, cudaGetLastError());
     return check_overflow_and_sync(c);
+}
+
+/* The arrays a run of steps changes, in the order they are packed into the
+ * snapshot: the integrated state and everything a re-sort permutes (the
+ * list, cells and sorted bonded lists are rebuilt after a restore). */
+struct snap_part {
+    void *dev;
+    size_t bytes;
+};
+static std::vector<snap_part> snap_parts(md_ctx *c)
+{
+    const size_t P = c->pitch;
+    std::vector<snap_part> v = {
+        {c->st, sizeof(md_devstate)},       {c->x, 3 * P * sizeof(double)},
+        {c->v, 3 * P * sizeof(double)},     {c->mass, P * sizeof(double)},
+        {c->kick, P * sizeof(double)},      {c->pos4, P * sizeof(float4)},
+        {c->type, P * sizeof(int)},         {c->perm, P * sizeof(int)},
+        {c->iperm, P * sizeof(int)},        {c->f, 3 * P * sizeof(long long)},
+        {c->vir, P * sizeof(float)},        {c->epot, P * sizeof(float)}};
+    if (c->batch) {
+        v.push_back({c->repst, c->nrep * sizeof(md_repstate)});
+        v.push_back({c->racc, 3 * (size_t)c->nrep * sizeof(unsigned long long)});
+        v.push_back({c->rep_upd, c->nrep * sizeof(int)});
+    }
+    return v;
+}
+
+/* Stream-ordered device copies of the state into the snapshot (or back). */
+static md_status snapshot(md_ctx *c, bool save)
+{
+    std::vector<snap_part> parts = snap_parts(c);
+    size_t total = 0;
+    for (const snap_part &p : parts) total += (p.bytes + 255) / 256 * 256;
+    if (save && c->snap_bytes < total) {
+        if (c->snap) cudaFree(c->snap);
+        c->snap = nullptr;
+        c->snap_bytes = 0;
+        MD_CUDA_TRY(c, cudaMalloc(&c->snap, total));
+        c->snap_bytes = total;
+    }
+    if (save) {
+        c->snap_p4 = c->pos4;
+        c->snap_p4alt = c->pos4_alt;
+        c->snap_host_step = c->host_step;
+    } else {
+        c->pos4 = c->snap_p4;
+        c->pos4_alt = c->snap_p4alt;
+        c->host_step = c->snap_host_step;
+        parts = snap_parts(c);   /* pos4 is the buffer current at the save */
+    }
+    size_t off = 0;
+    for (const snap_part &p : parts) {
+        char *s = (char *)c->snap + off;
+        MD_CUDA_TRY(c, cudaMemcpyAsync(save ? (void *)s : p.dev, save ? p.dev : (const void *)s, p.bytes,
+                                       cudaMemcpyDeviceToDevice, c->stream));
+        off += (p.bytes + 255) / 256 * 256;
+    }
+    return MD_OK;
+}
+
+/* A list overflow inside a run of steps truncates rows, so every step after
+ * the rebuild that overflowed is wrong.  md_step therefore saves the state
+ * on the device when it starts (a few device-to-device copies, ~170 B per
+ * atom) and, when the run ends with an overflow, restores it, grows the
+ * list to 5/4 of the longest row plus 16, rebuilds it at the restored
+ * positions (forces recomputed for velocity Verlet) and runs the same steps
+ * again, up to three times. */
+md_status md_step(md_ctx *c, int nsteps, int energy_every)
+{
+    if (!c || nsteps < 0 || energy_every < 0) return MD_ERR_ARG;
+    if (!c->overflow_retry || nsteps == 0) return step_body(c, nsteps, energy_every);
+    md_status s = snapshot(c, true);
+    if (s != MD_OK) return s;
+    s = step_body(c, nsteps, energy_every);
+    for (int tries = 0; s == MD_ERR_LIST_OVERFLOW && tries < 3; tries++) {
+        md_devstate h;
+        MD_CUDA_TRY(c, cudaMemcpy(&h, c->st, sizeof(h), cudaMemcpyDeviceToHost));
+        const int cap = ((h.list_overflow * 5 / 4 + 16) + 31) / 32 * 32;
+        s = snapshot(c, false);   /* the saved state has no overflow recorded */
+        if (s != MD_OK) return s;
+        if (c->gexec) {           /* the step graph holds the old capacity */
+            cudaGraphExecDestroy(c->gexec);
+            c->gexec = nullptr;
+        }
+        s = alloc_list(c, std::max(cap, c->cap));
+        if (s == MD_OK) s = initial_build(c);
+        if (s == MD_OK) s = refresh_state(c);
+        if (s != MD_OK) return s;
+        c->regrows++;
+        s = step_body(c, nsteps, energy_every);
+    }
+    return s;
 }
 
 md_status md_last_step_ms(md_ctx *c, float *ms)
@@ -1776,6 +1867,7 @@ md_status md_get_info(md_ctx *c, md_info *out)
     out->positions_centered = c->centered;
     out->fused_step = md_can_fuse(c) ? 1 : 0;
     out->rebuild_inline = (c->rebuild_inline && !c->batch) ? 1 : 0;
+    out->list_regrows = c->regrows;
     out->list_threads_per_atom = c->list_tpa;
     out->builds = h.builds;
     out->max_neighbors = *std::max_element(cnt.begin(), cnt.begin() + c->n);
@@ -1929,6 +2021,26 @@ md_status md_autotune(md_ctx *c, int *pair_tpa, int *list_tpa)
     }
     if (pair_tpa) *pair_tpa = bp;
     if (list_tpa) *list_tpa = bl;
+    return MD_OK;
+}
+
+md_status md_debug_list_capacity(md_ctx *c, int capacity, int retry)
+{
+    if (!c || capacity < 32 || capacity % 32) return MD_ERR_ARG;
+    MD_CUDA_TRY(c, cudaStreamSynchronize(c->stream));
+    if (c->gexec) {
+        cudaGraphExecDestroy(c->gexec);
+        c->gexec = nullptr;
+    }
+    md_status s = alloc_list(c, capacity);
+    if (s != MD_OK) return s;
+    const int one = 1;
+    MD_CUDA_TRY(c, cudaMemcpy(&c->st->update, &one, sizeof(int), cudaMemcpyHostToDevice));
+    if (c->batch) {   /* every replica rebuilds */
+        std::vector<int> ones(c->nrep, 1);
+        MD_CUDA_TRY(c, cudaMemcpy(c->rep_upd, ones.data(), sizeof(int) * c->nrep, cudaMemcpyHostToDevice));
+    }
+    c->overflow_retry = retry ? 1 : 0;
     return MD_OK;
 }
 

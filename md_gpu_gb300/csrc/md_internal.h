@@ -253,6 +253,15 @@ struct md_ctx {
     int2 *grid_tab = nullptr;     /* the MD_NGRID replica-aligned grids, concatenated */
     int grid_off[MD_NGRID] = {0}, grid_cnt[MD_NGRID] = {0};
 
+    /* state at the start of an md_step call, kept on the device so that a
+     * call whose list overflowed can be run again with a larger list */
+    void *snap = nullptr;          /* one allocation holding every array below */
+    size_t snap_bytes = 0;
+    float4 *snap_p4 = nullptr, *snap_p4alt = nullptr;   /* the position buffers' roles */
+    long long snap_host_step = 0;
+    int overflow_retry = 1;        /* 0: report a list overflow inside md_step without re-running */
+    int regrows = 0;               /* md_step calls re-run after a list overflow */
+
     /* timing of the last md_step call (CUDA events on the stream) */
     cudaEvent_t ev0 = nullptr, ev1 = nullptr;
 };

@@ -68,7 +68,7 @@ class Info(C.Structure):
                 ("builds", C.c_int), ("max_neighbors", C.c_int), ("kernels_per_step", C.c_int),
                 ("kernels_per_rebuild", C.c_int), ("kernels_per_graph", C.c_int),
                 ("pair_entries_per_lane", C.c_int), ("positions_centered", C.c_int),
-                ("fused_step", C.c_int), ("rebuild_inline", C.c_int)]
+                ("fused_step", C.c_int), ("rebuild_inline", C.c_int), ("list_regrows", C.c_int)]
 
 
 def _make_desc(keep, *, box, itype, charge, pos, vel, type_mass, lj1, lj2, lkspace, rcutsq,
@@ -159,6 +159,7 @@ def library(path: Optional[str] = None):
     L.md_set_graphs.argtypes = [vp, C.c_int]
     L.md_debug_rebuild_barrier.argtypes = [vp, C.c_double, C.c_int]
     L.md_set_precision.argtypes = [vp, C.c_int]
+    L.md_debug_list_capacity.argtypes = [vp, C.c_int, C.c_int]
     L.md_get_replica_history.argtypes = [vp, vp, C.c_int, C.POINTER(C.c_int)]
     L.md_set_fused_step.argtypes = [vp, C.c_int]
     L.md_set_graph_rebuild.argtypes = [vp, C.c_int]
@@ -406,7 +407,8 @@ class MDSystem:
                 "kernels_per_graph": i.kernels_per_graph,
                 "pair_depth": i.pair_entries_per_lane,
                 "centered": bool(i.positions_centered),
-                "fused_step": bool(i.fused_step), "rebuild_inline": bool(i.rebuild_inline)}
+                "fused_step": bool(i.fused_step), "rebuild_inline": bool(i.rebuild_inline),
+                "list_regrows": i.list_regrows}
 
     def neighbor_list(self, nmax):
         """Reference layout (neighborlist.cu:284): (nnlist[pitch*nmax], nnlist_max[pitch])."""
