@@ -568,6 +568,16 @@ def run_ours(args):
                           "m = 1 g/mol, rc 2.5, skin 0.3, T* 0.72, velocity Verlet NVE dt 0.5 fs"),
                 **system_leg("argon", synth.argon_fcc(10, seed=1, integrator="vv"), "velocity Verlet NVE",
                              0.5, args, flush))
+            import dataclasses
+            melt = synth.nacl_melt64k() if args.ncell == 20 else synth.nacl_rocksalt(ncell=args.ncell, seed=1)
+            npt_inp = dict(melt.inp, ensemble="npt", press=1.0, tau_p=1000.0, compressibility=4.5e-5)
+            others["nacl64k_npt"] = dict(
+                workload=("the benchmark's melted 64000-ion NaCl at constant pressure: Berendsen leapfrog "
+                          "with the Berendsen thermostat (1200 K, tau 100 fs) and barostat (1 bar, tau_p "
+                          "1000 fs, compressibility 4.5e-5/bar), dt 2 fs; a batch of one replica (the box "
+                          "read by the kernels from device memory)"),
+                **system_leg("nacl_npt", dataclasses.replace(melt, inp=npt_inp),
+                             "Berendsen leapfrog NPT", 2.0, args, flush))
             others["water98k"] = dict(
                 workload=("flexible 3-site water, 32768 molecules (98304 atoms) at 0.997 g/cm^3, harmonic "
                           "O-H bonds and H-O-H angles, H-H excluded, Wolf alpha 0.2/A rc 10 A skin 1 A, "

@@ -29,7 +29,7 @@ typedef enum {
     MD_ERR_CUDA = 4,           /* CUDA runtime error (see md_last_error) */
     MD_ERR_LIST_OVERFLOW = 5,  /* an atom has more neighbours than the list holds */
     MD_ERR_BONDED = 6,         /* more than four bonds / angles on one atom */
-    MD_ERR_UNSUPPORTED = 7,    /* option not implemented (e.g. NPT) */
+    MD_ERR_UNSUPPORTED = 7,    /* option not implemented */
     MD_ERR_BOX = 8             /* cutoff + skin larger than half the box */
 } md_status;
 
@@ -69,7 +69,8 @@ typedef struct {
     float alfa;                 /* damping alpha, 1/A (lkspace 1, 2) */
     float skin;                 /* list skin, A */
     int nmaxlist;               /* list capacity per atom (minimum) */
-    int enstype;                /* 0 NVE, 1 NVT */
+    int enstype;                /* 0 NVE, 1 NVT, 2 NPT (Berendsen leapfrog; md_create makes
+                                   the context a batch of one replica, see md_set_barostat) */
     float temper_0;             /* K */
     float dt;                   /* fs */
     float tau_t;                /* thermostat time constant, fs (Berendsen and NH) */
@@ -301,6 +302,25 @@ md_status md_set_type_exclusions(md_ctx *ctx, const unsigned *mask);
  * contexts run no fused step and no adjoint (md_adjoint_run returns
  * MD_ERR_UNSUPPORTED). */
 md_status md_set_precision(md_ctx *ctx, int bits);
+/* NPT: the Berendsen barostat the reference sketches (npt_leapfrog_ber.cu:
+ * 28-125 sums the kinetic energy and virial of a leapfrog step but never
+ * changes the box, and integrator.cu:157-164 leaves it uncalled).  Each step
+ * of a leapfrog NPT context (enstype 2: Berendsen thermostat as in NVT)
+ * computes every replica's pressure P = (2 KE + sum over pairs of F.r) /
+ * (3 V) from its kinetic energy and virial, and the next step scales the
+ * replica's positions and box by mu = 1 - beta dt / (3 tau_p) (P0 - P)
+ * (|mu - 1| <= 1e-4 per step), on the device.  press_bar = P0 in bar (the
+ * .inp's npt line), tau_p_fs (default 1000; ".inp" extension line
+ * "tau_p: <fs>"), compressibility_per_bar = beta (default 4.5e-5;
+ * "compressibility: <1/bar>").  The cell grid is laid out 3% longer than
+ * the list needs, so a box may shrink ~3% per axis before the context
+ * reports MD_ERR_BOX and must be created again.  Bonds add their virial,
+ * angles none (as the reference's angle_forces). */
+md_status md_set_barostat(md_ctx *ctx, double press_bar, double tau_p_fs, double compressibility_per_bar);
+/* Box edges (nrep x 3, A) and last-step pressure (nrep, bar; may be NULL)
+ * of the replicas of a batch after the last md_step (NPT moves them); for a
+ * single system its fixed box and pressure 0.  Synchronises the stream. */
+md_status md_get_replica_box(md_ctx *ctx, double *box3, double *pressure_bar, int nrep);
 /* Test hook of the one-kernel list rebuild of a single system (no
  * counterpart in the reference, whose list build has no grid barriers):
  * its phases are separated by grid barriers whose waits give up after

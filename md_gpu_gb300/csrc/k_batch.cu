@@ -74,6 +74,17 @@ __device__ void finalize_b(const md_kparams &kp, const thermo_par &tp, int mode,
         const double a = fix_take(racc + 3 * r, MD_KFIX);
         double b = fix_take(racc + 3 * r + 1, MD_EFIX);
         double c = fix_take(racc + 3 * r + 2, MD_EFIX);
+        if (tp.npt && mode == 0) {
+            /* P = (2 KE + sum_pairs F.r) / (3 V); c = sum over atoms of ff r^2,
+             * every pair counted from both atoms; V of the box the forces saw */
+            const double V = R.boxd[0] * R.boxd[1] * R.boxd[2];
+            const double P = (2.0 * a + 0.5 * c) / (3.0 * V);
+            double mu = 1.0 - R.mu_k * (R.p0 - P);
+            mu = fmin(fmax(mu, 1.0 - R.mu_max), 1.0 + R.mu_max);
+            repst[r].pressure = P;
+            repst[r].mu_used = repst[r].mu_next;
+            repst[r].mu_next = mu;
+        }
         if (!tp.energy) b = c = 0.0;
         thermo_par t = tp;
         t.t0 = R.t0;
@@ -137,15 +148,25 @@ __global__ void __launch_bounds__(3 * MD_LA) k_leapfrog_b(md_kparams kp, thermo_
     const size_t o = (size_t)d * kp.pitch + s;
     double ke2 = 0.0, pe = 0.0, w = 0.0;
     if (act) {
-        const axis_par ax = axis_of(d, R.wlim, R.boxd, R.box2i);
+        axis_par ax = axis_of(d, R.wlim, R.boxd, R.box2i);
         double vv = v[o] + (double)f[o] * kick[s];
         if (tp.berendsen) vv *= repst[bt.x].lam_next;
         v[o] = vv;
         double xx = x[o] + vv * kp.dt;
+        if (tp.npt) {
+            /* Berendsen barostat: positions and box scaled by the factor the
+             * last step's pressure gave; wrap into the scaled box */
+            const double mu = repst[bt.x].mu_next;
+            xx *= mu;
+            ax.L *= mu;
+            ax.two_over_l = 2.0 / ax.L;
+            ax.lim = 0.4999f * (float)ax.L;
+        }
         s_x[d][a] = wrap(xx, ax.lim, ax.L, ax.two_over_l);
         x[o] = xx;
         ke2 = mass[s] * (vv * vv);
-        if (d == 0 && tp.energy) { pe = epot[s]; w = vir[s]; }
+        if (d == 0 && tp.energy) pe = epot[s];
+        if (d == 0 && (tp.energy || tp.npt)) w = vir[s];
     }
     __syncthreads();
     if (d == 0 && act) {
@@ -156,7 +177,7 @@ __global__ void __launch_bounds__(3 * MD_LA) k_leapfrog_b(md_kparams kp, thermo_
             rep_upd[bt.x] = 1;
         }
     }
-    block_fix_add(ke2, pe, w, tp.energy, racc + 3 * bt.x, shl);
+    block_fix_add(ke2, pe, w, tp.energy || tp.npt, racc + 3 * bt.x, shl);
     if (md_last_block(io.counter)) {
         finalize_b(kp, tp, 0, nrep, reps, repst, racc, io.st, io.rec, io.rec_cap, io.rep_hist, sh);
         if (threadIdx.x == 0) {
@@ -252,6 +273,38 @@ __global__ void __launch_bounds__(3 * MD_LA) k_vv_second_b(md_kparams kp, thermo
     }
 }
 
+/* NPT: after a leapfrog step, one thread per replica scales the replica's box
+ * by the factor the step applied to its positions (mu_used) and refreshes
+ * what the kernels derive from it: the FP32 box and its inverse as the
+ * reference rounds it (simulation.cu:290-292), 2/L, the wrap limit and the
+ * cell side.  The cell grid keeps its cell counts and stencil, so a box
+ * whose cells shrink below half the list radius (or whose list radius
+ * exceeds half the box) can no longer be listed correctly: that sets the
+ * sticky status 2, which the host reports; the grid is laid out with a 3%
+ * margin, which the per-step clamp of mu (1e-4) lets no md_step call
+ * shorter than 300 steps exhaust. */
+__global__ void k_npt_box_b(int nrep, md_rep *reps, const md_repstate *__restrict__ repst, md_devstate *st)
+{
+    const int r = blockIdx.x * blockDim.x + threadIdx.x;
+    if (r >= nrep) return;
+    md_rep &R = reps[r];
+    if (!R.npt) return;
+    const double mu = repst[r].mu_used;
+    bool bad = false;
+    for (int d = 0; d < 3; d++) {
+        const double L = R.boxd[d] * mu;
+        R.boxd[d] = L;
+        R.box[d] = (float)L;
+        R.boxi[d] = (float)(1.0 / L);
+        R.box2i[d] = 2.0 / L;
+        R.wlim[d] = 0.4999f * R.box[d];
+        R.binlen[d] = R.box[d] / (float)R.ncell[d];
+        if (R.stencil[d] >= 0 && R.binlen[d] < R.rl_half) bad = true;
+        if (2.0f * R.rl_half > 0.5f * R.box[d]) bad = true;
+    }
+    if (bad) atomicOr(&st->status, 2);
+}
+
 template <int KIND, bool ENERGY>
 void pair_dispatch_b(md_ctx *c, const md_kparams &kp)
 {
@@ -308,11 +361,23 @@ void launch_forces_b(md_ctx *c, const md_kparams &kp, bool energy, int terms)
 void launch_leapfrog_b(md_ctx *c, const md_kparams &kp, int energy, unsigned long long cond,
                        int has_cond)
 {
+    struct npt_after {   /* the box follows the positions the step scaled */
+        md_ctx *c;
+        ~npt_after()
+        {
+            if (c->enstype == 2) launch_npt_box_b(c);
+        }
+    } after{c};
     md_launch_pdl(k_leapfrog_b, dim3(grid_int_blocks(c)), dim3(3 * MD_LA), c->stream, kp,
                   make_tp(c, energy), make_io(c, cond, has_cond), c->nrep, grid_int(c),
                   (const md_rep *)c->reps_dev, c->repst, c->rep_upd, c->racc, c->x, c->v,
                   (const double *)c->mass, (const double *)c->kick, c->pos4,
                   (const long long *)c->f, (const float *)c->epot, (const float *)c->vir);
+}
+
+void launch_npt_box_b(md_ctx *c)
+{
+    k_npt_box_b<<<(c->nrep + 127) / 128, 128, 0, c->stream>>>(c->nrep, c->reps_dev, c->repst, c->st);
 }
 
 void launch_vv_first_b(md_ctx *c, const md_kparams &kp, unsigned long long cond, int has_cond)

@@ -33,6 +33,7 @@ struct parsed_run {
     std::vector<std::string> names;   /* per type, from the .fld */
     int timprn = 1;
     float rdel = 0.02f;
+    float press0 = 1.0f, tau_p = 1000.0f, beta = 4.5e-5f;   /* NPT: bar, fs, 1/bar */
 };
 
 /* .inp (simulation.cu:58-105): label tokens skipped; reacf and alfa derived
@@ -53,9 +54,9 @@ md_status parse_inp(const char *path, parsed_run &r)
     if (!strcmp(ens, "nvt")) {
         d.enstype = 1;
         if (fscanf(fin, "%255s %f", lab, &d.temper_0) != 2) goto out;
-    } else if (!strcmp(ens, "npt")) {
-        st = MD_ERR_UNSUPPORTED;
-        goto out;
+    } else if (!strcmp(ens, "npt")) {   /* simulation.cu:71-75: T0 and P0 */
+        d.enstype = 2;
+        if (fscanf(fin, "%255s %f %f", lab, &d.temper_0, &r.press0) != 3) goto out;
     }
     if (fscanf(fin, "%255s %d %d %d %f", lab, &timeq, &timrun, &r.timprn, &d.dt) != 5) goto out;
     if (fscanf(fin, "%255s %f %d", lab, &rc, &d.lkspace) != 3) goto out;
@@ -78,6 +79,8 @@ md_status parse_inp(const char *path, parsed_run &r)
         char val[64];
         while (fscanf(fin, "%255s %63s", lab, val) == 2) {
             if (!strcmp(lab, "tau_t:")) d.tau_t = strtof(val, nullptr);
+            else if (!strcmp(lab, "tau_p:")) r.tau_p = strtof(val, nullptr);
+            else if (!strcmp(lab, "compressibility:")) r.beta = strtof(val, nullptr);
             else if (!strcmp(lab, "integrator:"))
                 d.integrator = !strcmp(val, "vv") ? MD_VV : (!strcmp(val, "nh") ? MD_NH : MD_LEAPFROG);
         }
@@ -263,6 +266,11 @@ md_status check_overflow_and_sync(md_ctx *c)
     MD_CUDA_TRY(c, cudaStreamSynchronize(c->stream));
     md_devstate h;
     MD_CUDA_TRY(c, cudaMemcpy(&h, c->st, sizeof(h), cudaMemcpyDeviceToHost));
+    if (h.status & 2)
+        return fail(c, MD_ERR_BOX,
+                    "NPT: a replica's box shrank below its cell grid (cells shorter than half the list "
+                    "radius, or the list radius beyond half the box); create the context again from the "
+                    "current positions and boxes (md_get_positions, md_get_replica_box)");
     if (h.status != 0)
         return fail(c, MD_ERR_CUDA, "a grid barrier of the list rebuild timed out (device state invalid)");
     if (h.list_overflow > 0)
@@ -817,8 +825,11 @@ md_status md_create(const md_system_desc *d, void *stream, md_ctx **out)
     if (d->nangle > 0 && (!d->angles || !d->ang1 || !d->ang2))
         return fail(nullptr, MD_ERR_ARG, "md_create: angles without tables");
     if (d->lkspace < 0 || d->lkspace > 2 || d->rcutsq <= 0 || d->skin < 0 || d->dt <= 0 ||
-        d->integrator < 0 || d->integrator > 2 || d->enstype < 0 || d->enstype > 1)
+        d->integrator < 0 || d->integrator > 2 || d->enstype < 0 || d->enstype > 2)
         return fail(nullptr, MD_ERR_ARG, "md_create: invalid run parameters");
+    /* NPT: the box becomes a per-step device quantity, which the batch kernels
+     * read from their replica table; a single NPT system is a batch of one */
+    if (d->enstype == 2) return md_create_batch(d, 1, stream, out);
     md_ctx *c = new (std::nothrow) md_ctx();
     if (!c) return fail(nullptr, MD_ERR_ARG, "out of host memory");
     const int n = d->natom;
@@ -934,6 +945,21 @@ md_status md_create(const md_system_desc *d, void *stream, md_ctx **out)
     return setup_device(c, stream, h, out);
 }
 
+/* bar per kJ/mol/A^3 (1 kJ/mol/A^3 = 1.66053907e9 Pa) */
+constexpr double MD_BAR = 16605.3907;
+
+/* The Berendsen barostat's constants of every replica of an NPT batch from
+ * c->baro (target pressure in bar, tau_p in fs, compressibility in 1/bar):
+ * mu = 1 - beta dt / (3 tau_p) (P0 - P), pressures in kJ/mol/A^3. */
+static void apply_barostat(md_ctx *c)
+{
+    for (md_rep &R : c->reps) {
+        if (!R.npt) continue;
+        R.p0 = c->baro[0] / MD_BAR;
+        R.mu_k = c->baro[2] * MD_BAR * (double)c->dt / (3.0 * c->baro[1]);
+    }
+}
+
 md_status md_create_batch(const md_system_desc *descs, int nrep, void *stream, md_ctx **out)
 {
     if (!descs || !out || nrep < 1) return fail(nullptr, MD_ERR_ARG, "md_create_batch: null argument");
@@ -964,8 +990,11 @@ md_status md_create_batch(const md_system_desc *descs, int nrep, void *stream, m
                             "md_create_batch: replicas with different bonded parameters" + at);
         }
         if (d->lkspace < 0 || d->lkspace > 2 || d->rcutsq <= 0 || d->skin < 0 || d->dt <= 0 ||
-            d->integrator < 0 || d->integrator > 2 || d->enstype < 0 || d->enstype > 1)
+            d->integrator < 0 || d->integrator > 2 || d->enstype < 0 || d->enstype > 2)
             return fail(nullptr, MD_ERR_ARG, "md_create_batch: invalid run parameters" + at);
+        if (d->enstype == 2 && d->integrator != MD_LEAPFROG)
+            return fail(nullptr, MD_ERR_UNSUPPORTED,
+                        "md_create_batch: NPT runs the Berendsen leapfrog (npt_leapfrog_ber.cu)" + at);
         if (d->lkspace != d0.lkspace || d->integrator != d0.integrator || d->enstype != d0.enstype ||
             d->dt != d0.dt || d->tau_t != d0.tau_t)
             return fail(nullptr, MD_ERR_ARG,
@@ -1107,7 +1136,13 @@ md_status md_create_batch(const md_system_desc *descs, int nrep, void *stream, m
         R.rmaxdif = d->skin * d->skin / 4.0f;                                 /* neighborlist.cu:36 */
         md_shift_consts(d->lkspace, d->rcutsq, d->alfa, R.reacf, &R.ucc, &R.rc6i, &R.rcinv);
         cell_grid g;
-        make_cell_grid(d->box, sqrtf(d->rcutsq) + d->skin, g);
+        /* NPT: cells 3% longer than half the list radius, so the box may
+         * shrink that far before the stencil of +-2 cells stops covering it */
+        const float rl = sqrtf(d->rcutsq) + d->skin;
+        make_cell_grid(d->box, d->enstype == 2 ? rl * 1.03f : rl, g);
+        R.rl_half = 0.5f * rl;
+        R.npt = d->enstype == 2 ? 1 : 0;
+        R.mu_max = 1e-4;
         for (int k = 0; k < 3; k++) {
             R.ncell[k] = g.ncell[k];
             R.stencil[k] = g.stencil[k];
@@ -1161,6 +1196,7 @@ md_status md_create_batch(const md_system_desc *descs, int nrep, void *stream, m
         memset(&S, 0, sizeof(S));
         S.temper = R.t0;
         S.vscale = S.lambda = S.lam_next = S.kick_scale = 1.0;
+        S.mu_next = S.mu_used = 1.0;
         atom0 += d->natom;
         cell0 += g.ncells;
     }
@@ -1197,6 +1233,7 @@ md_status md_create_batch(const md_system_desc *descs, int nrep, void *stream, m
         }
         c->grid_cnt[k] = (int)h.grid.size() - c->grid_off[k];
     }
+    apply_barostat(c);
     return setup_device(c, stream, h, out);
 }
 
@@ -1269,6 +1306,7 @@ md_status md_create_from_files(const char *base, void *stream, md_ctx **out)
     if (s == MD_OK) {
         (*out)->timprn = r.timprn;
         (*out)->type_names = r.names;
+        if (d.enstype == 2) s = md_set_barostat(*out, r.press0, r.tau_p, r.beta);
     }
     return s;
 }
@@ -1455,9 +1493,22 @@ md_status md_integrate_cor(md_ctx *c, int energy)
     return check_overflow_and_sync(c);
 }
 
-static md_status step_body(md_ctx *c, int nsteps, int energy_every)
+/* The host copy of the replica table after steps that moved the boxes. */
+static md_status sync_reps(md_ctx *c)
 {
-    MD_CUDA_TRY(c, cudaEventRecord(c->ev0, c->stream));
+    if (!c->batch || c->enstype != 2) return MD_OK;
+    MD_CUDA_TRY(c, cudaMemcpy(c->reps.data(), c->reps_dev, sizeof(md_rep) * c->nrep, cudaMemcpyDeviceToHost));
+    for (int k = 0; k < 3; k++) {   /* the context-wide box: replica 0's */
+        c->box[k] = c->reps[0].box[k];
+        c->boxi[k] = c->reps[0].boxi[k];
+        c->binlen[k] = c->reps[0].binlen[k];
+    }
+    return MD_OK;
+}
+
+static md_status step_body(md_ctx *c, int nsteps, int energy_every, bool mark_start)
+{
+    if (mark_start) MD_CUDA_TRY(c, cudaEventRecord(c->ev0, c->stream));
     int left = nsteps;
     while (left > 0) {
         int aligned = energy_every > 0 ? (int)(c->host_step % energy_every == 0) : 1;
@@ -1514,6 +1565,7 @@ static std::vector<snap_part> snap_parts(md_ctx *c)
         v.push_back({c->repst, c->nrep * sizeof(md_repstate)});
         v.push_back({c->racc, 3 * (size_t)c->nrep * sizeof(unsigned long long)});
         v.push_back({c->rep_upd, c->nrep * sizeof(int)});
+        v.push_back({c->reps_dev, c->nrep * sizeof(md_rep)});   /* NPT moves the boxes */
     }
     return v;
 }
@@ -1561,15 +1613,21 @@ static md_status snapshot(md_ctx *c, bool save)
 md_status md_step(md_ctx *c, int nsteps, int energy_every)
 {
     if (!c || nsteps < 0 || energy_every < 0) return MD_ERR_ARG;
-    if (!c->overflow_retry || nsteps == 0) return step_body(c, nsteps, energy_every);
+    if (!c->overflow_retry || nsteps == 0) {
+        md_status s0 = step_body(c, nsteps, energy_every, true);
+        return s0 == MD_OK ? sync_reps(c) : s0;
+    }
+    /* the call's device time (md_last_step_ms) includes the snapshot */
+    MD_CUDA_TRY(c, cudaEventRecord(c->ev0, c->stream));
     md_status s = snapshot(c, true);
     if (s != MD_OK) return s;
-    s = step_body(c, nsteps, energy_every);
+    s = step_body(c, nsteps, energy_every, false);
     for (int tries = 0; s == MD_ERR_LIST_OVERFLOW && tries < 3; tries++) {
         md_devstate h;
         MD_CUDA_TRY(c, cudaMemcpy(&h, c->st, sizeof(h), cudaMemcpyDeviceToHost));
         const int cap = ((h.list_overflow * 5 / 4 + 16) + 31) / 32 * 32;
         s = snapshot(c, false);   /* the saved state has no overflow recorded */
+        if (s == MD_OK) s = sync_reps(c);
         if (s != MD_OK) return s;
         if (c->gexec) {           /* the step graph holds the old capacity */
             cudaGraphExecDestroy(c->gexec);
@@ -1580,8 +1638,9 @@ md_status md_step(md_ctx *c, int nsteps, int energy_every)
         if (s == MD_OK) s = refresh_state(c);
         if (s != MD_OK) return s;
         c->regrows++;
-        s = step_body(c, nsteps, energy_every);
+        s = step_body(c, nsteps, energy_every, false);
     }
+    if (s == MD_OK) s = sync_reps(c);
     return s;
 }
 
@@ -2024,6 +2083,44 @@ md_status md_autotune(md_ctx *c, int *pair_tpa, int *list_tpa)
     return MD_OK;
 }
 
+md_status md_set_barostat(md_ctx *c, double press_bar, double tau_p_fs, double compressibility_per_bar)
+{
+    if (!c || tau_p_fs <= 0 || compressibility_per_bar < 0) return MD_ERR_ARG;
+    if (!c->batch || c->enstype != 2) {
+        c->last_error = "md_set_barostat: not an NPT context";
+        return MD_ERR_ARG;
+    }
+    MD_CUDA_TRY(c, cudaStreamSynchronize(c->stream));
+    md_status s = sync_reps(c);
+    if (s != MD_OK) return s;
+    c->baro[0] = press_bar;
+    c->baro[1] = tau_p_fs;
+    c->baro[2] = compressibility_per_bar;
+    apply_barostat(c);
+    MD_CUDA_TRY(c, cudaMemcpy(c->reps_dev, c->reps.data(), sizeof(md_rep) * c->nrep, cudaMemcpyHostToDevice));
+    return MD_OK;
+}
+
+md_status md_get_replica_box(md_ctx *c, double *box3, double *pressure_bar, int nrep)
+{
+    if (!c || !box3 || nrep < 1) return MD_ERR_ARG;
+    MD_CUDA_TRY(c, cudaStreamSynchronize(c->stream));
+    if (!c->batch) {
+        for (int k = 0; k < 3; k++) box3[k] = (double)c->box[k];
+        if (pressure_bar) pressure_bar[0] = 0.0;
+        return MD_OK;
+    }
+    std::vector<md_rep> reps(c->nrep);
+    std::vector<md_repstate> rs(c->nrep);
+    MD_CUDA_TRY(c, cudaMemcpy(reps.data(), c->reps_dev, sizeof(md_rep) * c->nrep, cudaMemcpyDeviceToHost));
+    MD_CUDA_TRY(c, cudaMemcpy(rs.data(), c->repst, sizeof(md_repstate) * c->nrep, cudaMemcpyDeviceToHost));
+    for (int r = 0; r < std::min(nrep, c->nrep); r++) {
+        for (int k = 0; k < 3; k++) box3[3 * r + k] = reps[r].boxd[k];
+        if (pressure_bar) pressure_bar[r] = rs[r].pressure * MD_BAR;
+    }
+    return MD_OK;
+}
+
 md_status md_debug_list_capacity(md_ctx *c, int capacity, int retry)
 {
     if (!c || capacity < 32 || capacity % 32) return MD_ERR_ARG;
@@ -2047,6 +2144,10 @@ md_status md_debug_list_capacity(md_ctx *c, int capacity, int retry)
 md_status md_set_precision(md_ctx *c, int bits)
 {
     if (!c || (bits != 32 && bits != 64)) return MD_ERR_ARG;
+    if (bits == 64 && c->enstype == 2) {
+        c->last_error = "md_set_precision: the FP64 mode takes a fixed box (no NPT)";
+        return MD_ERR_UNSUPPORTED;
+    }
     if (bits == 64 && !c->p64_dev) {
         const int nm = c->batch ? c->nrep : 1;
         std::vector<md_p64> h(nm);

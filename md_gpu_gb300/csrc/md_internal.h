@@ -111,6 +111,13 @@ struct md_rep {
     int ablk0, anblk;    /* its blocks of the MD_ADJ_ATOMS-atom grid of the adjoint kernels */
     int ndf;
     double t0, q_nh, inv_ndfr, inv_q;   /* 1/(ndf R), 1/Q */
+    /* Berendsen barostat (NPT): target pressure (kJ/mol/A^3), the factor
+     * k of mu = 1 - k (p0 - P) (compressibility dt / (3 tau_p)), the
+     * largest |mu - 1| of a step, and half the list radius the cell grid
+     * must keep (binlen >= rl/2) */
+    double p0, mu_k, mu_max;
+    int npt;
+    float rl_half;
 };
 
 /* Constants of the FP64 force law of one system or replica (the FP64 mode,
@@ -131,6 +138,9 @@ struct md_repstate {
     double vscale, lambda, lam_next, kick_scale;
     int builds;          /* neighbour-list builds of this replica */
     int pad;
+    double mu_next;      /* NPT: box scale the next step applies */
+    double mu_used;      /* NPT: box scale the last step applied */
+    double pressure;     /* NPT: pressure of the last step, kJ/mol/A^3 */
 };
 
 /* Replica-aligned launch grids of a batch: for A atoms per block (A = 4 ..
@@ -235,6 +245,7 @@ struct md_ctx {
     int centered = 0;    /* every position in [-L/2, L/2] (set at upload; the wraps keep it) */
     int list_tpa = 0;    /* list build: 0 = one warp per cell, else threads per atom */
     int fp64 = 0;        /* 1: force kernels in FP64 on the FP64 positions (md_set_precision) */
+    double baro[3] = {1.0, 1000.0, 4.5e-5};   /* NPT: target bar, tau_p fs, compressibility 1/bar */
     md_p64 *p64_dev = nullptr;        /* FP64 model constants per replica (1 for a single system) */
     std::vector<float> rep_alfa;      /* damping alpha per replica of a batch */
 
@@ -340,6 +351,9 @@ void launch_leapfrog_b(md_ctx *c, const md_kparams &kp, int energy, unsigned lon
                        int has_cond);
 void launch_vv_first_b(md_ctx *c, const md_kparams &kp, unsigned long long cond, int has_cond);
 void launch_vv_second_b(md_ctx *c, const md_kparams &kp, int energy, int kick);
+/* NPT: every replica's box and cell geometry scaled by the factor its last
+ * step applied to its positions (after each leapfrog step of an NPT batch) */
+void launch_npt_box_b(md_ctx *c);
 
 /* List entries each pair-kernel lane loads per batch for the context's
  * lanes per atom: the autotuner's choice, else the default (TPA * depth

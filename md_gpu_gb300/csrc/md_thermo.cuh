@@ -17,6 +17,7 @@ struct thermo_par {
     double inv_q;      /* 1 / Q (Nose-Hoover mass) */
     double dt_tau;     /* dt / tau (Berendsen) */
     int ndf, berendsen, nh, energy;
+    int npt;   /* Berendsen barostat (batches): virial summed every step, box scaled */
 };
 
 /* Per-step bookkeeping buffers and the graph condition to set. */
@@ -321,7 +322,8 @@ inline thermo_par make_tp(const md_ctx *c, int energy)
     tp.inv_ndfr = 1.0 / (tp.ndf * RGAS);
     tp.inv_q = 1.0 / tp.q_nh;
     tp.dt_tau = (double)c->dt / tp.tau;
-    tp.berendsen = (c->enstype == 1 && c->integrator == MD_LEAPFROG) ? 1 : 0;
+    tp.berendsen = (c->enstype >= 1 && c->integrator == MD_LEAPFROG) ? 1 : 0;
+    tp.npt = (c->enstype == 2 && c->batch) ? 1 : 0;
     tp.nh = (c->integrator == MD_NH) ? 1 : 0;
     tp.energy = energy;
     return tp;

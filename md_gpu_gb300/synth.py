@@ -270,7 +270,7 @@ def to_arrays(sys_: System) -> Dict[str, object]:
                 type_mass=mass, lj1=lj1, lj2=lj2, lkspace=lk, rcutsq=float(rc32 * rc32),
                 reacf=float(reacf), alfa=float(alfa), skin=float(f32(p["skin"][0])),
                 nmaxlist=int(p["skin"][1]), dt=float(f32(p["times"][3])),
-                enstype=1 if p["ensemble"] == "nvt" else 0,
+                enstype={"nve": 0, "nvt": 1, "npt": 2}[p["ensemble"]],
                 temper_0=float(f32(p.get("temper", 0.0))), tau_t=float(f32(p.get("tau_t", 100.0))),
                 integrator=integ)
 
@@ -336,6 +336,8 @@ def write_case(sys_: System, directory: str, name: Optional[str] = None) -> str:
     lines = [f"ensemble: {p['ensemble']}"]
     if p["ensemble"] == "nvt":
         lines.append(f"temper: {p['temper']!r}")
+    elif p["ensemble"] == "npt":   # simulation.cu:71-75: T0 and P0 (bar)
+        lines.append(f"temper: {p['temper']!r} {p.get('press', 1.0)!r}")
     t = p["times"]
     lines.append(f"times: {t[0]} {t[1]} {t[2]} {t[3]!r}")
     rc, lk = p["cutoff"]
@@ -351,6 +353,10 @@ def write_case(sys_: System, directory: str, name: Optional[str] = None) -> str:
     lines.append(f"rdel: {p.get('rdel', 0.02)!r}")
     if "tau_t" in p:
         lines.append(f"tau_t: {p['tau_t']!r}")
+    if "tau_p" in p:
+        lines.append(f"tau_p: {p['tau_p']!r}")
+    if "compressibility" in p:
+        lines.append(f"compressibility: {p['compressibility']!r}")
     if p.get("integrator", "leapfrog") != "leapfrog":
         lines.append(f"integrator: {p['integrator']}")
     with open(base + ".inp", "w") as fh:

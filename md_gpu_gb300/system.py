@@ -159,6 +159,8 @@ def library(path: Optional[str] = None):
     L.md_set_graphs.argtypes = [vp, C.c_int]
     L.md_debug_rebuild_barrier.argtypes = [vp, C.c_double, C.c_int]
     L.md_set_precision.argtypes = [vp, C.c_int]
+    L.md_set_barostat.argtypes = [vp, C.c_double, C.c_double, C.c_double]
+    L.md_get_replica_box.argtypes = [vp, vp, vp, C.c_int]
     L.md_debug_list_capacity.argtypes = [vp, C.c_int, C.c_int]
     L.md_get_replica_history.argtypes = [vp, vp, C.c_int, C.POINTER(C.c_int)]
     L.md_set_fused_step.argtypes = [vp, C.c_int]
@@ -465,6 +467,20 @@ class MDSystem:
         """32: FP32 pair arithmetic (the default); 64: every force term in FP64
         on the FP64 positions (the plain FP64 form, for reference runs)."""
         _check(library().md_set_precision(self._ctx, int(bits)), self._ctx)
+
+    def set_barostat(self, press_bar, tau_p_fs=1000.0, compressibility_per_bar=4.5e-5):
+        """NPT contexts: the Berendsen barostat's target pressure (bar), time
+        constant (fs) and compressibility (1/bar)."""
+        _check(library().md_set_barostat(self._ctx, float(press_bar), float(tau_p_fs),
+                                         float(compressibility_per_bar)), self._ctx)
+
+    def replica_boxes(self):
+        """(box edges (nrep, 3) in A, last-step pressures (nrep,) in bar)."""
+        n = len(getattr(self, "replica_sizes", [self.natom]))
+        box = np.zeros((n, 3))
+        p = np.zeros(n)
+        _check(library().md_get_replica_box(self._ctx, box.ctypes.data, p.ctypes.data, n), self._ctx)
+        return box, p
 
     def set_fused_step(self, fused=True):
         """Leapfrog without bonded terms: pair forces and update in one kernel."""

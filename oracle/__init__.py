@@ -399,6 +399,40 @@ def md_ref_run_cont(case: Case, pos4, vel4, nsteps, state: RefLoopState, temper=
     return rc, float(t.value)
 
 
+BAR = 16605.3907   # bar per kJ/mol/A^3
+
+
+def md_plain_npt(case: Case, x, v, nsteps, press_bar, tau_p_fs, beta_per_bar, mu_max=1e-4):
+    """FP64 plain-form NPT run (Berendsen leapfrog thermostat and barostat,
+    all pairs, small N); x, v (N, 3) float64 in/out.  Returns (box[3],
+    records[nsteps, 4] = Lx, P (bar), T, the scale the step applied)."""
+    n = x.shape[0]
+    m = case.mass.astype(np.float64)
+    box = case.box.astype(np.float64).copy()
+    rec = np.zeros((max(nsteps, 1), 4))
+    fld = case.fld
+    b = np.ascontiguousarray(case.bonds, np.int32)
+    a = np.ascontiguousarray(case.angles, np.int32)
+    fld.nbonds, fld.nangle = b.shape[0], a.shape[0]
+    fld.bonds = _p(b, C.c_int)
+    fld.angles = _p(a, C.c_int)
+    it = np.ascontiguousarray(case.itype, np.int32)
+    mu_k = beta_per_bar * BAR * float(case.params.dt) / (3.0 * tau_p_fs)
+    L = lib()
+    L.orc_md_plain_npt.argtypes = [C.c_void_p, C.c_void_p, C.c_int, C.c_void_p, C.c_void_p, C.c_void_p,
+                                   C.c_void_p, C.c_void_p, C.c_void_p, C.c_int, C.c_double, C.c_double,
+                                   C.c_double, C.c_void_p]
+    rc = L.orc_md_plain_npt(C.addressof(case.params), C.addressof(fld), n, x.ctypes.data, v.ctypes.data,
+                            it.ctypes.data, case.q.ctypes.data, m.ctypes.data, box.ctypes.data, nsteps,
+                            press_bar / BAR, mu_k, mu_max, rec.ctypes.data)
+    fld.bonds = C.POINTER(C.c_int)()
+    fld.angles = C.POINTER(C.c_int)()
+    if rc != 0:
+        raise ValueError("orc_md_plain_npt: angles are not supported")
+    rec[:, 1] *= BAR
+    return box, rec[:nsteps]
+
+
 def md_plain_run(case: Case, x, v, nsteps, integrator, state=None, records=True):
     """FP64 plain-form run (all pairs, small N); returns (state[4], records[nsteps,3])."""
     n = x.shape[0]

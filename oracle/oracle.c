@@ -1223,6 +1223,89 @@ int orc_md_plain_run(const orc_params *p, const orc_ffield *f, int n, double *x,
 }
 
 
+/* Pair and bond forces of the plain form (FP64, all pairs, double box) with
+ * the virial W = sum over atoms of ff r^2 (every pair counted from both
+ * atoms, as the reference's force.w); angles are not supported here. */
+static double npt_forces(const orc_params *p, const orc_ffield *f, int n, const double *x, const int *itype,
+                         const float *q, const double L[3], const unsigned *excl, double *fr)
+{
+    int kind = p->lkspace == 0 ? 0 : 1;
+    pairmodel m;
+    pairmodel_init(&m, kind, 0, p->rcutsq, p->reacf, p->alfa);
+    const double qfac = (double)ORC_QFAC;
+    double W = 0.0;
+#pragma omp parallel for schedule(dynamic, 16) reduction(+ : W)
+    for (int i = 0; i < n; i++) {
+        double fx = 0, fy = 0, fz = 0;
+        for (int j = 0; j < n; j++) {
+            if (j == i || is_excluded(excl, i, j)) continue;
+            double d[3];
+            for (int k = 0; k < 3; k++) { d[k] = x[3 * i + k] - x[3 * j + k]; d[k] -= L[k] * rint(d[k] / L[k]); }
+            double rsq = d[0] * d[0] + d[1] * d[1] + d[2] * d[2];
+            if (rsq > m.rcsq) continue;
+            int t = itype[i] * f->ntype + itype[j];
+            double ff, uu;
+            pair_eval_f64(&m, rsq, qfac * (double)q[i] * (double)q[j], f->lj1[t], f->lj2[t], &ff, &uu);
+            fx += ff * d[0]; fy += ff * d[1]; fz += ff * d[2];
+            W += ff * rsq;
+        }
+        fr[3 * i] = fx; fr[3 * i + 1] = fy; fr[3 * i + 2] = fz;
+    }
+    for (int it = 0; it < f->nbonds; it++) {
+        int t = f->bonds[3 * it] - 1, i = f->bonds[3 * it + 1] - 1, j = f->bonds[3 * it + 2] - 1;
+        double d[3];
+        for (int k = 0; k < 3; k++) { d[k] = x[3 * i + k] - x[3 * j + k]; d[k] -= L[k] * rint(d[k] / L[k]); }
+        double rsq = d[0] * d[0] + d[1] * d[1] + d[2] * d[2];
+        double fa = (double)f->bnd1[t] * ((double)f->bnd2[t] / sqrt(rsq) - 1.0);
+        for (int k = 0; k < 3; k++) { fr[3 * i + k] += fa * d[k]; fr[3 * j + k] -= fa * d[k]; }
+        W += 2.0 * fa * rsq;
+    }
+    return W;
+}
+
+int orc_md_plain_npt(const orc_params *p, const orc_ffield *f, int n, double *x, double *v, const int *itype,
+                     const float *q, const double *m, double box[3], int nsteps, double p0, double mu_k,
+                     double mu_max, double *rec_out)
+{
+    if (f->nangle > 0) return -1;
+    unsigned *excl = (unsigned *)malloc(sizeof(unsigned) * 4 * (size_t)n);
+    double *fr = (double *)malloc(sizeof(double) * 3 * (size_t)n);
+    orc_build_exclusions(n, f->nbonds, f->bonds, excl);
+    const double dt = p->dt, t0 = p->temper_0, tau = p->tau_t > 0 ? p->tau_t : 100.0;
+    const int ndf = 3 * n - 3;
+    double L[3] = {box[0], box[1], box[2]};
+    double W = npt_forces(p, f, n, x, itype, q, L, excl, fr);
+    double temper = t0, mu_next = 1.0;
+    for (int t = 0; t < nsteps; t++) {
+        const double scale = sqrt(1.0 + dt / tau * (t0 / temper - 1.0));
+        double Ln[3];
+        for (int k = 0; k < 3; k++) Ln[k] = L[k] * mu_next;
+        double ke = 0.0;
+        for (int i = 0; i < n; i++)
+            for (int k = 0; k < 3; k++) {
+                double vv = (v[3 * i + k] + fr[3 * i + k] * dt / m[i]) * scale;
+                v[3 * i + k] = vv;
+                double xx = (x[3 * i + k] + vv * dt) * mu_next;
+                xx -= Ln[k] * trunc(xx * 2.0 / Ln[k]);
+                x[3 * i + k] = xx;
+                ke += 0.5 * m[i] * vv * vv;
+            }
+        temper = 2.0 * ke / (ndf * ORC_RGAS);
+        const double P = (2.0 * ke + 0.5 * W) / (3.0 * L[0] * L[1] * L[2]);
+        const double mu_used = mu_next;
+        mu_next = 1.0 - mu_k * (p0 - P);
+        mu_next = fmin(fmax(mu_next, 1.0 - mu_max), 1.0 + mu_max);
+        for (int k = 0; k < 3; k++) L[k] = Ln[k];
+        W = npt_forces(p, f, n, x, itype, q, L, excl, fr);
+        if (rec_out) {
+            rec_out[4 * t] = L[0]; rec_out[4 * t + 1] = P; rec_out[4 * t + 2] = temper; rec_out[4 * t + 3] = mu_used;
+        }
+    }
+    for (int k = 0; k < 3; k++) box[k] = L[k];
+    free(excl); free(fr);
+    return 0;
+}
+
 /* ====================================================================== */
 /* Adjoint of velocity-Verlet NVE (FP64, all pairs).                      */
 /*                                                                        */

@@ -186,6 +186,20 @@ int orc_md_ref_run_cont(const orc_params *p, const orc_ffield *f, int n, float *
                         unsigned *nnl, unsigned *nnm, float *pold, int *have_list,
                         float *force4_out, float *temper_io, float *temps_out);
 
+/* FP64 plain-form NPT run: leapfrog with the Berendsen thermostat (the
+ * previous step's temperature, tau_t) and the Berendsen barostat the library
+ * runs (no reference implementation: npt_leapfrog_ber.cu never scales the
+ * box).  Each step: v = (v + F dt/m) lambda; x = (x + v dt) mu_next, wrapped
+ * into the box scaled by mu_next; P = (2 KE + W/2) / (3 V) with W = sum over
+ * atoms of ff r^2 of the step's forces and V the box they saw; mu_next = 1 -
+ * mu_k (p0 - P) clamped to 1 +- mu_max.  All pairs, FP64 positions and box,
+ * pair and bond terms (returns -1 with angles).  box in/out (A); p0 in
+ * kJ/mol/A^3; rec_out (may be NULL): per step Lx, P (kJ/mol/A^3), T, the mu
+ * the step applied. */
+int orc_md_plain_npt(const orc_params *p, const orc_ffield *f, int n, double *x, double *v, const int *itype,
+                     const float *q, const double *m, double box[3], int nsteps, double p0, double mu_k,
+                     double mu_max, double *rec_out);
+
 /* FP64 plain-form run: integrator 0 leapfrog(+Berendsen if enstype 1),
  * 1 velocity Verlet NVE, 2 Nose-Hoover VV.  All-pairs forces inside rc
  * (cell-free O(N^2), for small N only).  Writes per-step total energy

@@ -63,7 +63,12 @@ def test_malformed_inputs(lib):
     with tempfile.TemporaryDirectory() as tmp:
         base = _case(tmp)
         with open(base + ".inp", "w") as fh:
-            fh.write("ensemble: npt\ntemper: 300 1\n")
+            fh.write("ensemble: npt\ntemper: 300 1\n")   # the rest of the file is missing
+        with pytest.raises(MDError) as e:
+            MDSystem.from_files(base)
+        assert e.value.status == 3
+    with tempfile.TemporaryDirectory() as tmp:   # NPT runs the Berendsen leapfrog only
+        base = synth.write_case(synth.nacl_rocksalt(ncell=5, seed=1, ensemble="npt", integrator="vv"), tmp, "c")
         with pytest.raises(MDError) as e:
             MDSystem.from_files(base)
         assert e.value.status == 7
