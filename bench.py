@@ -345,13 +345,18 @@ def system_leg(name, sys_, integrator_name, dt_fs, args, flush):
             "list_builder": "warp per cell" if lt == 0 else f"{lt} threads per atom"}
 
 
-def batch_leg(args, flush):
-    """Throughput of the 512-replica batch (atom-steps/s over all replicas)."""
+def batch_leg(args, flush, rank=0, world=1):
+    """Throughput of the 512-replica batch (atom-steps/s over all replicas).
+    Under torchrun the replicas are shared out across the ranks (a contiguous
+    part per rank, balanced by atoms), each rank runs its part as one batch,
+    and the rate is the total atom-steps over the slowest rank's time."""
     import torch
 
     from md_gpu_gb300 import MDSystem, synth
-    from md_gpu_gb300.replicas import equilibrate_batch
-    reps = synth.replica_batch(args.nrep, seed=1)
+    from md_gpu_gb300.replicas import aggregate_rate, equilibrate_batch, gather_per_replica, partition
+    reps_all = synth.replica_batch(args.nrep, seed=1)
+    idx = partition([r.natom for r in reps_all], world, rank)
+    reps = [reps_all[i] for i in idx]
     arrs = equilibrate_batch([synth.to_arrays(r) for r in reps])
     sizes = [r.natom for r in reps]
     with MDSystem.from_batch(arrs) as b:
@@ -370,40 +375,47 @@ def batch_leg(args, flush):
         pair_ms = b.time_pair(20)
     steps = args.md_steps * len(ms)
     rebuilt = sum(t["builds"] for t in th) - sum(rb0)
+    value, tmax = aggregate_rate(sum(sizes) * steps, sum(ms), world, device="cuda")
+    temps = gather_per_replica(np.array([t["temper"] for t in th]), idx, len(reps_all), world)
+    sizes_all = [r.natom for r in reps_all]
     return {
         "workload": (f"{args.nrep} NaCl-like replicas, N uniform in [256, 8192] (seed 1), 1.5 g/cm^3, "
                      "eps/sigma per type and charge scale uniform within +-10% of the molten-NaCl "
                      "values, Wolf alpha 0.2/A, rc 12 A (clamped to L/2 - skin for the smallest boxes), "
                      "skin 1 A, velocity Verlet NVE dt 2 fs, melted first by Berendsen leapfrog "
                      "(400 steps dt 0.5 fs tau 10 fs, 200 steps dt 2 fs tau 100 fs) at 1200 K"),
-        "value": sum(sizes) * steps / (sum(ms) * 1e-3), "unit": UNIT,
-        "natom": int(sum(sizes)), "nrep": len(sizes), "min_natom": int(min(sizes)),
-        "max_natom": int(max(sizes)), "md_steps": steps, "ms_per_md_step": sum(ms) / steps,
+        "value": value, "unit": UNIT, "ranks": world, "replicas_per_rank_0": len(sizes),
+        "natom": int(sum(sizes_all)), "nrep": len(sizes_all), "min_natom": int(min(sizes_all)),
+        "max_natom": int(max(sizes_all)), "md_steps": steps, "ms_per_md_step": tmax / steps,
         "pair_ms": pair_ms, "pair_threads_per_atom": pt, "pair_entries_per_lane": info["pair_depth"],
         "batch_rebuild_events": info["builds"] - builds0,
         "replica_rebuilds_per_replica_step": rebuilt / (len(sizes) * steps),
-        "temperature_K": {"min": min(t["temper"] for t in th), "mean": float(np.mean([t["temper"] for t in th])),
-                          "max": max(t["temper"] for t in th)},
+        "temperature_K": {"min": float(temps.min()), "mean": float(temps.mean()), "max": float(temps.max())},
         "l2": "flushed (512 MB write) before every timed segment",
     }
 
 
-def adjoint_leg(args):
+def adjoint_leg(args, rank=0, world=1):
     """Differentiable MD: gradients of <U>/N + RDF loss of 64 x 8000-ion NaCl
     over 2000 VV steps w.r.t. (eps_Na, sigma_Na, eps_Cl, sigma_Cl, charge
-    scale), by the library's adjoint with checkpoints every 50 steps."""
+    scale), by the library's adjoint with checkpoints every 50 steps.  Under
+    torchrun the replicas are shared out across the ranks and the gradients
+    gathered in replica order; the time is the slowest rank's."""
     import torch
 
     from md_gpu_gb300 import MDSystem, params, synth
-    nrep, natom, K = args.adj_nrep, args.adj_natom, args.adj_steps
+    from md_gpu_gb300.replicas import gather_per_replica, partition
+    nrep_all, natom, K = args.adj_nrep, args.adj_natom, args.adj_steps
+    mine = partition([natom] * nrep_all, world, rank)
+    nrep = len(mine)
     eps = np.array([synth.NACL_LJ["Na"][1], synth.NACL_LJ["Cl"][1]]) * synth.KCAL
     sig = np.array([synth.NACL_LJ["Na"][0], synth.NACL_LJ["Cl"][0]])
 
     def batch(scale):
         l1, l2 = params.lb_tables(eps * scale, sig * scale)
         out = []
-        for r in range(nrep):
-            a = synth.to_arrays(synth.nacl_replica(natom, seed=7000 + r, integrator="vv", ensemble="nve"))
+        for r in mine:
+            a = synth.to_arrays(synth.nacl_replica(natom, seed=7000 + int(r), integrator="vv", ensemble="nve"))
             a.update(lj1=l1.astype(np.float32), lj2=l2.astype(np.float32),
                      charge=(a["charge"] * scale).astype(np.float32))
             out.append(a)
@@ -426,8 +438,13 @@ def adjoint_leg(args):
     for r in range(nrep):
         de, ds = params.lb_chain(out["dlj1"][r], out["dlj2"][r], eps, sig)
         grads.append([de[0], ds[0], de[1], ds[1], out["dlns"][r]])
-    grads = np.array(grads)
+    grads = gather_per_replica(np.array(grads).reshape(-1, 5), mine, nrep_all, world)
     n_grads = grads.size
+    if world > 1:   # the slowest rank's times
+        import torch.distributed as dist
+        tt = torch.tensor([t_adj, t_fwd], dtype=torch.float64, device="cuda")
+        dist.all_reduce(tt, op=dist.ReduceOp.MAX)
+        t_adj, t_fwd = float(tt[0]), float(tt[1])
     # the stated baseline: per-system plain FP64 runs on the same GPU, central
     # differences of the five parameters (two K-step runs each) of one replica
     one = batch(1.0)[0]
@@ -442,7 +459,7 @@ def adjoint_leg(args):
         ms_per_step64 = ms64 / (2 * n64)
     fp64_rate = 5.0 / (10 * K * ms_per_step64 * 1e-3)
     return {
-        "workload": (f"{nrep} replicas of {natom}-ion molten NaCl (LJ + Wolf, rc 12 A), {K} velocity-Verlet "
+        "workload": (f"{nrep_all} replicas of {natom}-ion molten NaCl (LJ + Wolf, rc 12 A), {K} velocity-Verlet "
                      "NVE steps at dt 2 fs from 1200 K; loss = <U>/N + sum_b (gbar_b - target_b)^2 of the "
                      "Gaussian-smoothed Na-Cl RDF (200 bins of 0.05 A, sigma 0.05 A), target from the same "
                      "run at eps, sigma and charges +5%; gradients w.r.t. eps_Na, sigma_Na, eps_Cl, "
@@ -516,6 +533,9 @@ def run_ours(args):
                                      device="cuda")
     md_steps_per_s = args.md_steps * args.steps / (total_ms * 1e-3)
 
+    # legs over batches of replicas: every rank runs its share of the replicas
+    extra_batch = batch_leg(args, flush, rank, world) if args.nrep > 0 else None
+    extra_adj = adjoint_leg(args, rank, world) if args.adj_nrep > 0 else None
     extra = {}
     if rank == 0:
         # roofline of the dominant kernel (pair forces), timed alone on the same state
@@ -557,9 +577,6 @@ def run_ours(args):
                "d2h_bytes_per_step": 2 * 3 * n * 8 + args.md_steps * 72,
                "call": "md_run_host (upload pos/vel, list build, md_steps steps, download records + pos/vel)"}
         ref_cuda = reference_cuda_leg(args, value, e2e["value"]) if args.ref_cuda_steps > 0 else None
-        if args.nrep > 0:
-            extra_batch = batch_leg(args, flush)
-        extra_adj = adjoint_leg(args) if args.adj_nrep > 0 else None
         others = {}
         if args.other_segments > 0:
             from md_gpu_gb300 import synth

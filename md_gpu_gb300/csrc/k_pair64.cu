@@ -100,7 +100,7 @@ __global__ void __launch_bounds__(P64_THREADS) k_pair64(int n, int pitch, int ca
     const double qi = m.qfac * (double)pos4[ii].w;
     const double2 *ljrow = lj + type[ii] * MD_MAXTYPE;
     const int cnt = active ? nl_n[ii] : 0;
-    const int npad = (cnt + MD_LIST_QUANTUM - 1) / MD_LIST_QUANTUM * MD_LIST_QUANTUM;
+    const int npad = (cnt + P64_TPA - 1) / P64_TPA * P64_TPA;   /* padding past it adds zero */
     /* a warp whose atoms all lie at least rc from every face (positions
      * centred in the box) needs no minimum-image shift for any pair inside
      * rc: the shift is L * 0 there, and a pair beyond L/2 is beyond rc */

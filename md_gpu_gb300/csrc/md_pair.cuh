@@ -391,7 +391,10 @@ __device__ __forceinline__ pair_total pair_sum(const G &g, int cap, int ii, bool
     static_assert(MD_LIST_QUANTUM % (TPA * B) == 0, "batch must divide the list padding");
     const float4 pi = pos4[ii];
     const int cnt = active ? nl_n[ii] : 0;
-    const int nb = ((cnt + MD_LIST_QUANTUM - 1) / MD_LIST_QUANTUM) * (MD_LIST_QUANTUM / (TPA * B));
+    /* batches of TPA * B entries up to the first that holds the row's last
+     * entry: the row is padded to a multiple of 32 (>= TPA * B) with entries
+     * that add exactly zero, so the padding past that batch is skipped */
+    const int nb = (cnt + TPA * B - 1) / (TPA * B);
     const float2 *ljrow = lj + type[ii] * MD_MAXTYPE;
     const float qi = QFAC * pi.w;
     pair_acc acc = {0.0f, 0.0f, 0.0f, 0.0f, 0.0f};

@@ -1,9 +1,12 @@
-"""Replica parallelism: one independent system per rank, no data exchange.
+"""Replica parallelism: independent systems per rank, no data-path exchange.
 
 A single md_gpu system is not split across GPUs (that needs a halo exchange
-the reference never had); several GPUs each run their own replica with its
-own seed.  The only collective is the end-of-run reduction of the throughput
-numbers: total atom-steps summed over ranks, time taken as the slowest rank.
+the reference never had).  Several GPUs either each run their own system
+with its own seed, or share out the replicas of one batch (partition): each
+rank runs its part as a batch of its own, and the only exchanges are on the
+host after the run: the per-replica observables or gradients gathered in
+replica order (gather_per_replica) and the throughput reduced as total
+atom-steps over the slowest rank's time (aggregate_rate).
 """
 from __future__ import annotations
 
@@ -11,6 +14,40 @@ from __future__ import annotations
 def replica_seed(base_seed: int, rank: int) -> int:
     """Seed of the replica a rank runs (distinct per rank, reproducible)."""
     return int(base_seed) + 1000003 * int(rank)
+
+
+def partition(sizes, world: int, rank: int):
+    """The replicas rank `rank` of `world` runs: a contiguous range of
+    replica indices, balanced by atom count (a replica goes to the rank whose
+    share of the total holds the middle of its atoms), so every replica is
+    run by exactly one rank and no rank has more than its share plus one
+    replica."""
+    import numpy as np
+    s = np.asarray(sizes, np.float64)
+    if world <= 1 or len(s) == 0:
+        return np.arange(len(s))
+    mid = np.cumsum(s) - 0.5 * s
+    owner = np.minimum((mid * world / s.sum()).astype(np.int64), world - 1)
+    return np.flatnonzero(owner == rank)
+
+
+def gather_per_replica(local, index, nrep: int, world: int):
+    """Per-replica results of every rank in replica order: `local` holds one
+    row per replica in `index` (this rank's partition); returns an array of
+    nrep rows on every rank (torch.distributed, any backend, when world > 1)."""
+    import numpy as np
+    local = np.asarray(local)
+    if world <= 1:
+        out = np.zeros((nrep,) + local.shape[1:], local.dtype)
+        out[np.asarray(index)] = local
+        return out
+    import torch.distributed as dist
+    parts = [None] * world
+    dist.all_gather_object(parts, (np.asarray(index), local))
+    out = np.zeros((nrep,) + local.shape[1:], local.dtype)
+    for idx, vals in parts:
+        out[idx] = vals
+    return out
 
 
 def aggregate_rate(atom_steps: float, elapsed_ms: float, world: int, device=None):
