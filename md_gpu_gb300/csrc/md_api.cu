@@ -1570,7 +1570,32 @@ static std::vector<snap_part> snap_parts(md_ctx *c)
     return v;
 }
 
-/* Stream-ordered device copies of the state into the snapshot (or back). */
+/* Up to MD_SNAP_PARTS device-to-device copies in one launch: blockIdx.y picks
+ * the copy, the x blocks stride through it in 16-byte words (every part
+ * starts on a 256-byte boundary in both buffers) and 4-byte words for a
+ * tail (every part is a multiple of 4 bytes). */
+#define MD_SNAP_PARTS 16
+struct snap_copies {
+    const char *src[MD_SNAP_PARTS];
+    char *dst[MD_SNAP_PARTS];
+    unsigned long long bytes[MD_SNAP_PARTS];
+};
+__global__ void k_snapshot(snap_copies cp)
+{
+    const int k = blockIdx.y;
+    const unsigned long long nb = cp.bytes[k], n16 = nb / 16;
+    const uint4 *s16 = (const uint4 *)cp.src[k];
+    uint4 *d16 = (uint4 *)cp.dst[k];
+    const unsigned long long stride = (unsigned long long)gridDim.x * blockDim.x;
+    for (unsigned long long i = blockIdx.x * (unsigned long long)blockDim.x + threadIdx.x; i < n16; i += stride)
+        d16[i] = s16[i];
+    if (blockIdx.x == 0)
+        for (unsigned long long i = n16 * 4 + threadIdx.x; i < nb / 4; i += blockDim.x)
+            ((unsigned *)cp.dst[k])[i] = ((const unsigned *)cp.src[k])[i];
+}
+
+/* Stream-ordered device copies of the state into the snapshot (or back),
+ * one kernel launch for all parts. */
 static md_status snapshot(md_ctx *c, bool save)
 {
     std::vector<snap_part> parts = snap_parts(c);
@@ -1593,13 +1618,21 @@ static md_status snapshot(md_ctx *c, bool save)
         c->host_step = c->snap_host_step;
         parts = snap_parts(c);   /* pos4 is the buffer current at the save */
     }
-    size_t off = 0;
-    for (const snap_part &p : parts) {
+    if (parts.size() > MD_SNAP_PARTS) return fail(c, MD_ERR_ARG, "snapshot: too many parts");
+    snap_copies cp;
+    memset(&cp, 0, sizeof(cp));
+    size_t off = 0, maxb = 0;
+    for (size_t k = 0; k < parts.size(); k++) {
         char *s = (char *)c->snap + off;
-        MD_CUDA_TRY(c, cudaMemcpyAsync(save ? (void *)s : p.dev, save ? p.dev : (const void *)s, p.bytes,
-                                       cudaMemcpyDeviceToDevice, c->stream));
-        off += (p.bytes + 255) / 256 * 256;
+        cp.src[k] = save ? (const char *)parts[k].dev : s;
+        cp.dst[k] = save ? s : (char *)parts[k].dev;
+        cp.bytes[k] = parts[k].bytes;
+        maxb = std::max(maxb, parts[k].bytes);
+        off += (parts[k].bytes + 255) / 256 * 256;
     }
+    const int bx = (int)std::min<size_t>(std::max<size_t>((maxb / 16 + 255) / 256, 1), 512);
+    k_snapshot<<<dim3(bx, (unsigned)parts.size()), 256, 0, c->stream>>>(cp);
+    MD_CUDA_TRY(c, cudaGetLastError());
     return MD_OK;
 }
 
