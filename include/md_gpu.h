@@ -261,6 +261,7 @@ typedef struct {
     int rebuild_inline;     /* 1: step graphs hold the rebuild passes inline, 0: behind a
                                conditional node */
     int list_regrows;       /* md_step calls run again after their list overflowed (md_step) */
+    int cell_regrids;       /* NPT batches: cell grids laid out again for a changed box (md_step) */
 } md_info;
 md_status md_get_info(md_ctx *ctx, md_info *out);
 /* Sorted -> original index map of the current atom order. */
@@ -313,9 +314,14 @@ md_status md_set_precision(md_ctx *ctx, int bits);
  * .inp's npt line), tau_p_fs (default 1000; ".inp" extension line
  * "tau_p: <fs>"), compressibility_per_bar = beta (default 4.5e-5;
  * "compressibility: <1/bar>").  The cell grid is laid out 3% longer than
- * the list needs, so a box may shrink ~3% per axis before the context
- * reports MD_ERR_BOX and must be created again.  Bonds add their virial,
- * angles none (as the reference's angle_forces). */
+ * the list needs; md_step runs NPT batches in chunks of at most 128 steps
+ * (whole multiples of energy_every) and, between chunks, lays the cells
+ * out again (and rebuilds the lists) for every replica whose cells have
+ * shrunk by half that margin or whose box has room for one more cell
+ * (md_info.cell_regrids counts these).  MD_ERR_BOX remains for a box that
+ * shrinks past the margin inside one step graph or below twice the list
+ * radius.  Bonds add their virial, angles none (as the reference's
+ * angle_forces). */
 md_status md_set_barostat(md_ctx *ctx, double press_bar, double tau_p_fs, double compressibility_per_bar);
 /* Box edges (nrep x 3, A) and last-step pressure (nrep, bar; may be NULL)
  * of the replicas of a batch after the last md_step (NPT moves them); for a

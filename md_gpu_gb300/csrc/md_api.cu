@@ -1643,15 +1643,120 @@ static md_status snapshot(md_ctx *c, bool save)
  * list to 5/4 of the longest row plus 16, rebuilds it at the restored
  * positions (forces recomputed for velocity Verlet) and runs the same steps
  * again, up to three times. */
+/* NPT: lay the cells of every replica of the batch out again for its
+ * current box (the same rule as at creation: cells of at least 1.03 times
+ * half the list radius), reallocate the cell tables when their total
+ * changes, and rebuild every replica's list on the new grid. */
+static md_status regrid_batch(md_ctx *c)
+{
+    std::vector<int> rank, lin, crep;
+    int cell0 = 0;
+    for (int r = 0; r < c->nrep; r++) {
+        md_rep &R = c->reps[r];
+        const float rl = 2.0f * R.rl_half;
+        cell_grid g;
+        make_cell_grid(R.box, R.npt ? rl * 1.03f : rl, g);
+        int nst = 1;
+        for (int k = 0; k < 3; k++) nst *= g.stencil[k] < 0 ? g.ncell[k] : 2 * g.stencil[k] + 1;
+        if (nst > 128) return fail(c, MD_ERR_UNSUPPORTED, "NPT regrid: stencil too large");
+        for (int k = 0; k < 3; k++) {
+            R.ncell[k] = g.ncell[k];
+            R.stencil[k] = g.stencil[k];
+            R.binlen[k] = g.binlen[k];
+        }
+        R.cell_shift = md_cell_shift(R.stencil, R.binlen, R.box);
+        R.cell0 = cell0;
+        R.ncells = g.ncells;
+        for (int k = 0; k < g.ncells; k++) {
+            rank.push_back(cell0 + g.rank[k]);
+            lin.push_back(g.lin[k]);
+            crep.push_back(r);
+        }
+        cell0 += g.ncells;
+    }
+    MD_CUDA_TRY(c, cudaStreamSynchronize(c->stream));
+    if (cell0 != c->ncells) {
+        int **arr[] = {&c->cell_rank, &c->cell_lin, &c->cell_count, &c->cell_start, &c->cell_fill, &c->cell_work,
+                       &c->crep};
+        for (int **a : arr) {
+            cudaFree(*a);
+            *a = nullptr;
+        }
+        c->ncells = cell0;
+        for (int **a : arr) MD_CUDA_TRY(c, dalloc(a, (size_t)cell0 + (a == &c->cell_start ? 1 : 0)));
+    }
+    std::vector<int> zeros(cell0, 0);
+    MD_CUDA_TRY(c, cudaMemcpy(c->cell_rank, rank.data(), sizeof(int) * cell0, cudaMemcpyHostToDevice));
+    MD_CUDA_TRY(c, cudaMemcpy(c->cell_lin, lin.data(), sizeof(int) * cell0, cudaMemcpyHostToDevice));
+    MD_CUDA_TRY(c, cudaMemcpy(c->crep, crep.data(), sizeof(int) * cell0, cudaMemcpyHostToDevice));
+    MD_CUDA_TRY(c, cudaMemcpy(c->cell_count, zeros.data(), sizeof(int) * cell0, cudaMemcpyHostToDevice));
+    MD_CUDA_TRY(c, cudaMemcpy(c->cell_fill, zeros.data(), sizeof(int) * cell0, cudaMemcpyHostToDevice));
+    MD_CUDA_TRY(c, cudaMemcpy(c->reps_dev, c->reps.data(), sizeof(md_rep) * c->nrep, cudaMemcpyHostToDevice));
+    for (int k = 0; k < 3; k++) {
+        c->ncell[k] = c->reps[0].ncell[k];
+        c->binlen[k] = c->reps[0].binlen[k];
+        c->stencil[k] = c->reps[0].stencil[k];
+    }
+    if (c->gexec) {   /* the step graphs hold the old cell count */
+        cudaGraphExecDestroy(c->gexec);
+        c->gexec = nullptr;
+    }
+    c->regrids++;
+    return initial_build(c);
+}
+
+/* NPT: whether a replica's cells have come within half the grid's 3%
+ * margin of half its list radius (regrid before they can fall below it),
+ * or its box has grown enough for one more cell with 1% to spare (fewer
+ * atoms per stencil; the 4% between the two keeps a box that fluctuates
+ * about one size from regridding back and forth). */
+static bool regrid_due(const md_ctx *c)
+{
+    if (!c->batch || c->enstype != 2) return false;
+    for (const md_rep &R : c->reps) {
+        if (!R.npt) continue;
+        for (int k = 0; k < 3; k++) {
+            if (R.stencil[k] >= 0 && R.binlen[k] < R.rl_half * 1.015f) return true;
+            const int fit = (int)floorf(R.box[k] / (R.rl_half * 1.03f * 1.0001f * 1.01f));
+            if (std::min(fit, 1024) > R.ncell[k]) return true;
+        }
+    }
+    return false;
+}
+
+static md_status md_step_impl(md_ctx *c, int nsteps, int energy_every, bool mark_start);
+
+/* NPT batches run in chunks of at most MD_NPT_CHUNK steps (a multiple of
+ * energy_every when it is set), each ending with the regrid check: at the
+ * per-step clamp of the box scale (1e-4) a chunk shrinks a box by at most
+ * 1.3%, less than the 1.5% left between the regrid threshold and the
+ * limit. */
+#define MD_NPT_CHUNK 128
 md_status md_step(md_ctx *c, int nsteps, int energy_every)
 {
     if (!c || nsteps < 0 || energy_every < 0) return MD_ERR_ARG;
+    if (!(c->batch && c->enstype == 2)) return md_step_impl(c, nsteps, energy_every, true);
+    const int chunk = energy_every > 0 ? std::max(energy_every, MD_NPT_CHUNK / energy_every * energy_every)
+                                       : MD_NPT_CHUNK;
+    int done = 0;
+    do {
+        const int k = std::min(chunk, nsteps - done);
+        md_status s = md_step_impl(c, k, energy_every, done == 0);
+        if (s == MD_OK && regrid_due(c)) s = regrid_batch(c);
+        if (s != MD_OK) return s;
+        done += k;
+    } while (done < nsteps);
+    return MD_OK;
+}
+
+static md_status md_step_impl(md_ctx *c, int nsteps, int energy_every, bool mark_start)
+{
     if (!c->overflow_retry || nsteps == 0) {
-        md_status s0 = step_body(c, nsteps, energy_every, true);
+        md_status s0 = step_body(c, nsteps, energy_every, mark_start);
         return s0 == MD_OK ? sync_reps(c) : s0;
     }
     /* the call's device time (md_last_step_ms) includes the snapshot */
-    MD_CUDA_TRY(c, cudaEventRecord(c->ev0, c->stream));
+    if (mark_start) MD_CUDA_TRY(c, cudaEventRecord(c->ev0, c->stream));
     md_status s = snapshot(c, true);
     if (s != MD_OK) return s;
     s = step_body(c, nsteps, energy_every, false);
@@ -1960,6 +2065,7 @@ md_status md_get_info(md_ctx *c, md_info *out)
     out->fused_step = md_can_fuse(c) ? 1 : 0;
     out->rebuild_inline = (c->rebuild_inline && !c->batch) ? 1 : 0;
     out->list_regrows = c->regrows;
+    out->cell_regrids = c->regrids;
     out->list_threads_per_atom = c->list_tpa;
     out->builds = h.builds;
     out->max_neighbors = *std::max_element(cnt.begin(), cnt.begin() + c->n);

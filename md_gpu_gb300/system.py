@@ -68,7 +68,8 @@ class Info(C.Structure):
                 ("builds", C.c_int), ("max_neighbors", C.c_int), ("kernels_per_step", C.c_int),
                 ("kernels_per_rebuild", C.c_int), ("kernels_per_graph", C.c_int),
                 ("pair_entries_per_lane", C.c_int), ("positions_centered", C.c_int),
-                ("fused_step", C.c_int), ("rebuild_inline", C.c_int), ("list_regrows", C.c_int)]
+                ("fused_step", C.c_int), ("rebuild_inline", C.c_int), ("list_regrows", C.c_int),
+                ("cell_regrids", C.c_int)]
 
 
 def _make_desc(keep, *, box, itype, charge, pos, vel, type_mass, lj1, lj2, lkspace, rcutsq,
@@ -410,7 +411,7 @@ class MDSystem:
                 "pair_depth": i.pair_entries_per_lane,
                 "centered": bool(i.positions_centered),
                 "fused_step": bool(i.fused_step), "rebuild_inline": bool(i.rebuild_inline),
-                "list_regrows": i.list_regrows}
+                "list_regrows": i.list_regrows, "cell_regrids": i.cell_regrids}
 
     def neighbor_list(self, nmax):
         """Reference layout (neighborlist.cu:284): (nnlist[pitch*nmax], nnlist_max[pitch])."""
