@@ -669,7 +669,11 @@ __device__ __forceinline__ void build_cell(
         int mycnt = 0;   /* list length of atom i0 + lane */
         /* The exact test of 32 queued candidates against every atom of the
          * group; a ballot appends the hits to each atom's row in candidate
-         * order. */
+         * order.  An atom's row offset changes only in its own iteration, so
+         * each iteration takes it from the counts at the start of the batch
+         * and the iterations are independent (unrolled by 4: 156 against 168
+         * us per build of 64000 ions with the count as a loop-carried
+         * register). */
         auto process = [&](int cnt) {
             const bool vj = lane < cnt;
             const float4 q = vj ? s_fq[w][lane] : make_float4(0.f, 0.f, 0.f, 0.f);
@@ -686,7 +690,9 @@ __device__ __forceinline__ void build_cell(
             /* two copies of the loop: with and without the exclusion tests */
             auto loop = [&](auto with_excl) {
                 unsigned *rowp = nl + (size_t)i0 * kp.cap;
-#pragma unroll 2
+                const int cnt0 = mycnt;
+                int inc = 0;
+#pragma unroll 4
                 for (int a = 0; a < ni; a++, rowp += kp.cap) {
                     const float4 p = s_p[w][a];
                     float rsq;
@@ -706,13 +712,14 @@ __device__ __forceinline__ void build_cell(
                              !((s_tm[w][a] >> tj) & 1u);
                     }
                     const unsigned bal = __ballot_sync(0xffffffffu, ok);
-                    const int base = __shfl_sync(0xffffffffu, mycnt, a);
+                    const int base = __shfl_sync(0xffffffffu, cnt0, a);
                     if (ok) {
                         const int slot = base + __popc(bal & lt);
                         if (slot < kp.cap) rowp[slot] = entry;
                     }
-                    if (lane == a) mycnt += __popc(bal);
+                    if (lane == a) inc += __popc(bal);
                 }
+                mycnt = cnt0 + inc;
             };
             if (excl_bits) {
                 loop(std::true_type());
@@ -726,6 +733,9 @@ __device__ __forceinline__ void build_cell(
                 const V QX = V::make(q.x, q.x), QY = V::make(q.y, q.y), QZ = V::make(q.z, q.z);
                 const V UX = V::make(ux, ux), UY = V::make(uy, uy), UZ = V::make(uz, uz);
                 const float far = vj ? G.rskinsq : -1.0f;   /* no hit in an empty slot */
+                const int cnt0 = mycnt;
+                int inc = 0;
+#pragma unroll 4
                 for (int a = 0; a < ni; a += 2) {
                     const float2 hx = *reinterpret_cast<const float2 *>(&s_h[w][0][a]);
                     const float2 hy = *reinterpret_cast<const float2 *>(&s_h[w][1][a]);
@@ -743,12 +753,13 @@ __device__ __forceinline__ void build_cell(
                     for (int h = 0; h < 2; h++) {
                         const bool ok = (h ? r1 : r0) < far && a + h != selfa;
                         const unsigned bal = __ballot_sync(0xffffffffu, ok);
-                        const int base = __shfl_sync(0xffffffffu, mycnt, a + h);
+                        const int base = __shfl_sync(0xffffffffu, cnt0, a + h);
                         const int slot = base + __popc(bal & lt);
                         if (ok && slot < kp.cap) nl[(size_t)(i0 + a + h) * kp.cap + slot] = entry;
-                        mycnt += lane == a + h ? __popc(bal) : 0;
+                        inc += lane == a + h ? __popc(bal) : 0;
                     }
                 }
+                mycnt = cnt0 + inc;
             } else {
                 loop(std::false_type());
             }
@@ -774,18 +785,34 @@ __device__ __forceinline__ void build_cell(
         const float near_sq = G.rskinsq * 1.001f + 1e-4f;
         int fill = 0;   /* queued candidates (in candidate order) */
         int kc = 0;     /* this lane's stencil cell: the largest k with s_pre[k] <= g */
+        /* software pipelined: the next round's candidate (its stencil cell,
+         * position and type) is located and loaded while this round's are
+         * filtered (144 against 156 us per build of 64000 ions) */
+        int jn = 0, cn = 0, tn = 0;
+        bool vn = lane < total;
+        float4 qn = make_float4(0.f, 0.f, 0.f, 0.f);
+        if (vn) {
+            while (s_pre[w][kc + 1] <= lane) kc++;
+            jn = s_jb[w][kc] + (lane - s_pre[w][kc]);
+            cn = s_sh[w][kc];
+            qn = pos4[jn];
+            tn = type[jn];
+        }
         for (int g0 = 0; g0 < total; g0 += 32) {
-            const int g = g0 + lane;
-            bool vj = g < total;
-            int j = 0, code = 0;
-            if (vj) {
-                /* g grows by 32 per round and a cell holds ~10 candidates:
-                 * a few steps forward (s_pre[nst] = total > g stops it) */
-                while (s_pre[w][kc + 1] <= g) kc++;
-                j = s_jb[w][kc] + (g - s_pre[w][kc]);
-                code = s_sh[w][kc];
+            const int j = jn, code = cn, tj = tn;
+            const bool vj = vn;
+            const float4 q = qn;
+            {
+                const int g = g0 + 32 + lane;
+                vn = g < total;
+                if (vn) {
+                    while (s_pre[w][kc + 1] <= g) kc++;
+                    jn = s_jb[w][kc] + (g - s_pre[w][kc]);
+                    cn = s_sh[w][kc];
+                    qn = pos4[jn];
+                    tn = type[jn];
+                }
             }
-            const float4 q = vj ? pos4[j] : make_float4(0.f, 0.f, 0.f, 0.f);
             bool near = vj;
             if (vj && G.shift) {
                 const float qx = q.x + ((code & 3) == 1 ? -L0 : ((code & 3) == 2 ? L0 : 0.0f));
@@ -800,7 +827,7 @@ __device__ __forceinline__ void build_cell(
             if (near) {
                 const int pos = fill + __popc(nb & lt);
                 s_fq[w][pos] = q;
-                s_fe[w][pos] = (unsigned)j | ((unsigned)type[j] << MD_TYPE_SHIFT);
+                s_fe[w][pos] = (unsigned)j | ((unsigned)tj << MD_TYPE_SHIFT);
                 s_fc[w][pos] = (unsigned char)code;
             }
             fill += __popc(nb);

@@ -57,9 +57,11 @@ __global__ void __launch_bounds__(FUSED_THREADS) k_pair_leapfrog(
     int gt = blockIdx.x * blockDim.x + threadIdx.x;
     int i = gt / TPA, lane = gt % TPA;
     bool active = i < kp.n;
-    /* one entry at a time (pair_term): the packed form measured slower in
-     * this kernel (85 against 82 us per step on 64000 ions) */
-    pair_total t = pair_sum<KIND, TPA, B, false, false>(geom_kp{kp, pc}, kp.cap, active ? i : 0, active, lane, pos4, type,
+    /* the pair loop of k_pair (entries two at a time in packed f32x2
+     * instructions for even B), so both step forms sum the same forces bit
+     * for bit: 76.3 against 78.7 us per step on 64000 ions with the scalar
+     * loop */
+    pair_total t = pair_sum<KIND, TPA, B, false, true>(geom_kp{kp, pc}, kp.cap, active ? i : 0, active, lane, pos4, type,
                                                  nl, nl_n, lj);
     if (lane == 0) {
         int a = threadIdx.x / TPA;

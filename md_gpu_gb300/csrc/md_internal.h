@@ -272,7 +272,7 @@ struct md_ctx {
     long long snap_host_step = 0;
     int overflow_retry = 1;        /* 0: report a list overflow inside md_step without re-running */
     int regrows = 0;               /* md_step calls re-run after a list overflow */
-    int regrids = 0;               /* NPT: cell grids laid out again for shrunken boxes */
+    int regrids = 0;               /* NPT: cell grids laid out again for changed boxes */
 
     /* timing of the last md_step call (CUDA events on the stream) */
     cudaEvent_t ev0 = nullptr, ev1 = nullptr;
