@@ -68,7 +68,8 @@ __device__ void finalize_b(const md_kparams &kp, const thermo_par &tp, int mode,
     double tke = 0.0, tpe = 0.0, tw = 0.0, tex = 0.0;
     /* the step this record belongs to (thread 0 advances it after the sums) */
     const long long step = ((volatile md_devstate *)st)->step;
-    double *hist = (rep_hist && mode != 2) ? rep_hist + (size_t)(step % rec_cap) * 3 * nrep : nullptr;
+    const int builds = ((volatile md_devstate *)st)->builds;
+    double *hist = (rep_hist && mode != 2) ? rep_hist + (size_t)(step & (rec_cap - 1)) * 3 * nrep : nullptr;
     for (int r = threadIdx.x; r < nrep; r += blockDim.x) {
         const md_rep &R = reps[r];
         const double a = fix_take(racc + 3 * r, MD_KFIX);
@@ -117,7 +118,7 @@ __device__ void finalize_b(const md_kparams &kp, const thermo_par &tp, int mode,
     }
     if (mode == 2) return;
     st->temper = 2.0 * KE * tp.inv_ndfr;
-    write_record(tp, tp.inv_ndfr, KE, PE, W, EX, 0.0, 1.0, st, rec, rec_cap);
+    write_record(tp, tp.inv_ndfr, KE, PE, W, EX, 0.0, 1.0, step, builds, st, rec, rec_cap);
 }
 
 /* Leapfrog of a batch (k_leapfrog per replica, one thread per (atom, axis)):

@@ -216,7 +216,7 @@ struct md_ctx {
     md_devstate *st = nullptr;
     md_thermo *rec = nullptr;                             /* device ring of records */
     double *rep_hist = nullptr;   /* batches: ring of per-replica (KE, PE, conserved) per step */
-    int rec_cap = 0;
+    int rec_cap = 0;              /* records in the ring (a power of two) */
     float *lj_dev = nullptr;                              /* lj1,lj2 interleaved (64 float2) */
     float *bonded_par = nullptr;                          /* bnd1,bnd2,ang1,ang2 (4x8) */
     unsigned *type_mask_dev = nullptr;

@@ -240,13 +240,13 @@ __device__ double thermo_advance(double dt, const thermo_par &tp, int mode, doub
     return ke;
 }
 
-/* Appends the step record and advances the step counter (thread 0). */
+/* Appends the record of step `step` (read by the caller before its sums,
+ * so the load is not on the path after them) and advances the step counter
+ * (thread 0).  rec_cap is a power of two. */
 __device__ void write_record(const thermo_par &tp, double inv_ndfr, double ke, double pe, double w,
-                             double extra, double xi, double lam, md_devstate *st, md_thermo *rec,
-                             int rec_cap)
+                             double extra, double xi, double lam, long long step, int builds,
+                             md_devstate *st, md_thermo *rec, int rec_cap)
 {
-    volatile md_devstate *vs = st;
-    long long step = vs->step;
     md_thermo r;
     r.step = step;
     r.ke = ke;
@@ -256,9 +256,9 @@ __device__ void write_record(const thermo_par &tp, double inv_ndfr, double ke, d
     r.conserved = tp.energy ? ke + pe + extra : 0.0;
     r.xi = xi;
     r.lambda = lam;
-    r.builds = vs->builds;
+    r.builds = builds;
     r.flags = tp.energy ? 1 : 0;
-    rec[step % rec_cap] = r;
+    rec[step & (rec_cap - 1)] = r;
     st->step = step + 1;
 }
 
@@ -269,6 +269,9 @@ __device__ void finalize(const md_kparams &kp, const thermo_par &tp, int mode, m
                          md_thermo *rec, int rec_cap)
 {
     if (threadIdx.x != 0) return;
+    volatile md_devstate *vs = st;
+    const long long step = vs->step;
+    const int builds = vs->builds;
     double ke = fix_take(&st->acc[0], MD_KFIX);
     double pe = fix_take(&st->acc[1], MD_EFIX);
     double w = fix_take(&st->acc[2], MD_EFIX);
@@ -277,7 +280,7 @@ __device__ void finalize(const md_kparams &kp, const thermo_par &tp, int mode, m
     ke = thermo_advance(kp.dt, tp, mode, ke, pe, w, st, &xi, &eta, &lam);
     if (mode == 2) return;
     double extra = tp.nh ? 0.5 * tp.q_nh * xi * xi + tp.ndf * RGAS * tp.t0 * eta : 0.0;
-    write_record(tp, tp.inv_ndfr, ke, pe, w, extra, xi, lam, st, rec, rec_cap);
+    write_record(tp, tp.inv_ndfr, ke, pe, w, extra, xi, lam, step, builds, st, rec, rec_cap);
 }
 
 /* Per-axis constants of an integrator thread (the axis is a runtime value:
