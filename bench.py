@@ -52,9 +52,10 @@ WORKLOAD = ("nacl64k: 64000-ion molten NaCl, rocksalt 20^3x8 at 1.5 g/cm^3 melte
 DT_FS = 2.0
 FLOPS_PER_PAIR = 60.0     # LJ + Wolf per unique pair inside rc (algorithmic count)
 # ncu dram__bytes_read.sum + dram__bytes_write.sum of one pair-kernel launch on
-# this workload, cold caches (75.28 + 1.54 MB), from an ncu capture of k_pair
-# with the tuning bench.py picks; not measured by bench.py itself.
-PAIR_TRAFFIC_BYTES = 76.82e6
+# this workload (the melted start state), cold caches (76.81 + 1.72 MB), from
+# an ncu capture of k_pair with the tuning bench.py picks; not measured by
+# bench.py itself.
+PAIR_TRAFFIC_BYTES = 78.53e6
 
 
 def rank_info():
@@ -549,6 +550,8 @@ def run_ours(args):
         peak = md.fp32_peak_tflops()
         roof = {"bound": "fp32", "achieved": achieved, "peak": peak, "unit": "TFLOP/s",
                 "frac": achieved / peak, "traffic": PAIR_TRAFFIC_BYTES,
+                "traffic_source": "ncu dram__bytes_read.sum + dram__bytes_write.sum of one k_pair launch "
+                                  "on this state (a separate capture, cold caches), not measured by this run",
                 "kernel": f"k_pair<Wolf> (LJ + Wolf, full list, {info['pair_tpa']} lanes per atom)",
                 "pair_ms": pair_ms, "pairs_inside_rc": int(pc), "flops_per_pair": FLOPS_PER_PAIR,
                 "peak_source": "measured FP32 FMA probe (md_probe_fp32_peak); no FP32 entry in "

@@ -391,19 +391,24 @@ __device__ __forceinline__ pair_total pair_sum(const G &g, int cap, int ii, bool
     static_assert(MD_LIST_QUANTUM % (TPA * B) == 0, "batch must divide the list padding");
     const float4 pi = pos4[ii];
     const int cnt = active ? nl_n[ii] : 0;
+    /* unrolling of the batch loop (0: the packed loop rolled, which measured
+     * fastest for a single system, 43 against 46 us per launch on 64000
+     * ions; the scalar one twice) */
+    constexpr int UNR = UNROLL ? UNROLL : ((PACK && !ENERGY && B % 2 == 0) ? 1 : 2);
     /* batches of TPA * B entries up to the first that holds the row's last
      * entry: the row is padded to a multiple of 32 (>= TPA * B) with entries
-     * that add exactly zero, so the padding past that batch is skipped */
-    const int nb = (cnt + TPA * B - 1) / (TPA * B);
+     * that add exactly zero, so the padding past that batch is skipped.  An
+     * unrolled loop takes whole unrolled rounds where the padding holds
+     * them (an odd count in some of a warp's rows made the unrolled loop's
+     * remainder run as an extra pass: 1.58 against 1.46 ms per launch on the
+     * 512-replica batch) */
+    constexpr int QE = (MD_LIST_QUANTUM % (TPA * B * UNR) == 0) ? TPA * B * UNR : TPA * B;
+    const int nb = (cnt + QE - 1) / QE * (QE / (TPA * B));
     const float2 *ljrow = lj + type[ii] * MD_MAXTYPE;
     const float qi = QFAC * pi.w;
     pair_acc acc = {0.0f, 0.0f, 0.0f, 0.0f, 0.0f};
     const unsigned *lp = nl + (size_t)ii * cap + lane;
     const bool inner = g.centered() && __all_sync(0xffffffffu, !active || interior(g, pi));
-    /* unrolling of the batch loop (0: the packed loop rolled, which measured
-     * fastest for a single system, 43 against 46 us per launch on 64000
-     * ions; the scalar one twice) */
-    constexpr int UNR = UNROLL ? UNROLL : ((PACK && !ENERGY && B % 2 == 0) ? 1 : 2);
     if (nb > 0) {
         if (inner)
             pair_loop<KIND, TPA, B, ENERGY, false, PACK, UNR>(g, pi, qi, nb, lp, pos4, ljrow, acc);
