@@ -131,6 +131,34 @@ def test_npt_regrid_keeps_the_fp64_trajectory():
     assert missing == 0 and far == 0
 
 
+def test_npt_regrid_when_the_box_grows():
+    """The same 2744-ion box pulled at -1e5 bar grows by the clamped 1e-4
+    per step; once a box edge holds a seventh cell of 1.03 times half the
+    list radius with 1% to spare (~1600 steps), md_step lays out 7 cells per
+    axis, and the list built on that grid holds every pair within the list
+    radius."""
+    with tempfile.TemporaryDirectory() as td:
+        base = _npt_case(td, ncell=7, seed=8, skin=2.4)
+        with MDSystem.from_files(base) as sim:
+            sim.set_barostat(-1e5, TAU_P, BETA)
+            L0 = sim.replica_boxes()[0][0].copy()
+            sim.step(1800)
+            b, p = sim.replica_boxes()
+            info = sim.info()
+            pos = sim.positions()
+            sim.update_neighbors(force=True)
+            nn, nm = sim.neighbor_list(640)
+            case = oracle.load(base)
+    assert info["cell_regrids"] >= 1 and info["ncell"] == [7, 7, 7]
+    assert np.all(p[0] > -1e5)          # the scale stayed clamped at 1 + 1e-4
+    # the first step scales by 1 (no pressure measured before it), the other
+    # 1799 by the clamped 1 + 1e-4
+    assert np.abs(b[0] - L0 * (1.0 + 1e-4) ** 1799).max() <= 1e-9 * L0[0]
+    rl = float(np.sqrt(case.params.rcutsq)) + 2.4
+    missing, far = _missing_pairs(pos, b[0], rl, nn, nm)
+    assert missing == 0 and far == 0
+
+
 def test_npt_box_below_twice_the_list_radius_is_reported():
     """1000 ions in a 31.86 A box with a list radius of 15.85 A (skin
     3.85 A): a target of 1e5 bar shrinks the box by 1e-4 per step, and after
