@@ -1650,6 +1650,7 @@ static md_status snapshot(md_ctx *c, bool save)
 static md_status regrid_batch(md_ctx *c)
 {
     std::vector<int> rank, lin, crep;
+    const std::vector<md_rep> reps_before = c->reps;
     int cell0 = 0;
     for (int r = 0; r < c->nrep; r++) {
         md_rep &R = c->reps[r];
@@ -1658,7 +1659,10 @@ static md_status regrid_batch(md_ctx *c)
         make_cell_grid(R.box, R.npt ? rl * 1.03f : rl, g);
         int nst = 1;
         for (int k = 0; k < 3; k++) nst *= g.stencil[k] < 0 ? g.ncell[k] : 2 * g.stencil[k] + 1;
-        if (nst > 128) return fail(c, MD_ERR_UNSUPPORTED, "NPT regrid: stencil too large");
+        if (nst > 128) {
+            c->reps = reps_before;
+            return fail(c, MD_ERR_UNSUPPORTED, "NPT regrid: stencil too large");
+        }
         for (int k = 0; k < 3; k++) {
             R.ncell[k] = g.ncell[k];
             R.stencil[k] = g.stencil[k];
@@ -1676,14 +1680,26 @@ static md_status regrid_batch(md_ctx *c)
     }
     MD_CUDA_TRY(c, cudaStreamSynchronize(c->stream));
     if (cell0 != c->ncells) {
+        /* the new tables first: on a failed allocation the context keeps
+         * its old grid (whose box check then reports MD_ERR_BOX) */
         int **arr[] = {&c->cell_rank, &c->cell_lin, &c->cell_count, &c->cell_start, &c->cell_fill, &c->cell_work,
                        &c->crep};
-        for (int **a : arr) {
-            cudaFree(*a);
-            *a = nullptr;
+        constexpr int NA = sizeof(arr) / sizeof(arr[0]);
+        int *fresh[NA] = {};
+        cudaError_t e = cudaSuccess;
+        for (int k = 0; k < NA && e == cudaSuccess; k++)
+            e = dalloc(&fresh[k], (size_t)cell0 + (arr[k] == &c->cell_start ? 1 : 0));
+        if (e != cudaSuccess) {
+            for (int *q : fresh) cudaFree(q);
+            (void)cudaGetLastError();
+            c->reps = reps_before;
+            return fail(c, MD_ERR_CUDA, std::string("NPT regrid: ") + cudaGetErrorString(e));
+        }
+        for (int k = 0; k < NA; k++) {
+            cudaFree(*arr[k]);
+            *arr[k] = fresh[k];
         }
         c->ncells = cell0;
-        for (int **a : arr) MD_CUDA_TRY(c, dalloc(a, (size_t)cell0 + (a == &c->cell_start ? 1 : 0)));
     }
     std::vector<int> zeros(cell0, 0);
     MD_CUDA_TRY(c, cudaMemcpy(c->cell_rank, rank.data(), sizeof(int) * cell0, cudaMemcpyHostToDevice));
@@ -1726,18 +1742,21 @@ static bool regrid_due(const md_ctx *c)
 
 static md_status md_step_impl(md_ctx *c, int nsteps, int energy_every, bool mark_start);
 
-/* NPT batches run in chunks of at most MD_NPT_CHUNK steps (a multiple of
- * energy_every when it is set), each ending with the regrid check: at the
+/* NPT batches run in chunks of at most MD_NPT_CHUNK steps (a whole
+ * multiple of energy_every when that fits, so that the chunks stay aligned
+ * with the energy steps), each ending with the regrid check: at the
  * per-step clamp of the box scale (1e-4) a chunk shrinks a box by at most
  * 1.3%, less than the 1.5% left between the regrid threshold and the
- * limit. */
+ * limit.  Energy steps are multiples of energy_every counted from the
+ * context's first step, so a chunk boundary never moves them. */
 #define MD_NPT_CHUNK 128
 md_status md_step(md_ctx *c, int nsteps, int energy_every)
 {
     if (!c || nsteps < 0 || energy_every < 0) return MD_ERR_ARG;
     if (!(c->batch && c->enstype == 2)) return md_step_impl(c, nsteps, energy_every, true);
-    const int chunk = energy_every > 0 ? std::max(energy_every, MD_NPT_CHUNK / energy_every * energy_every)
-                                       : MD_NPT_CHUNK;
+    const int chunk = (energy_every > 0 && energy_every <= MD_NPT_CHUNK)
+                          ? MD_NPT_CHUNK / energy_every * energy_every
+                          : MD_NPT_CHUNK;
     int done = 0;
     do {
         const int k = std::min(chunk, nsteps - done);
