@@ -598,6 +598,14 @@ def run_ours(args):
                           "read by the kernels from device memory)"),
                 **system_leg("nacl_npt", dataclasses.replace(melt, inp=npt_inp),
                              "Berendsen leapfrog NPT", 2.0, args, flush))
+            pme_inp = dict(melt.inp, cutoff=(12.0, 2), pme_spacing=1.2)
+            others["nacl64k_pme"] = dict(
+                workload=("the benchmark's melted 64000-ion NaCl with Ewald electrostatics in place of Wolf: "
+                          "the real-space erfc term (alpha = 3.09/rc = 0.2575/A, rc 12 A, skin 1 A) plus smooth "
+                          "particle-mesh Ewald on a 112^3 grid (spacing at most 1.2 A, cubic B-splines), Berendsen "
+                          "leapfrog NVT 1200 K, dt 2 fs"),
+                **system_leg("nacl_pme", dataclasses.replace(melt, inp=pme_inp),
+                             "Berendsen leapfrog NVT with PME", 2.0, args, flush))
             others["water98k"] = dict(
                 workload=("flexible 3-site water, 32768 molecules (98304 atoms) at 0.997 g/cm^3, harmonic "
                           "O-H bonds and H-O-H angles, H-H excluded, Wolf alpha 0.2/A rc 10 A skin 1 A, "

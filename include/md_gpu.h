@@ -41,7 +41,10 @@ typedef enum {
 typedef enum { MD_LEAPFROG = 0, MD_VV = 1, MD_NH = 2 } md_integrator;
 
 /* Force terms for md_compute_forces (bit mask). */
-enum { MD_TERM_PAIR = 1, MD_TERM_BOND = 2, MD_TERM_ANGLE = 4, MD_TERM_ALL = 7 };
+/* MD_TERM_RECIP: the reciprocal Ewald sum of md_set_pme (with its self,
+ * background and exclusion terms); no counterpart in the reference, whose
+ * lkspace 2 computes the real-space term only */
+enum { MD_TERM_PAIR = 1, MD_TERM_BOND = 2, MD_TERM_ANGLE = 4, MD_TERM_RECIP = 8, MD_TERM_ALL = 15 };
 
 /* A system as the reference holds it after SimulationInit (simulation.h:51-122). */
 typedef struct {
@@ -63,7 +66,8 @@ typedef struct {
     const int *angles;          /* 4*nangle: type, i, j (centre), k (0-based) */
     const float *ang1, *ang2;   /* per angle type: 2k, theta0 (rad) */
     /* run parameters (params / integr, simulation.h:88-122) */
-    int lkspace;                /* 0 reaction field, 1 Wolf, 2 Ewald real space (alpha only) */
+    int lkspace;                /* 0 reaction field, 1 Wolf, 2 Ewald real space (alpha only;
+                                   md_set_pme adds the reciprocal sum) */
     float rcutsq;               /* squared cutoff, A^2 */
     float reacf;                /* 2(eps-1)/(2eps+1)/rc^3 (lkspace 0) */
     float alfa;                 /* damping alpha, 1/A (lkspace 1, 2) */
@@ -262,6 +266,7 @@ typedef struct {
                                conditional node */
     int list_regrows;       /* md_step calls run again after their list overflowed (md_step) */
     int cell_regrids;       /* NPT batches: cell grids laid out again for a changed box (md_step) */
+    int pme_grid[3];        /* md_set_pme grid points per axis (0: no reciprocal sum) */
 } md_info;
 md_status md_get_info(md_ctx *ctx, md_info *out);
 /* Sorted -> original index map of the current atom order. */
@@ -323,6 +328,20 @@ md_status md_set_precision(md_ctx *ctx, int bits);
  * radius.  Bonds add their virial, angles none (as the reference's
  * angle_forces). */
 md_status md_set_barostat(md_ctx *ctx, double press_bar, double tau_p_fs, double compressibility_per_bar);
+/* Long-range electrostatics for lkspace 2 ("Ewald": the reference reads
+ * kmax but computes the real-space term only, simulation.cu:91-95,
+ * forces.cu:97-113; its k-space code is an unbuilt copy of GROMACS's
+ * pme.c): adds the reciprocal Ewald sum by smooth particle-mesh Ewald with
+ * cubic B-splines on a k0 x k1 x k2 grid (multiples of 8 in [16, 2048];
+ * all zero: off, the reference's behaviour), the self term
+ * -qfac alpha/sqrt(pi) sum q^2, the background of a net charge, and the
+ * removal of each atom's excluded partners' erf(alpha r)/r term.  Forces are
+ * added into the fixed-point forces in every force evaluation (md_step,
+ * md_compute_forces with MD_TERM_RECIP), energies into the per-atom
+ * energies.  Single systems only, FP32 mode, no type exclusions.  An .inp
+ * extension line "pme_spacing: <A>" sets the smallest such grid with at
+ * most that spacing.  No counterpart in the reference. */
+md_status md_set_pme(md_ctx *ctx, int k0, int k1, int k2);
 /* Box edges (nrep x 3, A) and last-step pressure (nrep, bar; may be NULL)
  * of the replicas of a batch after the last md_step (NPT moves them); for a
  * single system its fixed box and pressure 0.  Synchronises the stream. */

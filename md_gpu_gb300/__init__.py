@@ -7,4 +7,4 @@ sm_103a CUDA kernels behind a C ABI (include/md_gpu.h).
     print(sim.thermo())
 """
 from .system import (MDError, MDSystem, MD_LEAPFROG, MD_NH, MD_VV, TERM_ALL, TERM_ANGLE,  # noqa: F401
-                     TERM_BOND, TERM_PAIR, fp32_peak_tflops, library)
+                     TERM_BOND, TERM_PAIR, TERM_RECIP, fp32_peak_tflops, library)

@@ -11,10 +11,12 @@ CSRC = os.path.join(HERE, "csrc")
 BUILD = os.path.join(HERE, "_build")
 LIB = os.path.join(BUILD, "libmdgpu_gb300.so")
 SOURCES = ["md_api.cu", "k_cells.cu", "k_forces.cu", "k_integrate.cu", "k_probe.cu", "k_noalloc.cu", "k_fused.cu",
-           "k_batch.cu", "k_adjoint.cu", "md_compat.cu", "k_pair64.cu"]
+           "k_batch.cu", "k_adjoint.cu", "md_compat.cu", "k_pair64.cu", "k_pme.cu"]
 HEADERS = ["md_internal.h", "md_device.cuh", "md_pair.cuh", "md_thermo.cuh",
            os.path.join("..", "..", "include", "md_gpu.h"), os.path.join("..", "..", "include", "md_gpu_compat.h")]
 NVCC = os.environ.get("NVCC", "/usr/local/cuda/bin/nvcc")
+# cuFFT (the PME transforms) is found there at run time as well
+CUDA_LIB = os.path.join(os.path.dirname(os.path.dirname(NVCC)), "lib64")
 # host code: no FMA contraction, so x86-64 (no FMA in its baseline) and
 # aarch64 (FMA in its baseline) compute the same host-side constants
 FLAGS = ["-std=c++17", "-O3", "-gencode", "arch=compute_103a,code=sm_103a", "-lineinfo",
@@ -52,7 +54,8 @@ def build(force: bool = False, verbose: bool = False) -> str:
     if failed:
         raise RuntimeError("nvcc failed:\n" + "\n".join(f"== {s}\n{o}" for s, o in failed))
     if force or procs or not os.path.exists(LIB):
-        cmd = [NVCC, "-shared", "-gencode", "arch=compute_103a,code=sm_103a", "-o", LIB] + objs
+        cmd = [NVCC, "-shared", "-gencode", "arch=compute_103a,code=sm_103a", "-o", LIB] + objs + \
+              ["-lcufft", "-Xlinker", "-rpath", "-Xlinker", CUDA_LIB]
         r = subprocess.run(cmd, stdout=subprocess.PIPE, stderr=subprocess.STDOUT)
         if r.returncode != 0:
             raise RuntimeError("link failed:\n" + r.stdout.decode(errors="replace"))

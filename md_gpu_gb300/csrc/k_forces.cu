@@ -179,6 +179,7 @@ void launch_forces(md_ctx *c, const md_kparams &kp, bool energy, int terms)
         cudaMemsetAsync(c->epot, 0, sizeof(float) * (size_t)c->pitch, c->stream);
     }
     launch_bonded(c, kp, energy, terms);
+    if (c->pme.on && (terms & MD_TERM_RECIP)) launch_pme(c, kp, energy);
 }
 
 void launch_bonded(md_ctx *c, const md_kparams &kp, bool energy, int terms)

@@ -146,7 +146,7 @@ void fused_dispatch(md_ctx *c, const md_kparams &kp, const pair_consts &pc, cons
 bool md_can_fuse(const md_ctx *c)
 {
     return c->fuse_step && !c->batch && !c->fp64 && c->integrator == MD_LEAPFROG && !c->has_bonds &&
-           !c->has_angles;
+           !c->has_angles && !c->pme.on;
 }
 
 void launch_pair_leapfrog(md_ctx *c, const md_kparams &kp, unsigned long long cond, int has_cond)

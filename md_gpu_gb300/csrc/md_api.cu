@@ -34,6 +34,7 @@ struct parsed_run {
     int timprn = 1;
     float rdel = 0.02f;
     float press0 = 1.0f, tau_p = 1000.0f, beta = 4.5e-5f;   /* NPT: bar, fs, 1/bar */
+    float pme_spacing = 0.0f;   /* lkspace 2: PME grid spacing, A (0: real-space term only) */
 };
 
 /* .inp (simulation.cu:58-105): label tokens skipped; reacf and alfa derived
@@ -81,6 +82,7 @@ md_status parse_inp(const char *path, parsed_run &r)
             if (!strcmp(lab, "tau_t:")) d.tau_t = strtof(val, nullptr);
             else if (!strcmp(lab, "tau_p:")) r.tau_p = strtof(val, nullptr);
             else if (!strcmp(lab, "compressibility:")) r.beta = strtof(val, nullptr);
+            else if (!strcmp(lab, "pme_spacing:")) r.pme_spacing = strtof(val, nullptr);
             else if (!strcmp(lab, "integrator:"))
                 d.integrator = !strcmp(val, "vv") ? MD_VV : (!strcmp(val, "nh") ? MD_NH : MD_LEAPFROG);
         }
@@ -1307,6 +1309,20 @@ md_status md_create_from_files(const char *base, void *stream, md_ctx **out)
         (*out)->timprn = r.timprn;
         (*out)->type_names = r.names;
         if (d.enstype == 2) s = md_set_barostat(*out, r.press0, r.tau_p, r.beta);
+        if (s == MD_OK && d.lkspace == 2 && r.pme_spacing > 0.0f) {
+            /* the fewest grid points, in multiples of 8 (at least 16),
+             * that keep the spacing at most pme_spacing */
+            int K[3];
+            for (int k = 0; k < 3; k++)
+                K[k] = std::max(16, 8 * (int)ceil((double)d.box[k] / (8.0 * r.pme_spacing)));
+            s = md_set_pme(*out, K[0], K[1], K[2]);
+        }
+        if (s != MD_OK) {
+            const std::string msg = (*out)->last_error;
+            md_destroy(*out);
+            *out = nullptr;
+            md_set_global_error(msg);
+        }
     }
     return s;
 }
@@ -1316,6 +1332,7 @@ md_status md_destroy(md_ctx *c)
     if (!c) return MD_ERR_ARG;
     if (c->stream) cudaStreamSynchronize(c->stream);
     if (c->gexec) cudaGraphExecDestroy(c->gexec);
+    pme_free(c);
     free_device(c);
     if (c->ev0) cudaEventDestroy(c->ev0);
     if (c->ev1) cudaEventDestroy(c->ev1);
@@ -2093,6 +2110,10 @@ md_status md_get_info(md_ctx *c, md_info *out)
     out->kernels_per_step = md_can_fuse(c) ? 1
                                            : 1 + ((c->has_bonds || c->has_angles) ? 1 : 0) +
                                                  (c->integrator == MD_LEAPFROG ? 1 : 2);
+    /* PME: spread, solve, gather and (with exclusions) the correction, plus
+     * the kernels of cuFFT's two transforms, which are not counted */
+    if (c->pme.on) out->kernels_per_step += 3 + c->pme.excl;
+    for (int k = 0; k < 3; k++) out->pme_grid[k] = c->pme.K[k];
     /* single system: one cooperative kernel, or key, scan, scatter, order,
      * permute, copyback, remap (with bonds or angles), list, clear; batch:
      * flag (forced builds only, not counted), key, scan, scatter, order,
@@ -2125,6 +2146,9 @@ md_status md_get_cell_ranks(md_ctx *c, int *rank)
 md_status md_set_type_exclusions(md_ctx *c, const unsigned *mask)
 {
     if (!c || !mask) return MD_ERR_ARG;
+    if (c->pme.on)
+        return fail(c, MD_ERR_UNSUPPORTED, "md_set_type_exclusions: the reciprocal Ewald sum (md_set_pme) "
+                                           "takes no type exclusions");
     unsigned m[MD_MAXTYPE] = {0};
     for (int a = 0; a < c->ntype; a++)
         for (int b = 0; b < c->ntype; b++)
@@ -2134,6 +2158,34 @@ md_status md_set_type_exclusions(md_ctx *c, const unsigned *mask)
     md_status s = initial_build(c);
     if (s != MD_OK) return s;
     return refresh_state(c);
+}
+
+md_status md_set_pme(md_ctx *c, int k0, int k1, int k2)
+{
+    if (!c) return MD_ERR_ARG;
+    const int K[3] = {k0, k1, k2};
+    const bool off = k0 == 0 && k1 == 0 && k2 == 0;
+    if (!off) {
+        for (int d = 0; d < 3; d++)
+            if (K[d] < 16 || K[d] % 8 || K[d] > 2048)
+                return fail(c, MD_ERR_ARG, "md_set_pme: grid points per axis must be multiples of 8 in [16, 2048]");
+        if (c->lkspace != 2)
+            return fail(c, MD_ERR_UNSUPPORTED, "md_set_pme: needs the Ewald real-space term (lkspace 2)");
+        if (c->batch)
+            return fail(c, MD_ERR_UNSUPPORTED, "md_set_pme: single systems only");
+        if (c->fp64) return fail(c, MD_ERR_UNSUPPORTED, "md_set_pme: not in the FP64 mode");
+        for (int a = 0; a < MD_MAXTYPE; a++)
+            if (c->type_excl_mask[a])
+                return fail(c, MD_ERR_UNSUPPORTED, "md_set_pme: the context has type exclusions");
+    }
+    MD_CUDA_TRY(c, cudaStreamSynchronize(c->stream));
+    if (c->gexec) {   /* the step graphs hold the force kernels they were captured with */
+        cudaGraphExecDestroy(c->gexec);
+        c->gexec = nullptr;
+    }
+    md_status s = pme_setup(c, K);
+    if (s != MD_OK) return s;
+    return refresh_state(c);   /* the forces (and record) of the current state with the new sum */
 }
 
 /* Builds so far (synchronises the stream). */
@@ -2306,6 +2358,8 @@ md_status md_set_precision(md_ctx *c, int bits)
         c->last_error = "md_set_precision: the FP64 mode takes a fixed box (no NPT)";
         return MD_ERR_UNSUPPORTED;
     }
+    if (bits == 64 && c->pme.on)
+        return fail(c, MD_ERR_UNSUPPORTED, "md_set_precision: the FP64 mode has no reciprocal Ewald sum");
     if (bits == 64 && !c->p64_dev) {
         const int nm = c->batch ? c->nrep : 1;
         std::vector<md_p64> h(nm);

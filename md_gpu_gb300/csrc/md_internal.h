@@ -163,6 +163,23 @@ inline int md_grid_index(int atoms_per_block)
     return k;
 }
 
+/* Smooth particle-mesh Ewald of a single system (k_pme.cu, md_set_pme). */
+struct md_pme {
+    int on = 0;
+    int K[3] = {0, 0, 0};          /* grid points per axis (multiples of 8, >= 16) */
+    int ncand[3] = {0, 0, 0};      /* cells per axis searched for one brick's atoms */
+    float *grid = nullptr;         /* K0 K1 K2 reals: the charges, then the convolution */
+    void *spec = nullptr;          /* K0 K1 (K2/2+1) complex: the half spectrum */
+    float *infl = nullptr;         /* B(m) C(m) on the half spectrum */
+    int4 *org = nullptr;           /* per sorted atom: spline origin (x, y, z) */
+    float4 *wq = nullptr;          /* per sorted atom: offsets (x, y, z) and charge */
+    int fwd = 0, inv = 0;          /* cuFFT plans (cufftHandle) */
+    int plans = 0;                 /* plans created */
+    int excl = 0;                  /* the system has excluded pairs to remove */
+    int nsm = 1;
+    float e_bg = 0.0f;             /* background energy of a net charge, per atom */
+};
+
 struct md_ctx {
     /* ---- host copy of the run ---- */
     int n = 0, ntype = 0, pitch = 0, cap = 0;
@@ -273,6 +290,7 @@ struct md_ctx {
     int overflow_retry = 1;        /* 0: report a list overflow inside md_step without re-running */
     int regrows = 0;               /* md_step calls re-run after a list overflow */
     int regrids = 0;               /* NPT: cell grids laid out again for changed boxes */
+    md_pme pme;                    /* lkspace 2: the reciprocal Ewald sum (md_set_pme) */
 
     /* timing of the last md_step call (CUDA events on the stream) */
     cudaEvent_t ev0 = nullptr, ev1 = nullptr;
@@ -309,6 +327,12 @@ inline void md_shift_consts(int lkspace, float rcutsq, float alfa, float reacf, 
         *ucc = 0.0f;
     }
 }
+/* ---- smooth particle-mesh Ewald (k_pme.cu) ---- */
+/* grid K (all zero: off); lkspace 2 single systems only (md_set_pme checks) */
+md_status pme_setup(md_ctx *c, const int K[3]);
+void pme_free(md_ctx *c);
+/* spread, FFTs, solve and gather of the reciprocal sum, added into the forces */
+void launch_pme(md_ctx *c, const md_kparams &kp, bool energy);
 /* Message returned by md_last_error(NULL, ...). */
 void md_set_global_error(const std::string &msg);
 

@@ -357,6 +357,8 @@ def write_case(sys_: System, directory: str, name: Optional[str] = None) -> str:
         lines.append(f"tau_p: {p['tau_p']!r}")
     if "compressibility" in p:
         lines.append(f"compressibility: {p['compressibility']!r}")
+    if "pme_spacing" in p:   # lkspace 2: the reciprocal Ewald sum on a grid of at most this spacing
+        lines.append(f"pme_spacing: {p['pme_spacing']!r}")
     if p.get("integrator", "leapfrog") != "leapfrog":
         lines.append(f"integrator: {p['integrator']}")
     with open(base + ".inp", "w") as fh:

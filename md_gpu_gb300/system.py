@@ -18,7 +18,7 @@ HERE = os.path.dirname(os.path.abspath(__file__))
 LIB_PATH = os.path.join(HERE, "_build", "libmdgpu_gb300.so")
 
 MD_LEAPFROG, MD_VV, MD_NH = 0, 1, 2
-TERM_PAIR, TERM_BOND, TERM_ANGLE, TERM_ALL = 1, 2, 4, 7
+TERM_PAIR, TERM_BOND, TERM_ANGLE, TERM_RECIP, TERM_ALL = 1, 2, 4, 8, 15
 STATUS = {0: "ok", 1: "invalid argument", 2: "cannot open file", 3: "parse error", 4: "CUDA error",
           5: "neighbour list overflow", 6: "more than four bonds/angles on an atom",
           7: "unsupported option", 8: "cutoff + skin exceeds half the box"}
@@ -69,7 +69,7 @@ class Info(C.Structure):
                 ("kernels_per_rebuild", C.c_int), ("kernels_per_graph", C.c_int),
                 ("pair_entries_per_lane", C.c_int), ("positions_centered", C.c_int),
                 ("fused_step", C.c_int), ("rebuild_inline", C.c_int), ("list_regrows", C.c_int),
-                ("cell_regrids", C.c_int)]
+                ("cell_regrids", C.c_int), ("pme_grid", C.c_int * 3)]
 
 
 def _make_desc(keep, *, box, itype, charge, pos, vel, type_mass, lj1, lj2, lkspace, rcutsq,
@@ -161,6 +161,7 @@ def library(path: Optional[str] = None):
     L.md_debug_rebuild_barrier.argtypes = [vp, C.c_double, C.c_int]
     L.md_set_precision.argtypes = [vp, C.c_int]
     L.md_set_barostat.argtypes = [vp, C.c_double, C.c_double, C.c_double]
+    L.md_set_pme.argtypes = [vp, C.c_int, C.c_int, C.c_int]
     L.md_get_replica_box.argtypes = [vp, vp, vp, C.c_int]
     L.md_debug_list_capacity.argtypes = [vp, C.c_int, C.c_int]
     L.md_get_replica_history.argtypes = [vp, vp, C.c_int, C.POINTER(C.c_int)]
@@ -411,7 +412,8 @@ class MDSystem:
                 "pair_depth": i.pair_entries_per_lane,
                 "centered": bool(i.positions_centered),
                 "fused_step": bool(i.fused_step), "rebuild_inline": bool(i.rebuild_inline),
-                "list_regrows": i.list_regrows, "cell_regrids": i.cell_regrids}
+                "list_regrows": i.list_regrows, "cell_regrids": i.cell_regrids,
+                "pme_grid": list(i.pme_grid)}
 
     def neighbor_list(self, nmax):
         """Reference layout (neighborlist.cu:284): (nnlist[pitch*nmax], nnlist_max[pitch])."""
@@ -474,6 +476,13 @@ class MDSystem:
         constant (fs) and compressibility (1/bar)."""
         _check(library().md_set_barostat(self._ctx, float(press_bar), float(tau_p_fs),
                                          float(compressibility_per_bar)), self._ctx)
+
+    def set_pme(self, k0, k1=None, k2=None):
+        """lkspace 2: the reciprocal Ewald sum by smooth particle-mesh Ewald on
+        a k0 x k1 x k2 grid (multiples of 8, at least 16; 0: off)."""
+        k1 = k0 if k1 is None else k1
+        k2 = k0 if k2 is None else k2
+        _check(library().md_set_pme(self._ctx, int(k0), int(k1), int(k2)), self._ctx)
 
     def replica_boxes(self):
         """(box edges (nrep, 3) in A, last-step pressures (nrep,) in bar)."""
