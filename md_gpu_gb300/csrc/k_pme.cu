@@ -212,24 +212,30 @@ __global__ void __launch_bounds__(256) k_pme_spread(pme_par pp, const int4 *__re
             }
         }
         __syncthreads();
-        const int nw = s_nq * 64;
+        /* one (atom, x point, y point) row of 4 z points per item */
+        const int nw = s_nq * 16;
         for (int t = tid; t < nw; t += blockDim.x) {
-            const int at = t >> 6, j = (t >> 4) & 3, k = (t >> 2) & 3, l = t & 3;
+            const int at = t >> 4, j = (t >> 2) & 3, k = t & 3;
             const int rl = s_rel[at];
-            const int px = (rl & 255) - 3 + j, py = ((rl >> 8) & 255) - 3 + k, pz = (rl >> 16) - 3 + l;
-            if (px < 0 || px >= PB || py < 0 || py >= PB || pz < 0 || pz >= PB) continue;
-            const float v = s_th[at][12] * s_th[at][j] * s_th[at][4 + k] * s_th[at][8 + l];
-            const long long iv = __float2ll_rn(v * QSCALE);
-            const int pt = (px * PB + py) * PB + pz;
-            atomicAdd(&s_hi[pt], (int)(iv >> 20));
-            atomicAdd(&s_lo[pt], (int)(iv & 0xFFFFF));
+            const int px = (rl & 255) - 3 + j, py = ((rl >> 8) & 255) - 3 + k, pz0 = (rl >> 16) - 3;
+            if (px < 0 || px >= PB || py < 0 || py >= PB) continue;
+            const float vxy = s_th[at][12] * s_th[at][j] * s_th[at][4 + k];
+            const int row = (px * PB + py) * PB;
+#pragma unroll
+            for (int l = 0; l < 4; l++) {
+                const int pz = pz0 + l;
+                if (pz < 0 || pz >= PB) continue;
+                const long long iv = __float2ll_rn(vxy * s_th[at][8 + l] * QSCALE);
+                atomicAdd(&s_hi[row + pz], (int)(iv >> 20));
+                atomicAdd(&s_lo[row + pz], (int)(iv & 0xFFFFF));
+            }
         }
         __syncthreads();
     }
     for (int t = tid; t < PB * PB * PB; t += blockDim.x) {
         const int px = t / (PB * PB), py = (t / PB) % PB, pz = t % PB;
         grid[((size_t)(lo[0] + px) * pp.K[1] + (lo[1] + py)) * pp.K[2] + (lo[2] + pz)] =
-            (float)((double)((long long)s_hi[t] * 1048576ll + (long long)s_lo[t]) * (1.0 / QSCALE));
+            fmaf((float)s_lo[t], 1.0f / QSCALE, (float)s_hi[t] * (1048576.0f / QSCALE));
     }
 }
 
@@ -382,10 +388,12 @@ static md_status pme_fail(md_ctx *c, md_status s, const std::string &msg)
 
 /* Candidate cells per axis of a brick: the window of PW grid points plus
  * twice the margin, over the cell side, plus one for a window that starts
- * inside a cell. */
+ * inside a cell.  The window gets 0.01 A of slack, so that the FP32 window
+ * the kernel computes never spans one cell more than counted here (a cell
+ * too many only adds candidates that fail the test). */
 static int pme_cells_per_axis(double L, int K, float binlen, int nc, float margin)
 {
-    const double win = PW * L / K + 2.0 * margin;
+    const double win = PW * L / K + 2.0 * margin + 0.01;
     const int n = (int)floor(win / binlen) + 2;
     return std::min(n, nc);
 }
