@@ -46,6 +46,17 @@ def _case(tmp, **kw):
     return synth.write_case(synth.nacl_rocksalt(ncell=5, seed=1, **kw), tmp, "c")
 
 
+def test_setters_reject_a_null_context(lib):
+    """The reciprocal-sum, barostat and precision setters check their
+    context before any device work."""
+    lib.md_set_pme.argtypes = [C.c_void_p, C.c_int, C.c_int, C.c_int]
+    lib.md_set_barostat.argtypes = [C.c_void_p, C.c_double, C.c_double, C.c_double]
+    lib.md_set_precision.argtypes = [C.c_void_p, C.c_int]
+    assert lib.md_set_pme(None, 32, 32, 32) == 1
+    assert lib.md_set_barostat(None, 1.0, 1000.0, 4.5e-5) == 1
+    assert lib.md_set_precision(None, 64) == 1
+
+
 def test_missing_files(lib):
     with pytest.raises(MDError) as e:
         MDSystem.from_files("/nonexistent/run")
