@@ -1653,13 +1653,6 @@ static md_status snapshot(md_ctx *c, bool save)
     return MD_OK;
 }
 
-/* A list overflow inside a run of steps truncates rows, so every step after
- * the rebuild that overflowed is wrong.  md_step therefore saves the state
- * on the device when it starts (a few device-to-device copies, ~170 B per
- * atom) and, when the run ends with an overflow, restores it, grows the
- * list to 5/4 of the longest row plus 16, rebuilds it at the restored
- * positions (forces recomputed for velocity Verlet) and runs the same steps
- * again, up to three times. */
 /* NPT: lay the cells of every replica of the batch out again for its
  * current box (the same rule as at creation: cells of at least 1.03 times
  * half the list radius), reallocate the cell tables when their total
@@ -1785,6 +1778,13 @@ md_status md_step(md_ctx *c, int nsteps, int energy_every)
     return MD_OK;
 }
 
+/* A list overflow inside a run of steps truncates rows, so every step after
+ * the rebuild that overflowed is wrong.  md_step therefore saves the state
+ * on the device when it starts (a few device-to-device copies, ~170 B per
+ * atom) and, when the run ends with an overflow, restores it, grows the
+ * list to 5/4 of the longest row plus 16, rebuilds it at the restored
+ * positions (forces recomputed for velocity Verlet) and runs the same steps
+ * again, up to three times. */
 static md_status md_step_impl(md_ctx *c, int nsteps, int energy_every, bool mark_start)
 {
     if (!c->overflow_retry || nsteps == 0) {
