@@ -278,12 +278,13 @@ __global__ void __launch_bounds__(3 * MD_LA) k_vv_second_b(md_kparams kp, thermo
  * by the factor the step applied to its positions (mu_used) and refreshes
  * what the kernels derive from it: the FP32 box and its inverse as the
  * reference rounds it (simulation.cu:290-292), 2/L, the wrap limit and the
- * cell side.  The cell grid keeps its cell counts and stencil, so a box
- * whose cells shrink below half the list radius (or whose list radius
- * exceeds half the box) can no longer be listed correctly: that sets the
- * sticky status 2, which the host reports; the grid is laid out with a 3%
- * margin, which the per-step clamp of mu (1e-4) lets no md_step call
- * shorter than 300 steps exhaust. */
+ * cell side.  The cell grid keeps its cell counts and stencil until the
+ * host lays it out again (md_step does between chunks of at most 128
+ * steps, before the grid's 3% margin can be used up at the per-step clamp
+ * of mu, 1e-4), so a box whose cells shrink below half the list radius
+ * inside a chunk, or whose list radius exceeds half the box, can no longer
+ * be listed correctly: that sets the sticky status 2, which the host
+ * reports. */
 __global__ void k_npt_box_b(int nrep, md_rep *reps, const md_repstate *__restrict__ repst, md_devstate *st)
 {
     const int r = blockIdx.x * blockDim.x + threadIdx.x;
