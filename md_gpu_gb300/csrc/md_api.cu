@@ -270,9 +270,10 @@ md_status check_overflow_and_sync(md_ctx *c)
     MD_CUDA_TRY(c, cudaMemcpy(&h, c->st, sizeof(h), cudaMemcpyDeviceToHost));
     if (h.status & 2)
         return fail(c, MD_ERR_BOX,
-                    "NPT: a replica's box shrank below its cell grid (cells shorter than half the list "
-                    "radius, or the list radius beyond half the box); create the context again from the "
-                    "current positions and boxes (md_get_positions, md_get_replica_box)");
+                    "NPT: a replica's box shrank below its cell grid within one step chunk, or below "
+                    "twice the list radius; create the context again from the current positions and "
+                    "boxes (md_get_positions, md_get_replica_box), with a shorter cutoff or skin for the "
+                    "latter");
     if (h.status != 0)
         return fail(c, MD_ERR_CUDA, "a grid barrier of the list rebuild timed out (device state invalid)");
     if (h.list_overflow > 0)
