@@ -47,13 +47,16 @@ def _inputs(case):
     return (float(case.params.alfa), case.q.astype(np.float64), case.box.astype(np.float64))
 
 
-def test_recip_matches_fp64_spme():
+@pytest.mark.parametrize("grid", [(32, 32, 32), (24, 32, 40)])
+def test_recip_matches_fp64_spme(grid):
+    """On a cubic grid and on one with a different size per axis (the
+    axes' roles in the bricks, transforms and tables)."""
     with tempfile.TemporaryDirectory() as td:
         base = _nacl(td)
         case = oracle.load(base)
         with MDSystem.from_files(base) as sim:
-            sim.set_pme(32)
-            assert sim.info()["pme_grid"] == [32, 32, 32]
+            sim.set_pme(*grid)
+            assert sim.info()["pme_grid"] == list(grid)
             sim.compute_forces(TERM_RECIP, energy=True)
             F = sim.forces()[:, :3]
             E = sim.energies()
@@ -61,7 +64,7 @@ def test_recip_matches_fp64_spme():
             sim.compute_forces(TERM_RECIP, energy=True)
             F2 = sim.forces()[:, :3]
     alpha, q, box = _inputs(case)
-    e, f, e_atom = ew.spme_recip(x, q, box, (32, 32, 32), alpha)
+    e, f, e_atom = ew.spme_recip(x, q, box, grid, alpha)
     e_atom = e_atom - ew.QFAC * alpha / math.sqrt(math.pi) * q * q
     assert np.array_equal(F, F2)                       # the same grid, bit for bit
     assert _rms_rel(F, f) <= 1e-5
